@@ -1,0 +1,413 @@
+"""Python binding of libmastgpu.so (the C ABI in include/mastgpu.h).
+
+The product is the CUDA/C++ library; this module builds it in-tree with nvcc
+for sm_103a and exposes the ABI through ctypes for tests, the benchmark and
+Python callers.  It contains no numerical fallback: every operation below calls
+the library, and loading fails loudly when the library is missing.
+
+Structured-mesh helpers reproduce the libMesh build_cube / build_square
+numbering the reference's examples use (examples/structural/base/
+bracket_3d_model.h:172-205 calls MeshTools::Generation::build_cube).
+"""
+import ctypes
+import glob
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD, "libmastgpu.so")
+INCLUDE = os.path.join(REPO, "include")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"]
+
+
+def _sources():
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+
+
+def _headers():
+    return sorted(glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+                  glob.glob(os.path.join(INCLUDE, "*.h")))
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.sep not in c or os.path.exists(c)):
+            return c
+    return "nvcc"
+
+
+def build(force=False, verbose=False):
+    """Compile every CUDA translation unit for sm_103a and link libmastgpu.so."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = _sources()
+    hdr_mtime = max(os.path.getmtime(h) for h in _headers())
+    objs = []
+    jobs = []
+    for s in srcs:
+        o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
+        objs.append(o)
+        if force or not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_mtime):
+            jobs.append((s, o))
+
+    def compile_one(job):
+        s, o = job
+        cmd = [_nvcc()] + ARCH + NVCC_FLAGS + ["-I", INCLUDE, "-c", s, "-o", o]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (s, r.stdout, r.stderr))
+        if verbose and r.stderr.strip():
+            print(r.stderr)
+        return o
+
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            list(ex.map(compile_one, jobs))
+    if force or jobs or not os.path.exists(LIB_PATH) or \
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(o) for o in objs):
+        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB_PATH] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    return LIB_PATH
+
+
+# --------------------------------------------------------------------------- ABI
+MG_OK, MG_EINVAL, MG_ENOMEM, MG_ENOCONV, MG_EBREAKDOWN, MG_ENAN = 0, -1, -2, -3, -4, -5
+MG_ETIMEDOUT, MG_ECUDA, MG_ENOTSUP, MG_EBUSY, MG_EBADELEM = -6, -7, -8, -9, -10
+PHYS_HEX8, PHYS_MEMBRANE, PHYS_HEAT = 0, 1, 2
+PLAIN_FP64, MIXED_TF32, MIXED_BF16 = 0, 1, 2
+KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
+PARAM_DENSITY, PARAM_K0, PARAM_ELEM_SCALE = 0, 1, 2
+
+_vp = ctypes.c_void_p
+_i32, _i64, _dbl = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("physics", _i32), ("reserved0", _i32), ("n_nodes", _i64), ("n_elems", _i64),
+                ("coords", _vp), ("conn", _vp), ("grid_nx", _i32), ("grid_ny", _i32),
+                ("grid_nz", _i32), ("reserved1", _i32)]
+
+
+class MaterialDesc(ctypes.Structure):
+    _fields_ = [("E0", _dbl), ("Emin", _dbl), ("nu", _dbl), ("penal", _dbl), ("thickness", _dbl),
+                ("k0", _dbl), ("k_beta", _dbl)]
+
+
+class BcDesc(ctypes.Structure):
+    _fields_ = [("n_fixed", _i64), ("fixed_dofs", _vp), ("n_point_loads", _i64),
+                ("load_dofs", _vp), ("load_values", _vp), ("n_conv", _i64), ("conv_elems", _vp),
+                ("conv_sides", _vp), ("conv_h", _dbl), ("conv_Tinf", _dbl),
+                ("source_elem", _vp)]
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("precision", _i32), ("krylov", _i32), ("max_iterations", _i32),
+                ("max_newton", _i32), ("rtol", _dbl), ("newton_rtol", _dbl),
+                ("consistent_jacobian", _i32), ("max_refinements", _i32), ("inner_rtol", _dbl),
+                ("timeout_s", _dbl), ("warm_start", _i32), ("graph_chunk", _i32)]
+
+
+class SolveReport(ctypes.Structure):
+    _fields_ = [("status", _i32), ("newton_iterations", _i32), ("krylov_iterations", _i32),
+                ("refinements", _i32), ("relres", _dbl), ("residual_norm", _dbl),
+                ("seconds", _dbl)]
+
+
+_lib = None
+
+
+def lib(autobuild=True):
+    """Load libmastgpu.so (building it first if needed); raises if unavailable."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if autobuild:
+        build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libmastgpu.so is not built (%s)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    L.mg_version.restype = ctypes.c_int
+    L.mg_status_string.restype = ctypes.c_char_p
+    L.mg_status_string.argtypes = [ctypes.c_int]
+    L.mg_last_error.restype = ctypes.c_char_p
+    L.mg_device_info.argtypes = [ctypes.c_char_p, ctypes.c_int, _vp, _vp, _vp]
+    L.mg_default_solve_opts.argtypes = [ctypes.POINTER(SolveOpts)]
+    L.mg_default_solve_opts.restype = None
+    L.mg_problem_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(MaterialDesc),
+                                    ctypes.POINTER(BcDesc), ctypes.POINTER(_vp)]
+    L.mg_problem_destroy.argtypes = [_vp]
+    L.mg_problem_destroy.restype = None
+    L.mg_problem_info.argtypes = [_vp, _vp, _vp, _vp]
+    L.mg_problem_stream.argtypes = [_vp]
+    L.mg_problem_stream.restype = _vp
+    L.mg_set_design.argtypes = [_vp, _vp]
+    L.mg_set_design_device.argtypes = [_vp, _vp]
+    L.mg_set_elem_scale.argtypes = [_vp, _vp]
+    L.mg_residual_and_jacobian.argtypes = [_vp, _vp, _vp, ctypes.c_int]
+    L.mg_get_csr.argtypes = [_vp, _vp, _vp, _vp]
+    L.mg_element_matrices.argtypes = [_vp, _vp, _i64, _i64, _vp, _vp]
+    L.mg_spmv.argtypes = [_vp, _vp, _vp]
+    L.mg_solve.argtypes = [_vp, ctypes.POINTER(SolveOpts), _vp, ctypes.POINTER(SolveReport)]
+    L.mg_get_solution.argtypes = [_vp, _vp]
+    L.mg_solution_device.argtypes = [_vp]
+    L.mg_solution_device.restype = _vp
+    L.mg_sensitivity_assemble.argtypes = [_vp, _vp, _i32, _i64, _vp]
+    L.mg_compliance.argtypes = [_vp, _vp, _vp, _vp]
+    L.mg_mean_temperature.argtypes = [_vp, _vp, ctypes.POINTER(SolveOpts), _vp, _vp, _vp]
+    L.mg_debug_fail_alloc_after.argtypes = [ctypes.c_int]
+    L.mg_debug_fail_alloc_after.restype = None
+    _lib = L
+    return L
+
+
+class MastGpuError(RuntimeError):
+    def __init__(self, status, where):
+        L = lib(False)
+        msg = L.mg_status_string(status).decode()
+        detail = L.mg_last_error().decode()
+        super().__init__("%s: %s (%d) %s" % (where, msg, status, detail))
+        self.status = status
+
+
+def check(status, where):
+    if status != MG_OK:
+        raise MastGpuError(status, where)
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def default_opts(**kw):
+    o = SolveOpts()
+    lib().mg_default_solve_opts(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+# ------------------------------------------------------------------ structured meshes
+def grid_hex8(nx, ny, nz, lx=None, ly=None, lz=None):
+    """Unit-spaced (by default) HEX8 grid in libMesh build_cube numbering."""
+    lx = float(nx if lx is None else lx)
+    ly = float(ny if ly is None else ly)
+    lz = float(nz if lz is None else lz)
+    k, j, i = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    coords = np.stack([i * (lx / nx), j * (ly / ny), k * (lz / nz)], axis=-1).reshape(-1, 3)
+    NX, NY = nx + 1, ny + 1
+    ke, je, ie = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    n0 = (ie + NX * (je + NY * ke)).reshape(-1)
+    off = np.array([0, 1, 1 + NX, NX, NX * NY, 1 + NX * NY, 1 + NX + NX * NY, NX + NX * NY])
+    conn = (n0[:, None] + off[None, :]).astype(np.int32)
+    return np.ascontiguousarray(coords, dtype=np.float64), np.ascontiguousarray(conn)
+
+
+def grid_quad4(nx, ny, lx=1.0, ly=1.0):
+    j, i = np.meshgrid(np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    coords = np.stack([i * (lx / nx), j * (ly / ny)], axis=-1).reshape(-1, 2)
+    NX = nx + 1
+    je, ie = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    n0 = (ie + NX * je).reshape(-1)
+    conn = (n0[:, None] + np.array([0, 1, 1 + NX, NX])[None, :]).astype(np.int32)
+    return np.ascontiguousarray(coords, dtype=np.float64), np.ascontiguousarray(conn)
+
+
+# ------------------------------------------------------------------ problem handle
+class Problem:
+    """One mg_problem handle (mesh + design + device system on one stream)."""
+
+    def __init__(self, physics, coords, conn, material, fixed_dofs=(), load_dofs=(),
+                 load_values=(), conv_elems=(), conv_sides=(), conv_h=0.0, conv_Tinf=0.0,
+                 source_elem=None, grid=(0, 0, 0)):
+        L = lib()
+        self._keep = []
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int32)
+        self.physics = physics
+        self.dpn = {PHYS_HEX8: 3, PHYS_MEMBRANE: 2, PHYS_HEAT: 1}[physics]
+        self.n_nodes = self.coords.shape[0]
+        self.n_elems = self.conn.shape[0]
+        self.n_dofs = self.n_nodes * self.dpn
+        mesh = MeshDesc(physics, 0, self.n_nodes, self.n_elems, _p(self.coords), _p(self.conn),
+                        grid[0], grid[1], grid[2], 0)
+        mat = MaterialDesc(**material)
+        fx = np.ascontiguousarray(fixed_dofs, dtype=np.int64)
+        ld = np.ascontiguousarray(load_dofs, dtype=np.int64)
+        lv = np.ascontiguousarray(load_values, dtype=np.float64)
+        ce = np.ascontiguousarray(conv_elems, dtype=np.int32)
+        cs = np.ascontiguousarray(conv_sides, dtype=np.int32)
+        src = None if source_elem is None else np.ascontiguousarray(source_elem, dtype=np.float64)
+        self._keep += [fx, ld, lv, ce, cs, src]
+        bc = BcDesc(fx.shape[0], _p(fx), ld.shape[0], _p(ld), _p(lv), ce.shape[0], _p(ce), _p(cs),
+                    conv_h, conv_Tinf, _p(src))
+        h = ctypes.c_void_p()
+        check(L.mg_problem_create(ctypes.byref(mesh), ctypes.byref(mat), ctypes.byref(bc),
+                                  ctypes.byref(h)), "mg_problem_create")
+        self.h = h
+        n = ctypes.c_int64()
+        nnz = ctypes.c_int64()
+        nc = ctypes.c_int32()
+        check(L.mg_problem_info(self.h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(nc)),
+              "mg_problem_info")
+        self.nnz, self.n_colors = nnz.value, nc.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mg_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return lib().mg_problem_stream(self.h)
+
+    def set_design(self, rho):
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        check(lib().mg_set_design(self.h, _p(rho)), "mg_set_design")
+
+    def set_design_device(self, ptr):
+        check(lib().mg_set_design_device(self.h, ctypes.c_void_p(ptr)), "mg_set_design_device")
+
+    def set_elem_scale(self, s):
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        check(lib().mg_set_elem_scale(self.h, _p(s)), "mg_set_elem_scale")
+
+    def residual_and_jacobian(self, X, want_R=True, want_J=True):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        R = np.zeros(self.n_dofs) if want_R else None
+        check(lib().mg_residual_and_jacobian(self.h, _p(X), _p(R), int(want_J)),
+              "mg_residual_and_jacobian")
+        return R
+
+    def get_csr(self):
+        rowptr = np.zeros(self.n_dofs + 1, dtype=np.int32)
+        cols = np.zeros(self.nnz, dtype=np.int32)
+        vals = np.zeros(self.nnz)
+        check(lib().mg_get_csr(self.h, _p(rowptr), _p(cols), _p(vals)), "mg_get_csr")
+        return rowptr, cols, vals
+
+    def element_matrices(self, first, count, X=None):
+        nd = {PHYS_HEX8: 24, PHYS_MEMBRANE: 8, PHYS_HEAT: 4}[self.physics]
+        Ke = np.zeros((count, nd, nd))
+        fe = np.zeros((count, nd))
+        Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
+        check(lib().mg_element_matrices(self.h, _p(Xa), first, count, _p(Ke), _p(fe)),
+              "mg_element_matrices")
+        return Ke, fe
+
+    def spmv(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.n_dofs)
+        check(lib().mg_spmv(self.h, _p(x), _p(y)), "mg_spmv")
+        return y
+
+    def solve(self, opts=None, X=None, raise_on_error=True):
+        o = opts if opts is not None else default_opts()
+        Xa = np.zeros(self.n_dofs) if X is None else np.ascontiguousarray(X, dtype=np.float64).copy()
+        rep = SolveReport()
+        rc = lib().mg_solve(self.h, ctypes.byref(o), _p(Xa), ctypes.byref(rep))
+        if raise_on_error:
+            check(rc, "mg_solve")
+        return Xa, rep
+
+    def solve_resident(self, opts):
+        """Solve with all inputs already on the device; the solution stays there."""
+        rep = SolveReport()
+        rc = lib().mg_solve(self.h, ctypes.byref(opts), None, ctypes.byref(rep))
+        return rc, rep
+
+    def solution(self):
+        X = np.zeros(self.n_dofs)
+        check(lib().mg_get_solution(self.h, _p(X)), "mg_get_solution")
+        return X
+
+    def compliance(self, X=None, want_sens=True):
+        Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
+        c = ctypes.c_double()
+        dc = np.zeros(self.n_elems) if want_sens else None
+        check(lib().mg_compliance(self.h, _p(Xa), ctypes.byref(c), _p(dc)), "mg_compliance")
+        return c.value, dc
+
+    def mean_temperature(self, T=None, opts=None, want_sens=True):
+        Ta = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
+        q, dk0 = ctypes.c_double(), ctypes.c_double()
+        ds = np.zeros(self.n_elems) if want_sens else None
+        o = opts if opts is not None else default_opts(krylov=KRYLOV_BICGSTAB)
+        check(lib().mg_mean_temperature(self.h, _p(Ta), ctypes.byref(o), ctypes.byref(q),
+                                        ctypes.byref(dk0) if want_sens else None, _p(ds)),
+              "mg_mean_temperature")
+        return q.value, (dk0.value if want_sens else None), ds
+
+    def sensitivity_assemble(self, kind, index=0, X=None):
+        Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
+        out = np.zeros(self.n_dofs)
+        check(lib().mg_sensitivity_assemble(self.h, _p(Xa), kind, index, _p(out)),
+              "mg_sensitivity_assemble")
+        return out
+
+
+# ------------------------------------------------------------------ benchmark problems
+SIMP_MATERIAL = dict(E0=1.0, Emin=1e-9, nu=0.3, penal=3.0, thickness=1.0, k0=0.0, k_beta=0.0)
+
+
+def simp_cantilever(nx, ny, nz, load_y0=0, load_y1=None, material=None):
+    """HEX8 SIMP cantilever: x=0 face clamped, total -z unit load spread over the
+    nodes of the z=0 edge at x=max between node rows load_y0..load_y1."""
+    coords, conn = grid_hex8(nx, ny, nz)
+    NX, NY, NZ = nx + 1, ny + 1, nz + 1
+    k, j = np.meshgrid(np.arange(NZ), np.arange(NY), indexing="ij")
+    clamp = (NX * (j + NY * k)).reshape(-1)
+    fixed = (clamp[:, None] * 3 + np.arange(3)[None, :]).reshape(-1)
+    y1 = ny if load_y1 is None else load_y1
+    ys = np.arange(load_y0, y1 + 1)
+    load_nodes = nx + NX * ys
+    load_dofs = load_nodes * 3 + 2
+    load_vals = np.full(ys.shape[0], -1.0 / ys.shape[0])
+    return Problem(PHYS_HEX8, coords, conn, material or SIMP_MATERIAL, fixed_dofs=fixed,
+                   load_dofs=load_dofs, load_values=load_vals, grid=(nx, ny, nz))
+
+
+def heat_square(nx=200, ny=200, k0=1.0, beta=0.01, h=1.0, hc=10.0, Tinf=0.0, q=1.0,
+                lo=0.25, hi=0.75):
+    """QUAD4 conduction on [0,1]^2: T=0 at x=0, convection on x=1, source q on
+    the element-aligned box [lo,hi]^2."""
+    coords, conn = grid_quad4(nx, ny)
+    NX = nx + 1
+    fixed = (NX * np.arange(ny + 1)).astype(np.int64)
+    conv_elems = (nx - 1) + nx * np.arange(ny)
+    conv_sides = np.ones(ny, dtype=np.int32)
+    ic = (np.arange(nx) + 0.5) / nx
+    jc = (np.arange(ny) + 0.5) / ny
+    inside = ((jc[:, None] > lo) & (jc[:, None] < hi)) & ((ic[None, :] > lo) & (ic[None, :] < hi))
+    src = np.where(inside, q, 0.0).reshape(-1)
+    mat = dict(E0=0.0, Emin=0.0, nu=0.0, penal=1.0, thickness=h, k0=k0, k_beta=beta)
+    return Problem(PHYS_HEAT, coords, conn, mat, fixed_dofs=fixed, conv_elems=conv_elems,
+                   conv_sides=conv_sides, conv_h=hc, conv_Tinf=Tinf, source_elem=src,
+                   grid=(nx, ny, 0))
+
+
+def device_info():
+    name = ctypes.create_string_buffer(256)
+    sm, ma, mi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    check(lib().mg_device_info(name, 256, ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)),
+          "mg_device_info")
+    return dict(name=name.value.decode(), sm_count=sm.value, cc=(ma.value, mi.value))
