@@ -1,0 +1,344 @@
+"""Benchmark: SIMP cantilever design evaluations on one GB300.
+
+Workload: HEX8 SIMP cantilever 128x64x64 (524,288 elements, 1,635,075 dofs),
+densities iid U[0.01, 1] (numpy default_rng(0), element order x-fastest),
+E0 = 1, Emin = 1e-9, nu = 0.3, p = 3, x = 0 face clamped, unit -z load spread
+over the 65 nodes of the x = max, z = 0 edge.  One step = one design
+evaluation: solve to 1e-8 relative FP64 residual ||f - K u|| / ||f||, then the
+compliance f.u and dC/drho for all elements.
+
+value  -- solves/s of the mixed-precision form (tcgen05 TF32 matrix-free operator,
+          FP32 CG, FP64 refinement), inputs resident in HBM, L2 flushed between steps.
+e2e    -- the same through the C ABI with host buffers: densities and initial
+          guess copied in, solution and sensitivities copied out, every step.
+plain_fp64 -- the FP64 CSR Jacobi-PCG form on the same GPU (the 5x target's base).
+cpu_baseline -- the FP64 CPU restatement (oracle, Jacobi-PCG, all host threads):
+          assembly plus a bounded number of PCG iterations, extrapolated to the
+          oracle's own full-solve iteration count (tests/golden fixture).
+
+--impl reference runs that CPU implementation alone (the reference arm).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "mast-multiphysics_gb300"))
+
+NX, NY, NZ, SEED = 128, 64, 64, 0
+WORKLOAD = "simp_cantilever_hex8_128x64x64"
+METRIC = "solves/s @1e-8 FP64 residual (SIMP cantilever design evaluation)"
+GOLDEN = os.path.join(REPO, "tests", "golden", "simp_128x64x64_seed0.npz")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="tf32", choices=["tf32", "bf16", "bf16x3", "tf32x3"])
+    ap.add_argument("--cpu-iters", type=int, default=40, help="PCG iterations in the CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def cpu_sample(iters):
+    """Oracle (FP64 CPU restatement, all host threads): assembly + `iters`
+    Jacobi-PCG iterations of the 128x64x64 problem; solve time extrapolated with
+    the oracle's own full-solve iteration count at 1e-8."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    g = np.load(GOLDEN)
+    n_full = int(g["iterations_1e8"])
+    rho = np.random.default_rng(SEED).uniform(0.01, 1.0, NX * NY * NZ)
+    d = O.simp_desc(NX, NY, NZ, rtol=1e-8, maxit=iters)
+    t0 = time.time()
+    _, _, rep = O.simp_solve(d, rho, want_sens=False)
+    wall = time.time() - t0
+    t_iter = rep.t_solve / max(rep.iterations, 1)
+    t_solve = rep.t_assemble + n_full * t_iter
+    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": O.max_threads(), "kind": "port",
+            "sample": "assembly + %d Jacobi-PCG iterations of the 128x64x64 problem (%.1f s); "
+                      "solve time = t_assembly %.2f s + %d iterations x %.1f ms (the oracle's own "
+                      "iteration count to 1e-8)" % (rep.iterations, wall, rep.t_assemble, n_full,
+                                                   t_iter * 1e3),
+            "seconds_per_solve": t_solve}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_sample(max(5, args.cpu_iters // 4))
+    vals = []
+    t0 = time.time()
+    for _ in range(args.steps):
+        vals.append(cpu_sample(args.cpu_iters))
+    wall = time.time() - t0
+    v = statistics.median([x["value"] for x in vals])
+    cb = dict(vals[-1])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U[0.01,1] densities)",
+            "config": {"workload": WORKLOAD, "n_dofs": 1635075, "n_elems": 524288,
+                       "rtol": 1e-8, "solver": "FP64 CSR Jacobi-PCG (CPU restatement)",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import mastgpu as M
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    prec = {"tf32": M.MIXED_TF32, "bf16": M.MIXED_BF16,
+            "bf16x3": getattr(M, "MIXED_BF16X3", M.MIXED_BF16),
+            "tf32x3": getattr(M, "MIXED_TF32X3", M.MIXED_TF32)}[args.precision]
+    rho = np.random.default_rng(SEED).uniform(0.01, 1.0, NX * NY * NZ)
+    prob = M.simp_cantilever(NX, NY, NZ)
+    stream = torch.cuda.ExternalStream(prob.stream)
+    d_rho = torch.from_numpy(rho).to(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 512 MB > L2
+    opts = M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0)
+
+    def step_resident():
+        prob.set_design_device(d_rho.data_ptr())
+        rc, rep = prob.solve_resident(opts)
+        M.check(rc, "mg_solve")
+        c = ctypes.c_double()
+        M.check(M.lib().mg_compliance_resident(prob.h, ctypes.byref(c)), "mg_compliance_resident")
+        return rep, c.value
+
+    # ---------------- value: resident inputs, per-step CUDA events on the library stream
+    for _ in range(args.warmup):
+        step_resident()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = Clocks(local)
+    launches0 = M.lib().mg_launch_count()
+    ev = []
+    reps = []
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # evict L2 between steps (outside the events)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rep, comp = step_resident()
+        e1.record(stream)
+        ev.append((e0, e1))
+        reps.append((rep.krylov_iterations, rep.refinements, rep.relres, comp))
+    torch.cuda.synchronize()
+    t_wall = time.time() - t_wall0
+    launches = M.lib().mg_launch_count() - launches0
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    ms_step = sum(ms) / len(ms)
+    if world > 1:
+        t = torch.tensor([ms_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * 1e3 / ms_step
+
+    g = np.load(GOLDEN)
+    comp_err = abs(reps[-1][3] - float(g["compliance"])) / float(g["compliance"])
+    # ---------------- e2e: host buffers through the C ABI
+    X0 = np.zeros(prob.n_dofs)
+    e2e_ms = []
+    for i in range(max(1, args.steps)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prob.set_design(rho)
+        u, rep = prob.solve(opts, X=X0)
+        c, dch = prob.compliance()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    dc_err = float(np.abs(dch - g["dc"]).max() / np.abs(g["dc"]).max())
+    e2e_val = world * 1e3 / (sum(e2e_ms) / len(e2e_ms))
+    h2d = rho.nbytes + X0.nbytes
+    d2h = u.nbytes + dch.nbytes + 8
+
+    # ---------------- dominant kernel: tensor-core brick operator, timed alone
+    n = prob.n_dofs
+    n_el = NX * NY * NZ
+    reps_k = 50
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    M.check(M.lib().mg_debug_launch_apply(prob.h, prec, 5), "warm")
+    torch.cuda.synchronize()
+    k0.record(stream)
+    M.check(M.lib().mg_debug_launch_apply(prob.h, prec, reps_k), "apply")
+    k1.record(stream)
+    torch.cuda.synchronize()
+    k_ms = k0.elapsed_time(k1) / reps_k
+    # algorithmic bytes per launch: read z, p_old (4 B each per dof), write p_new, q,
+    # read E (4 B per element) and the node Dirichlet mask (1 B per node)
+    alg_bytes = 16 * n + 4 * n_el + n // 3
+    pk = peaks()
+    peak = pk.get("hbm_gbs", 6800.0)
+    roof = {"kernel": "mf_apply_kernel (tcgen05 %s brick operator, CG step)" % args.precision,
+            "bound": "hbm", "achieved": alg_bytes / (k_ms * 1e-3) / 1e9, "peak": peak,
+            "unit": "GB/s", "frac": alg_bytes / (k_ms * 1e-3) / 1e9 / peak,
+            "traffic": None, "bytes_per_launch": alg_bytes, "us_per_launch": k_ms * 1e3,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback"}
+
+    # ---------------- plain FP64 form on the same GPU
+    plain = None
+    if not args.no_plain:
+        popts = M.default_opts(precision=M.PLAIN_FP64, rtol=1e-8, timeout_s=600.0)
+        prob.set_design(rho)
+        prob.solve(popts)  # assemble + warm
+        pt = []
+        for _ in range(2):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            p0 = torch.cuda.Event(enable_timing=True)
+            p1 = torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
+            prob.set_design_device(d_rho.data_ptr())
+            rc, prep = prob.solve_resident(popts)
+            M.check(M.lib().mg_compliance_resident(prob.h, ctypes.byref(ctypes.c_double())), "c")
+            p1.record(stream)
+            torch.cuda.synchronize()
+            pt.append(p0.elapsed_time(p1))
+        sp0 = torch.cuda.Event(enable_timing=True)
+        sp1 = torch.cuda.Event(enable_timing=True)
+        M.check(M.lib().mg_debug_launch_apply(prob.h, M.PLAIN_FP64, 3), "spmv warm")
+        torch.cuda.synchronize()
+        sp0.record(stream)
+        M.check(M.lib().mg_debug_launch_apply(prob.h, M.PLAIN_FP64, 20), "spmv")
+        sp1.record(stream)
+        torch.cuda.synchronize()
+        sp_ms = sp0.elapsed_time(sp1) / 20
+        nnz = prob.nnz
+        sp_bytes = 8 * nnz + 4 * nnz // 3 + 4 * (n // 3) + 32 * n
+        plain = {"solves_per_s": 1e3 / statistics.median(pt), "ms_per_solve": statistics.median(pt),
+                 "iterations": prep.krylov_iterations, "relres": prep.relres,
+                 "spmv_us": sp_ms * 1e3, "spmv_GBps": sp_bytes / (sp_ms * 1e-3) / 1e9,
+                 "spmv_frac": sp_bytes / (sp_ms * 1e-3) / 1e9 / peak}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(args.cpu_iters)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 (TF32 tensor-core operator) / f64 refinement" if args.precision.startswith("tf32")
+                else "f32 (BF16 tensor-core operator) / f64 refinement",
+                "data": "synthetic (seeded U[0.01,1] densities, default_rng(0))",
+                "config": {"workload": WORKLOAD, "n_dofs": n, "n_elems": n_el, "rtol": 1e-8,
+                           "precision": args.precision, "inner_rtol": 1e-3,
+                           "l2": "flushed between steps (512 MB write)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "dof_per_s": value * n,
+                "iterations": reps[-1][0], "refinements": reps[-1][1],
+                "relres_fp64": reps[-1][2], "compliance_rel_err_vs_oracle": comp_err,
+                "sens_rel_err_vs_oracle": dc_err,
+                "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
+                "roofline": roof, "plain_fp64": plain,
+                "speedup_vs_plain_fp64": (value / plain["solves_per_s"]) if plain else None,
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+                "wall_s_timed": t_wall}
+        print(json.dumps(line), flush=True)
+    prob.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -180,6 +180,21 @@ int mg_mean_temperature(mg_problem *p, const double *T, const mg_solve_opts *opt
 /* Host-side fault injection: the countdown-th next device allocation made by
    the library reports MG_ENOMEM (-1 disables).  No GPU fault is involved. */
 void mg_debug_fail_alloc_after(int countdown);
+/* One application of the mixed-precision matrix-free operator y = A x
+   (precision MG_MIXED_TF32 / MG_MIXED_BF16; x must be zero on Dirichlet dofs). */
+int mg_debug_matfree_apply(mg_problem *p, int precision, const double *x, double *y);
+
+/* ---- device-resident outputs and diagnostics ---- */
+/* Compliance f.u (to *compliance on the host) and dC/drho_e into the handle's
+   device buffer mg_sensitivities_device(p), from the resident solution. */
+int mg_compliance_resident(mg_problem *p, double *compliance);
+const double *mg_sensitivities_device(mg_problem *p);
+/* Kernel launches issued by the library so far (graph nodes included). */
+long long mg_launch_count(void);
+/* Enqueues `reps` launches of the dominant Krylov kernel on the handle's stream
+   without synchronising (for event timing): the fused CSR SpMV of the CG step
+   (MG_PLAIN_FP64) or the tensor-core brick operator (MG_MIXED_*). */
+int mg_debug_launch_apply(mg_problem *p, int precision, int reps);
 
 /* parameter kinds for mg_sensitivity_assemble */
 #define MG_PARAM_DENSITY 0      /* rho_e of element param_index (elasticity) */

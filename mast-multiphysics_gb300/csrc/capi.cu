@@ -18,6 +18,9 @@
 namespace mg {
 
 static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 static std::atomic<int> g_alloc_countdown{-1};
 
 void set_error(const char *fmt, ...) {
@@ -435,6 +438,7 @@ int newton_heat(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
 }
 
 int solve_linear(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
+    if (!p->jacobian_valid) count_launches(p->n_colors + 2);
     MG_TRY(assemble_system(p, p->d_X, nullptr, true, false));
     int its = 0;
     double rr = 0;
@@ -649,6 +653,7 @@ int mg_solve(mg_problem *p, const mg_solve_opts *opts, double *X, mg_solve_repor
         if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) { set_error("mixed precision needs HEX8 SIMP"); return MG_ENOTSUP; }
         rc = matfree_solve(p, o, &r);
     }
+    p->last_solve_mixed = (o.precision != MG_PLAIN_FP64);
     if (X && (rc == MG_OK || rc == MG_ENOCONV)) {
         int rc2 = to_host_vec(p, p->d_X, X, p->n_dofs);
         if (rc2 != MG_OK) rc = rc2;
@@ -688,6 +693,10 @@ int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc
         dX = p->d_tmp;
     }
     if (compliance) MG_TRY(dot(p, p->d_F, dX, p->n_dofs, compliance));
+    if (dc && p->last_solve_mixed && !X) {
+        // structured grid after a mixed solve: shared-K0 FP64 sensitivity kernel
+        return matfree_sensitivity(p, dc);
+    }
     if (dc) {
         // dC/drho_e = -dE_e u_e^T K1_e u_e (compliance adjoint = -u)
         MG_TRY(elem_sensitivity(p, dX, dX, MG_PARAM_DENSITY, p->d_elem_out));
@@ -739,6 +748,35 @@ int mg_mean_temperature(mg_problem *p, const double *T, const mg_solve_opts *opt
         MG_TRY(to_host_vec(p, p->d_elem_out, dq_ds, p->n_elems));
     }
     return MG_OK;
+}
+
+long long mg_launch_count(void) { return g_launches.load(); }
+
+int mg_compliance_resident(mg_problem *p, double *compliance) {
+    if (!p) return MG_EINVAL;
+    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) return MG_ENOTSUP;
+    if (p->last_solve_mixed) return matfree_compliance_resident(p, compliance);
+    if (compliance) MG_TRY(dot(p, p->d_F, p->d_X, p->n_dofs, compliance));
+    count_launches(2);
+    MG_TRY(elem_sensitivity(p, p->d_X, p->d_X, MG_PARAM_DENSITY, p->d_elem_out));
+    count_launches(1);
+    return MG_OK;
+}
+
+const double *mg_sensitivities_device(mg_problem *p) { return p ? p->d_elem_out : nullptr; }
+
+int mg_debug_launch_apply(mg_problem *p, int precision, int reps) {
+    if (!p || reps <= 0) return MG_EINVAL;
+    if (precision == MG_PLAIN_FP64) return krylov_launch_spmv_cg(p, reps);
+    return matfree_launch_apply(p, precision, reps);
+}
+
+// Applies the mixed-precision matrix-free operator once (FP32 in/out through
+// host FP64 buffers); Dirichlet entries of x must be zero.
+int mg_debug_matfree_apply(mg_problem *p, int precision, const double *x, double *y) {
+    if (!p || !x || !y) return MG_EINVAL;
+    if (precision != MG_MIXED_TF32 && precision != MG_MIXED_BF16) return MG_EINVAL;
+    return matfree_apply_debug(p, precision, x, y);
 }
 
 }  // extern "C"

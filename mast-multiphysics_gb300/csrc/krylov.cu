@@ -401,6 +401,11 @@ __global__ void gather_kernel(const double *__restrict__ src, const int32_t *__r
 
 inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+__global__ void fill_f64_kernel(double *__restrict__ a, double v, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
 template <int MODE>
 void launch_spmv(const CsrMatrix &A, cudaStream_t s, int grid, const double *x, const double *z,
                  const double *p_old, double *p_new, double *y, const double *aux,
@@ -508,6 +513,26 @@ int transpose_csr(mg_problem *p, const CsrMatrix &A, CsrMatrix *At) {
     return MG_OK;
 }
 
+// enqueue `reps` fused CG SpMV launches (timing hook; state reset, no sync)
+int krylov_launch_spmv_cg(mg_problem *p, int reps) {
+    if (!p->jacobian_valid) MG_TRY(assemble_system(p, p->d_X, nullptr, true, false));
+    KrylovWork &w = p->kw;
+    KrylovState init{};
+    init.maxit = 1 << 30;
+    MG_CUDA_TRY(cudaMemcpyAsync(w.state, &init, sizeof(KrylovState), cudaMemcpyHostToDevice, p->stream));
+    // nonzero search direction so that every timed launch does the full work
+    fill_f64_kernel<<<blocks_for(p->n_dofs, 256), 256, 0, p->stream>>>(w.z, 1.0, p->n_dofs);
+    const int sg = spmv_grid(p->A);
+    for (int i = 0; i < reps; i++) {
+        double *pold = (i & 1) ? w.p1 : w.p0, *pnew = (i & 1) ? w.p0 : w.p1;
+        launch_spmv<1>(p->A, p->stream, sg, nullptr, w.z, pold, pnew, w.q, nullptr, w.state,
+                       w.partials, w.grid);
+    }
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(reps);
+    return MG_OK;
+}
+
 void free_csr(CsrMatrix *A) {
     // only the values are owned by a transposed view
     dev_free(A->vals);
@@ -534,6 +559,7 @@ int krylov_solve(mg_problem *p, const CsrMatrix &A, const double *d_b, double *d
     krylov_init_kernel<<<vg, kBS, 0, s>>>(n, d_b, w.q, w.r, w.z, w.p0, w.rh, w.v, w.dinv, w.state,
                                          w.partials, nparts);
     MG_CUDA_TRY(cudaGetLastError());
+    count_launches(3);
     if (krylov == MG_KRYLOV_CG) {
         // p0 = 0 and beta = 0, so the first fused SpMV forms p = z
         MG_CUDA_TRY(cudaMemsetAsync(w.p1, 0, n * sizeof(double), s));
@@ -584,6 +610,7 @@ int krylov_solve(mg_problem *p, const CsrMatrix &A, const double *d_b, double *d
             break;
         }
         ce = cudaGraphLaunch(exec, s);
+        count_launches((long long)chunk * (krylov == MG_KRYLOV_CG ? 2 : 5));
         if (ce != cudaSuccess) {
             set_error("graph launch: %s", cudaGetErrorString(ce));
             rc = MG_ECUDA;

@@ -1,14 +1,1340 @@
-// matfree.cu -- mixed-precision matrix-free SIMP operator (placeholder).
-#include "mg_internal.h"
+// matfree.cu -- mixed-precision matrix-free SIMP operator on the 5th-generation
+// tensor cores, FP32 inner CG and FP64 iterative refinement.
+//
+// Operator: y = sum_e E_e P_e^T K0 P_e u on a structured HEX8 grid (every
+// element shares the reference stiffness K0 of StructuralElement3D,
+// src/elasticity/solid_element_3d.cpp:135-423, scaled by the SIMP modulus of
+// examples/structural/example_6/example_6.cpp:100-137).  Dirichlet dofs are
+// eliminated (identity rows, zero columns) as in the plain form.
+//
+// Brick kernel (one CTA per 8x8x8 block of owned nodes, persistent grid):
+//   1. stage u over the (8+2)^3 node halo and E over the 9^3 elements that
+//      touch the owned nodes in shared memory;
+//   2. per 128-element tile, write the element displacement rows U (128 x 24,
+//      TF32 or BF16) in the canonical no-swizzle K-major UMMA layout and issue
+//      tcgen05.mma: D(128 x 32, FP32, TMEM) = U K0^T (K0 zero-padded to N = 32);
+//   3. tcgen05.ld the accumulator, scale each row by E_e (the rho^p epilogue)
+//      and park the 24 element forces in shared memory;
+//   4. every owned node sums its 8 element contributions in a fixed order:
+//      deterministic, no atomics, no colouring, one write per output dof.
+// Elements in the one-element halo are evaluated by both neighbouring bricks
+// (729 evaluations per 512 owned nodes); the tensor-core work is negligible
+// next to the gathers, so the recomputation buys determinism for free.
+//
+// Reductions are per problem and deterministic: every brick (chunk) writes a
+// partial, and the last brick (chunk) of a problem -- found with a per-problem
+// counter -- sums that problem's partials in index order.  A problem's result
+// is therefore bitwise independent of which other problems share the batch.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "matfree.cuh"
 
 namespace mg {
 
-int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
-    (void)p; (void)o; (void)rep;
-    set_error("mixed-precision path not built");
-    return MG_ENOTSUP;
+namespace {
+
+constexpr int kThreads = 256;
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-void matfree_free(mg_problem *p) { (void)p; }
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+// UMMA shared-memory descriptor, no swizzle, K-major canonical layout:
+// 8-row x 16-byte core matrices; LBO = byte step between core matrices along K,
+// SBO = byte step between 8-row groups; version field = 1 (sm_100 family).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;  // base offset 0, LBO mode 0, layout type 0 (SWIZZLE_NONE)
+}
+
+// instruction descriptor: D F32, A/B K-major, N = 32, M = 128
+template <int PREC>
+__host__ __device__ constexpr uint32_t umma_idesc() {
+    return (1u << 4) |                                   // D format F32
+           ((PREC == MG_MIXED_TF32 ? 2u : 1u) << 7) |    // A: TF32 (kind::tf32) / BF16 (kind::f16)
+           ((PREC == MG_MIXED_TF32 ? 2u : 1u) << 10) |   // B
+           ((32u >> 3) << 17) |                          // N >> 3
+           ((128u >> 4) << 24);                          // M >> 4
+}
+
+template <int PREC>
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                     uint32_t accumulate) {
+    if (PREC == MG_MIXED_TF32) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<PREC>()), "r"(accumulate));
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<PREC>()), "r"(accumulate));
+    }
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false after the iteration cap (the caller records the error)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t phase) {
+    for (int i = 0; i < (1 << 22); i++)
+        if (mbar_try_wait(mbar, phase)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tmem_alloc32(uint32_t slot) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(slot)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc32(uint32_t taddr) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(taddr) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// libMesh HEX8 local node a -> corner bits
+__host__ __device__ __forceinline__ void corner_bits(int a, int &dx, int &dy, int &dz) {
+    dx = ((a + 1) >> 1) & 1;
+    dy = (a >> 1) & 1;
+    dz = (a >> 2) & 1;
+}
+__host__ __device__ __forceinline__ int corner_index(int dx, int dy, int dz) {
+    return dz * 4 + (dy ? (dx ? 2 : 3) : (dx ? 1 : 0));
+}
+
+// --------------------------------------------------------------- block helpers
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < kThreads / 32; i++) s += sh[i];
+    return s;  // valid in thread 0
+}
+
+// fixed-order sum of part[begin .. begin+count) over the block; valid in thread 0
+__device__ __forceinline__ double ordered_sum(const double *part, int begin, int count,
+                                              double *sh) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < count; i += kThreads) s += __ldcg(part + begin + i);
+    __shared__ double tree[kThreads];
+    tree[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) tree[threadIdx.x] += tree[threadIdx.x + w];
+        __syncthreads();
+    }
+    (void)sh;
+    return tree[0];
+}
+
+__device__ __forceinline__ bool is_bad(double x) { return !isfinite(x); }
+
+// ------------------------------------------------------------------ apply
+// dynamic shared memory layout (bytes)
+constexpr int kOffB = 0;                        // K0 operand (<= 3 KB)
+constexpr int kOffA = 4096;                     // U tile (<= 12 KB)
+constexpr int kOffU = kOffA + 12288;            // staged u (1000 x 3 floats)
+constexpr int kOffE = kOffU + kBU * kBU * kBU * 3 * 4;  // element moduli (729 floats)
+constexpr int kOffRes = ((kOffE + kNEL * 4) + 15) / 16 * 16;
+constexpr int kOffBar = ((kOffRes + kNEL * kResStride * 4) + 15) / 16 * 16;
+constexpr int kApplySmem = kOffBar + 64;
+
+// MODE 0: y = A x.   MODE 1: CG step, x_gather = z + beta p_old, p_new (owned)
+// written, q = A p_new, per-problem alpha = rz / (p.q).
+template <int PREC, int MODE>
+__global__ void __launch_bounds__(kThreads, 2) mf_apply_kernel(
+    const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int n_bricks,
+    const float *__restrict__ E32, const uint8_t *__restrict__ node_fix,
+    const float *__restrict__ xin, const float *__restrict__ z, const float *__restrict__ p_old,
+    float *__restrict__ p_new, float *__restrict__ y, MfState *states,
+    double *__restrict__ brick_part, const uint32_t *__restrict__ Bop, int *err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ double red_sh[kThreads / 32];
+    __shared__ int sh_last;
+    uint32_t *sB = reinterpret_cast<uint32_t *>(smem + kOffB);
+    uint8_t *sA = smem + kOffA;
+    float *su = reinterpret_cast<float *>(smem + kOffU);
+    float *sE = reinterpret_cast<float *>(smem + kOffE);
+    float *sres = reinterpret_cast<float *>(smem + kOffRes);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBar);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBar + 8);
+    const uint32_t bar_addr = smem_u32(bar);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // any work for this block at all? (uniform)
+    bool any = false;
+    for (int bi = blockIdx.x; bi < n_bricks; bi += gridDim.x)
+        if (MODE == 0 || !states[bricks[bi].prob].done) { any = true; break; }
+    if (!any) return;
+
+    if (tid == 0) mbar_init(bar_addr, 1);
+    if (warp == 0) tmem_alloc32(smem_u32(tslot));
+    constexpr int kBWords = (PREC == MG_MIXED_TF32) ? 768 : 512;
+    for (int i = tid; i < kBWords; i += kThreads) sB[i] = Bop[i];
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    uint32_t phase = 0;
+    bool failed = false;
+
+    for (int bi = blockIdx.x; bi < n_bricks && !failed; bi += gridDim.x) {
+        const MfBrick br = bricks[bi];
+        const MfProblem P = probs[br.prob];
+        MfState *st = states + br.prob;
+        if (MODE == 1 && st->done) continue;
+        const float beta = (MODE == 1) ? (float)st->beta : 0.0f;
+        const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
+        // ---- stage u on the node halo (masked Dirichlet dofs -> 0)
+        for (int i = tid; i < kBU * kBU * kBU * 3; i += kThreads) {
+            const int node = i / 3, c = i - node * 3;
+            const int ux = node % kBU, uy = (node / kBU) % kBU, uz = node / (kBU * kBU);
+            const int gx = gx0 - 1 + ux, gy = gy0 - 1 + uy, gz = gz0 - 1 + uz;
+            float v = 0.0f;
+            if (gx >= 0 && gx < P.NX && gy >= 0 && gy < P.NY && gz >= 0 && gz < P.NZ) {
+                const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
+                const int64_t gd = P.dof_off + gn * 3 + c;
+                if (!((node_fix[P.node_off + gn] >> c) & 1)) {
+                    if (MODE == 1)
+                        v = fmaf(beta, p_old[gd], z[gd]);
+                    else
+                        v = xin[gd];
+                }
+            }
+            su[i] = v;
+        }
+        for (int l = tid; l < kNEL; l += kThreads) {
+            const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+            const int gx = gx0 - 1 + ex, gy = gy0 - 1 + ey, gz = gz0 - 1 + ez;
+            float e = 0.0f;
+            if (gx >= 0 && gx < P.nx && gy >= 0 && gy < P.ny && gz >= 0 && gz < P.nz)
+                e = E32[P.elem_off + gx + (int64_t)P.nx * (gy + (int64_t)P.ny * gz)];
+            sE[l] = e;
+        }
+        __syncthreads();
+        // ---- tensor-core element products, one 128-element tile at a time
+        for (int t = 0; t < kNTILE; t++) {
+            if (PREC == MG_MIXED_TF32) {
+                // 128 rows x 6 core columns of 4 tf32; chunk id -> byte offset 16 id
+                for (int id = tid; id < 128 * 6; id += kThreads) {
+                    const int rg = id / 48, kc = (id >> 3) % 6, rr = id & 7;
+                    const int l = t * 128 + rg * 8 + rr;
+                    uint4 w = make_uint4(0, 0, 0, 0);
+                    if (l < kNEL) {
+                        const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+                        uint32_t vv[4];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int k = kc * 4 + j, a = k / 3, c = k - a * 3;
+                            int dx, dy, dz;
+                            corner_bits(a, dx, dy, dz);
+                            vv[j] = to_tf32(su[(((ez + dz) * kBU + ey + dy) * kBU + ex + dx) * 3 + c]);
+                        }
+                        w = make_uint4(vv[0], vv[1], vv[2], vv[3]);
+                    }
+                    *reinterpret_cast<uint4 *>(sA + id * 16) = w;
+                }
+            } else {
+                // 128 rows x 4 core columns of 8 bf16 (K padded 24 -> 32)
+                for (int id = tid; id < 128 * 4; id += kThreads) {
+                    const int rg = id / 32, kc = (id >> 3) & 3, rr = id & 7;
+                    const int l = t * 128 + rg * 8 + rr;
+                    uint4 w = make_uint4(0, 0, 0, 0);
+                    if (l < kNEL && kc < 3) {
+                        const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+                        float f[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) {
+                            const int k = kc * 8 + j, a = k / 3, c = k - a * 3;
+                            int dx, dy, dz;
+                            corner_bits(a, dx, dy, dz);
+                            f[j] = su[(((ez + dz) * kBU + ey + dy) * kBU + ex + dx) * 3 + c];
+                        }
+                        w = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
+                                       pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+                    }
+                    *reinterpret_cast<uint4 *>(sA + id * 16) = w;
+                }
+            }
+            fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after();
+                const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+                if (PREC == MG_MIXED_TF32) {
+#pragma unroll
+                    for (int s = 0; s < 3; s++)
+                        umma<PREC>(tmem, umma_desc(a0 + s * 256, 128, 768),
+                                   umma_desc(b0 + s * 256, 128, 768), s > 0);
+                } else {
+#pragma unroll
+                    for (int s = 0; s < 2; s++)
+                        umma<PREC>(tmem, umma_desc(a0 + s * 256, 128, 512),
+                                   umma_desc(b0 + s * 256, 128, 512), s > 0);
+                }
+                umma_commit(bar_addr);
+            }
+            const bool ok = mbar_wait_bounded(bar_addr, phase);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                if (tid == 0) atomicOr(err, 1);
+                break;
+            }
+            fence_after();
+            // ---- epilogue: D row m -> element l = 128 t + m, scale by E_l
+            const int lg = warp & 3;
+            const int m = lg * 32 + lane, l = t * 128 + m;
+            const uint32_t taddr = tmem + ((uint32_t)(lg * 32) << 16);
+            if (warp < 4) {
+                float v[16];
+                tmem_ld16(taddr, v);
+                if (l < kNEL) {
+                    const float e = sE[l];
+#pragma unroll
+                    for (int n = 0; n < 16; n++) sres[l * kResStride + n] = e * v[n];
+                }
+            } else {
+                float v[8];
+                tmem_ld8(taddr + 16, v);
+                if (l < kNEL) {
+                    const float e = sE[l];
+#pragma unroll
+                    for (int n = 0; n < 8; n++) sres[l * kResStride + 16 + n] = e * v[n];
+                }
+            }
+            fence_before();
+            __syncthreads();
+        }
+        if (failed) break;
+        // ---- node sums over the 8 surrounding elements (fixed order)
+        double part = 0.0;
+        for (int i = tid; i < kBN * kBN * kBN * 3; i += kThreads) {
+            const int node = i / 3, c = i - node * 3;
+            const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
+            const int gx = gx0 + ox, gy = gy0 + oy, gz = gz0 + oz;
+            if (gx >= P.NX || gy >= P.NY || gz >= P.NZ) continue;
+            float acc = 0.0f;
+#pragma unroll
+            for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+                for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+                    for (int dx = 0; dx < 2; dx++) {
+                        const int l = (ox + 1 - dx) + kBE * ((oy + 1 - dy) + kBE * (oz + 1 - dz));
+                        acc += sres[l * kResStride + 3 * corner_index(dx, dy, dz) + c];
+                    }
+            const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
+            const int64_t gd = P.dof_off + gn * 3 + c;
+            const float pv = su[(((oz + 1) * kBU + oy + 1) * kBU + ox + 1) * 3 + c];
+            if ((node_fix[P.node_off + gn] >> c) & 1) acc = pv;  // identity row (pv = 0)
+            y[gd] = acc;
+            if (MODE == 1) {
+                p_new[gd] = pv;
+                part += (double)pv * (double)acc;
+            }
+        }
+        if (MODE == 1) {
+            const double s = block_sum(part, red_sh);
+            if (tid == 0) {
+                brick_part[bi] = s;
+                __threadfence();
+                const unsigned t = atomicAdd(&st->cnt_apply, 1u);
+                sh_last = (t == (unsigned)P.brick_count - 1);
+            }
+            __syncthreads();
+            if (sh_last) {
+                const double pq = ordered_sum(brick_part, P.brick_begin, P.brick_count, red_sh);
+                if (tid == 0) {
+                    st->cnt_apply = 0;
+                    st->pq = pq;
+                    if (is_bad(pq)) { st->status = MG_ENAN; st->done = 1; }
+                    else if (!(pq > 0.0)) { st->status = MG_EBREAKDOWN; st->done = 1; }
+                    else st->alpha = st->rz / pq;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc32(tmem);
+}
+
+// ---------------------------------------------------------------- vector phase
+__global__ void __launch_bounds__(kThreads) mf_update_kernel(
+    const MfChunkDesc *__restrict__ chunks, int n_chunks, const MfProblem *__restrict__ probs,
+    float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
+    const float *__restrict__ p, const float *__restrict__ q, const float *__restrict__ dinv,
+    MfState *states, double *__restrict__ chunk_part) {
+    __shared__ double red_sh[kThreads / 32];
+    __shared__ int sh_last;
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+        const MfChunkDesc C = chunks[ci];
+        MfState *st = states + C.prob;
+        if (st->done) continue;
+        const float alpha = (float)st->alpha;
+        double rz = 0.0, rr = 0.0;
+        for (int64_t i = C.begin + threadIdx.x; i < C.end; i += kThreads) {
+            x[i] = fmaf(alpha, p[i], x[i]);
+            const float ri = fmaf(-alpha, q[i], r[i]);
+            r[i] = ri;
+            const float zi = dinv[i] * ri;
+            z[i] = zi;
+            rz += (double)ri * zi;
+            rr += (double)ri * ri;
+        }
+        const double srz = block_sum(rz, red_sh);
+        const double srr = block_sum(rr, red_sh);
+        const MfProblem &P = probs[C.prob];
+        if (threadIdx.x == 0) {
+            chunk_part[ci] = srz;
+            chunk_part[n_chunks + ci] = srr;
+            __threadfence();
+            const unsigned t = atomicAdd(&st->cnt_update, 1u);
+            sh_last = (t == (unsigned)P.chunk_count - 1);
+        }
+        __syncthreads();
+        if (sh_last) {
+            const double trz = ordered_sum(chunk_part, P.chunk_begin, P.chunk_count, red_sh);
+            const double trr = ordered_sum(chunk_part + n_chunks, P.chunk_begin, P.chunk_count, red_sh);
+            if (threadIdx.x == 0) {
+                st->cnt_update = 0;
+                st->iter += 1;
+                st->total_iter += 1;
+                st->rr = trr;
+                if (is_bad(trz) || is_bad(trr)) { st->status = MG_ENAN; st->done = 1; }
+                else {
+                    st->beta = trz / st->rz;
+                    st->rz = trz;
+                    if (trr <= st->tol2) st->done = 1;
+                    else if (st->iter >= st->maxit) { st->status = MG_ENOCONV; st->done = 1; }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// inner CG start: b = scale * r64 (unit norm), x = 0, r = b, z = D^-1 r, p_old = 0
+__global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
+    const MfChunkDesc *__restrict__ chunks, int n_chunks, const MfProblem *__restrict__ probs,
+    const double *__restrict__ r64, float *__restrict__ x, float *__restrict__ r,
+    float *__restrict__ z, float *__restrict__ p_old, const float *__restrict__ dinv,
+    MfState *states, double *__restrict__ chunk_part, double inner_rtol2, int maxit) {
+    __shared__ double red_sh[kThreads / 32];
+    __shared__ int sh_last;
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+        const MfChunkDesc C = chunks[ci];
+        MfState *st = states + C.prob;
+        if (st->ref_done) {
+            if (threadIdx.x == 0) st->done = 1;  // converged problems sit out the inner loop
+            continue;
+        }
+        const double scale = st->scale;
+        double rz = 0.0, rr = 0.0;
+        for (int64_t i = C.begin + threadIdx.x; i < C.end; i += kThreads) {
+            const float bi = (float)(r64[i] * scale);
+            x[i] = 0.0f;
+            r[i] = bi;
+            const float zi = dinv[i] * bi;
+            z[i] = zi;
+            p_old[i] = 0.0f;
+            rz += (double)bi * zi;
+            rr += (double)bi * bi;
+        }
+        const double srz = block_sum(rz, red_sh);
+        const double srr = block_sum(rr, red_sh);
+        const MfProblem &P = probs[C.prob];
+        if (threadIdx.x == 0) {
+            chunk_part[ci] = srz;
+            chunk_part[n_chunks + ci] = srr;
+            __threadfence();
+            const unsigned t = atomicAdd(&st->cnt_update, 1u);
+            sh_last = (t == (unsigned)P.chunk_count - 1);
+        }
+        __syncthreads();
+        if (sh_last) {
+            const double trz = ordered_sum(chunk_part, P.chunk_begin, P.chunk_count, red_sh);
+            const double trr = ordered_sum(chunk_part + n_chunks, P.chunk_begin, P.chunk_count, red_sh);
+            if (threadIdx.x == 0) {
+                st->cnt_update = 0;
+                st->rz = trz;
+                st->rr = trr;
+                st->bb = trr;
+                st->tol2 = inner_rtol2 * trr;
+                st->beta = 0.0;
+                st->iter = 0;
+                st->maxit = maxit;
+                st->status = 0;
+                st->done = (trr <= st->tol2 || trr == 0.0) ? 1 : 0;
+                if (is_bad(trr)) { st->status = MG_ENAN; st->done = 1; }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// refinement update u += x / scale (free dofs; x is 0 on Dirichlet dofs)
+__global__ void mf_refine_kernel(const MfChunkDesc *__restrict__ chunks, int n_chunks,
+                                 const float *__restrict__ x, double *__restrict__ u64,
+                                 const MfState *states) {
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+        const MfChunkDesc C = chunks[ci];
+        const MfState *st = states + C.prob;
+        if (st->ref_done || st->status != 0) continue;
+        const double inv = 1.0 / st->scale;
+        for (int64_t i = C.begin + threadIdx.x; i < C.end; i += blockDim.x)
+            u64[i] = fma((double)x[i], inv, u64[i]);
+    }
+}
+
+// FP64 outer residual r = f - K u (CUDA-core FP64, node-centric: each owned dof
+// sums E_e K0[row, :] u_e over its 8 elements), per-problem ||r||^2 -> scale
+constexpr int kOffU64 = 0;
+constexpr int kOffK64 = kBU * kBU * kBU * 3 * 8;            // 24000
+constexpr int kOffE64 = kOffK64 + 576 * 8;                   // +4608
+constexpr int kResidSmem = kOffE64 + kNEL * 8;               // +5832
+
+__global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
+    const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int n_bricks,
+    const double *__restrict__ E64, const uint8_t *__restrict__ node_fix,
+    const double *__restrict__ u64, const double *__restrict__ f64, const double *__restrict__ K0,
+    double *__restrict__ r64, MfState *states, double *__restrict__ brick_part, double rtol2,
+    int max_ref) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ double red_sh[kThreads / 32];
+    __shared__ int sh_last;
+    double *su = reinterpret_cast<double *>(smem + kOffU64);
+    double *sK = reinterpret_cast<double *>(smem + kOffK64);
+    double *sE = reinterpret_cast<double *>(smem + kOffE64);
+    for (int i = threadIdx.x; i < 576; i += kThreads) sK[i] = K0[i];
+    for (int bi = blockIdx.x; bi < n_bricks; bi += gridDim.x) {
+        const MfBrick br = bricks[bi];
+        const MfProblem P = probs[br.prob];
+        MfState *st = states + br.prob;
+        if (st->ref_done) continue;
+        const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
+        __syncthreads();
+        for (int i = threadIdx.x; i < kBU * kBU * kBU * 3; i += kThreads) {
+            const int node = i / 3, c = i - node * 3;
+            const int ux = node % kBU, uy = (node / kBU) % kBU, uz = node / (kBU * kBU);
+            const int gx = gx0 - 1 + ux, gy = gy0 - 1 + uy, gz = gz0 - 1 + uz;
+            double v = 0.0;
+            if (gx >= 0 && gx < P.NX && gy >= 0 && gy < P.NY && gz >= 0 && gz < P.NZ) {
+                const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
+                if (!((node_fix[P.node_off + gn] >> c) & 1)) v = u64[P.dof_off + gn * 3 + c];
+            }
+            su[i] = v;
+        }
+        for (int l = threadIdx.x; l < kNEL; l += kThreads) {
+            const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+            const int gx = gx0 - 1 + ex, gy = gy0 - 1 + ey, gz = gz0 - 1 + ez;
+            double e = 0.0;
+            if (gx >= 0 && gx < P.nx && gy >= 0 && gy < P.ny && gz >= 0 && gz < P.nz)
+                e = E64[P.elem_off + gx + (int64_t)P.nx * (gy + (int64_t)P.ny * gz)];
+            sE[l] = e;
+        }
+        __syncthreads();
+        double part = 0.0;
+        for (int i = threadIdx.x; i < kBN * kBN * kBN * 3; i += kThreads) {
+            const int node = i / 3, c = i - node * 3;
+            const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
+            const int gx = gx0 + ox, gy = gy0 + oy, gz = gz0 + oz;
+            if (gx >= P.NX || gy >= P.NY || gz >= P.NZ) continue;
+            double acc = 0.0;
+            for (int dz = 0; dz < 2; dz++)
+                for (int dy = 0; dy < 2; dy++)
+                    for (int dx = 0; dx < 2; dx++) {
+                        const int ex = ox + 1 - dx, ey = oy + 1 - dy, ez = oz + 1 - dz;
+                        const double e = sE[ex + kBE * (ey + kBE * ez)];
+                        if (e == 0.0) continue;
+                        const double *Krow = sK + (3 * corner_index(dx, dy, dz) + c) * 24;
+                        double s = 0.0;
+#pragma unroll
+                        for (int b = 0; b < 8; b++) {
+                            int bx, by, bz;
+                            corner_bits(b, bx, by, bz);
+                            const double *ub = su + (((ez + bz) * kBU + ey + by) * kBU + ex + bx) * 3;
+                            s = fma(Krow[3 * b], ub[0], s);
+                            s = fma(Krow[3 * b + 1], ub[1], s);
+                            s = fma(Krow[3 * b + 2], ub[2], s);
+                        }
+                        acc = fma(e, s, acc);
+                    }
+            const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
+            const int64_t gd = P.dof_off + gn * 3 + c;
+            double rv = f64[gd] - acc;
+            if ((node_fix[P.node_off + gn] >> c) & 1) rv = 0.0;
+            r64[gd] = rv;
+            part = fma(rv, rv, part);
+        }
+        const double s = block_sum(part, red_sh);
+        if (threadIdx.x == 0) {
+            brick_part[bi] = s;
+            __threadfence();
+            const unsigned t = atomicAdd(&st->cnt_res, 1u);
+            sh_last = (t == (unsigned)P.brick_count - 1);
+        }
+        __syncthreads();
+        if (sh_last) {
+            const double rr = ordered_sum(brick_part, P.brick_begin, P.brick_count, red_sh);
+            if (threadIdx.x == 0) {
+                st->cnt_res = 0;
+                st->rr64 = rr;
+                st->scale = rr > 0.0 ? 1.0 / sqrt(rr) : 1.0;
+                if (is_bad(rr)) { st->ref_status = MG_ENAN; st->ref_done = 1; }
+                else if (rr <= rtol2 * st->ff64) st->ref_done = 1;
+                else if (st->refine >= max_ref) { st->ref_status = MG_ENOCONV; st->ref_done = 1; }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Jacobi diagonal of the mixed operator: sum_e E_e K0[3a+c][3a+c]
+__global__ void mf_diag_kernel(const MfProblem *__restrict__ probs, int n_probs,
+                               const float *__restrict__ E32, const uint8_t *__restrict__ node_fix,
+                               const double *__restrict__ K0, float *__restrict__ dinv) {
+    const int pi = blockIdx.y;
+    if (pi >= n_probs) return;
+    const MfProblem P = probs[pi];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_dofs;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t gn = i / 3;
+        const int c = (int)(i - gn * 3);
+        const int gx = (int)(gn % P.NX), gy = (int)((gn / P.NX) % P.NY), gz = (int)(gn / ((int64_t)P.NX * P.NY));
+        double d = 0.0;
+        for (int dz = 0; dz < 2; dz++)
+            for (int dy = 0; dy < 2; dy++)
+                for (int dx = 0; dx < 2; dx++) {
+                    const int ex = gx - dx, ey = gy - dy, ez = gz - dz;
+                    if (ex < 0 || ey < 0 || ez < 0 || ex >= P.nx || ey >= P.ny || ez >= P.nz) continue;
+                    const int k = 3 * corner_index(dx, dy, dz) + c;
+                    d += (double)E32[P.elem_off + ex + (int64_t)P.nx * (ey + (int64_t)P.ny * ez)] * K0[k * 24 + k];
+                }
+        const bool fixed = (node_fix[P.node_off + gn] >> c) & 1;
+        dinv[P.dof_off + i] = (fixed || d == 0.0) ? 1.0f : (float)(1.0 / d);
+    }
+}
+
+// compliance adjoint sensitivity dC/drho_e = -dE_e u_e^T K0 u_e (FP64)
+__global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
+                               const double *__restrict__ dE64, const uint8_t *__restrict__ node_fix,
+                               const double *__restrict__ u64, const double *__restrict__ K0,
+                               double *__restrict__ dc) {
+    __shared__ double sK[576];
+    for (int i = threadIdx.x; i < 576; i += blockDim.x) sK[i] = K0[i];
+    __syncthreads();
+    const int pi = blockIdx.y;
+    if (pi >= n_probs) return;
+    const MfProblem P = probs[pi];
+    const int64_t ne = (int64_t)P.nx * P.ny * P.nz;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int ex = (int)(e % P.nx), ey = (int)((e / P.nx) % P.ny), ez = (int)(e / ((int64_t)P.nx * P.ny));
+        double ue[24];
+        for (int a = 0; a < 8; a++) {
+            int dx, dy, dz;
+            corner_bits(a, dx, dy, dz);
+            const int64_t gn = (ex + dx) + (int64_t)P.NX * ((ey + dy) + (int64_t)P.NY * (ez + dz));
+            const uint8_t fx = node_fix[P.node_off + gn];
+            for (int c = 0; c < 3; c++)
+                ue[3 * a + c] = ((fx >> c) & 1) ? 0.0 : u64[P.dof_off + gn * 3 + c];
+        }
+        double s = 0.0;
+        for (int i = 0; i < 24; i++) {
+            double t = 0.0;
+            for (int j = 0; j < 24; j++) t = fma(sK[i * 24 + j], ue[j], t);
+            s = fma(ue[i], t, s);
+        }
+        dc[P.elem_off + e] = -dE64[P.elem_off + e] * s;
+    }
+}
+
+// per-chunk partial of f.u (compliance); host sums each problem's chunks in order
+__global__ void mf_dot_chunks_kernel(const MfChunkDesc *__restrict__ chunks, int n_chunks,
+                                     const double *__restrict__ a, const double *__restrict__ b,
+                                     double *__restrict__ part) {
+    __shared__ double red_sh[kThreads / 32];
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+        const MfChunkDesc C = chunks[ci];
+        double s = 0.0;
+        for (int64_t i = C.begin + threadIdx.x; i < C.end; i += kThreads) s = fma(a[i], b[i], s);
+        const double t = block_sum(s, red_sh);
+        if (threadIdx.x == 0) part[ci] = t;
+        __syncthreads();
+    }
+}
+
+__global__ void fill_f32_kernel(float *__restrict__ a, float v, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+__global__ void to_f32_kernel(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// K0 in the UMMA K-major no-swizzle layout (B operand, N = 32 rows, zero padded)
+void pack_b_operand(const double *K0, std::vector<uint32_t> &tf32, std::vector<uint32_t> &bf16) {
+    auto tf32_round = [](float x) -> uint32_t {
+        // round to nearest (ties away) on the 10-bit mantissa, as cvt.rna.tf32.f32
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
+        return u;
+    };
+    auto bf16_bits = [](float x) -> uint16_t {
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        uint32_t lsb = (u >> 16) & 1u;
+        u += 0x7fffu + lsb;  // round to nearest even
+        return (uint16_t)(u >> 16);
+    };
+    tf32.assign(768, 0u);
+    bf16.assign(512, 0u);
+    for (int n = 0; n < 32; n++) {
+        const int rg = n / 8, rr = n % 8;
+        for (int kc = 0; kc < 6; kc++)
+            for (int j = 0; j < 4; j++) {
+                const int k = kc * 4 + j;
+                float v = (n < 24) ? (float)K0[n * 24 + k] : 0.0f;
+                tf32[((rg * 6 + kc) * 128 + rr * 16) / 4 + j] = tf32_round(v);
+            }
+        for (int kc = 0; kc < 4; kc++)
+            for (int j = 0; j < 8; j += 2) {
+                const int k = kc * 8 + j;
+                float lo = (n < 24 && k < 24) ? (float)K0[n * 24 + k] : 0.0f;
+                float hi = (n < 24 && k + 1 < 24) ? (float)K0[n * 24 + k + 1] : 0.0f;
+                bf16[((rg * 4 + kc) * 128 + rr * 16) / 4 + j / 2] =
+                    (uint32_t)bf16_bits(lo) | ((uint32_t)bf16_bits(hi) << 16);
+            }
+    }
+}
+
+template <int PREC, int MODE>
+void launch_apply(MfBatch &b, const float *xin, const float *z, const float *pold, float *pnew,
+                  float *y) {
+    const uint32_t *Bop = (PREC == MG_MIXED_TF32) ? b.Bop_tf32 : b.Bop_bf16;
+    mf_apply_kernel<PREC, MODE><<<b.apply_grid, kThreads, kApplySmem, b.stream>>>(
+        b.probs, b.bricks, b.n_bricks, b.E32, b.node_fix, xin, z, pold, pnew, y, b.states,
+        b.brick_part, Bop, b.err);
+}
+
+int configure_kernels() {
+    static bool done = false;
+    if (done) return MG_OK;
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_TF32, 0>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_TF32, 1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_BF16, 0>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_BF16, 1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_residual64_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kResidSmem));
+    done = true;
+    return MG_OK;
+}
+
+int read_states(MfBatch &b) {
+    MG_CUDA_TRY(cudaMemcpyAsync(b.states_host, b.states, b.n_probs * sizeof(MfState),
+                                cudaMemcpyDeviceToHost, b.stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
+    int herr = 0;
+    MG_CUDA_TRY(cudaMemcpy(&herr, b.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        set_error("tensor-core pipeline wait exceeded its bound (error flag %d)", herr);
+        return MG_ETIMEDOUT;
+    }
+    return MG_OK;
+}
+
+int build_graph(MfBatch &b, int prec, int chunk) {
+    if (b.graph && b.graph_prec == prec && b.graph_chunk == chunk) return MG_OK;
+    if (b.graph) {
+        cudaGraphExecDestroy(b.graph);
+        b.graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    MG_CUDA_TRY(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < chunk; it++) {
+        float *pold = (it & 1) ? b.p1 : b.p0;
+        float *pnew = (it & 1) ? b.p0 : b.p1;
+        if (prec == MG_MIXED_TF32)
+            launch_apply<MG_MIXED_TF32, 1>(b, nullptr, b.z, pold, pnew, b.q);
+        else
+            launch_apply<MG_MIXED_BF16, 1>(b, nullptr, b.z, pold, pnew, b.q);
+        mf_update_kernel<<<b.vec_grid, kThreads, 0, b.stream>>>(b.chunks, b.n_chunks, b.probs, b.x,
+                                                               b.r, b.z, pnew, b.q, b.dinv,
+                                                               b.states, b.chunk_part);
+    }
+    cudaError_t e = cudaStreamEndCapture(b.stream, &g);
+    if (e != cudaSuccess) {
+        set_error("graph capture: %s", cudaGetErrorString(e));
+        return MG_ECUDA;
+    }
+    e = cudaGraphInstantiate(&b.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        set_error("graph instantiate: %s", cudaGetErrorString(e));
+        return MG_ECUDA;
+    }
+    b.graph_prec = prec;
+    b.graph_chunk = chunk;
+    return MG_OK;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------- host
+void hex8_box_stiffness(double hx, double hy, double hz, double nu, double K[576]) {
+    // same quadrature as the FP64 element kernel: 2x2x2 Gauss, E = 1
+    const double gp = 0.57735026918962576451;
+    const double lam = nu / (1.0 - nu - 2.0 * nu * nu), mu = 1.0 / (2.0 * (1.0 + nu));
+    double S[8][8][9];
+    memset(S, 0, sizeof(S));
+    for (int q = 0; q < 8; q++) {
+        const double xi = (q & 1) ? gp : -gp, eta = (q >> 1 & 1) ? gp : -gp, zeta = (q >> 2 & 1) ? gp : -gp;
+        const double w = (hx * hy * hz) / 8.0;  // det J, unit weights
+        double g[8][3];
+        for (int a = 0; a < 8; a++) {
+            int dx, dy, dz;
+            corner_bits(a, dx, dy, dz);
+            const double sx = dx ? 1 : -1, sy = dy ? 1 : -1, sz = dz ? 1 : -1;
+            const double fx = 0.5 * (1 + sx * xi), fy = 0.5 * (1 + sy * eta), fz = 0.5 * (1 + sz * zeta);
+            g[a][0] = 0.5 * sx * fy * fz * (2.0 / hx);
+            g[a][1] = 0.5 * sy * fx * fz * (2.0 / hy);
+            g[a][2] = 0.5 * sz * fx * fy * (2.0 / hz);
+        }
+        for (int a = 0; a < 8; a++)
+            for (int b = 0; b < 8; b++)
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) S[a][b][i * 3 + j] += w * g[a][i] * g[b][j];
+    }
+    for (int a = 0; a < 8; a++)
+        for (int b = 0; b < 8; b++) {
+            const double *s = S[a][b];
+            const double tr = s[0] + s[4] + s[8];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    K[(3 * a + i) * 24 + 3 * b + j] = lam * s[i * 3 + j] + mu * s[j * 3 + i] + (i == j ? mu * tr : 0.0);
+        }
+}
+
+int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, double hy,
+                  double hz, double nu, cudaStream_t stream) {
+    MG_TRY(configure_kernels());
+    b.stream = stream;
+    b.hx = hx; b.hy = hy; b.hz = hz; b.nu = nu;
+    b.n_probs = (int)shapes.size();
+    b.h_probs = shapes;
+    int64_t dof = 0, el = 0, nd = 0;
+    int nb = 0, nc = 0;
+    b.h_bricks.clear();
+    b.h_chunks.clear();
+    for (auto &P : b.h_probs) {
+        if (P.nx <= 0 || P.ny <= 0 || P.nz <= 0 || P.nx >= 32767 * kBN || P.ny >= 32767 * kBN ||
+            P.nz >= 32767 * kBN) {
+            set_error("bad grid %dx%dx%d", P.nx, P.ny, P.nz);
+            return MG_EINVAL;
+        }
+        P.NX = P.nx + 1; P.NY = P.ny + 1; P.NZ = P.nz + 1;
+        P.n_dofs = (int64_t)P.NX * P.NY * P.NZ * 3;
+        if (P.elem_off < 0) { P.elem_off = el; el += (int64_t)P.nx * P.ny * P.nz; }
+        else el = std::max(el, P.elem_off + (int64_t)P.nx * P.ny * P.nz);
+        P.dof_off = dof;
+        P.node_off = nd;
+        dof += P.n_dofs;
+        nd += (int64_t)P.NX * P.NY * P.NZ;
+        const int bx = (P.NX + kBN - 1) / kBN, by = (P.NY + kBN - 1) / kBN, bz = (P.NZ + kBN - 1) / kBN;
+        P.brick_begin = nb;
+        P.brick_count = bx * by * bz;
+        for (int k = 0; k < bz; k++)
+            for (int j = 0; j < by; j++)
+                for (int i = 0; i < bx; i++)
+                    b.h_bricks.push_back(MfBrick{(int)(&P - b.h_probs.data()), (int16_t)i, (int16_t)j, (int16_t)k, 0});
+        nb += P.brick_count;
+        P.chunk_begin = nc;
+        P.chunk_count = (int)((P.n_dofs + kChunk - 1) / kChunk);
+        for (int c = 0; c < P.chunk_count; c++) {
+            MfChunkDesc C;
+            C.prob = (int)(&P - b.h_probs.data());
+            C.pad = 0;
+            C.begin = P.dof_off + (int64_t)c * kChunk;
+            C.end = std::min(P.dof_off + P.n_dofs, C.begin + kChunk);
+            b.h_chunks.push_back(C);
+        }
+        nc += P.chunk_count;
+    }
+    b.n_bricks = nb;
+    b.n_chunks = nc;
+    b.n_dofs = dof;
+    b.n_elems = el;
+    b.n_nodes = nd;
+    int dev = 0, sms = 0;
+    MG_CUDA_TRY(cudaGetDevice(&dev));
+    MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    b.apply_grid = std::max(1, std::min(nb, 2 * sms));
+    b.vec_grid = std::max(1, std::min(nc, 4 * sms));
+    MG_TRY(dev_alloc_n(&b.probs, b.h_probs.size()));
+    MG_TRY(dev_alloc_n(&b.bricks, b.h_bricks.size()));
+    MG_TRY(dev_alloc_n(&b.chunks, b.h_chunks.size()));
+    MG_TRY(dev_alloc_n(&b.states, (size_t)b.n_probs));
+    MG_CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&b.states_host), b.n_probs * sizeof(MfState)));
+    MG_TRY(dev_alloc_n(&b.E32, (size_t)el));
+    MG_TRY(dev_alloc_n(&b.E64, (size_t)el));
+    MG_TRY(dev_alloc_n(&b.dE64, (size_t)el));
+    MG_TRY(dev_alloc_n(&b.node_fix, (size_t)nd));
+    float **f32s[] = {&b.x, &b.r, &b.z, &b.p0, &b.p1, &b.q, &b.dinv};
+    for (float **v : f32s) MG_TRY(dev_alloc_n(v, (size_t)dof));
+    MG_TRY(dev_alloc_n(&b.u64, (size_t)dof));
+    MG_TRY(dev_alloc_n(&b.r64, (size_t)dof));
+    MG_TRY(dev_alloc_n(&b.f64, (size_t)dof));
+    MG_TRY(dev_alloc_n(&b.brick_part, (size_t)nb));
+    MG_TRY(dev_alloc_n(&b.chunk_part, (size_t)2 * nc));
+    MG_TRY(dev_alloc_n(&b.err, 1));
+    MG_TRY(dev_alloc_n(&b.Bop_tf32, 768));
+    MG_TRY(dev_alloc_n(&b.Bop_bf16, 512));
+    MG_TRY(dev_alloc_n(&b.K0, 576));
+    double K0[576];
+    hex8_box_stiffness(hx, hy, hz, nu, K0);
+    std::vector<uint32_t> tf, bf;
+    pack_b_operand(K0, tf, bf);
+    cudaStream_t s = b.stream;
+    MG_CUDA_TRY(cudaMemcpyAsync(b.probs, b.h_probs.data(), b.h_probs.size() * sizeof(MfProblem), cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.bricks, b.h_bricks.data(), b.h_bricks.size() * sizeof(MfBrick), cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.Bop_tf32, tf.data(), 768 * 4, cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.Bop_bf16, bf.data(), 512 * 4, cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.err, 0, sizeof(int), s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.u64, 0, dof * 8, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.f64, 0, dof * 8, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.node_fix, 0, nd, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.E32, 0, el * 4, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.E64, 0, el * 8, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.dE64, 0, el * 8, s));
+    float *zero_vecs[] = {b.x, b.r, b.z, b.p0, b.p1, b.q};
+    for (float *v : zero_vecs) MG_CUDA_TRY(cudaMemsetAsync(v, 0, dof * 4, s));
+    MG_CUDA_TRY(cudaStreamSynchronize(s));
+    return MG_OK;
+}
+
+void mf_batch_free(MfBatch &b) {
+    if (b.stream) cudaStreamSynchronize(b.stream);
+    if (b.graph) cudaGraphExecDestroy(b.graph);
+    void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.E32, b.E64, b.dE64, b.node_fix,
+                    b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.u64, b.r64, b.f64, b.brick_part,
+                    b.chunk_part, b.err, b.Bop_tf32, b.Bop_bf16, b.K0};
+    for (void *q : ptrs) dev_free(q);
+    if (b.states_host) cudaFreeHost(b.states_host);
+    if (b.owns_stream && b.stream) cudaStreamDestroy(b.stream);
+    b = MfBatch();
+}
+
+int mf_batch_set_problem(MfBatch &b, int i, const uint8_t *node_fix_host, const double *f_host,
+                         const double *E_dev, const double *dE_dev) {
+    if (i < 0 || i >= b.n_probs) return MG_EINVAL;
+    const MfProblem &P = b.h_probs[i];
+    const int64_t nn = (int64_t)P.NX * P.NY * P.NZ, ne = (int64_t)P.nx * P.ny * P.nz;
+    cudaStream_t s = b.stream;
+    if (node_fix_host)
+        MG_CUDA_TRY(cudaMemcpyAsync(b.node_fix + P.node_off, node_fix_host, nn, cudaMemcpyHostToDevice, s));
+    if (f_host)
+        MG_CUDA_TRY(cudaMemcpyAsync(b.f64 + P.dof_off, f_host, P.n_dofs * 8, cudaMemcpyHostToDevice, s));
+    if (E_dev) {
+        MG_CUDA_TRY(cudaMemcpyAsync(b.E64 + P.elem_off, E_dev, ne * 8, cudaMemcpyDeviceToDevice, s));
+        to_f32_kernel<<<blocks_for(ne, 256), 256, 0, s>>>(b.E64 + P.elem_off, b.E32 + P.elem_off, ne);
+        MG_CUDA_TRY(cudaGetLastError());
+    }
+    if (dE_dev)
+        MG_CUDA_TRY(cudaMemcpyAsync(b.dE64 + P.elem_off, dE_dev, ne * 8, cudaMemcpyDeviceToDevice, s));
+    return MG_OK;
+}
+
+int mf_apply(MfBatch &b, int precision, const float *x, float *y) {
+    if (precision == MG_MIXED_TF32)
+        launch_apply<MG_MIXED_TF32, 0>(b, x, nullptr, nullptr, nullptr, y);
+    else
+        launch_apply<MG_MIXED_BF16, 0>(b, x, nullptr, nullptr, nullptr, y);
+    MG_CUDA_TRY(cudaGetLastError());
+    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
+    int herr = 0;
+    MG_CUDA_TRY(cudaMemcpy(&herr, b.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        set_error("tensor-core pipeline wait exceeded its bound");
+        return MG_ETIMEDOUT;
+    }
+    return MG_OK;
+}
+
+// FP64 iterative refinement around FP32 tensor-core CG:
+//   r = f - K u (FP64);  stop when ||r|| <= rtol ||f||;
+//   solve A d = r / ||r|| with FP32 CG to inner_rtol;  u += ||r|| d.
+int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start) {
+    cudaStream_t s = b.stream;
+    const double t0 = wall_time();
+    // Jacobi diagonal from the current moduli
+    {
+        dim3 grid(std::max(1u, std::min(blocks_for(b.n_dofs, 256), 4096u)), b.n_probs);
+        mf_diag_kernel<<<grid, 256, 0, s>>>(b.probs, b.n_probs, b.E32, b.node_fix, b.K0, b.dinv);
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(2);
+    }
+    if (!warm_start) MG_CUDA_TRY(cudaMemsetAsync(b.u64, 0, b.n_dofs * 8, s));
+    // reset states and compute ||f||^2 per problem
+    MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), s));
+    mf_dot_chunks_kernel<<<b.vec_grid, kThreads, 0, s>>>(b.chunks, b.n_chunks, b.f64, b.f64, b.chunk_part);
+    MG_CUDA_TRY(cudaGetLastError());
+    {
+        std::vector<double> part(b.n_chunks);
+        MG_CUDA_TRY(cudaMemcpyAsync(part.data(), b.chunk_part, b.n_chunks * 8, cudaMemcpyDeviceToHost, s));
+        MG_CUDA_TRY(cudaStreamSynchronize(s));
+        std::vector<MfState> init(b.n_probs);
+        memset(init.data(), 0, init.size() * sizeof(MfState));
+        for (int i = 0; i < b.n_probs; i++) {
+            const MfProblem &P = b.h_probs[i];
+            double ff = 0;
+            for (int c = 0; c < P.chunk_count; c++) ff += part[P.chunk_begin + c];
+            init[i].ff64 = ff > 0 ? ff : 1.0;
+            if (ff == 0.0) init[i].ref_done = 1;  // zero load: u = 0
+        }
+        MG_CUDA_TRY(cudaMemcpyAsync(b.states, init.data(), b.n_probs * sizeof(MfState), cudaMemcpyHostToDevice, s));
+    }
+    const int chunk = prm.graph_chunk > 0 ? (prm.graph_chunk + 1) / 2 * 2 : 16;
+    MG_TRY(build_graph(b, prm.precision, chunk));
+    const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
+    const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
+    for (int ref = 0;; ref++) {
+        // outer FP64 residual (also marks converged problems ref_done)
+        mf_residual64_kernel<<<b.apply_grid, kThreads, kResidSmem, s>>>(
+            b.probs, b.bricks, b.n_bricks, b.E64, b.node_fix, b.u64, b.f64, b.K0, b.r64, b.states,
+            b.brick_part, prm.rtol * prm.rtol, max_ref);
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(1);
+        MG_TRY(read_states(b));
+        bool all_done = true;
+        for (int i = 0; i < b.n_probs; i++) all_done &= b.states_host[i].ref_done != 0;
+        if (all_done) break;
+        // inner FP32 CG on the normalised residual
+        mf_inner_init_kernel<<<b.vec_grid, kThreads, 0, s>>>(
+            b.chunks, b.n_chunks, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.dinv, b.states,
+            b.chunk_part, prm.inner_rtol * prm.inner_rtol, maxit);
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(1);
+        // problems already converged keep done = 1 through the inner loop
+        for (;;) {
+            MG_TRY(read_states(b));
+            bool inner_done = true;
+            for (int i = 0; i < b.n_probs; i++)
+                inner_done &= (b.states_host[i].done != 0 || b.states_host[i].ref_done != 0);
+            if (inner_done) break;
+            if (prm.timeout_s > 0 && wall_time() - t0 > prm.timeout_s) {
+                set_error("mixed solve exceeded %.1f s", prm.timeout_s);
+                return MG_ETIMEDOUT;
+            }
+            MG_CUDA_TRY(cudaGraphLaunch(b.graph, s));
+            count_launches(2LL * chunk);
+        }
+        // a breakdown/NaN in the inner solve ends that problem's refinement
+        {
+            for (int i = 0; i < b.n_probs; i++) {
+                MfState &h = b.states_host[i];
+                if (!h.ref_done && h.status != 0 && h.status != MG_ENOCONV) {
+                    h.ref_done = 1;
+                    h.ref_status = h.status;
+                }
+                if (!h.ref_done) h.refine += 1;
+                h.done = h.ref_done ? 1 : 0;
+                h.status = (h.status == MG_ENOCONV) ? 0 : h.status;
+            }
+            // host copy of the per-problem flags goes back (counters are zero here)
+            MG_CUDA_TRY(cudaMemcpyAsync(b.states, b.states_host, b.n_probs * sizeof(MfState),
+                                        cudaMemcpyHostToDevice, s));
+        }
+        mf_refine_kernel<<<b.vec_grid, kThreads, 0, s>>>(b.chunks, b.n_chunks, b.x, b.u64, b.states);
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(1);
+        if (prm.timeout_s > 0 && wall_time() - t0 > prm.timeout_s) {
+            set_error("mixed solve exceeded %.1f s", prm.timeout_s);
+            return MG_ETIMEDOUT;
+        }
+    }
+    int rc = MG_OK;
+    for (int i = 0; i < b.n_probs; i++)
+        if (b.states_host[i].ref_status != 0) rc = b.states_host[i].ref_status;
+    return rc;
+}
+
+int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_dev_all) {
+    cudaStream_t s = b.stream;
+    if (compliance_host) {
+        mf_dot_chunks_kernel<<<b.vec_grid, kThreads, 0, s>>>(b.chunks, b.n_chunks, b.f64, b.u64, b.chunk_part);
+        MG_CUDA_TRY(cudaGetLastError());
+        std::vector<double> part(b.n_chunks);
+        MG_CUDA_TRY(cudaMemcpyAsync(part.data(), b.chunk_part, b.n_chunks * 8, cudaMemcpyDeviceToHost, s));
+        MG_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int i = 0; i < b.n_probs; i++) {
+            const MfProblem &P = b.h_probs[i];
+            double c = 0;
+            for (int k = 0; k < P.chunk_count; k++) c += part[P.chunk_begin + k];
+            compliance_host[i] = c;
+        }
+    }
+    if (dc_dev_all) {
+        int64_t max_ne = 1;
+        for (auto &P : b.h_probs) max_ne = std::max<int64_t>(max_ne, (int64_t)P.nx * P.ny * P.nz);
+        dim3 grid(std::max(1u, std::min(blocks_for(max_ne, 128), 4096u)), b.n_probs);
+        mf_sens_kernel<<<grid, 128, 0, s>>>(b.probs, b.n_probs, b.dE64, b.node_fix, b.u64, b.K0, dc_dev_all);
+        MG_CUDA_TRY(cudaGetLastError());
+    }
+    return MG_OK;
+}
+
+// ----------------------------------------------------- single-problem mixed path
+struct MatfreeWork {
+    MfBatch batch;
+    float *xs = nullptr, *ys = nullptr;
+};
+
+namespace {
+
+int matfree_setup(mg_problem *p) {
+    if (p->mf) return MG_OK;
+    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8 || p->grid_nx <= 0 || p->grid_ny <= 0 ||
+        p->grid_nz <= 0 || (int64_t)p->grid_nx * p->grid_ny * p->grid_nz != p->n_elems) {
+        set_error("the mixed form needs the structured HEX8 grid (grid dims)");
+        return MG_ENOTSUP;
+    }
+    const int nx = p->grid_nx, ny = p->grid_ny, nz = p->grid_nz;
+    // the grid must be uniform: coords(i,j,k) = (i hx, j hy, k hz) + origin
+    const double *c = p->h_coords.data();
+    const int64_t NX = nx + 1, NY = ny + 1;
+    const double hx = c[3] - c[0], hy = c[NX * 3 + 1] - c[1], hz = c[NX * NY * 3 + 2] - c[2];
+    for (int64_t n = 0; n < p->n_nodes; n++) {
+        const int64_t i = n % NX, j = (n / NX) % NY, k = n / (NX * NY);
+        if (fabs(c[n * 3] - (c[0] + i * hx)) > 1e-9 * (1 + fabs(hx) * nx) ||
+            fabs(c[n * 3 + 1] - (c[1] + j * hy)) > 1e-9 * (1 + fabs(hy) * ny) ||
+            fabs(c[n * 3 + 2] - (c[2] + k * hz)) > 1e-9 * (1 + fabs(hz) * nz)) {
+            set_error("mesh is not a uniform structured grid");
+            return MG_ENOTSUP;
+        }
+    }
+    for (int64_t e = 0; e < p->n_elems; e++) {
+        const int64_t i = e % nx, j = (e / nx) % ny, k = e / ((int64_t)nx * ny);
+        if (p->h_conn[e * 8] != (int32_t)(i + NX * (j + NY * k))) {
+            set_error("connectivity is not the libMesh grid numbering");
+            return MG_ENOTSUP;
+        }
+    }
+    MatfreeWork *w = new MatfreeWork();
+    MfProblem P{};
+    P.nx = nx; P.ny = ny; P.nz = nz;
+    P.elem_off = -1;
+    int rc = mf_batch_init(w->batch, {P}, hx, hy, hz, p->mat.nu, p->stream);
+    if (rc == MG_OK) {
+        std::vector<uint8_t> nf(p->n_nodes, 0);
+        for (int64_t n = 0; n < p->n_nodes; n++)
+            for (int cc = 0; cc < 3; cc++)
+                if (p->h_fixed[n * 3 + cc]) nf[n] |= (uint8_t)(1u << cc);
+        rc = mf_batch_set_problem(w->batch, 0, nf.data(), p->h_F.data(), nullptr, nullptr);
+    }
+    if (rc != MG_OK) {
+        mf_batch_free(w->batch);
+        delete w;
+        return rc;
+    }
+    p->mf = w;
+    return MG_OK;
+}
+
+}  // namespace
+
+int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
+    MG_TRY(matfree_setup(p));
+    MfBatch &b = p->mf->batch;
+    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
+    count_launches(1);
+    MG_CUDA_TRY(cudaMemcpyAsync(b.u64, p->d_X, p->n_dofs * 8, cudaMemcpyDeviceToDevice, p->stream));
+    MfSolveParams prm;
+    prm.precision = o.precision;
+    prm.rtol = o.rtol;
+    prm.inner_rtol = o.inner_rtol > 0 ? o.inner_rtol : 1e-4;
+    prm.max_iterations = o.max_iterations;
+    prm.max_refinements = o.max_refinements;
+    prm.graph_chunk = o.graph_chunk;
+    prm.timeout_s = o.timeout_s;
+    int rc = mf_batch_solve(b, prm, true);
+    MG_CUDA_TRY(cudaMemcpyAsync(p->d_X, b.u64, p->n_dofs * 8, cudaMemcpyDeviceToDevice, p->stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    const MfState &h = b.states_host[0];
+    if (rep) {
+        rep->newton_iterations = 1;
+        rep->krylov_iterations = h.total_iter;
+        rep->refinements = h.refine;
+        rep->relres = sqrt(h.rr64 / h.ff64);
+        rep->residual_norm = sqrt(h.rr64);
+    }
+    return rc;
+}
+
+int matfree_apply_debug(mg_problem *p, int precision, const double *x_host, double *y_host) {
+    MG_TRY(matfree_setup(p));
+    MfBatch &b = p->mf->batch;
+    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
+    MatfreeWork *w = p->mf;
+    if (!w->xs) {
+        MG_TRY(dev_alloc_n(&w->xs, (size_t)p->n_dofs));
+        MG_TRY(dev_alloc_n(&w->ys, (size_t)p->n_dofs));
+    }
+    std::vector<float> hx(p->n_dofs);
+    for (int64_t i = 0; i < p->n_dofs; i++) hx[i] = (float)x_host[i];
+    MG_CUDA_TRY(cudaMemcpyAsync(w->xs, hx.data(), p->n_dofs * 4, cudaMemcpyHostToDevice, p->stream));
+    MG_TRY(mf_apply(b, precision, w->xs, w->ys));
+    MG_CUDA_TRY(cudaMemcpyAsync(hx.data(), w->ys, p->n_dofs * 4, cudaMemcpyDeviceToHost, p->stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    for (int64_t i = 0; i < p->n_dofs; i++) y_host[i] = hx[i];
+    return MG_OK;
+}
+
+// dC/drho from the resident solution with the shared K0 (FP64)
+int matfree_sensitivity(mg_problem *p, double *dc_host) {
+    MG_TRY(matfree_setup(p));
+    MfBatch &b = p->mf->batch;
+    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.u64, p->d_X, p->n_dofs * 8, cudaMemcpyDeviceToDevice, p->stream));
+    MG_TRY(mf_batch_compliance(b, nullptr, p->d_elem_out));
+    MG_CUDA_TRY(cudaMemcpyAsync(dc_host, p->d_elem_out, p->n_elems * 8, cudaMemcpyDeviceToHost, p->stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return MG_OK;
+}
+
+int matfree_compliance_resident(mg_problem *p, double *compliance) {
+    MG_TRY(matfree_setup(p));
+    MfBatch &b = p->mf->batch;
+    double c = 0.0;
+    MG_TRY(mf_batch_compliance(b, &c, p->d_elem_out));
+    count_launches(2);
+    if (compliance) *compliance = c;
+    return MG_OK;
+}
+
+int matfree_launch_apply(mg_problem *p, int precision, int reps) {
+    MG_TRY(matfree_setup(p));
+    MfBatch &b = p->mf->batch;
+    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
+    MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
+    // nonzero search direction so that every timed launch does the full work
+    fill_f32_kernel<<<blocks_for(b.n_dofs, 256), 256, 0, b.stream>>>(b.z, 1.0f, b.n_dofs);
+    for (int i = 0; i < reps; i++) {
+        float *pold = (i & 1) ? b.p1 : b.p0, *pnew = (i & 1) ? b.p0 : b.p1;
+        if (precision == MG_MIXED_TF32)
+            launch_apply<MG_MIXED_TF32, 1>(b, nullptr, b.z, pold, pnew, b.q);
+        else
+            launch_apply<MG_MIXED_BF16, 1>(b, nullptr, b.z, pold, pnew, b.q);
+    }
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(reps);
+    return MG_OK;
+}
+
+void matfree_free(mg_problem *p) {
+    if (!p->mf) return;
+    dev_free(p->mf->xs);
+    dev_free(p->mf->ys);
+    mf_batch_free(p->mf->batch);
+    delete p->mf;
+    p->mf = nullptr;
+}
 
 }  // namespace mg

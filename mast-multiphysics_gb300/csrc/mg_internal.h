@@ -110,6 +110,7 @@ struct mg_problem {
     int64_t *d_fix_diag = nullptr;    // CSR diagonal positions of fixed rows
     int64_t n_fix_zero = 0, n_fix_diag = 0;
     bool jacobian_valid = false;
+    bool last_solve_mixed = false;
 
     // state vectors
     double *d_X = nullptr, *d_R = nullptr, *d_tmp = nullptr, *d_tmp2 = nullptr;
@@ -147,8 +148,16 @@ void free_csr(CsrMatrix *A);
 
 // ---- matfree.cu ----
 int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep);
+int matfree_apply_debug(mg_problem *p, int precision, const double *x_host, double *y_host);
+int matfree_sensitivity(mg_problem *p, double *dc_host);
+int matfree_compliance_resident(mg_problem *p, double *compliance);
+int matfree_launch_apply(mg_problem *p, int precision, int reps);
+int krylov_launch_spmv_cg(mg_problem *p, int reps);
 void matfree_free(mg_problem *p);
 
 double wall_time();
+
+// number of kernel launches issued by this library (graph nodes included)
+void count_launches(long long n);
 
 }  // namespace mg

@@ -162,6 +162,12 @@ def lib(autobuild=True):
     L.mg_sensitivity_assemble.argtypes = [_vp, _vp, _i32, _i64, _vp]
     L.mg_compliance.argtypes = [_vp, _vp, _vp, _vp]
     L.mg_mean_temperature.argtypes = [_vp, _vp, ctypes.POINTER(SolveOpts), _vp, _vp, _vp]
+    L.mg_debug_matfree_apply.argtypes = [_vp, ctypes.c_int, _vp, _vp]
+    L.mg_compliance_resident.argtypes = [_vp, _vp]
+    L.mg_sensitivities_device.argtypes = [_vp]
+    L.mg_sensitivities_device.restype = _vp
+    L.mg_launch_count.restype = ctypes.c_longlong
+    L.mg_debug_launch_apply.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
     L.mg_debug_fail_alloc_after.argtypes = [ctypes.c_int]
     L.mg_debug_fail_alloc_after.restype = None
     _lib = L
@@ -334,6 +340,14 @@ class Problem:
         rep = SolveReport()
         rc = lib().mg_solve(self.h, ctypes.byref(opts), None, ctypes.byref(rep))
         return rc, rep
+
+    def matfree_apply(self, x, precision=MIXED_TF32):
+        """One application of the mixed-precision operator (x zero on Dirichlet dofs)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.n_dofs)
+        check(lib().mg_debug_matfree_apply(self.h, precision, _p(x), _p(y)),
+              "mg_debug_matfree_apply")
+        return y
 
     def solution(self):
         X = np.zeros(self.n_dofs)

@@ -1,0 +1,66 @@
+"""Mixed-precision matrix-free SIMP form (tcgen05 TF32 / BF16 operator, FP32
+inner CG, FP64 refinement) against the FP64 oracle.
+
+Accuracy bar: FP64 outer residual ||f - K u|| / ||f|| <= 1e-8 and at most 1e-6
+relative error in compliance and sensitivities against the FP64 oracle.
+Operator check: one application against the FP64 CSR product, relative error
+below the input rounding of the format (TF32 2^-11, BF16 2^-8) times a small
+factor.
+"""
+import numpy as np
+import pytest
+
+import mastgpu as M
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_OP = {M.MIXED_TF32: 4e-3, M.MIXED_BF16: 3e-2}
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+@pytest.mark.parametrize("prec", [M.MIXED_TF32, M.MIXED_BF16])
+@pytest.mark.parametrize("shape", [(8, 4, 4), (16, 8, 8), (12, 7, 5)])
+def test_operator_matches_fp64_csr(prec, shape):
+    nx, ny, nz = shape
+    rng = np.random.default_rng(1)
+    rho = rng.uniform(0.01, 1.0, nx * ny * nz)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        x = rng.standard_normal(p.n_dofs)
+        fixed = O.simp_fixed_mask(O.simp_desc(nx, ny, nz))
+        x[fixed == 1] = 0.0
+        p.residual_and_jacobian(np.zeros(p.n_dofs), want_R=False)
+        y_ref = p.spmv(x)
+        y = p.matfree_apply(x, prec)
+    y_ref[fixed == 1] = 0.0
+    assert rel(y, y_ref) < TOL_OP[prec]
+
+
+@pytest.mark.parametrize("prec", [M.MIXED_TF32, M.MIXED_BF16])
+def test_mixed_solve_matches_oracle(prec):
+    nx, ny, nz = 16, 8, 8
+    rho = np.random.default_rng(3).uniform(0.01, 1.0, nx * ny * nz)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        u, rep = p.solve(M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3))
+        c, dc = p.compliance()
+    assert rep.status == 0 and rep.relres <= 1e-8, (rep.status, rep.relres)
+    _, dc_ref, r = O.simp_solve(O.simp_desc(nx, ny, nz, rtol=1e-12, maxit=10 ** 6), rho)
+    assert abs(c - r.compliance) / r.compliance < 1e-6
+    assert np.abs(dc - dc_ref).max() / np.abs(dc_ref).max() < 1e-6
+
+
+def test_mixed_solve_is_deterministic():
+    nx, ny, nz = 16, 8, 8
+    rho = np.random.default_rng(4).uniform(0.01, 1.0, nx * ny * nz)
+    outs = []
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        for _ in range(2):
+            u, rep = p.solve(M.default_opts(precision=M.MIXED_TF32, rtol=1e-8))
+            outs.append((u, rep.krylov_iterations))
+    assert np.array_equal(outs[0][0], outs[1][0]) and outs[0][1] == outs[1][1]
