@@ -196,6 +196,28 @@ long long mg_launch_count(void);
    (MG_PLAIN_FP64) or the tensor-core brick operator (MG_MIXED_*). */
 int mg_debug_launch_apply(mg_problem *p, int precision, int reps);
 
+/* ---- allocation-free solve ---- */
+/* No counterpart in the reference (MAST hands its linear systems to PETSc).
+   Jacobi-preconditioned CG on a caller-owned CSR (n rows, int32 rowptr/cols,
+   FP64 values, all device pointers) with right-hand side b and initial guess /
+   solution x (device pointers), to ||b - A x|| <= rtol ||b||, enqueued on
+   `stream` (a cudaStream_t; NULL = default stream).  It is for callers that
+   cannot call cudaMalloc: code that must not allocate after start-up (a
+   request loop running inside a fixed device-memory budget) and host
+   applications whose own pool owns all device memory.  The library allocates
+   nothing here: its scratch is one static device array of about 6.3 MB that
+   every GPU loading the library holds until exit, which limits n to
+   MG_STATIC_PCG_MAX_N (larger n returns MG_EINVAL).  The first call on a
+   device looks the array's address up (cudaGetSymbolAddress); make that first
+   call before any stream capture.  All calls share the array, so calls that
+   overlap on the GPU race; serialise them.  Returns MG_OK, MG_ENOCONV,
+   MG_EBREAKDOWN or MG_ENAN; *iterations and *relres (nullable) report the
+   iteration count and final relative residual. */
+#define MG_STATIC_PCG_MAX_N 131072
+int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t *cols, const double *vals,
+                      const double *b, double *x, double rtol, int32_t max_iterations,
+                      void *stream, int32_t *iterations, double *relres);
+
 /* parameter kinds for mg_sensitivity_assemble */
 #define MG_PARAM_DENSITY 0      /* rho_e of element param_index (elasticity) */
 #define MG_PARAM_K0 1           /* conductivity k0 (heat) */

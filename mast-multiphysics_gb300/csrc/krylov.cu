@@ -17,6 +17,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "mg_internal.h"
 
@@ -626,3 +627,113 @@ int krylov_solve(mg_problem *p, const CsrMatrix &A, const double *d_b, double *d
 }
 
 }  // namespace mg
+
+// ---------------------------------------------------------------------------
+// Allocation-free Jacobi-PCG on a caller-owned CSR (mg_pcg_csr_static).
+//
+// The solver scratch (r, z, two search directions, A p, the Jacobi inverse,
+// the per-block partial sums and the solver state) lives in the file-scope
+// device array below instead of memory from cudaMalloc.  Every GPU that loads
+// this library holds the array (about 6.3 MB) until the process exits.  All
+// calls on a device share it and it keeps the last call's contents, so each
+// call re-initialises what must start at zero; calls that overlap on the GPU
+// (different streams or threads) race on it.
+// ---------------------------------------------------------------------------
+namespace mg {
+namespace {
+
+constexpr int64_t kStaticMaxN = MG_STATIC_PCG_MAX_N;
+constexpr int64_t kStaticParts = 3 * 152 * 16;  // 3 x the largest grid of the kernels
+constexpr int64_t kStaticStateDoubles = 32;     // >= sizeof(KrylovState) / 8
+static_assert(sizeof(KrylovState) <= kStaticStateDoubles * sizeof(double), "state slot");
+
+static __device__ __align__(256) double g_static_pcg_scratch[6 * kStaticMaxN + kStaticParts +
+                                                            kStaticStateDoubles];
+
+std::mutex g_static_mutex;
+double *g_static_ptr[128] = {nullptr};
+
+// device address of the static array for the current device (looked up once)
+int static_scratch(double **out) {
+    int dev = 0;
+    MG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) {
+        set_error("device ordinal %d out of range", dev);
+        return MG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_ptr[dev]) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_pcg_scratch);
+        if (e != cudaSuccess || !ptr) {
+            set_error("cudaGetSymbolAddress(static PCG scratch): %s", cudaGetErrorString(e));
+            return MG_ECUDA;
+        }
+        g_static_ptr[dev] = static_cast<double *>(ptr);
+    }
+    *out = g_static_ptr[dev];
+    return MG_OK;
+}
+
+}  // namespace
+}  // namespace mg
+
+extern "C" int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t *cols,
+                                 const double *vals, const double *b, double *x, double rtol,
+                                 int32_t max_iterations, void *stream, int32_t *iterations,
+                                 double *relres) {
+    using namespace mg;
+    if (n <= 0 || !rowptr || !cols || !vals || !b || !x || !(rtol > 0.0)) {
+        set_error("mg_pcg_csr_static: invalid argument");
+        return MG_EINVAL;
+    }
+    if (n > kStaticMaxN) {
+        set_error("mg_pcg_csr_static: n = %lld exceeds the static scratch limit of %lld dofs "
+                  "(MG_STATIC_PCG_MAX_N)", (long long)n, (long long)kStaticMaxN);
+        return MG_EINVAL;
+    }
+    double *base = nullptr;
+    MG_TRY(static_scratch(&base));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double *r = base, *z = base + kStaticMaxN, *p0 = base + 2 * kStaticMaxN,
+           *p1 = base + 3 * kStaticMaxN, *q = base + 4 * kStaticMaxN,
+           *dinv = base + 5 * kStaticMaxN, *partials = base + 6 * kStaticMaxN;
+    KrylovState *state = reinterpret_cast<KrylovState *>(base + 6 * kStaticMaxN + kStaticParts);
+    CsrMatrix A;
+    A.n = n;
+    A.nnz = 0;
+    A.dpn = 1;  // general CSR: one row per group of lanes
+    A.rowptr = const_cast<int32_t *>(rowptr);
+    A.cols = const_cast<int32_t *>(cols);
+    A.vals = const_cast<double *>(vals);
+    const int sg = spmv_grid(A), vg = vec_grid(n);
+    const int nparts = std::max(sg, vg);
+    jacobi_kernel<<<blocks_for(n, 256), 256, 0, s>>>(rowptr, cols, vals, n, dinv);
+    KrylovState init{};
+    init.tol2 = rtol * rtol;
+    init.maxit = max_iterations > 0 ? max_iterations : 100000;
+    MG_CUDA_TRY(cudaMemcpyAsync(state, &init, sizeof(KrylovState), cudaMemcpyHostToDevice, s));
+    launch_spmv<0>(A, s, sg, x, nullptr, nullptr, nullptr, q, nullptr, nullptr, nullptr, 0);
+    krylov_init_kernel<<<vg, kBS, 0, s>>>(n, b, q, r, z, p0, nullptr, nullptr, dinv, state,
+                                         partials, nparts);
+    MG_CUDA_TRY(cudaMemsetAsync(p1, 0, n * sizeof(double), s));
+    MG_CUDA_TRY(cudaGetLastError());
+    KrylovState h{};
+    for (;;) {
+        MG_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(KrylovState), cudaMemcpyDeviceToHost, s));
+        MG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (h.done) break;
+        for (int it = 0; it < 16; it++) {
+            double *pold = (it & 1) ? p1 : p0, *pnew = (it & 1) ? p0 : p1;
+            launch_spmv<1>(A, s, sg, nullptr, z, pold, pnew, q, nullptr, state, partials, nparts);
+            cg_update_kernel<<<vg, kBS, 0, s>>>(n, x, r, z, pnew, q, dinv, state, partials,
+                                                nparts);
+        }
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(32);
+    }
+    if (iterations) *iterations = h.iter;
+    if (relres) *relres = h.bb > 0 ? sqrt(h.rr / h.bb) : sqrt(h.rr);
+    return h.status;
+}
+
