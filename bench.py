@@ -7,8 +7,10 @@ over the 65 nodes of the x = max, z = 0 edge.  One step = one design
 evaluation: solve to 1e-8 relative FP64 residual ||f - K u|| / ||f||, then the
 compliance f.u and dC/drho for all elements.
 
-value  -- solves/s of the mixed-precision form (tcgen05 TF32 matrix-free operator,
-          FP32 CG, FP64 refinement), inputs resident in HBM, L2 flushed between steps.
+value  -- solves/s of the mixed-precision form (tcgen05 split-TF32 matrix-free
+          operator, FP32 CG preconditioned by a geometric multigrid V-cycle whose
+          smoothers use the same tensor-core operator, FP64 refinement), inputs
+          resident in HBM, L2 flushed between steps.
 e2e    -- the same through the C ABI with host buffers: densities and initial
           guess copied in, solution and sensitivities copied out, every step.
 plain_fp64 -- the FP64 CSR Jacobi-PCG form on the same GPU (the 5x target's base).
@@ -44,7 +46,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="tf32", choices=["tf32", "bf16", "bf16x3", "tf32x3"])
+    ap.add_argument("--precision", default="tf32x3", choices=["tf32", "bf16", "bf16x3", "tf32x3"])
+    ap.add_argument("--preconditioner", default="multigrid", choices=["multigrid", "jacobi"])
     ap.add_argument("--cpu-iters", type=int, default=40, help="PCG iterations in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -181,14 +184,16 @@ def main():
         torch.cuda.set_device(0)
     dev = torch.device("cuda", torch.cuda.current_device())
     prec = {"tf32": M.MIXED_TF32, "bf16": M.MIXED_BF16,
-            "bf16x3": getattr(M, "MIXED_BF16X3", M.MIXED_BF16),
-            "tf32x3": getattr(M, "MIXED_TF32X3", M.MIXED_TF32)}[args.precision]
+            "bf16x3": M.MIXED_BF16X3,
+            "tf32x3": M.MIXED_TF32X3}[args.precision]
     rho = np.random.default_rng(SEED).uniform(0.01, 1.0, NX * NY * NZ)
     prob = M.simp_cantilever(NX, NY, NZ)
     stream = torch.cuda.ExternalStream(prob.stream)
     d_rho = torch.from_numpy(rho).to(dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 512 MB > L2
-    opts = M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0)
+    pc = M.PC_MULTIGRID if args.preconditioner == "multigrid" else M.PC_JACOBI
+    opts = M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0,
+                          preconditioner=pc)
 
     def step_resident():
         prob.set_design_device(d_rho.data_ptr())
@@ -322,6 +327,7 @@ def main():
                 "data": "synthetic (seeded U[0.01,1] densities, default_rng(0))",
                 "config": {"workload": WORKLOAD, "n_dofs": n, "n_elems": n_el, "rtol": 1e-8,
                            "precision": args.precision, "inner_rtol": 1e-3,
+                           "preconditioner": args.preconditioner,
                            "l2": "flushed between steps (512 MB write)",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "dof_per_s": value * n,

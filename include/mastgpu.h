@@ -75,7 +75,10 @@ typedef enum mg_physics {
 typedef enum mg_precision {
     MG_PLAIN_FP64 = 0,  /* FP64 element quadrature, CSR, Krylov */
     MG_MIXED_TF32 = 1,  /* matrix-free tcgen05 TF32 operator, FP32 CG, FP64 refinement */
-    MG_MIXED_BF16 = 2   /* as above with BF16 operands (FP32 accumulation) */
+    MG_MIXED_BF16 = 2,  /* as above with BF16 operands (FP32 accumulation) */
+    MG_MIXED_TF32X3 = 3, /* split TF32: (u_hi + u_lo)(K_hi + K_lo) minus the lo*lo term,
+                            three TF32 products per element, FP32 accumulation */
+    MG_MIXED_BF16X3 = 4  /* split BF16, three BF16 products, FP32 accumulation */
 } mg_precision;
 
 typedef enum mg_krylov { MG_KRYLOV_CG = 0, MG_KRYLOV_BICGSTAB = 1 } mg_krylov;
@@ -126,7 +129,15 @@ typedef struct mg_solve_opts {
     double timeout_s;        /* host wall-clock limit for the solve (0 = none) */
     int32_t warm_start;      /* 1: start from the resident solution */
     int32_t graph_chunk;     /* Krylov iterations per captured CUDA graph (0 = default) */
+    int32_t preconditioner;  /* mixed form: MG_PC_MULTIGRID (default) or MG_PC_JACOBI;
+                                the plain form is Jacobi-preconditioned */
+    int32_t smooth_degree;   /* multigrid: Chebyshev degree of the smoothers (0 = 2) */
+    int32_t coarse_degree;   /* multigrid: Chebyshev degree on the coarsest grid (0 = 8) */
+    int32_t reserved;
 } mg_solve_opts;
+
+#define MG_PC_JACOBI 0
+#define MG_PC_MULTIGRID 1
 
 typedef struct mg_solve_report {
     int32_t status;

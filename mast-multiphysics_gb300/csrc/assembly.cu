@@ -472,8 +472,19 @@ __global__ void simp_modulus_kernel(const double *__restrict__ rho, int64_t n, d
     if (e >= n) return;
     double r = rho ? rho[e] : 1.0;
     if (!(r >= 0.0 && r <= 1.0)) atomicOr(status, 4);  // NaN or out of range
-    E[e] = E0 * (rmin + (1.0 - rmin) * pow(r, penal));
-    dE[e] = E0 * (1.0 - rmin) * penal * pow(r, penal - 1.0);
+    double rp, rp1;
+    const int ip = (int)penal;
+    if ((double)ip == penal && ip >= 1 && ip <= 8) {
+        // integer penalty: repeated products (FP64 pow is slow on this part)
+        rp1 = 1.0;
+        for (int k = 1; k < ip; k++) rp1 *= r;
+        rp = rp1 * r;
+    } else {
+        rp = pow(r, penal);
+        rp1 = pow(r, penal - 1.0);
+    }
+    E[e] = E0 * (rmin + (1.0 - rmin) * rp);
+    dE[e] = E0 * (1.0 - rmin) * penal * rp1;
 }
 
 // residual fix-up: constrained rows R_d = X_d, point loads enter as -F

@@ -516,7 +516,10 @@ void mg_default_solve_opts(mg_solve_opts *o) {
     o->inner_rtol = 1e-4;
     o->timeout_s = 0.0;
     o->warm_start = 0;
-    o->graph_chunk = 16;
+    o->graph_chunk = 0;
+    o->preconditioner = MG_PC_MULTIGRID;
+    o->smooth_degree = 2;
+    o->coarse_degree = 8;
 }
 
 int mg_problem_create(const mg_mesh_desc *mesh, const mg_material_desc *mat, const mg_bc_desc *bc,
@@ -775,7 +778,7 @@ int mg_debug_launch_apply(mg_problem *p, int precision, int reps) {
 // host FP64 buffers); Dirichlet entries of x must be zero.
 int mg_debug_matfree_apply(mg_problem *p, int precision, const double *x, double *y) {
     if (!p || !x || !y) return MG_EINVAL;
-    if (precision != MG_MIXED_TF32 && precision != MG_MIXED_BF16) return MG_EINVAL;
+    if (precision < MG_MIXED_TF32 || precision > MG_MIXED_BF16X3) return MG_EINVAL;
     return matfree_apply_debug(p, precision, x, y);
 }
 

@@ -26,6 +26,9 @@ namespace mg {
 namespace {
 
 constexpr int kBS = 256;
+// lanes per node in the SpMV: few lanes keep the FP64 work near one FMA per
+// stored value (GB300's FP64 rate is the binding limit next to HBM)
+constexpr int kSpmvLanes = 4;
 
 template <int NV>
 __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *partials, int stride) {
@@ -88,9 +91,8 @@ __device__ __forceinline__ bool bad(double x) { return !isfinite(x); }
 
 // ---------------------------------------------------------------------------
 // SpMV kernels (G lanes per node, DPN rows per node)
-// MODE 0: y = A x;  partial0 = y.x
-// MODE 1: CG: xg = z + beta p_old on the fly, p_new (own rows) = same, q = A xg,
-//         partial0 = p_new.q, last block: alpha = rz / pq
+// MODE 0: y = A x
+// MODE 1: CG: q = A p (x = p), partial0 = p.q, last block: alpha = rz / pq
 // MODE 2: BiCGStab v = A y, partial0 = rh.v, last block alpha = rho / (rh.v)
 // MODE 3: BiCGStab t = A z, partial0 = t.s, partial1 = t.t, last: omega
 // ---------------------------------------------------------------------------
@@ -102,7 +104,6 @@ __global__ void __launch_bounds__(kBS) spmv_kernel(
     double *__restrict__ y, const double *__restrict__ aux, KrylovState *st,
     double *__restrict__ partials, int nparts) {
     if (MODE != 0 && st->done) return;
-    const double beta = (MODE == 1) ? st->beta : 0.0;
     const int sub = threadIdx.x % G;
     constexpr int kGroupsPerWarp = 32 / G;
     const int64_t warp = ((int64_t)blockIdx.x * kBS + threadIdx.x) >> 5;
@@ -123,11 +124,7 @@ __global__ void __launch_bounds__(kBS) spmv_kernel(
         for (int d = 0; d < DPN; d++) acc[d] = 0.0;
         for (int32_t k = sub; k < len; k += G) {
             const int32_t c = __ldg(cols + rp[0] + k);
-            double xc;
-            if (MODE == 1)
-                xc = fma(beta, p_old[c], z[c]);
-            else
-                xc = x[c];
+            const double xc = x[c];
 #pragma unroll
             for (int d = 0; d < DPN; d++) acc[d] = fma(__ldg(vals + rp[d] + k), xc, acc[d]);
         }
@@ -145,9 +142,7 @@ __global__ void __launch_bounds__(kBS) spmv_kernel(
             if (MODE == 0) {
                 d0 = fma(mine, x[row], d0);
             } else if (MODE == 1) {
-                const double pn = fma(beta, p_old[row], z[row]);
-                p_new[row] = pn;
-                d0 = fma(pn, mine, d0);
+                d0 = fma(x[row], mine, d0);  // p.q
             } else if (MODE == 2) {
                 d0 = fma(aux[row], mine, d0);  // aux = r-hat
             } else {
@@ -181,6 +176,18 @@ __global__ void __launch_bounds__(kBS) spmv_kernel(
             else st->omega = (tot[1] > 0.0) ? tot[0] / tot[1] : 0.0;
         }
     }
+}
+
+// CG search direction p = z + beta p (its own launch: the SpMV that follows
+// reads p at neighbouring rows)
+__global__ void __launch_bounds__(kBS) cg_pupdate_kernel(int64_t n, const double *__restrict__ z,
+                                                        double *__restrict__ p,
+                                                        const KrylovState *st) {
+    if (st->done) return;
+    const double beta = st->beta;
+    for (int64_t i = (int64_t)blockIdx.x * kBS + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * kBS)
+        p[i] = fma(beta, p[i], z[i]);
 }
 
 // CG vector phase: x += alpha p; r -= alpha q; z = D^-1 r; rz, rr -> beta, stop test
@@ -413,19 +420,19 @@ void launch_spmv(const CsrMatrix &A, cudaStream_t s, int grid, const double *x, 
                  KrylovState *st, double *partials, int nparts) {
     const int64_t nodes = A.n / A.dpn;
     if (A.dpn == 3)
-        spmv_kernel<3, 32, MODE><<<grid, kBS, 0, s>>>(A.rowptr, A.cols, A.vals, nodes, x, z, p_old,
-                                                      p_new, y, aux, st, partials, nparts);
+        spmv_kernel<3, kSpmvLanes, MODE><<<grid, kBS, 0, s>>>(A.rowptr, A.cols, A.vals, nodes, x, z,
+                                                              p_old, p_new, y, aux, st, partials, nparts);
     else if (A.dpn == 2)
-        spmv_kernel<2, 16, MODE><<<grid, kBS, 0, s>>>(A.rowptr, A.cols, A.vals, nodes, x, z, p_old,
-                                                      p_new, y, aux, st, partials, nparts);
+        spmv_kernel<2, kSpmvLanes, MODE><<<grid, kBS, 0, s>>>(A.rowptr, A.cols, A.vals, nodes, x, z,
+                                                              p_old, p_new, y, aux, st, partials, nparts);
     else
-        spmv_kernel<1, 8, MODE><<<grid, kBS, 0, s>>>(A.rowptr, A.cols, A.vals, nodes, x, z, p_old,
-                                                     p_new, y, aux, st, partials, nparts);
+        spmv_kernel<1, kSpmvLanes, MODE><<<grid, kBS, 0, s>>>(A.rowptr, A.cols, A.vals, nodes, x, z,
+                                                              p_old, p_new, y, aux, st, partials, nparts);
 }
 
 int spmv_grid(const CsrMatrix &A) {
     const int64_t nodes = A.n / A.dpn;
-    const int G = A.dpn == 3 ? 32 : (A.dpn == 2 ? 16 : 8);
+    const int G = kSpmvLanes;
     int64_t need = (nodes * G + kBS - 1) / kBS;
     return (int)std::max<int64_t>(1, std::min<int64_t>(need, 152 * 16));
 }
@@ -514,7 +521,7 @@ int transpose_csr(mg_problem *p, const CsrMatrix &A, CsrMatrix *At) {
     return MG_OK;
 }
 
-// enqueue `reps` fused CG SpMV launches (timing hook; state reset, no sync)
+// enqueue `reps` CG SpMV launches q = A p (timing hook; state reset, no sync)
 int krylov_launch_spmv_cg(mg_problem *p, int reps) {
     if (!p->jacobian_valid) MG_TRY(assemble_system(p, p->d_X, nullptr, true, false));
     KrylovWork &w = p->kw;
@@ -524,11 +531,9 @@ int krylov_launch_spmv_cg(mg_problem *p, int reps) {
     // nonzero search direction so that every timed launch does the full work
     fill_f64_kernel<<<blocks_for(p->n_dofs, 256), 256, 0, p->stream>>>(w.z, 1.0, p->n_dofs);
     const int sg = spmv_grid(p->A);
-    for (int i = 0; i < reps; i++) {
-        double *pold = (i & 1) ? w.p1 : w.p0, *pnew = (i & 1) ? w.p0 : w.p1;
-        launch_spmv<1>(p->A, p->stream, sg, nullptr, w.z, pold, pnew, w.q, nullptr, w.state,
+    for (int i = 0; i < reps; i++)
+        launch_spmv<1>(p->A, p->stream, sg, w.z, nullptr, nullptr, nullptr, w.q, nullptr, w.state,
                        w.partials, w.grid);
-    }
     MG_CUDA_TRY(cudaGetLastError());
     count_launches(reps);
     return MG_OK;
@@ -561,21 +566,17 @@ int krylov_solve(mg_problem *p, const CsrMatrix &A, const double *d_b, double *d
                                          w.partials, nparts);
     MG_CUDA_TRY(cudaGetLastError());
     count_launches(3);
-    if (krylov == MG_KRYLOV_CG) {
-        // p0 = 0 and beta = 0, so the first fused SpMV forms p = z
-        MG_CUDA_TRY(cudaMemsetAsync(w.p1, 0, n * sizeof(double), s));
-    }
-    const int chunk = o.graph_chunk > 0 ? (o.graph_chunk + 1) / 2 * 2 : 16;
+    // CG: p0 = 0 and beta = 0, so the first p update forms p = z
+    const int chunk = o.graph_chunk > 0 ? o.graph_chunk : 16;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     MG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < chunk; it++) {
         if (krylov == MG_KRYLOV_CG) {
-            double *pold = (it & 1) ? w.p1 : w.p0;
-            double *pnew = (it & 1) ? w.p0 : w.p1;
-            launch_spmv<1>(A, s, sg, nullptr, w.z, pold, pnew, w.q, nullptr, w.state, w.partials,
-                           nparts);
-            cg_update_kernel<<<vg, kBS, 0, s>>>(n, d_x, w.r, w.z, pnew, w.q, w.dinv, w.state,
+            cg_pupdate_kernel<<<vg, kBS, 0, s>>>(n, w.z, w.p0, w.state);
+            launch_spmv<1>(A, s, sg, w.p0, nullptr, nullptr, nullptr, w.q, nullptr, w.state,
+                           w.partials, nparts);
+            cg_update_kernel<<<vg, kBS, 0, s>>>(n, d_x, w.r, w.z, w.p0, w.q, w.dinv, w.state,
                                                 w.partials, nparts);
         } else {
             bicg_p_kernel<<<vg, kBS, 0, s>>>(n, w.r, w.p0, w.v, w.y, w.dinv, w.state);
@@ -611,7 +612,7 @@ int krylov_solve(mg_problem *p, const CsrMatrix &A, const double *d_b, double *d
             break;
         }
         ce = cudaGraphLaunch(exec, s);
-        count_launches((long long)chunk * (krylov == MG_KRYLOV_CG ? 2 : 5));
+        count_launches((long long)chunk * (krylov == MG_KRYLOV_CG ? 3 : 5));
         if (ce != cudaSuccess) {
             set_error("graph launch: %s", cudaGetErrorString(ce));
             rc = MG_ECUDA;
@@ -696,7 +697,7 @@ extern "C" int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t
     MG_TRY(static_scratch(&base));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     double *r = base, *z = base + kStaticMaxN, *p0 = base + 2 * kStaticMaxN,
-           *p1 = base + 3 * kStaticMaxN, *q = base + 4 * kStaticMaxN,
+           *q = base + 4 * kStaticMaxN,
            *dinv = base + 5 * kStaticMaxN, *partials = base + 6 * kStaticMaxN;
     KrylovState *state = reinterpret_cast<KrylovState *>(base + 6 * kStaticMaxN + kStaticParts);
     CsrMatrix A;
@@ -716,7 +717,6 @@ extern "C" int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t
     launch_spmv<0>(A, s, sg, x, nullptr, nullptr, nullptr, q, nullptr, nullptr, nullptr, 0);
     krylov_init_kernel<<<vg, kBS, 0, s>>>(n, b, q, r, z, p0, nullptr, nullptr, dinv, state,
                                          partials, nparts);
-    MG_CUDA_TRY(cudaMemsetAsync(p1, 0, n * sizeof(double), s));
     MG_CUDA_TRY(cudaGetLastError());
     KrylovState h{};
     for (;;) {
@@ -724,13 +724,13 @@ extern "C" int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t
         MG_CUDA_TRY(cudaStreamSynchronize(s));
         if (h.done) break;
         for (int it = 0; it < 16; it++) {
-            double *pold = (it & 1) ? p1 : p0, *pnew = (it & 1) ? p0 : p1;
-            launch_spmv<1>(A, s, sg, nullptr, z, pold, pnew, q, nullptr, state, partials, nparts);
-            cg_update_kernel<<<vg, kBS, 0, s>>>(n, x, r, z, pnew, q, dinv, state, partials,
-                                                nparts);
+            cg_pupdate_kernel<<<vg, kBS, 0, s>>>(n, z, p0, state);
+            launch_spmv<1>(A, s, sg, p0, nullptr, nullptr, nullptr, q, nullptr, state, partials,
+                           nparts);
+            cg_update_kernel<<<vg, kBS, 0, s>>>(n, x, r, z, p0, q, dinv, state, partials, nparts);
         }
         MG_CUDA_TRY(cudaGetLastError());
-        count_launches(32);
+        count_launches(48);
     }
     if (iterations) *iterations = h.iter;
     if (relres) *relres = h.bb > 0 ? sqrt(h.rr / h.bb) : sqrt(h.rr);

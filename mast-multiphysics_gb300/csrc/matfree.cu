@@ -5,26 +5,34 @@
 // element shares the reference stiffness K0 of StructuralElement3D,
 // src/elasticity/solid_element_3d.cpp:135-423, scaled by the SIMP modulus of
 // examples/structural/example_6/example_6.cpp:100-137).  Dirichlet dofs are
-// eliminated (identity rows, zero columns) as in the plain form.
+// eliminated (identity rows, zero columns) as in the plain form; they are
+// marked by a zero Jacobi inverse, which keeps r, z and p zero there.
 //
-// Brick kernel (one CTA per 8x8x8 block of owned nodes, persistent grid):
-//   1. stage u over the (8+2)^3 node halo and E over the 9^3 elements that
-//      touch the owned nodes in shared memory;
-//   2. per 128-element tile, write the element displacement rows U (128 x 24,
-//      TF32 or BF16) in the canonical no-swizzle K-major UMMA layout and issue
-//      tcgen05.mma: D(128 x 32, FP32, TMEM) = U K0^T (K0 zero-padded to N = 32);
-//   3. tcgen05.ld the accumulator, scale each row by E_e (the rho^p epilogue)
-//      and park the 24 element forces in shared memory;
-//   4. every owned node sums its 8 element contributions in a fixed order:
-//      deterministic, no atomics, no colouring, one write per output dof.
+// Brick kernel (one CTA per 8x8x8 block of owned nodes, persistent grid,
+// two CTAs per SM):
+//   1. one thread issues three TMA tile loads (cp.async.bulk.tensor.3d) into
+//      shared memory: the (8+2)^3 node halo of z and of p_old, and the 9^3
+//      element moduli around the owned nodes; out-of-grid parts arrive as 0;
+//   2. per 128-element tile, all threads write the element displacement rows
+//      U = z + beta p_old (128 x 24) as TF32 or BF16 in the canonical
+//      no-swizzle K-major UMMA layout (the split variants also write the
+//      rounding remainder U_lo), and one thread issues tcgen05.mma:
+//      D(128 x 32, FP32, TMEM) = U K0^T [+ U_lo K0^T + U K0_lo^T];
+//      two A buffers and two TMEM accumulators let tile t's MMA run while
+//      tile t-1 is drained;
+//   3. tcgen05.ld drains D, each row is scaled by E_e (the rho^p epilogue) and
+//      parked in a 128-row shared buffer;
+//   4. every owned dof adds the contributions of its (up to 8) elements found
+//      in that tile, in a fixed order, into a register accumulator: no atomics,
+//      no colouring, deterministic, one global write per output dof.
 // Elements in the one-element halo are evaluated by both neighbouring bricks
-// (729 evaluations per 512 owned nodes); the tensor-core work is negligible
-// next to the gathers, so the recomputation buys determinism for free.
+// (729 evaluations per 512 owned nodes).
 //
 // Reductions are per problem and deterministic: every brick (chunk) writes a
-// partial, and the last brick (chunk) of a problem -- found with a per-problem
+// partial and the last brick (chunk) of a problem -- found with a per-problem
 // counter -- sums that problem's partials in index order.  A problem's result
 // is therefore bitwise independent of which other problems share the batch.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -40,6 +48,15 @@ namespace mg {
 namespace {
 
 constexpr int kThreads = 256;
+
+template <int P>
+struct Prec {
+    static constexpr bool kTf32 = (P == MG_MIXED_TF32 || P == MG_MIXED_TF32X3);
+    static constexpr bool kSplit = (P == MG_MIXED_TF32X3 || P == MG_MIXED_BF16X3);
+    static constexpr int kCols = kTf32 ? 6 : 4;     // 16-byte core columns per A row
+    static constexpr int kKsteps = kTf32 ? 3 : 2;   // MMAs per A/B pair (K = 8 / 16 each)
+    static constexpr uint32_t kSbo = kCols * 128;   // bytes between 8-row groups
+};
 
 // ------------------------------------------------------------------ PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -57,6 +74,10 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
+__device__ __forceinline__ float bf16_round(float x) {
+    return __bfloat162float(__float2bfloat16_rn(x));
+}
+
 // UMMA shared-memory descriptor, no swizzle, K-major canonical layout:
 // 8-row x 16-byte core matrices; LBO = byte step between core matrices along K,
 // SBO = byte step between 8-row groups; version field = 1 (sm_100 family).
@@ -70,28 +91,28 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
 }
 
 // instruction descriptor: D F32, A/B K-major, N = 32, M = 128
-template <int PREC>
+template <bool TF32>
 __host__ __device__ constexpr uint32_t umma_idesc() {
-    return (1u << 4) |                                   // D format F32
-           ((PREC == MG_MIXED_TF32 ? 2u : 1u) << 7) |    // A: TF32 (kind::tf32) / BF16 (kind::f16)
-           ((PREC == MG_MIXED_TF32 ? 2u : 1u) << 10) |   // B
-           ((32u >> 3) << 17) |                          // N >> 3
-           ((128u >> 4) << 24);                          // M >> 4
+    return (1u << 4) |                   // D format F32
+           ((TF32 ? 2u : 1u) << 7) |     // A: TF32 (kind::tf32) / BF16 (kind::f16)
+           ((TF32 ? 2u : 1u) << 10) |    // B
+           ((32u >> 3) << 17) |          // N >> 3
+           ((128u >> 4) << 24);          // M >> 4
 }
 
-template <int PREC>
+template <bool TF32>
 __device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                      uint32_t accumulate) {
-    if (PREC == MG_MIXED_TF32) {
+    if (TF32) {
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<PREC>()), "r"(accumulate));
+            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<TF32>()), "r"(accumulate));
     } else {
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<PREC>()), "r"(accumulate));
+            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<TF32>()), "r"(accumulate));
     }
 }
 
@@ -114,6 +135,11 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes)
+                 : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t phase) {
     uint32_t ok;
     asm volatile(
@@ -132,14 +158,26 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t phase)
     return false;
 }
 
-__device__ __forceinline__ void tmem_alloc32(uint32_t slot) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(slot)
+// 3D TMA tile load global -> shared, completion on an mbarrier
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            int z, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(mbar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+                 "r"(ncols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_dealloc32(uint32_t taddr) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(taddr) : "memory");
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
@@ -178,6 +216,10 @@ __host__ __device__ __forceinline__ int corner_index(int dx, int dy, int dz) {
     return dz * 4 + (dy ? (dx ? 2 : 3) : (dx ? 1 : 0));
 }
 
+__device__ __forceinline__ int64_t dof_index(const MfProblem &P, int gx, int gy, int gz, int c) {
+    return P.dof_off + ((int64_t)gz * P.NY + gy) * P.pitch + 3 * gx + c;
+}
+
 // --------------------------------------------------------------- block helpers
 __device__ __forceinline__ double block_sum(double v, double *sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -192,242 +234,352 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
     return s;  // valid in thread 0
 }
 
+// FP32 warp sums, FP64 across the block's warps; valid in thread 0
+__device__ __forceinline__ double block_sum_f(float v, double *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) sh[w] = (double)v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < kThreads / 32; i++) s += sh[i];
+    return s;
+}
+
 // fixed-order sum of part[begin .. begin+count) over the block; valid in thread 0
-__device__ __forceinline__ double ordered_sum(const double *part, int begin, int count,
-                                              double *sh) {
+__device__ __forceinline__ double ordered_sum(const double *part, int begin, int count) {
+    __shared__ double tree[kThreads];
     double s = 0.0;
     for (int i = threadIdx.x; i < count; i += kThreads) s += __ldcg(part + begin + i);
-    __shared__ double tree[kThreads];
+    __syncthreads();
     tree[threadIdx.x] = s;
     __syncthreads();
     for (int w = kThreads / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) tree[threadIdx.x] += tree[threadIdx.x + w];
         __syncthreads();
     }
-    (void)sh;
     return tree[0];
 }
 
 __device__ __forceinline__ bool is_bad(double x) { return !isfinite(x); }
 
 // ------------------------------------------------------------------ apply
-// dynamic shared memory layout (bytes)
-constexpr int kOffB = 0;                        // K0 operand (<= 3 KB)
-constexpr int kOffA = 4096;                     // U tile (<= 12 KB)
-constexpr int kOffU = kOffA + 12288;            // staged u (1000 x 3 floats)
-constexpr int kOffE = kOffU + kBU * kBU * kBU * 3 * 4;  // element moduli (729 floats)
-constexpr int kOffRes = ((kOffE + kNEL * 4) + 15) / 16 * 16;
-constexpr int kOffBar = ((kOffRes + kNEL * kResStride * 4) + 15) / 16 * 16;
-constexpr int kApplySmem = kOffBar + 64;
+// TMA boxes: nodes {32 floats, 10, 10} starting one float before the x
+// component of node gx0-1 (a 16-byte aligned start: 3(8b-1)-1 = 24b-4);
+// elements {12, 9, 9} starting at element gx0-4.
+constexpr int kBoxNX = 32;
+constexpr int kBoxNodeBytes = kBoxNX * kBU * kBU * 4;  // 12800
+constexpr int kBoxEX = 12;
+constexpr int kBoxElemBytes = kBoxEX * kBE * kBE * 4;  // 3888
+constexpr int kResStride = 25;
+constexpr int kApplyThreads = 512;
 
-// MODE 0: y = A x.   MODE 1: CG step, x_gather = z + beta p_old, p_new (owned)
-// written, q = A p_new, per-problem alpha = rz / (p.q).
+constexpr int kOffB = 0;                                   // B: hi at 0, lo at 4096
+constexpr int kOffA = 8192;                                // 2 buffers x (hi, lo) x 12 KB
+constexpr int kABytes = 12288;
+constexpr int kOffBox = kOffA + 4 * kABytes;               // 57344: 2 x (z, p, E)
+constexpr int kBoxSet = 12800 + 12800 + 3968;              // 29568 (multiple of 128)
+constexpr int kOffRes = kOffBox + 2 * kBoxSet;             // 116480
+constexpr int kOffBar = kOffRes + kNEL * kResStride * 4;   // 189380 -> aligned below
+constexpr int kOffBarA = (kOffBar + 127) / 128 * 128;
+constexpr int kApplySmem = kOffBarA + 64;
+static_assert(kOffBox % 128 == 0 && kBoxSet % 128 == 0, "TMA destinations");
+
+// offset of element-row value k (node a = k/3, component c) inside the node box,
+// relative to the element's base corner
+__device__ __forceinline__ int box_offset(int k) {
+    const int a = (k * 11) >> 5, c = k - 3 * a;  // k / 3 for k < 24
+    int dx, dy, dz;
+    corner_bits(a, dx, dy, dz);
+    return (dz * kBU + dy) * kBoxNX + 3 * dx + c;
+}
+
+// Bricks brick_lo .. brick_hi-1; the input vector is tensor map `in_slot`.
+// MODE 1: CG step, gathered u = z + beta p_old (z = in_slot, p_old = map 1 +
+//         parity), p_new (owned) = u, q = A u, per-problem alpha = rz / (p.q).
+// MODE 2: y = rhs - A x.   MODE 3: y = A x.   (Both 0 on Dirichlet dofs.)
 template <int PREC, int MODE>
-__global__ void __launch_bounds__(kThreads, 2) mf_apply_kernel(
-    const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int n_bricks,
-    const float *__restrict__ E32, const uint8_t *__restrict__ node_fix,
-    const float *__restrict__ xin, const float *__restrict__ z, const float *__restrict__ p_old,
-    float *__restrict__ p_new, float *__restrict__ y, MfState *states,
-    double *__restrict__ brick_part, const uint32_t *__restrict__ Bop, int *err) {
+__global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
+    const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int brick_lo,
+    int brick_hi, const CUtensorMap *__restrict__ tmaps, int in_slot, int parity,
+    const uint32_t *__restrict__ Bop, const float *__restrict__ dinv,
+    const float *__restrict__ rhs, float *__restrict__ p0, float *__restrict__ p1,
+    float *__restrict__ y, MfState *states, double *__restrict__ brick_part, int *err) {
+    const int n_bricks = brick_hi;
+    using PR = Prec<PREC>;
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ double red_sh[kThreads / 32];
+    __shared__ double red_sh[kApplyThreads / 32];
+    __shared__ double tree[kApplyThreads];
     __shared__ int sh_last;
-    uint32_t *sB = reinterpret_cast<uint32_t *>(smem + kOffB);
-    uint8_t *sA = smem + kOffA;
-    float *su = reinterpret_cast<float *>(smem + kOffU);
-    float *sE = reinterpret_cast<float *>(smem + kOffE);
+    uint8_t *sB = smem + kOffB;
     float *sres = reinterpret_cast<float *>(smem + kOffRes);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBar);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBar + 8);
-    const uint32_t bar_addr = smem_u32(bar);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kOffBarA);  // tma[2], mma[2]
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBarA + 48);
+    const uint32_t tma_bar0 = smem_u32(&bars[0]);
+    const uint32_t mma_bar0 = smem_u32(&bars[2]);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float *p_new = (MODE == 1) ? (parity ? p0 : p1) : nullptr;
 
-    // any work for this block at all? (uniform)
-    bool any = false;
-    for (int bi = blockIdx.x; bi < n_bricks; bi += gridDim.x)
-        if (MODE == 0 || !states[bricks[bi].prob].done) { any = true; break; }
-    if (!any) return;
+    auto usable = [&](int bi) { return !states[probs[bricks[bi].prob].root].done; };
+    int bi = brick_lo + blockIdx.x;
+    while (bi < n_bricks && !usable(bi)) bi += gridDim.x;
+    if (bi >= n_bricks) return;  // uniform: no work for this block
 
-    if (tid == 0) mbar_init(bar_addr, 1);
-    if (warp == 0) tmem_alloc32(smem_u32(tslot));
-    constexpr int kBWords = (PREC == MG_MIXED_TF32) ? 768 : 512;
-    for (int i = tid; i < kBWords; i += kThreads) sB[i] = Bop[i];
+    if (tid == 0) {
+        mbar_init(tma_bar0, 1);
+        mbar_init(tma_bar0 + 8, 1);
+        mbar_init(mma_bar0, 1);
+        mbar_init(mma_bar0 + 8, 1);
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tslot), 64);
+    {
+        // B operands: [tf32 hi 768 | tf32 lo 768 | bf16 hi 512 | bf16 lo 512] words
+        const uint32_t *src = Bop + (PR::kTf32 ? 0 : 1536);
+        const int words = PR::kTf32 ? 768 : 512;
+        uint32_t *dst = reinterpret_cast<uint32_t *>(sB);
+        for (int i = tid; i < 2 * words; i += kApplyThreads) dst[(i / words) * 1024 + i % words] = src[i];
+    }
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    uint32_t phase = 0;
-    bool failed = false;
+    const uint32_t b_hi = smem_u32(sB), b_lo = b_hi + 4096;
 
-    for (int bi = blockIdx.x; bi < n_bricks && !failed; bi += gridDim.x) {
+    // A-build roles: row r = tid / 4 of each 128-row tile, chunks q, q + 4 (q = tid % 4)
+    const int arow = tid >> 2, aq = tid & 3;
+    constexpr int kPer = PR::kTf32 ? 4 : 8;   // operand values per 16-byte chunk
+    int aoff[2][kPer];
+    bool achunk[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int kc = aq + 4 * h;
+        achunk[h] = kc < PR::kCols;
+#pragma unroll
+        for (int j = 0; j < kPer; j++) {
+            const int k = kc * kPer + j;
+            aoff[h][j] = (achunk[h] && k < 24) ? box_offset(k) : -1;
+        }
+    }
+    // output roles: dofs i = tid + 512 j, j < 3 (512 owned nodes x 3)
+    int obase[3], obox[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const int i = tid + j * kApplyThreads;
+        const int node = i / 3, c = i - node * 3;
+        const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
+        obase[j] = ((ox + 1) + kBE * ((oy + 1) + kBE * (oz + 1))) * kResStride + c;
+        obox[j] = ((oz + 1) * kBU + oy + 1) * kBoxNX + 3 * (ox + 1) + c + 1;
+    }
+
+    uint32_t tma_phase[2] = {0, 0}, mma_phase[2] = {0, 0};
+    bool failed = false;
+    // TMA issue for brick `b` into box set `set`
+    auto issue_tma = [&](int b, int set) {
+        const MfBrick br = bricks[b];
+        const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
+        const CUtensorMap *maps = tmaps + (size_t)br.prob * kMapsPerProblem;
+        uint8_t *box = smem + kOffBox + set * kBoxSet;
+        const uint32_t bar = tma_bar0 + 8 * set;
+        const uint32_t bytes = (MODE == 1 ? 2 : 1) * kBoxNodeBytes + kBoxElemBytes;
+        mbar_expect_tx(bar, bytes);
+        const int xn = 3 * (gx0 - 1) - 1;
+        tma_load_3d(smem_u32(box), maps + in_slot, xn, gy0 - 1, gz0 - 1, bar);
+        if (MODE == 1)
+            tma_load_3d(smem_u32(box + 12800), maps + 1 + parity, xn, gy0 - 1, gz0 - 1, bar);
+        tma_load_3d(smem_u32(box + 25600), maps + 3, gx0 - 4, gy0 - 1, gz0 - 1, bar);
+    };
+    if (tid == 0) {
+        fence_async_smem();
+        issue_tma(bi, 0);
+    }
+    int set = 0;
+    for (; bi < n_bricks && !failed;) {
+        // next usable brick of this block, prefetched into the other box set
+        int nbi = bi + gridDim.x;
+        while (nbi < n_bricks && !usable(nbi)) nbi += gridDim.x;
         const MfBrick br = bricks[bi];
         const MfProblem P = probs[br.prob];
         MfState *st = states + br.prob;
-        if (MODE == 1 && st->done) continue;
         const float beta = (MODE == 1) ? (float)st->beta : 0.0f;
         const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
-        // ---- stage u on the node halo (masked Dirichlet dofs -> 0)
-        for (int i = tid; i < kBU * kBU * kBU * 3; i += kThreads) {
-            const int node = i / 3, c = i - node * 3;
-            const int ux = node % kBU, uy = (node / kBU) % kBU, uz = node / (kBU * kBU);
-            const int gx = gx0 - 1 + ux, gy = gy0 - 1 + uy, gz = gz0 - 1 + uz;
-            float v = 0.0f;
-            if (gx >= 0 && gx < P.NX && gy >= 0 && gy < P.NY && gz >= 0 && gz < P.NZ) {
-                const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
-                const int64_t gd = P.dof_off + gn * 3 + c;
-                if (!((node_fix[P.node_off + gn] >> c) & 1)) {
-                    if (MODE == 1)
-                        v = fmaf(beta, p_old[gd], z[gd]);
-                    else
-                        v = xin[gd];
+        const float *sZ = reinterpret_cast<const float *>(smem + kOffBox + set * kBoxSet);
+        const float *sP = sZ + 12800 / 4;
+        const float *sE = sZ + 25600 / 4;
+        // one thread waits for the halo; the barrier releases the others
+        bool tma_ok = true;
+        if (tid == 0) tma_ok = mbar_wait_bounded(tma_bar0 + 8 * set, tma_phase[set]);
+        tma_phase[set] ^= 1u;
+        if (__syncthreads_or(!tma_ok)) {
+            failed = true;
+            if (tid == 0) atomicOr(err, 2);
+            break;
+        }
+        if (tid == 0 && nbi < n_bricks) {
+            fence_async_smem();
+            issue_tma(nbi, set ^ 1);  // the other set was released at the end of the last brick
+        }
+        // ---- tiles: build A(t) | wait MMA(t-1) | barrier | MMA(t) issue, drain t-1
+        for (int t = 0; t <= kNTILE; t++) {
+            if (t < kNTILE) {
+                const int buf = t & 1;
+                uint8_t *A_hi = smem + kOffA + (buf * 2) * kABytes;
+                uint8_t *A_lo = A_hi + kABytes;
+                const int l = t * 128 + arow;
+                int base = -1;
+                if (l < kNEL) {
+                    const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+                    base = (ez * kBU + ey) * kBoxNX + 3 * ex + 1;
                 }
-            }
-            su[i] = v;
-        }
-        for (int l = tid; l < kNEL; l += kThreads) {
-            const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
-            const int gx = gx0 - 1 + ex, gy = gy0 - 1 + ey, gz = gz0 - 1 + ez;
-            float e = 0.0f;
-            if (gx >= 0 && gx < P.nx && gy >= 0 && gy < P.ny && gz >= 0 && gz < P.nz)
-                e = E32[P.elem_off + gx + (int64_t)P.nx * (gy + (int64_t)P.ny * gz)];
-            sE[l] = e;
-        }
-        __syncthreads();
-        // ---- tensor-core element products, one 128-element tile at a time
-        for (int t = 0; t < kNTILE; t++) {
-            if (PREC == MG_MIXED_TF32) {
-                // 128 rows x 6 core columns of 4 tf32; chunk id -> byte offset 16 id
-                for (int id = tid; id < 128 * 6; id += kThreads) {
-                    const int rg = id / 48, kc = (id >> 3) % 6, rr = id & 7;
-                    const int l = t * 128 + rg * 8 + rr;
-                    uint4 w = make_uint4(0, 0, 0, 0);
-                    if (l < kNEL) {
-                        const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
-                        uint32_t vv[4];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    if (!achunk[h]) continue;
+                    const int kc = aq + 4 * h;
+                    float f[kPer];
+#pragma unroll
+                    for (int j = 0; j < kPer; j++) {
+                        const int o = aoff[h][j];
+                        float v = 0.0f;
+                        if (base >= 0 && o >= 0)
+                            v = (MODE == 1) ? fmaf(beta, sP[base + o], sZ[base + o]) : sZ[base + o];
+                        f[j] = v;
+                    }
+                    uint4 whi, wlo;
+                    if (PR::kTf32) {
+                        uint32_t hb[4], lb[4];
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            const int k = kc * 4 + j, a = k / 3, c = k - a * 3;
-                            int dx, dy, dz;
-                            corner_bits(a, dx, dy, dz);
-                            vv[j] = to_tf32(su[(((ez + dz) * kBU + ey + dy) * kBU + ex + dx) * 3 + c]);
+                            hb[j] = to_tf32(f[j]);
+                            lb[j] = PR::kSplit ? to_tf32(f[j] - __uint_as_float(hb[j])) : 0u;
                         }
-                        w = make_uint4(vv[0], vv[1], vv[2], vv[3]);
-                    }
-                    *reinterpret_cast<uint4 *>(sA + id * 16) = w;
-                }
-            } else {
-                // 128 rows x 4 core columns of 8 bf16 (K padded 24 -> 32)
-                for (int id = tid; id < 128 * 4; id += kThreads) {
-                    const int rg = id / 32, kc = (id >> 3) & 3, rr = id & 7;
-                    const int l = t * 128 + rg * 8 + rr;
-                    uint4 w = make_uint4(0, 0, 0, 0);
-                    if (l < kNEL && kc < 3) {
-                        const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
-                        float f[8];
+                        whi = make_uint4(hb[0], hb[1], hb[2], hb[3]);
+                        wlo = make_uint4(lb[0], lb[1], lb[2], lb[3]);
+                    } else {
+                        float g[kPer];
 #pragma unroll
-                        for (int j = 0; j < 8; j++) {
-                            const int k = kc * 8 + j, a = k / 3, c = k - a * 3;
-                            int dx, dy, dz;
-                            corner_bits(a, dx, dy, dz);
-                            f[j] = su[(((ez + dz) * kBU + ey + dy) * kBU + ex + dx) * 3 + c];
-                        }
-                        w = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
-                                       pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+                        for (int j = 0; j < kPer; j++) g[j] = PR::kSplit ? f[j] - bf16_round(f[j]) : 0.0f;
+                        whi = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
+                                         pack_bf16(f[4 % kPer], f[5 % kPer]), pack_bf16(f[6 % kPer], f[7 % kPer]));
+                        wlo = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]),
+                                         pack_bf16(g[4 % kPer], g[5 % kPer]), pack_bf16(g[6 % kPer], g[7 % kPer]));
                     }
-                    *reinterpret_cast<uint4 *>(sA + id * 16) = w;
+                    const int off = ((arow >> 3) * PR::kCols + kc) * 128 + (arow & 7) * 16;
+                    *reinterpret_cast<uint4 *>(A_hi + off) = whi;
+                    if (PR::kSplit) *reinterpret_cast<uint4 *>(A_lo + off) = wlo;
                 }
             }
+            // MMA(t-1) must be complete before its accumulator is drained and before
+            // A[(t+1)&1] (= A[(t-1)&1]) is rewritten in the next iteration
+            bool ok = true;
+            if (t >= 1 && tid == 0) {
+                const int bufp = (t - 1) & 1;
+                ok = mbar_wait_bounded(mma_bar0 + 8 * bufp, mma_phase[bufp]);
+            }
+            if (t >= 1) mma_phase[(t - 1) & 1] ^= 1u;
             fence_async_smem();
-            __syncthreads();
-            if (tid == 0) {
-                fence_after();
-                const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-                if (PREC == MG_MIXED_TF32) {
-#pragma unroll
-                    for (int s = 0; s < 3; s++)
-                        umma<PREC>(tmem, umma_desc(a0 + s * 256, 128, 768),
-                                   umma_desc(b0 + s * 256, 128, 768), s > 0);
-                } else {
-#pragma unroll
-                    for (int s = 0; s < 2; s++)
-                        umma<PREC>(tmem, umma_desc(a0 + s * 256, 128, 512),
-                                   umma_desc(b0 + s * 256, 128, 512), s > 0);
-                }
-                umma_commit(bar_addr);
-            }
-            const bool ok = mbar_wait_bounded(bar_addr, phase);
-            phase ^= 1u;
+            fence_before();
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 if (tid == 0) atomicOr(err, 1);
                 break;
             }
             fence_after();
-            // ---- epilogue: D row m -> element l = 128 t + m, scale by E_l
-            const int lg = warp & 3;
-            const int m = lg * 32 + lane, l = t * 128 + m;
-            const uint32_t taddr = tmem + ((uint32_t)(lg * 32) << 16);
-            if (warp < 4) {
-                float v[16];
-                tmem_ld16(taddr, v);
-                if (l < kNEL) {
-                    const float e = sE[l];
+            if (t < kNTILE && tid == 0) {
+                const int buf = t & 1;
+                const uint32_t a_hi = smem_u32(smem + kOffA + (buf * 2) * kABytes), a_lo = a_hi + kABytes;
+                const uint32_t d = tmem + buf * 32;
 #pragma unroll
-                    for (int n = 0; n < 16; n++) sres[l * kResStride + n] = e * v[n];
-                }
-            } else {
-                float v[8];
-                tmem_ld8(taddr + 16, v);
-                if (l < kNEL) {
-                    const float e = sE[l];
+                for (int s = 0; s < PR::kKsteps; s++)
+                    umma<PR::kTf32>(d, umma_desc(a_hi + s * 256, 128, PR::kSbo),
+                                    umma_desc(b_hi + s * 256, 128, PR::kSbo), s > 0 ? 1u : 0u);
+                if (PR::kSplit) {
 #pragma unroll
-                    for (int n = 0; n < 8; n++) sres[l * kResStride + 16 + n] = e * v[n];
+                    for (int s = 0; s < PR::kKsteps; s++) {
+                        umma<PR::kTf32>(d, umma_desc(a_hi + s * 256, 128, PR::kSbo),
+                                        umma_desc(b_lo + s * 256, 128, PR::kSbo), 1u);
+                        umma<PR::kTf32>(d, umma_desc(a_lo + s * 256, 128, PR::kSbo),
+                                        umma_desc(b_hi + s * 256, 128, PR::kSbo), 1u);
+                    }
                 }
+                umma_commit(mma_bar0 + 8 * buf);
             }
-            fence_before();
-            __syncthreads();
+            if (t >= 1) {
+                // drain tile t-1 while MMA(t) runs: rows of lane group lg, 8 columns per group cg
+                const int tp = t - 1, bufp = tp & 1, lg = warp & 3, cg = warp >> 2;
+                if (cg < 3) {
+                    const int m = lg * 32 + lane, l = tp * 128 + m;
+                    float v[8];
+                    tmem_ld8(tmem + bufp * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
+                    if (l < kNEL) {
+                        const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+                        const float e = sE[(ez * kBE + ey) * kBoxEX + ex + 3];
+#pragma unroll
+                        for (int n = 0; n < 8; n++) sres[l * kResStride + cg * 8 + n] = e * v[n];
+                    }
+                }
+                fence_before();
+            }
         }
         if (failed) break;
-        // ---- node sums over the 8 surrounding elements (fixed order)
-        double part = 0.0;
-        for (int i = tid; i < kBN * kBN * kBN * 3; i += kThreads) {
+        __syncthreads();  // sres complete
+        // ---- node sums over the 8 surrounding elements (fixed order) and outputs
+        float part = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const int i = tid + j * kApplyThreads;
             const int node = i / 3, c = i - node * 3;
             const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
             const int gx = gx0 + ox, gy = gy0 + oy, gz = gz0 + oz;
-            if (gx >= P.NX || gy >= P.NY || gz >= P.NZ) continue;
             float acc = 0.0f;
 #pragma unroll
-            for (int dz = 0; dz < 2; dz++)
-#pragma unroll
-                for (int dy = 0; dy < 2; dy++)
-#pragma unroll
-                    for (int dx = 0; dx < 2; dx++) {
-                        const int l = (ox + 1 - dx) + kBE * ((oy + 1 - dy) + kBE * (oz + 1 - dz));
-                        acc += sres[l * kResStride + 3 * corner_index(dx, dy, dz) + c];
-                    }
-            const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
-            const int64_t gd = P.dof_off + gn * 3 + c;
-            const float pv = su[(((oz + 1) * kBU + oy + 1) * kBU + ox + 1) * 3 + c];
-            if ((node_fix[P.node_off + gn] >> c) & 1) acc = pv;  // identity row (pv = 0)
-            y[gd] = acc;
+            for (int a = 0; a < 8; a++) {
+                int dx, dy, dz;
+                corner_bits(a, dx, dy, dz);
+                acc += sres[obase[j] - (dx + kBE * dy + kBE * kBE * dz) * kResStride + 3 * a];
+            }
+            if (gx >= P.NX || gy >= P.NY || gz >= P.NZ) continue;
+            const int64_t gd = dof_index(P, gx, gy, gz, c);
             if (MODE == 1) {
+                const float pv = fmaf(beta, sP[obox[j]], sZ[obox[j]]);
+                y[gd] = acc;
                 p_new[gd] = pv;
-                part += (double)pv * (double)acc;
+                part = fmaf(pv, acc, part);
+            } else if (MODE == 2) {
+                y[gd] = (dinv[gd] == 0.0f) ? 0.0f : rhs[gd] - acc;
+            } else {
+                y[gd] = (dinv[gd] == 0.0f) ? 0.0f : acc;
             }
         }
         if (MODE == 1) {
-            const double s = block_sum(part, red_sh);
+            // block sum of the brick partial (FP32 within a warp, FP64 across warps:
+            // FP64 issue is scarce on this part), then the per-problem reduction
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            if (lane == 0) red_sh[warp] = (double)part;
+            __syncthreads();
             if (tid == 0) {
+                double s = 0.0;
+                for (int w = 0; w < kApplyThreads / 32; w++) s += red_sh[w];
                 brick_part[bi] = s;
                 __threadfence();
-                const unsigned t = atomicAdd(&st->cnt_apply, 1u);
-                sh_last = (t == (unsigned)P.brick_count - 1);
+                const unsigned tk = atomicAdd(&st->cnt_apply, 1u);
+                sh_last = (tk == (unsigned)P.brick_count - 1);
             }
             __syncthreads();
             if (sh_last) {
-                const double pq = ordered_sum(brick_part, P.brick_begin, P.brick_count, red_sh);
+                double s = 0.0;
+                for (int k = tid; k < P.brick_count; k += kApplyThreads)
+                    s += __ldcg(brick_part + P.brick_begin + k);
+                tree[tid] = s;
+                __syncthreads();
+                for (int w = kApplyThreads / 2; w > 0; w >>= 1) {
+                    if (tid < w) tree[tid] += tree[tid + w];
+                    __syncthreads();
+                }
                 if (tid == 0) {
+                    const double pq = tree[0];
                     st->cnt_apply = 0;
                     st->pq = pq;
                     if (is_bad(pq)) { st->status = MG_ENAN; st->done = 1; }
@@ -436,20 +588,32 @@ __global__ void __launch_bounds__(kThreads, 2) mf_apply_kernel(
                 }
             }
         }
-        __syncthreads();
+        __syncthreads();  // box set and sres are reused
+        bi = nbi;
+        set ^= 1;
+    }
+    // after a failed wait, give an outstanding halo prefetch a bounded chance to land
+    if (failed) {
+        int nb2 = bi + gridDim.x;
+        while (nb2 < n_bricks && !usable(nb2)) nb2 += gridDim.x;
+        if (nb2 < n_bricks) (void)mbar_wait_bounded(tma_bar0 + 8 * (set ^ 1), tma_phase[set ^ 1]);
     }
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0) tmem_dealloc32(tmem);
+    if (warp == 0) tmem_dealloc(tmem, 64);
 }
 
 // ---------------------------------------------------------------- vector phase
+// x += alpha p; r -= alpha q (r stays 0 on Dirichlet dofs, D^-1 = 0 there);
+// z = D^-1 r; rz, rr -> beta, stop test.  float4 over 16-byte aligned chunks.
+// mg = 1: z comes from the multigrid V-cycle; only rr (stop test) is reduced
+// here and beta is formed after the V-cycle (mf_dot_rz_kernel).
 __global__ void __launch_bounds__(kThreads) mf_update_kernel(
     const MfChunkDesc *__restrict__ chunks, int n_chunks, const MfProblem *__restrict__ probs,
     float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
     const float *__restrict__ p, const float *__restrict__ q, const float *__restrict__ dinv,
-    MfState *states, double *__restrict__ chunk_part) {
+    MfState *states, double *__restrict__ chunk_part, int mg) {
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
@@ -457,18 +621,28 @@ __global__ void __launch_bounds__(kThreads) mf_update_kernel(
         MfState *st = states + C.prob;
         if (st->done) continue;
         const float alpha = (float)st->alpha;
-        double rz = 0.0, rr = 0.0;
-        for (int64_t i = C.begin + threadIdx.x; i < C.end; i += kThreads) {
-            x[i] = fmaf(alpha, p[i], x[i]);
-            const float ri = fmaf(-alpha, q[i], r[i]);
-            r[i] = ri;
-            const float zi = dinv[i] * ri;
-            z[i] = zi;
-            rz += (double)ri * zi;
-            rr += (double)ri * ri;
+        float rz = 0.0f, rr = 0.0f;
+        for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
+            const float4 pv = *reinterpret_cast<const float4 *>(p + i);
+            const float4 qv = *reinterpret_cast<const float4 *>(q + i);
+            const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
+            float4 xv = *reinterpret_cast<const float4 *>(x + i);
+            float4 rv = *reinterpret_cast<const float4 *>(r + i);
+            xv.x = fmaf(alpha, pv.x, xv.x); xv.y = fmaf(alpha, pv.y, xv.y);
+            xv.z = fmaf(alpha, pv.z, xv.z); xv.w = fmaf(alpha, pv.w, xv.w);
+            rv.x = dv.x != 0.0f ? fmaf(-alpha, qv.x, rv.x) : 0.0f;
+            rv.y = dv.y != 0.0f ? fmaf(-alpha, qv.y, rv.y) : 0.0f;
+            rv.z = dv.z != 0.0f ? fmaf(-alpha, qv.z, rv.z) : 0.0f;
+            rv.w = dv.w != 0.0f ? fmaf(-alpha, qv.w, rv.w) : 0.0f;
+            const float4 zv = make_float4(dv.x * rv.x, dv.y * rv.y, dv.z * rv.z, dv.w * rv.w);
+            *reinterpret_cast<float4 *>(x + i) = xv;
+            *reinterpret_cast<float4 *>(r + i) = rv;
+            if (!mg) *reinterpret_cast<float4 *>(z + i) = zv;
+            rz = fmaf(rv.x, zv.x, fmaf(rv.y, zv.y, fmaf(rv.z, zv.z, fmaf(rv.w, zv.w, rz))));
+            rr = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, fmaf(rv.w, rv.w, rr))));
         }
-        const double srz = block_sum(rz, red_sh);
-        const double srr = block_sum(rr, red_sh);
+        const double srz = block_sum_f(rz, red_sh);
+        const double srr = block_sum_f(rr, red_sh);
         const MfProblem &P = probs[C.prob];
         if (threadIdx.x == 0) {
             chunk_part[ci] = srz;
@@ -479,17 +653,19 @@ __global__ void __launch_bounds__(kThreads) mf_update_kernel(
         }
         __syncthreads();
         if (sh_last) {
-            const double trz = ordered_sum(chunk_part, P.chunk_begin, P.chunk_count, red_sh);
-            const double trr = ordered_sum(chunk_part + n_chunks, P.chunk_begin, P.chunk_count, red_sh);
+            const double trz = ordered_sum(chunk_part, P.chunk_begin, P.chunk_count);
+            const double trr = ordered_sum(chunk_part + n_chunks, P.chunk_begin, P.chunk_count);
             if (threadIdx.x == 0) {
                 st->cnt_update = 0;
                 st->iter += 1;
                 st->total_iter += 1;
                 st->rr = trr;
-                if (is_bad(trz) || is_bad(trr)) { st->status = MG_ENAN; st->done = 1; }
+                if (is_bad(trr) || (!mg && is_bad(trz))) { st->status = MG_ENAN; st->done = 1; }
                 else {
-                    st->beta = trz / st->rz;
-                    st->rz = trz;
+                    if (!mg) {
+                        st->beta = trz / st->rz;
+                        st->rz = trz;
+                    }
                     if (trr <= st->tol2) st->done = 1;
                     else if (st->iter >= st->maxit) { st->status = MG_ENOCONV; st->done = 1; }
                 }
@@ -499,7 +675,190 @@ __global__ void __launch_bounds__(kThreads) mf_update_kernel(
     }
 }
 
-// inner CG start: b = scale * r64 (unit norm), x = 0, r = b, z = D^-1 r, p_old = 0
+// rz = r . z after the V-cycle; init: beta = 0, else beta = rz / rz_old
+__global__ void __launch_bounds__(kThreads) mf_dot_rz_kernel(
+    const MfChunkDesc *__restrict__ chunks, int n_chunks, const MfProblem *__restrict__ probs,
+    const float *__restrict__ r, const float *__restrict__ z, MfState *states,
+    double *__restrict__ chunk_part, int init) {
+    __shared__ double red_sh[kThreads / 32];
+    __shared__ int sh_last;
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+        const MfChunkDesc C = chunks[ci];
+        MfState *st = states + C.prob;
+        if (st->done) continue;
+        float rz = 0.0f;
+        for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
+            const float4 rv = *reinterpret_cast<const float4 *>(r + i);
+            const float4 zv = *reinterpret_cast<const float4 *>(z + i);
+            rz = fmaf(rv.x, zv.x, fmaf(rv.y, zv.y, fmaf(rv.z, zv.z, fmaf(rv.w, zv.w, rz))));
+        }
+        const double srz = block_sum_f(rz, red_sh);
+        const MfProblem &P = probs[C.prob];
+        if (threadIdx.x == 0) {
+            chunk_part[ci] = srz;
+            __threadfence();
+            const unsigned t = atomicAdd(&st->cnt_update, 1u);
+            sh_last = (t == (unsigned)P.chunk_count - 1);
+        }
+        __syncthreads();
+        if (sh_last) {
+            const double trz = ordered_sum(chunk_part, P.chunk_begin, P.chunk_count);
+            if (threadIdx.x == 0) {
+                st->cnt_update = 0;
+                if (is_bad(trz) || !(trz > 0.0)) {
+                    // a preconditioner that is not positive on r: stop with breakdown
+                    st->status = is_bad(trz) ? MG_ENAN : MG_EBREAKDOWN;
+                    st->done = 1;
+                } else {
+                    st->beta = init ? 0.0 : trz / st->rz;
+                    st->rz = trz;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ multigrid kernels
+// Chebyshev-Jacobi smoothing (first step): mr = rin; md = D^-1 rin / theta;
+// mx = md (x0_zero) or mx + md.  Skips designs whose CG has stopped.
+__global__ void __launch_bounds__(kThreads) mg_cheb_first_kernel(
+    const MfChunkDesc *__restrict__ chunks, int lo, int hi, const MfProblem *__restrict__ probs,
+    const MfState *states, const float *__restrict__ rin, float *__restrict__ mr,
+    float *__restrict__ md, float *__restrict__ mx, const float *__restrict__ dinv,
+    float inv_theta, int x0_zero) {
+    for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
+        const MfChunkDesc C = chunks[ci];
+        if (states[probs[C.prob].root].done) continue;
+        for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
+            const float4 rv = *reinterpret_cast<const float4 *>(rin + i);
+            const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
+            const float4 d = make_float4(dv.x * rv.x * inv_theta, dv.y * rv.y * inv_theta,
+                                         dv.z * rv.z * inv_theta, dv.w * rv.w * inv_theta);
+            float4 xv = x0_zero ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(mx + i);
+            xv.x += d.x; xv.y += d.y; xv.z += d.z; xv.w += d.w;
+            if (mr != rin) *reinterpret_cast<float4 *>(mr + i) = rv;
+            *reinterpret_cast<float4 *>(md + i) = d;
+            *reinterpret_cast<float4 *>(mx + i) = xv;
+        }
+    }
+}
+
+// Chebyshev step: mr -= A md (= my); md = c1 md + c2 D^-1 mr; mx += md
+__global__ void __launch_bounds__(kThreads) mg_cheb_next_kernel(
+    const MfChunkDesc *__restrict__ chunks, int lo, int hi, const MfProblem *__restrict__ probs,
+    const MfState *states, const float *__restrict__ my, float *__restrict__ mr,
+    float *__restrict__ md, float *__restrict__ mx, const float *__restrict__ dinv, float c1,
+    float c2) {
+    for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
+        const MfChunkDesc C = chunks[ci];
+        if (states[probs[C.prob].root].done) continue;
+        for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
+            const float4 yv = *reinterpret_cast<const float4 *>(my + i);
+            const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
+            float4 rv = *reinterpret_cast<const float4 *>(mr + i);
+            float4 d = *reinterpret_cast<const float4 *>(md + i);
+            float4 xv = *reinterpret_cast<const float4 *>(mx + i);
+            rv.x -= yv.x; rv.y -= yv.y; rv.z -= yv.z; rv.w -= yv.w;
+            d.x = fmaf(c1, d.x, c2 * dv.x * rv.x); d.y = fmaf(c1, d.y, c2 * dv.y * rv.y);
+            d.z = fmaf(c1, d.z, c2 * dv.z * rv.z); d.w = fmaf(c1, d.w, c2 * dv.w * rv.w);
+            xv.x += d.x; xv.y += d.y; xv.z += d.z; xv.w += d.w;
+            *reinterpret_cast<float4 *>(mr + i) = rv;
+            *reinterpret_cast<float4 *>(md + i) = d;
+            *reinterpret_cast<float4 *>(mx + i) = xv;
+        }
+    }
+}
+
+// restriction (transpose of trilinear interpolation) into the coarse problems
+// plo..phi-1: mb_c[I] = sum_d w(d) my_f[2I + d], d in {-1,0,1}^3, w = prod (1 - |d|/2)
+__global__ void mg_restrict_kernel(const MfProblem *__restrict__ probs, int plo,
+                                   const MfState *states, const float *__restrict__ my,
+                                   float *__restrict__ mb, const float *__restrict__ dinv) {
+    const MfProblem C = probs[plo + blockIdx.y];
+    if (states[C.root].done) return;
+    const MfProblem F = probs[C.fine];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < C.n_pad;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = i / C.pitch;
+        const int xin = (int)(i - row * C.pitch);
+        float out = 0.0f;
+        const int64_t o = C.dof_off + i;
+        if (xin < 3 * C.NX && dinv[o] != 0.0f) {
+            const int I = xin / 3, c = xin - 3 * I;
+            const int J = (int)(row % C.NY), K = (int)(row / C.NY);
+            for (int dz = -1; dz <= 1; dz++) {
+                const int k = 2 * K + dz;
+                if (k < 0 || k >= F.NZ) continue;
+                const float wz = dz ? 0.5f : 1.0f;
+                for (int dy = -1; dy <= 1; dy++) {
+                    const int j = 2 * J + dy;
+                    if (j < 0 || j >= F.NY) continue;
+                    const float wy = wz * (dy ? 0.5f : 1.0f);
+                    const float *rowp = my + F.dof_off + ((int64_t)k * F.NY + j) * F.pitch;
+                    for (int dx = -1; dx <= 1; dx++) {
+                        const int ii = 2 * I + dx;
+                        if (ii < 0 || ii >= F.NX) continue;
+                        out = fmaf(wy * (dx ? 0.5f : 1.0f), rowp[3 * ii + c], out);
+                    }
+                }
+            }
+        }
+        mb[o] = out;
+    }
+}
+
+// prolongation (trilinear) from the coarse levels into the fine problems
+// plo..phi-1: mx_f[i] += sum_I w mx_c[I] (skips Dirichlet dofs and padding)
+__global__ void mg_prolong_kernel(const MfProblem *__restrict__ probs, int plo,
+                                  const MfState *states, float *__restrict__ mx,
+                                  const float *__restrict__ dinv) {
+    const MfProblem F = probs[plo + blockIdx.y];
+    if (states[F.root].done) return;
+    const MfProblem C = probs[F.coarse];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F.n_pad;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = i / F.pitch;
+        const int xin = (int)(i - row * F.pitch);
+        const int64_t o = F.dof_off + i;
+        if (xin >= 3 * F.NX || dinv[o] == 0.0f) continue;
+        const int ii = xin / 3, c = xin - 3 * ii;
+        const int j = (int)(row % F.NY), k = (int)(row / F.NY);
+        const int I0 = ii >> 1, I1 = (ii + 1) >> 1, J0 = j >> 1, J1 = (j + 1) >> 1, K0 = k >> 1,
+                  K1 = (k + 1) >> 1;
+        const float wx = (ii & 1) ? 0.5f : 1.0f, wy = (j & 1) ? 0.5f : 1.0f, wz = (k & 1) ? 0.5f : 1.0f;
+        float acc = 0.0f;
+        const int Is[2] = {I0, I1}, Js[2] = {J0, J1}, Ks[2] = {K0, K1};
+        for (int a = 0; a < ((k & 1) ? 2 : 1); a++)
+            for (int bb = 0; bb < ((j & 1) ? 2 : 1); bb++)
+                for (int cc = 0; cc < ((ii & 1) ? 2 : 1); cc++)
+                    acc = fmaf(wx * wy * wz,
+                               mx[C.dof_off + ((int64_t)Ks[a] * C.NY + Js[bb]) * C.pitch + 3 * Is[cc] + c], acc);
+        mx[o] += acc;
+    }
+}
+
+// coarse moduli: E_c = 2 mean(E of the 8 children); the factor 2 is the
+// element-size scaling of the 3D stiffness (K(2h) = 2 K(h)), so every level
+// uses the fine-grid reference stiffness K0
+__global__ void mg_coarsen_kernel(const MfProblem *__restrict__ probs, int plo,
+                                  float *__restrict__ E32) {
+    const MfProblem C = probs[plo + blockIdx.y];
+    const MfProblem F = probs[C.fine];
+    const int64_t ne = (int64_t)C.nx * C.ny * C.nz;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int ex = (int)(e % C.nx), ey = (int)((e / C.nx) % C.ny), ez = (int)(e / ((int64_t)C.nx * C.ny));
+        float s = 0.0f;
+        for (int dz = 0; dz < 2; dz++)
+            for (int dy = 0; dy < 2; dy++)
+                for (int dx = 0; dx < 2; dx++)
+                    s += E32[F.elem_off + ((int64_t)(2 * ez + dz) * F.ny + 2 * ey + dy) * F.pitch_e + 2 * ex + dx];
+        E32[C.elem_off + ((int64_t)ez * C.ny + ey) * C.pitch_e + ex] = 0.25f * s;
+    }
+}
+
+// inner CG start: b = scale r64 (unit norm), x = 0, r = b, z = D^-1 r, p_old = 0
 __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
     const MfChunkDesc *__restrict__ chunks, int n_chunks, const MfProblem *__restrict__ probs,
     const double *__restrict__ r64, float *__restrict__ x, float *__restrict__ r,
@@ -515,19 +874,19 @@ __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
             continue;
         }
         const double scale = st->scale;
-        double rz = 0.0, rr = 0.0;
+        float rz = 0.0f, rr = 0.0f;
         for (int64_t i = C.begin + threadIdx.x; i < C.end; i += kThreads) {
-            const float bi = (float)(r64[i] * scale);
+            const float bi = dinv[i] != 0.0f ? (float)(r64[i] * scale) : 0.0f;
             x[i] = 0.0f;
             r[i] = bi;
             const float zi = dinv[i] * bi;
             z[i] = zi;
             p_old[i] = 0.0f;
-            rz += (double)bi * zi;
-            rr += (double)bi * bi;
+            rz = fmaf(bi, zi, rz);
+            rr = fmaf(bi, bi, rr);
         }
-        const double srz = block_sum(rz, red_sh);
-        const double srr = block_sum(rr, red_sh);
+        const double srz = block_sum_f(rz, red_sh);
+        const double srr = block_sum_f(rr, red_sh);
         const MfProblem &P = probs[C.prob];
         if (threadIdx.x == 0) {
             chunk_part[ci] = srz;
@@ -538,8 +897,8 @@ __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
         }
         __syncthreads();
         if (sh_last) {
-            const double trz = ordered_sum(chunk_part, P.chunk_begin, P.chunk_count, red_sh);
-            const double trr = ordered_sum(chunk_part + n_chunks, P.chunk_begin, P.chunk_count, red_sh);
+            const double trz = ordered_sum(chunk_part, P.chunk_begin, P.chunk_count);
+            const double trr = ordered_sum(chunk_part + n_chunks, P.chunk_begin, P.chunk_count);
             if (threadIdx.x == 0) {
                 st->cnt_update = 0;
                 st->rz = trz;
@@ -558,7 +917,7 @@ __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
     }
 }
 
-// refinement update u += x / scale (free dofs; x is 0 on Dirichlet dofs)
+// refinement update u += x / scale (x is 0 on Dirichlet dofs and padding)
 __global__ void mf_refine_kernel(const MfChunkDesc *__restrict__ chunks, int n_chunks,
                                  const float *__restrict__ x, double *__restrict__ u64,
                                  const MfState *states) {
@@ -606,7 +965,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
             double v = 0.0;
             if (gx >= 0 && gx < P.NX && gy >= 0 && gy < P.NY && gz >= 0 && gz < P.NZ) {
                 const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
-                if (!((node_fix[P.node_off + gn] >> c) & 1)) v = u64[P.dof_off + gn * 3 + c];
+                if (!((node_fix[P.node_off + gn] >> c) & 1)) v = u64[dof_index(P, gx, gy, gz, c)];
             }
             su[i] = v;
         }
@@ -615,7 +974,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
             const int gx = gx0 - 1 + ex, gy = gy0 - 1 + ey, gz = gz0 - 1 + ez;
             double e = 0.0;
             if (gx >= 0 && gx < P.nx && gy >= 0 && gy < P.ny && gz >= 0 && gz < P.nz)
-                e = E64[P.elem_off + gx + (int64_t)P.nx * (gy + (int64_t)P.ny * gz)];
+                e = E64[P.elem_off + ((int64_t)gz * P.ny + gy) * P.pitch_e + gx];
             sE[l] = e;
         }
         __syncthreads();
@@ -646,7 +1005,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
                         acc = fma(e, s, acc);
                     }
             const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
-            const int64_t gd = P.dof_off + gn * 3 + c;
+            const int64_t gd = dof_index(P, gx, gy, gz, c);
             double rv = f64[gd] - acc;
             if ((node_fix[P.node_off + gn] >> c) & 1) rv = 0.0;
             r64[gd] = rv;
@@ -661,7 +1020,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
         }
         __syncthreads();
         if (sh_last) {
-            const double rr = ordered_sum(brick_part, P.brick_begin, P.brick_count, red_sh);
+            const double rr = ordered_sum(brick_part, P.brick_begin, P.brick_count);
             if (threadIdx.x == 0) {
                 st->cnt_res = 0;
                 st->rr64 = rr;
@@ -675,37 +1034,46 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
     }
 }
 
-// Jacobi diagonal of the mixed operator: sum_e E_e K0[3a+c][3a+c]
+// Jacobi inverse of the mixed operator: 1 / sum_e E_e K0[3a+c][3a+c];
+// 0 on Dirichlet dofs and padding (marks them for the vector kernels)
 __global__ void mf_diag_kernel(const MfProblem *__restrict__ probs, int n_probs,
                                const float *__restrict__ E32, const uint8_t *__restrict__ node_fix,
                                const double *__restrict__ K0, float *__restrict__ dinv) {
     const int pi = blockIdx.y;
     if (pi >= n_probs) return;
     const MfProblem P = probs[pi];
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_dofs;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_pad;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t gn = i / 3;
-        const int c = (int)(i - gn * 3);
-        const int gx = (int)(gn % P.NX), gy = (int)((gn / P.NX) % P.NY), gz = (int)(gn / ((int64_t)P.NX * P.NY));
-        double d = 0.0;
-        for (int dz = 0; dz < 2; dz++)
-            for (int dy = 0; dy < 2; dy++)
-                for (int dx = 0; dx < 2; dx++) {
-                    const int ex = gx - dx, ey = gy - dy, ez = gz - dz;
-                    if (ex < 0 || ey < 0 || ez < 0 || ex >= P.nx || ey >= P.ny || ez >= P.nz) continue;
-                    const int k = 3 * corner_index(dx, dy, dz) + c;
-                    d += (double)E32[P.elem_off + ex + (int64_t)P.nx * (ey + (int64_t)P.ny * ez)] * K0[k * 24 + k];
-                }
-        const bool fixed = (node_fix[P.node_off + gn] >> c) & 1;
-        dinv[P.dof_off + i] = (fixed || d == 0.0) ? 1.0f : (float)(1.0 / d);
+        const int64_t row = i / P.pitch;
+        const int xin = (int)(i - row * P.pitch);
+        float out = 0.0f;
+        if (xin < 3 * P.NX) {
+            const int gx = xin / 3, c = xin - 3 * gx;
+            const int gy = (int)(row % P.NY), gz = (int)(row / P.NY);
+            const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
+            double d = 0.0;
+            for (int dz = 0; dz < 2; dz++)
+                for (int dy = 0; dy < 2; dy++)
+                    for (int dx = 0; dx < 2; dx++) {
+                        const int ex = gx - dx, ey = gy - dy, ez = gz - dz;
+                        if (ex < 0 || ey < 0 || ez < 0 || ex >= P.nx || ey >= P.ny || ez >= P.nz) continue;
+                        const int k = 3 * corner_index(dx, dy, dz) + c;
+                        d += (double)E32[P.elem_off + ((int64_t)ez * P.ny + ey) * P.pitch_e + ex] *
+                             K0[k * 24 + k];
+                    }
+            const bool fixed = (node_fix[P.node_off + gn] >> c) & 1;
+            out = (fixed || d == 0.0) ? 0.0f : (float)(1.0 / d);
+        }
+        dinv[P.dof_off + i] = out;
     }
 }
 
-// compliance adjoint sensitivity dC/drho_e = -dE_e u_e^T K0 u_e (FP64)
+// compliance adjoint sensitivity dC/drho_e = -dE_e u_e^T K0 u_e (FP64), written
+// unpadded (element order x-fastest) at dc + out_off[prob]
 __global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
                                const double *__restrict__ dE64, const uint8_t *__restrict__ node_fix,
                                const double *__restrict__ u64, const double *__restrict__ K0,
-                               double *__restrict__ dc) {
+                               const int64_t *__restrict__ out_off, double *__restrict__ dc) {
     __shared__ double sK[576];
     for (int i = threadIdx.x; i < 576; i += blockDim.x) sK[i] = K0[i];
     __syncthreads();
@@ -723,7 +1091,7 @@ __global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
             const int64_t gn = (ex + dx) + (int64_t)P.NX * ((ey + dy) + (int64_t)P.NY * (ez + dz));
             const uint8_t fx = node_fix[P.node_off + gn];
             for (int c = 0; c < 3; c++)
-                ue[3 * a + c] = ((fx >> c) & 1) ? 0.0 : u64[P.dof_off + gn * 3 + c];
+                ue[3 * a + c] = ((fx >> c) & 1) ? 0.0 : u64[dof_index(P, ex + dx, ey + dy, ez + dz, c)];
         }
         double s = 0.0;
         for (int i = 0; i < 24; i++) {
@@ -731,11 +1099,11 @@ __global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
             for (int j = 0; j < 24; j++) t = fma(sK[i * 24 + j], ue[j], t);
             s = fma(ue[i], t, s);
         }
-        dc[P.elem_off + e] = -dE64[P.elem_off + e] * s;
+        dc[out_off[pi] + e] = -dE64[P.elem_off + ((int64_t)ez * P.ny + ey) * P.pitch_e + ex] * s;
     }
 }
 
-// per-chunk partial of f.u (compliance); host sums each problem's chunks in order
+// per-chunk partial of a.b; host sums each problem's chunks in order
 __global__ void mf_dot_chunks_kernel(const MfChunkDesc *__restrict__ chunks, int n_chunks,
                                      const double *__restrict__ a, const double *__restrict__ b,
                                      double *__restrict__ part) {
@@ -750,78 +1118,189 @@ __global__ void mf_dot_chunks_kernel(const MfChunkDesc *__restrict__ chunks, int
     }
 }
 
-__global__ void fill_f32_kernel(float *__restrict__ a, float v, int64_t n) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a[i] = v;
+// unpadded element array (x-fastest) -> padded FP32 / FP64 tables of problem P
+__global__ void pack_elems_kernel(const MfProblem *__restrict__ probs, int pi,
+                                  const double *__restrict__ E, const double *__restrict__ dE,
+                                  float *__restrict__ E32, double *__restrict__ E64,
+                                  double *__restrict__ dE64) {
+    const MfProblem P = probs[pi];
+    const int64_t ne = (int64_t)P.nx * P.ny * P.nz;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t ex = e % P.nx, row = e / P.nx;
+        const int64_t o = P.elem_off + row * P.pitch_e + ex;
+        if (E) {
+            E64[o] = E[e];
+            E32[o] = (float)E[e];
+        }
+        if (dE) dE64[o] = dE[e];
+    }
 }
 
-__global__ void to_f32_kernel(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+// padded <-> unpadded node-interleaved FP64 vectors of problem P
+__global__ void unpack_vec_kernel(const MfProblem *__restrict__ probs, int pi,
+                                  double *__restrict__ padded, double *__restrict__ flat,
+                                  int to_flat) {
+    const MfProblem P = probs[pi];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_dofs;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = i / (3 * P.NX), xin = i - row * 3 * P.NX;
+        const int64_t o = P.dof_off + row * P.pitch + xin;
+        if (to_flat) flat[i] = padded[o];
+        else padded[o] = flat[i];
+    }
+}
+
+__global__ void fill_f32_kernel(float *__restrict__ a, const float *__restrict__ mask, float v,
+                                int64_t n) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
+    if (i < n) a[i] = (mask[i] != 0.0f) ? v : 0.0f;
 }
 
 inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-// K0 in the UMMA K-major no-swizzle layout (B operand, N = 32 rows, zero padded)
-void pack_b_operand(const double *K0, std::vector<uint32_t> &tf32, std::vector<uint32_t> &bf16) {
-    auto tf32_round = [](float x) -> uint32_t {
-        // round to nearest (ties away) on the 10-bit mantissa, as cvt.rna.tf32.f32
+// K0 in the UMMA K-major no-swizzle layout (B operand, N = 32 rows, zero padded):
+// [tf32 hi 768 | tf32 lo 768 | bf16 hi 512 | bf16 lo 512] 32-bit words
+void pack_b_operand(const double *K0, std::vector<uint32_t> &out) {
+    auto tf32_round = [](float x) -> float {
         uint32_t u;
         memcpy(&u, &x, 4);
-        if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
+        if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;  // nearest, ties away
+        float r;
+        memcpy(&r, &u, 4);
+        return r;
+    };
+    auto bf16_round_h = [](float x) -> float {
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        u = (u + 0x7fffu + ((u >> 16) & 1u)) & 0xffff0000u;  // nearest even
+        float r;
+        memcpy(&r, &u, 4);
+        return r;
+    };
+    auto bits = [](float x) -> uint32_t {
+        uint32_t u;
+        memcpy(&u, &x, 4);
         return u;
     };
-    auto bf16_bits = [](float x) -> uint16_t {
-        uint32_t u;
-        memcpy(&u, &x, 4);
-        uint32_t lsb = (u >> 16) & 1u;
-        u += 0x7fffu + lsb;  // round to nearest even
-        return (uint16_t)(u >> 16);
-    };
-    tf32.assign(768, 0u);
-    bf16.assign(512, 0u);
+    out.assign(2560, 0u);
     for (int n = 0; n < 32; n++) {
         const int rg = n / 8, rr = n % 8;
         for (int kc = 0; kc < 6; kc++)
             for (int j = 0; j < 4; j++) {
                 const int k = kc * 4 + j;
-                float v = (n < 24) ? (float)K0[n * 24 + k] : 0.0f;
-                tf32[((rg * 6 + kc) * 128 + rr * 16) / 4 + j] = tf32_round(v);
+                const float v = (n < 24) ? (float)K0[n * 24 + k] : 0.0f;
+                const float h = tf32_round(v);
+                const int w = ((rg * 6 + kc) * 128 + rr * 16) / 4 + j;
+                out[w] = bits(h);
+                out[768 + w] = bits(tf32_round((n < 24) ? (float)(K0[n * 24 + k] - (double)h) : 0.0f));
             }
         for (int kc = 0; kc < 4; kc++)
             for (int j = 0; j < 8; j += 2) {
                 const int k = kc * 8 + j;
-                float lo = (n < 24 && k < 24) ? (float)K0[n * 24 + k] : 0.0f;
-                float hi = (n < 24 && k + 1 < 24) ? (float)K0[n * 24 + k + 1] : 0.0f;
-                bf16[((rg * 4 + kc) * 128 + rr * 16) / 4 + j / 2] =
-                    (uint32_t)bf16_bits(lo) | ((uint32_t)bf16_bits(hi) << 16);
+                const double v0 = (n < 24 && k < 24) ? K0[n * 24 + k] : 0.0;
+                const double v1 = (n < 24 && k + 1 < 24) ? K0[n * 24 + k + 1] : 0.0;
+                const float h0 = bf16_round_h((float)v0), h1 = bf16_round_h((float)v1);
+                const float l0 = bf16_round_h((float)(v0 - (double)h0));
+                const float l1 = bf16_round_h((float)(v1 - (double)h1));
+                const int w = ((rg * 4 + kc) * 128 + rr * 16) / 4 + j / 2;
+                out[1536 + w] = (bits(h0) >> 16) | (bits(h1) & 0xffff0000u);
+                out[2048 + w] = (bits(l0) >> 16) | (bits(l1) & 0xffff0000u);
             }
     }
 }
 
+struct ApplyArgs {
+    int brick_lo, brick_hi, in_slot, parity;
+    const float *rhs;
+    float *y;
+};
+
 template <int PREC, int MODE>
-void launch_apply(MfBatch &b, const float *xin, const float *z, const float *pold, float *pnew,
-                  float *y) {
-    const uint32_t *Bop = (PREC == MG_MIXED_TF32) ? b.Bop_tf32 : b.Bop_bf16;
-    mf_apply_kernel<PREC, MODE><<<b.apply_grid, kThreads, kApplySmem, b.stream>>>(
-        b.probs, b.bricks, b.n_bricks, b.E32, b.node_fix, xin, z, pold, pnew, y, b.states,
-        b.brick_part, Bop, b.err);
+void launch_apply(MfBatch &b, const ApplyArgs &a) {
+    const int nb = a.brick_hi - a.brick_lo;
+    if (nb <= 0) return;
+    const int grid = std::max(1, std::min(nb, b.apply_grid));
+    mf_apply_kernel<PREC, MODE><<<grid, kApplyThreads, kApplySmem, b.stream>>>(
+        b.probs, b.bricks, a.brick_lo, a.brick_hi, b.tmaps, a.in_slot, a.parity, b.Bop, b.dinv,
+        a.rhs, b.p0, b.p1, a.y, b.states, b.brick_part, b.err);
+}
+
+template <int MODE>
+void launch_apply_prec(MfBatch &b, int prec, const ApplyArgs &a) {
+    switch (prec) {
+        case MG_MIXED_TF32: launch_apply<MG_MIXED_TF32, MODE>(b, a); break;
+        case MG_MIXED_BF16: launch_apply<MG_MIXED_BF16, MODE>(b, a); break;
+        case MG_MIXED_TF32X3: launch_apply<MG_MIXED_TF32X3, MODE>(b, a); break;
+        default: launch_apply<MG_MIXED_BF16X3, MODE>(b, a); break;
+    }
+}
+
+// CG step on the level-0 bricks (z from map in_slot)
+void launch_cg_apply(MfBatch &b, int prec, int in_slot, int parity) {
+    ApplyArgs a{b.lvl_brick_lo[0], b.lvl_brick_hi[0], in_slot, parity, nullptr, b.q};
+    launch_apply_prec<1>(b, prec, a);
+}
+
+template <int PREC>
+int set_apply_attrs() {
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<PREC, 1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<PREC, 2>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<PREC, 3>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    return MG_OK;
 }
 
 int configure_kernels() {
     static bool done = false;
     if (done) return MG_OK;
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_TF32, 0>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_TF32, 1>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_BF16, 0>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<MG_MIXED_BF16, 1>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_TRY(set_apply_attrs<MG_MIXED_TF32>());
+    MG_TRY(set_apply_attrs<MG_MIXED_BF16>());
+    MG_TRY(set_apply_attrs<MG_MIXED_TF32X3>());
+    MG_TRY(set_apply_attrs<MG_MIXED_BF16X3>());
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_residual64_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kResidSmem));
     done = true;
+    return MG_OK;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encode_fn(EncodeTiledFn *fn) {
+    static EncodeTiledFn cached = nullptr;
+    if (!cached) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        MG_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                     cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p) {
+            set_error("cuTensorMapEncodeTiled unavailable");
+            return MG_ECUDA;
+        }
+        cached = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    *fn = cached;
+    return MG_OK;
+}
+
+int make_map(EncodeTiledFn fn, CUtensorMap *m, void *base, uint64_t d0, uint64_t d1, uint64_t d2,
+             uint64_t stride1_bytes, uint64_t stride2_bytes, uint32_t b0, uint32_t b1, uint32_t b2) {
+    cuuint64_t dims[3] = {d0, d1, d2};
+    cuuint64_t strides[2] = {stride1_bytes, stride2_bytes};
+    cuuint32_t box[3] = {b0, b1, b2};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return MG_ECUDA;
+    }
     return MG_OK;
 }
 
@@ -838,6 +1317,12 @@ int read_states(MfBatch &b) {
     return MG_OK;
 }
 
+void launch_update(MfBatch &b, float *pnew, bool mg) {
+    const int n0 = b.lvl_chunk_hi[0];
+    mf_update_kernel<<<std::max(1, std::min(n0, b.vec_grid)), kThreads, 0, b.stream>>>(
+        b.chunks, n0, b.probs, b.x, b.r, b.z, pnew, b.q, b.dinv, b.states, b.chunk_part, mg ? 1 : 0);
+}
+
 int build_graph(MfBatch &b, int prec, int chunk) {
     if (b.graph && b.graph_prec == prec && b.graph_chunk == chunk) return MG_OK;
     if (b.graph) {
@@ -847,15 +1332,10 @@ int build_graph(MfBatch &b, int prec, int chunk) {
     cudaGraph_t g = nullptr;
     MG_CUDA_TRY(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < chunk; it++) {
-        float *pold = (it & 1) ? b.p1 : b.p0;
-        float *pnew = (it & 1) ? b.p0 : b.p1;
-        if (prec == MG_MIXED_TF32)
-            launch_apply<MG_MIXED_TF32, 1>(b, nullptr, b.z, pold, pnew, b.q);
-        else
-            launch_apply<MG_MIXED_BF16, 1>(b, nullptr, b.z, pold, pnew, b.q);
-        mf_update_kernel<<<b.vec_grid, kThreads, 0, b.stream>>>(b.chunks, b.n_chunks, b.probs, b.x,
-                                                               b.r, b.z, pnew, b.q, b.dinv,
-                                                               b.states, b.chunk_part);
+        const int parity = it & 1;  // p_old = p0 on even iterations
+        float *pnew = parity ? b.p0 : b.p1;
+        launch_cg_apply(b, prec, 0, parity);
+        launch_update(b, pnew, false);
     }
     cudaError_t e = cudaStreamEndCapture(b.stream, &g);
     if (e != cudaSuccess) {
@@ -870,6 +1350,14 @@ int build_graph(MfBatch &b, int prec, int chunk) {
     }
     b.graph_prec = prec;
     b.graph_chunk = chunk;
+    return MG_OK;
+}
+
+int compute_diag(MfBatch &b) {
+    dim3 grid(std::max(1u, std::min(blocks_for(b.n_pad, 256), 4096u)), b.n_probs);
+    mf_diag_kernel<<<grid, 256, 0, b.stream>>>(b.probs, b.n_probs, b.E32, b.node_fix, b.K0, b.dinv);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
     return MG_OK;
 }
 
@@ -911,29 +1399,79 @@ void hex8_box_stiffness(double hx, double hy, double hz, double nu, double K[576
 }
 
 int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, double hy,
-                  double hz, double nu, cudaStream_t stream) {
+                  double hz, double nu, cudaStream_t stream, int max_levels) {
     MG_TRY(configure_kernels());
+    EncodeTiledFn enc = nullptr;
+    MG_TRY(encode_fn(&enc));
     b.stream = stream;
     b.hx = hx; b.hy = hy; b.hz = hz; b.nu = nu;
-    b.n_probs = (int)shapes.size();
-    b.h_probs = shapes;
+    // level 0: the designs; then every design's coarse levels, ordered by level
+    b.n_fine = (int)shapes.size();
+    b.h_probs.clear();
+    for (size_t i = 0; i < shapes.size(); i++) {
+        MfProblem P = shapes[i];
+        P.level = 0;
+        P.root = (int)i;
+        P.coarse = -1;
+        P.fine = -1;
+        b.h_probs.push_back(P);
+    }
+    b.lvl_prob_lo.assign(1, 0);
+    b.lvl_prob_hi.assign(1, b.n_fine);
+    for (int lev = 1; lev < std::max(1, std::min(max_levels, kMaxLevels)); lev++) {
+        const int lo = b.lvl_prob_lo.back(), hi = b.lvl_prob_hi.back();
+        const int start = (int)b.h_probs.size();
+        for (int f = lo; f < hi; f++) {
+            const MfProblem F = b.h_probs[f];
+            if (F.nx % 2 || F.ny % 2 || F.nz % 2 || F.nx < 4 || F.ny < 4 || F.nz < 4) continue;
+            MfProblem C{};
+            C.nx = F.nx / 2; C.ny = F.ny / 2; C.nz = F.nz / 2;
+            C.level = lev;
+            C.root = F.root;
+            C.fine = f;
+            C.coarse = -1;
+            // a load case sharing its design's moduli shares the coarse moduli too
+            C.share_elems = (F.share_elems >= 0) ? b.h_probs[F.share_elems].coarse : -1;
+            b.h_probs[f].coarse = (int)b.h_probs.size();
+            b.h_probs.push_back(C);
+        }
+        if ((int)b.h_probs.size() == start) break;
+        b.lvl_prob_lo.push_back(start);
+        b.lvl_prob_hi.push_back((int)b.h_probs.size());
+    }
+    b.n_levels = (int)b.lvl_prob_lo.size();
+    b.n_probs = (int)b.h_probs.size();
     int64_t dof = 0, el = 0, nd = 0;
     int nb = 0, nc = 0;
     b.h_bricks.clear();
     b.h_chunks.clear();
-    for (auto &P : b.h_probs) {
+    for (size_t pi = 0; pi < b.h_probs.size(); pi++) {
+        MfProblem &P = b.h_probs[pi];
         if (P.nx <= 0 || P.ny <= 0 || P.nz <= 0 || P.nx >= 32767 * kBN || P.ny >= 32767 * kBN ||
             P.nz >= 32767 * kBN) {
             set_error("bad grid %dx%dx%d", P.nx, P.ny, P.nz);
             return MG_EINVAL;
         }
         P.NX = P.nx + 1; P.NY = P.ny + 1; P.NZ = P.nz + 1;
+        P.pitch = (3 * P.NX + 3) / 4 * 4;
+        P.pitch_e = (P.nx + 3) / 4 * 4;
         P.n_dofs = (int64_t)P.NX * P.NY * P.NZ * 3;
-        if (P.elem_off < 0) { P.elem_off = el; el += (int64_t)P.nx * P.ny * P.nz; }
-        else el = std::max(el, P.elem_off + (int64_t)P.nx * P.ny * P.nz);
+        P.n_pad = (int64_t)P.pitch * P.NY * P.NZ;
+        if (P.share_elems >= 0 && P.share_elems < (int)pi) {
+            const MfProblem &S = b.h_probs[P.share_elems];
+            if (S.nx != P.nx || S.ny != P.ny || S.nz != P.nz) {
+                set_error("shared element tables need equal grids");
+                return MG_EINVAL;
+            }
+            P.elem_off = S.elem_off;
+        } else {
+            P.share_elems = -1;
+            P.elem_off = el;
+            el += (int64_t)P.pitch_e * P.ny * P.nz;
+        }
         P.dof_off = dof;
         P.node_off = nd;
-        dof += P.n_dofs;
+        dof += P.n_pad;
         nd += (int64_t)P.NX * P.NY * P.NZ;
         const int bx = (P.NX + kBN - 1) / kBN, by = (P.NY + kBN - 1) / kBN, bz = (P.NZ + kBN - 1) / kBN;
         P.brick_begin = nb;
@@ -941,40 +1479,50 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         for (int k = 0; k < bz; k++)
             for (int j = 0; j < by; j++)
                 for (int i = 0; i < bx; i++)
-                    b.h_bricks.push_back(MfBrick{(int)(&P - b.h_probs.data()), (int16_t)i, (int16_t)j, (int16_t)k, 0});
+                    b.h_bricks.push_back(MfBrick{(int)pi, (int16_t)i, (int16_t)j, (int16_t)k, 0});
         nb += P.brick_count;
         P.chunk_begin = nc;
-        P.chunk_count = (int)((P.n_dofs + kChunk - 1) / kChunk);
+        P.chunk_count = (int)((P.n_pad + kChunk - 1) / kChunk);
         for (int c = 0; c < P.chunk_count; c++) {
             MfChunkDesc C;
-            C.prob = (int)(&P - b.h_probs.data());
+            C.prob = (int)pi;
             C.pad = 0;
             C.begin = P.dof_off + (int64_t)c * kChunk;
-            C.end = std::min(P.dof_off + P.n_dofs, C.begin + kChunk);
+            C.end = std::min(P.dof_off + P.n_pad, C.begin + kChunk);
             b.h_chunks.push_back(C);
         }
         nc += P.chunk_count;
     }
     b.n_bricks = nb;
     b.n_chunks = nc;
-    b.n_dofs = dof;
-    b.n_elems = el;
+    b.lvl_brick_lo.clear(); b.lvl_brick_hi.clear(); b.lvl_chunk_lo.clear(); b.lvl_chunk_hi.clear();
+    for (int l = 0; l < b.n_levels; l++) {
+        const MfProblem &A = b.h_probs[b.lvl_prob_lo[l]], &Z = b.h_probs[b.lvl_prob_hi[l] - 1];
+        b.lvl_brick_lo.push_back(A.brick_begin);
+        b.lvl_brick_hi.push_back(Z.brick_begin + Z.brick_count);
+        b.lvl_chunk_lo.push_back(A.chunk_begin);
+        b.lvl_chunk_hi.push_back(Z.chunk_begin + Z.chunk_count);
+    }
+    b.n_pad = dof;
+    b.n_elem_pad = el;
     b.n_nodes = nd;
     int dev = 0, sms = 0;
     MG_CUDA_TRY(cudaGetDevice(&dev));
     MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    b.apply_grid = std::max(1, std::min(nb, 2 * sms));
-    b.vec_grid = std::max(1, std::min(nc, 4 * sms));
+    b.apply_grid = std::max(1, std::min(nb, sms));
+    b.vec_grid = std::max(1, std::min(nc, 8 * sms));
     MG_TRY(dev_alloc_n(&b.probs, b.h_probs.size()));
     MG_TRY(dev_alloc_n(&b.bricks, b.h_bricks.size()));
     MG_TRY(dev_alloc_n(&b.chunks, b.h_chunks.size()));
     MG_TRY(dev_alloc_n(&b.states, (size_t)b.n_probs));
+    MG_TRY(dev_alloc_n(&b.tmaps, (size_t)b.n_probs * kMapsPerProblem));
     MG_CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&b.states_host), b.n_probs * sizeof(MfState)));
-    MG_TRY(dev_alloc_n(&b.E32, (size_t)el));
-    MG_TRY(dev_alloc_n(&b.E64, (size_t)el));
-    MG_TRY(dev_alloc_n(&b.dE64, (size_t)el));
+    MG_TRY(dev_alloc_n(&b.E32, (size_t)el + 4));
+    MG_TRY(dev_alloc_n(&b.E64, (size_t)el + 4));
+    MG_TRY(dev_alloc_n(&b.dE64, (size_t)el + 4));
     MG_TRY(dev_alloc_n(&b.node_fix, (size_t)nd));
-    float **f32s[] = {&b.x, &b.r, &b.z, &b.p0, &b.p1, &b.q, &b.dinv};
+    float **f32s[] = {&b.x, &b.r, &b.z, &b.p0, &b.p1, &b.q, &b.dinv, &b.xdbg,
+                      &b.mb, &b.mx, &b.md, &b.my, &b.mr};
     for (float **v : f32s) MG_TRY(dev_alloc_n(v, (size_t)dof));
     MG_TRY(dev_alloc_n(&b.u64, (size_t)dof));
     MG_TRY(dev_alloc_n(&b.r64, (size_t)dof));
@@ -982,29 +1530,50 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.brick_part, (size_t)nb));
     MG_TRY(dev_alloc_n(&b.chunk_part, (size_t)2 * nc));
     MG_TRY(dev_alloc_n(&b.err, 1));
-    MG_TRY(dev_alloc_n(&b.Bop_tf32, 768));
-    MG_TRY(dev_alloc_n(&b.Bop_bf16, 512));
+    MG_TRY(dev_alloc_n(&b.Bop, 2560));
     MG_TRY(dev_alloc_n(&b.K0, 576));
     double K0[576];
     hex8_box_stiffness(hx, hy, hz, nu, K0);
-    std::vector<uint32_t> tf, bf;
-    pack_b_operand(K0, tf, bf);
+    // Gershgorin bound of D^-1 A: every assembled row is a positive combination
+    // of K0 rows, so max_i sum_j |K0_ij| / K0_ii bounds it on every level
+    b.cheb_lmax = 0.0;
+    for (int i = 0; i < 24; i++) {
+        double sabs = 0.0;
+        for (int j = 0; j < 24; j++) sabs += fabs(K0[i * 24 + j]);
+        b.cheb_lmax = std::max(b.cheb_lmax, sabs / K0[i * 24 + i]);
+    }
+    std::vector<uint32_t> bop;
+    pack_b_operand(K0, bop);
+    // tensor maps: z, p0, p1, E, debug x per problem
+    std::vector<CUtensorMap> maps(b.n_probs * kMapsPerProblem);
+    for (int pi = 0; pi < b.n_probs; pi++) {
+        const MfProblem &P = b.h_probs[pi];
+        float *vecs[5] = {b.z, b.p0, b.p1, b.mx, b.md};
+        const int slot[5] = {0, 1, 2, 4, 5};
+        for (int k = 0; k < 5; k++)
+            MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + slot[k]], vecs[k] + P.dof_off,
+                            3 * (uint64_t)P.NX, P.NY, P.NZ, (uint64_t)P.pitch * 4,
+                            (uint64_t)P.pitch * P.NY * 4, kBoxNX, kBU, kBU));
+        MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 3], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
+                        (uint64_t)P.pitch_e * 4, (uint64_t)P.pitch_e * P.ny * 4, kBoxEX, kBE, kBE));
+    }
     cudaStream_t s = b.stream;
+    MG_CUDA_TRY(cudaMemcpyAsync(b.tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.probs, b.h_probs.data(), b.h_probs.size() * sizeof(MfProblem), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.bricks, b.h_bricks.data(), b.h_bricks.size() * sizeof(MfBrick), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
-    MG_CUDA_TRY(cudaMemcpyAsync(b.Bop_tf32, tf.data(), 768 * 4, cudaMemcpyHostToDevice, s));
-    MG_CUDA_TRY(cudaMemcpyAsync(b.Bop_bf16, bf.data(), 512 * 4, cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.Bop, bop.data(), bop.size() * 4, cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), s));
     MG_CUDA_TRY(cudaMemsetAsync(b.err, 0, sizeof(int), s));
     MG_CUDA_TRY(cudaMemsetAsync(b.u64, 0, dof * 8, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.r64, 0, dof * 8, s));
     MG_CUDA_TRY(cudaMemsetAsync(b.f64, 0, dof * 8, s));
     MG_CUDA_TRY(cudaMemsetAsync(b.node_fix, 0, nd, s));
-    MG_CUDA_TRY(cudaMemsetAsync(b.E32, 0, el * 4, s));
-    MG_CUDA_TRY(cudaMemsetAsync(b.E64, 0, el * 8, s));
-    MG_CUDA_TRY(cudaMemsetAsync(b.dE64, 0, el * 8, s));
-    float *zero_vecs[] = {b.x, b.r, b.z, b.p0, b.p1, b.q};
+    MG_CUDA_TRY(cudaMemsetAsync(b.E32, 0, (el + 4) * 4, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.E64, 0, (el + 4) * 8, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.dE64, 0, (el + 4) * 8, s));
+    float *zero_vecs[] = {b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.mb, b.mx, b.md, b.my, b.mr};
     for (float *v : zero_vecs) MG_CUDA_TRY(cudaMemsetAsync(v, 0, dof * 4, s));
     MG_CUDA_TRY(cudaStreamSynchronize(s));
     return MG_OK;
@@ -1013,76 +1582,271 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
 void mf_batch_free(MfBatch &b) {
     if (b.stream) cudaStreamSynchronize(b.stream);
     if (b.graph) cudaGraphExecDestroy(b.graph);
-    void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.E32, b.E64, b.dE64, b.node_fix,
-                    b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.u64, b.r64, b.f64, b.brick_part,
-                    b.chunk_part, b.err, b.Bop_tf32, b.Bop_bf16, b.K0};
+    if (b.graph_mg) cudaGraphExecDestroy(b.graph_mg);
+    void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
+                    b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
+                    b.f64, b.brick_part, b.chunk_part, b.err, b.Bop, b.K0, b.mb, b.mx, b.md,
+                    b.my, b.mr};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
-    if (b.owns_stream && b.stream) cudaStreamDestroy(b.stream);
     b = MfBatch();
 }
 
-int mf_batch_set_problem(MfBatch &b, int i, const uint8_t *node_fix_host, const double *f_host,
-                         const double *E_dev, const double *dE_dev) {
+int mf_batch_set_bc(MfBatch &b, int i, const uint8_t *node_fix_host, const double *f_host) {
     if (i < 0 || i >= b.n_probs) return MG_EINVAL;
     const MfProblem &P = b.h_probs[i];
-    const int64_t nn = (int64_t)P.NX * P.NY * P.NZ, ne = (int64_t)P.nx * P.ny * P.nz;
+    const int64_t nn = (int64_t)P.NX * P.NY * P.NZ;
     cudaStream_t s = b.stream;
-    if (node_fix_host)
+    if (node_fix_host) {
         MG_CUDA_TRY(cudaMemcpyAsync(b.node_fix + P.node_off, node_fix_host, nn, cudaMemcpyHostToDevice, s));
-    if (f_host)
-        MG_CUDA_TRY(cudaMemcpyAsync(b.f64 + P.dof_off, f_host, P.n_dofs * 8, cudaMemcpyHostToDevice, s));
-    if (E_dev) {
-        MG_CUDA_TRY(cudaMemcpyAsync(b.E64 + P.elem_off, E_dev, ne * 8, cudaMemcpyDeviceToDevice, s));
-        to_f32_kernel<<<blocks_for(ne, 256), 256, 0, s>>>(b.E64 + P.elem_off, b.E32 + P.elem_off, ne);
-        MG_CUDA_TRY(cudaGetLastError());
+        // coarse levels: a coarse node is constrained where its fine node (2I,2J,2K) is
+        std::vector<uint8_t> fine(node_fix_host, node_fix_host + nn), coarse;
+        for (int f = i; b.h_probs[f].coarse >= 0; f = b.h_probs[f].coarse) {
+            const MfProblem &F = b.h_probs[f], &C = b.h_probs[F.coarse];
+            coarse.assign((size_t)C.NX * C.NY * C.NZ, 0);
+            for (int K = 0; K < C.NZ; K++)
+                for (int J = 0; J < C.NY; J++)
+                    for (int I = 0; I < C.NX; I++)
+                        coarse[I + (size_t)C.NX * (J + (size_t)C.NY * K)] =
+                            fine[2 * I + (size_t)F.NX * (2 * J + (size_t)F.NY * 2 * K)];
+            MG_CUDA_TRY(cudaMemcpyAsync(b.node_fix + C.node_off, coarse.data(), coarse.size(),
+                                        cudaMemcpyHostToDevice, s));
+            MG_CUDA_TRY(cudaStreamSynchronize(s));
+            fine.swap(coarse);
+        }
     }
-    if (dE_dev)
-        MG_CUDA_TRY(cudaMemcpyAsync(b.dE64 + P.elem_off, dE_dev, ne * 8, cudaMemcpyDeviceToDevice, s));
+    if (f_host) {
+        std::vector<double> pad(P.n_pad, 0.0);
+        for (int64_t row = 0; row < (int64_t)P.NY * P.NZ; row++)
+            memcpy(pad.data() + row * P.pitch, f_host + row * 3 * P.NX, 3 * P.NX * sizeof(double));
+        MG_CUDA_TRY(cudaMemcpyAsync(b.f64 + P.dof_off, pad.data(), P.n_pad * 8, cudaMemcpyHostToDevice, s));
+        MG_CUDA_TRY(cudaStreamSynchronize(s));  // pad is a host temporary
+    }
+    if (node_fix_host) MG_CUDA_TRY(cudaStreamSynchronize(s));
     return MG_OK;
 }
 
-int mf_apply(MfBatch &b, int precision, const float *x, float *y) {
-    if (precision == MG_MIXED_TF32)
-        launch_apply<MG_MIXED_TF32, 0>(b, x, nullptr, nullptr, nullptr, y);
-    else
-        launch_apply<MG_MIXED_BF16, 0>(b, x, nullptr, nullptr, nullptr, y);
+int mf_batch_set_moduli(MfBatch &b, int i, const double *E_dev, const double *dE_dev) {
+    if (i < 0 || i >= b.n_probs) return MG_EINVAL;
+    const MfProblem &P = b.h_probs[i];
+    const int64_t ne = (int64_t)P.nx * P.ny * P.nz;
+    pack_elems_kernel<<<std::min(blocks_for(ne, 256), 4096u), 256, 0, b.stream>>>(
+        b.probs, i, E_dev, dE_dev, b.E32, b.E64, b.dE64);
     MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    if (E_dev)
+        for (int f = i; b.h_probs[f].coarse >= 0; f = b.h_probs[f].coarse) {
+            const int c = b.h_probs[f].coarse;
+            const MfProblem &C = b.h_probs[c];
+            const int64_t nc = (int64_t)C.nx * C.ny * C.nz;
+            dim3 grid(std::min(blocks_for(nc, 256), 4096u), 1);
+            mg_coarsen_kernel<<<grid, 256, 0, b.stream>>>(b.probs, c, b.E32);
+            MG_CUDA_TRY(cudaGetLastError());
+            count_launches(1);
+        }
+    return MG_OK;
+}
+
+int mf_batch_get_u(MfBatch &b, int i, double *u_dev) {
+    const MfProblem &P = b.h_probs[i];
+    unpack_vec_kernel<<<std::min(blocks_for(P.n_dofs, 256), 4096u), 256, 0, b.stream>>>(
+        b.probs, i, b.u64, u_dev, 1);
+    MG_CUDA_TRY(cudaGetLastError());
+    return MG_OK;
+}
+
+int mf_batch_set_u(MfBatch &b, int i, const double *u_dev) {
+    const MfProblem &P = b.h_probs[i];
+    unpack_vec_kernel<<<std::min(blocks_for(P.n_dofs, 256), 4096u), 256, 0, b.stream>>>(
+        b.probs, i, b.u64, const_cast<double *>(u_dev), 0);
+    MG_CUDA_TRY(cudaGetLastError());
+    return MG_OK;
+}
+
+int mf_apply(MfBatch &b, int precision, const double *x_host, double *y_host, int prob) {
+    MG_TRY(compute_diag(b));
+    const MfProblem &P = b.h_probs[prob];
+    std::vector<float> pad(P.n_pad, 0.0f);
+    for (int64_t row = 0; row < (int64_t)P.NY * P.NZ; row++)
+        for (int64_t k = 0; k < 3 * P.NX; k++) pad[row * P.pitch + k] = (float)x_host[row * 3 * P.NX + k];
+    MG_CUDA_TRY(cudaMemcpyAsync(b.mx + P.dof_off, pad.data(), P.n_pad * 4, cudaMemcpyHostToDevice, b.stream));
+    MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
+    ApplyArgs a{P.brick_begin, P.brick_begin + P.brick_count, 4, 0, nullptr, b.my};
+    launch_apply_prec<3>(b, precision, a);
+    MG_CUDA_TRY(cudaGetLastError());
+    MG_CUDA_TRY(cudaMemcpyAsync(pad.data(), b.my + P.dof_off, P.n_pad * 4, cudaMemcpyDeviceToHost, b.stream));
     MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
     int herr = 0;
     MG_CUDA_TRY(cudaMemcpy(&herr, b.err, sizeof(int), cudaMemcpyDeviceToHost));
     if (herr) {
-        set_error("tensor-core pipeline wait exceeded its bound");
+        set_error("tensor-core pipeline wait exceeded its bound (error flag %d)", herr);
         return MG_ETIMEDOUT;
     }
+    for (int64_t row = 0; row < (int64_t)P.NY * P.NZ; row++)
+        for (int64_t k = 0; k < 3 * P.NX; k++) y_host[row * 3 * P.NX + k] = pad[row * P.pitch + k];
     return MG_OK;
 }
 
+// enqueue `reps` CG-mode operator launches on the level-0 bricks (timing hook; no sync)
+int mf_launch_apply(MfBatch &b, int precision, int reps) {
+    MG_TRY(compute_diag(b));
+    MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
+    // nonzero search direction (zero on Dirichlet dofs) so every launch does the full work
+    fill_f32_kernel<<<blocks_for(b.n_pad, 256), 256, 0, b.stream>>>(b.z, b.dinv, 1.0f, b.n_pad);
+    for (int i = 0; i < reps; i++) launch_cg_apply(b, precision, 0, i & 1);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(reps + 2);
+    return MG_OK;
+}
+
+namespace {
+
+// precision of the multigrid smoothers: the single-product form of the family
+int mg_precision(int prec) {
+    return (prec == MG_MIXED_BF16 || prec == MG_MIXED_BF16X3) ? MG_MIXED_BF16 : MG_MIXED_TF32;
+}
+
+// Chebyshev coefficients for degree `deg` on [lmax/30, lmax]
+struct Cheb {
+    float inv_theta;
+    float c1[32], c2[32];
+};
+Cheb cheb_coeffs(double lmax, int deg) {
+    Cheb c{};
+    const double lmin = lmax / 30.0, theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    const double sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    c.inv_theta = (float)(1.0 / theta);
+    for (int k = 1; k < deg && k < 32; k++) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        c.c1[k] = (float)(rn * rho);
+        c.c2[k] = (float)(2.0 * rn / delta);
+        rho = rn;
+    }
+    return c;
+}
+
+// one Chebyshev smoothing pass of degree deg on level l: mx (+)= S(rin)
+long long enqueue_smooth(MfBatch &b, int prec, int l, const float *rin, int x0_zero, int deg,
+                         const Cheb &cc) {
+    const int clo = b.lvl_chunk_lo[l], chi = b.lvl_chunk_hi[l];
+    const int grid = std::max(1, std::min(chi - clo, b.vec_grid));
+    mg_cheb_first_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, rin,
+                                                          b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero);
+    long long n = 1;
+    for (int k = 1; k < deg; k++) {
+        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 5, 0, nullptr, b.my};
+        launch_apply_prec<3>(b, prec, a);
+        mg_cheb_next_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, b.my,
+                                                             b.mr, b.md, b.mx, b.dinv, cc.c1[k], cc.c2[k]);
+        n += 2;
+    }
+    return n;
+}
+
+// V-cycle z = M r on every design at once (level-0 rhs = CG residual r, z = mx)
+long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
+    const Cheb cs = cheb_coeffs(b.cheb_lmax, sdeg), cc = cheb_coeffs(b.cheb_lmax, cdeg);
+    const int L = b.n_levels;
+    long long n = 0;
+    for (int l = 0; l < L - 1; l++) {
+        const float *rin = (l == 0) ? b.r : b.mb;
+        n += enqueue_smooth(b, prec, l, rin, 1, sdeg, cs);
+        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my};
+        launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
+        const int clo = b.lvl_prob_lo[l + 1], chi = b.lvl_prob_hi[l + 1];
+        int64_t maxpad = 1;
+        for (int pi = clo; pi < chi; pi++) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
+        dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), chi - clo);
+        mg_restrict_kernel<<<grid, 256, 0, b.stream>>>(b.probs, clo, b.states, b.my, b.mb, b.dinv);
+        n += 2;
+    }
+    n += enqueue_smooth(b, prec, L - 1, L == 1 ? b.r : b.mb, 1, cdeg, cc);
+    for (int l = L - 2; l >= 0; l--) {
+        const float *rin = (l == 0) ? b.r : b.mb;
+        const int flo = b.lvl_prob_lo[l], fhi = b.lvl_prob_hi[l];
+        int64_t maxpad = 1;
+        for (int pi = flo; pi < fhi; pi++)
+            if (b.h_probs[pi].coarse >= 0) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
+        dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), fhi - flo);
+        mg_prolong_kernel<<<grid, 256, 0, b.stream>>>(b.probs, flo, b.states, b.mx, b.dinv);
+        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my};
+        launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
+        n += 2 + enqueue_smooth(b, prec, l, b.my, 0, sdeg, cs);
+    }
+    return n;
+}
+
+int build_graph_mg(MfBatch &b, int prec, int chunk, int sdeg, int cdeg, long long *launches) {
+    if (b.graph_mg && b.graph_mg_prec == prec && b.graph_mg_chunk == chunk &&
+        b.graph_mg_sdeg == sdeg && b.graph_mg_cdeg == cdeg)
+        return MG_OK;
+    if (b.graph_mg) {
+        cudaGraphExecDestroy(b.graph_mg);
+        b.graph_mg = nullptr;
+    }
+    const int mprec = mg_precision(prec);
+    const int n0 = b.lvl_chunk_hi[0];
+    long long n = 0;
+    cudaGraph_t g = nullptr;
+    MG_CUDA_TRY(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < chunk; it++) {
+        const int parity = it & 1;
+        float *pnew = parity ? b.p0 : b.p1;
+        launch_cg_apply(b, prec, 4, parity);  // p = z + beta p_old, q = A p, alpha
+        launch_update(b, pnew, true);         // x, r, stop test
+        n += 2 + enqueue_vcycle(b, mprec, sdeg, cdeg);
+        mf_dot_rz_kernel<<<std::max(1, std::min(n0, b.vec_grid)), kThreads, 0, b.stream>>>(
+            b.chunks, n0, b.probs, b.r, b.mx, b.states, b.chunk_part, 0);
+        n += 1;
+    }
+    cudaError_t e = cudaStreamEndCapture(b.stream, &g);
+    if (e != cudaSuccess) {
+        set_error("graph capture: %s", cudaGetErrorString(e));
+        return MG_ECUDA;
+    }
+    e = cudaGraphInstantiate(&b.graph_mg, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        set_error("graph instantiate: %s", cudaGetErrorString(e));
+        return MG_ECUDA;
+    }
+    b.graph_mg_prec = prec;
+    b.graph_mg_chunk = chunk;
+    b.graph_mg_sdeg = sdeg;
+    b.graph_mg_cdeg = cdeg;
+    *launches = n;
+    return MG_OK;
+}
+
+}  // namespace
+
 // FP64 iterative refinement around FP32 tensor-core CG:
 //   r = f - K u (FP64);  stop when ||r|| <= rtol ||f||;
-//   solve A d = r / ||r|| with FP32 CG to inner_rtol;  u += ||r|| d.
+//   solve A d = r / ||r|| with FP32 CG to inner_rtol (Jacobi or multigrid
+//   V-cycle preconditioned);  u += ||r|| d.
 int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start) {
     cudaStream_t s = b.stream;
     const double t0 = wall_time();
-    // Jacobi diagonal from the current moduli
-    {
-        dim3 grid(std::max(1u, std::min(blocks_for(b.n_dofs, 256), 4096u)), b.n_probs);
-        mf_diag_kernel<<<grid, 256, 0, s>>>(b.probs, b.n_probs, b.E32, b.node_fix, b.K0, b.dinv);
-        MG_CUDA_TRY(cudaGetLastError());
-        count_launches(2);
-    }
-    if (!warm_start) MG_CUDA_TRY(cudaMemsetAsync(b.u64, 0, b.n_dofs * 8, s));
+    const int n0 = b.lvl_chunk_hi[0];            // level-0 chunks
+    const int nb0 = b.lvl_brick_hi[0];           // level-0 bricks
+    const int vg0 = std::max(1, std::min(n0, b.vec_grid));
+    const bool use_mg = prm.mg && b.n_levels > 1;
+    const int sdeg = prm.smooth_deg > 0 ? prm.smooth_deg : 2;
+    const int cdeg = prm.coarse_deg > 0 ? prm.coarse_deg : 8;
+    MG_TRY(compute_diag(b));
+    if (!warm_start) MG_CUDA_TRY(cudaMemsetAsync(b.u64, 0, b.n_pad * 8, s));
     // reset states and compute ||f||^2 per problem
-    MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), s));
-    mf_dot_chunks_kernel<<<b.vec_grid, kThreads, 0, s>>>(b.chunks, b.n_chunks, b.f64, b.f64, b.chunk_part);
+    mf_dot_chunks_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.f64, b.f64, b.chunk_part);
     MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
     {
-        std::vector<double> part(b.n_chunks);
-        MG_CUDA_TRY(cudaMemcpyAsync(part.data(), b.chunk_part, b.n_chunks * 8, cudaMemcpyDeviceToHost, s));
+        std::vector<double> part(n0);
+        MG_CUDA_TRY(cudaMemcpyAsync(part.data(), b.chunk_part, n0 * 8, cudaMemcpyDeviceToHost, s));
         MG_CUDA_TRY(cudaStreamSynchronize(s));
         std::vector<MfState> init(b.n_probs);
         memset(init.data(), 0, init.size() * sizeof(MfState));
-        for (int i = 0; i < b.n_probs; i++) {
+        for (int i = 0; i < b.n_fine; i++) {
             const MfProblem &P = b.h_probs[i];
             double ff = 0;
             for (int c = 0; c < P.chunk_count; c++) ff += part[P.chunk_begin + c];
@@ -1090,59 +1854,67 @@ int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start) {
             if (ff == 0.0) init[i].ref_done = 1;  // zero load: u = 0
         }
         MG_CUDA_TRY(cudaMemcpyAsync(b.states, init.data(), b.n_probs * sizeof(MfState), cudaMemcpyHostToDevice, s));
+        MG_CUDA_TRY(cudaStreamSynchronize(s));
     }
-    const int chunk = prm.graph_chunk > 0 ? (prm.graph_chunk + 1) / 2 * 2 : 16;
-    MG_TRY(build_graph(b, prm.precision, chunk));
+    const int chunk = prm.graph_chunk > 0 ? (prm.graph_chunk + 1) / 2 * 2 : (use_mg ? 2 : 16);
+    long long per_graph = 2LL * chunk;
+    if (use_mg) MG_TRY(build_graph_mg(b, prm.precision, chunk, sdeg, cdeg, &per_graph));
+    else MG_TRY(build_graph(b, prm.precision, chunk));
     const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
     const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
     for (int ref = 0;; ref++) {
         // outer FP64 residual (also marks converged problems ref_done)
-        mf_residual64_kernel<<<b.apply_grid, kThreads, kResidSmem, s>>>(
-            b.probs, b.bricks, b.n_bricks, b.E64, b.node_fix, b.u64, b.f64, b.K0, b.r64, b.states,
+        mf_residual64_kernel<<<std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s>>>(
+            b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.K0, b.r64, b.states,
             b.brick_part, prm.rtol * prm.rtol, max_ref);
         MG_CUDA_TRY(cudaGetLastError());
         count_launches(1);
         MG_TRY(read_states(b));
         bool all_done = true;
-        for (int i = 0; i < b.n_probs; i++) all_done &= b.states_host[i].ref_done != 0;
+        for (int i = 0; i < b.n_fine; i++) all_done &= b.states_host[i].ref_done != 0;
         if (all_done) break;
         // inner FP32 CG on the normalised residual
-        mf_inner_init_kernel<<<b.vec_grid, kThreads, 0, s>>>(
-            b.chunks, b.n_chunks, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.dinv, b.states,
+        mf_inner_init_kernel<<<vg0, kThreads, 0, s>>>(
+            b.chunks, n0, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.dinv, b.states,
             b.chunk_part, prm.inner_rtol * prm.inner_rtol, maxit);
         MG_CUDA_TRY(cudaGetLastError());
         count_launches(1);
-        // problems already converged keep done = 1 through the inner loop
+        if (use_mg) {
+            // z0 = M r0, rz0 (beta = 0)
+            count_launches(enqueue_vcycle(b, mg_precision(prm.precision), sdeg, cdeg));
+            mf_dot_rz_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.probs, b.r, b.mx, b.states,
+                                                     b.chunk_part, 1);
+            MG_CUDA_TRY(cudaGetLastError());
+            count_launches(1);
+        }
         for (;;) {
             MG_TRY(read_states(b));
             bool inner_done = true;
-            for (int i = 0; i < b.n_probs; i++)
+            for (int i = 0; i < b.n_fine; i++)
                 inner_done &= (b.states_host[i].done != 0 || b.states_host[i].ref_done != 0);
             if (inner_done) break;
             if (prm.timeout_s > 0 && wall_time() - t0 > prm.timeout_s) {
                 set_error("mixed solve exceeded %.1f s", prm.timeout_s);
                 return MG_ETIMEDOUT;
             }
-            MG_CUDA_TRY(cudaGraphLaunch(b.graph, s));
-            count_launches(2LL * chunk);
+            MG_CUDA_TRY(cudaGraphLaunch(use_mg ? b.graph_mg : b.graph, s));
+            count_launches(per_graph);
         }
         // a breakdown/NaN in the inner solve ends that problem's refinement
-        {
-            for (int i = 0; i < b.n_probs; i++) {
-                MfState &h = b.states_host[i];
-                if (!h.ref_done && h.status != 0 && h.status != MG_ENOCONV) {
-                    h.ref_done = 1;
-                    h.ref_status = h.status;
-                }
-                if (!h.ref_done) h.refine += 1;
-                h.done = h.ref_done ? 1 : 0;
-                h.status = (h.status == MG_ENOCONV) ? 0 : h.status;
+        for (int i = 0; i < b.n_fine; i++) {
+            MfState &h = b.states_host[i];
+            if (!h.ref_done && h.status != 0 && h.status != MG_ENOCONV) {
+                h.ref_done = 1;
+                h.ref_status = h.status;
             }
-            // host copy of the per-problem flags goes back (counters are zero here)
-            MG_CUDA_TRY(cudaMemcpyAsync(b.states, b.states_host, b.n_probs * sizeof(MfState),
-                                        cudaMemcpyHostToDevice, s));
+            if (!h.ref_done) h.refine += 1;
+            h.done = h.ref_done ? 1 : 0;
+            h.status = (h.status == MG_ENOCONV) ? 0 : h.status;
         }
-        mf_refine_kernel<<<b.vec_grid, kThreads, 0, s>>>(b.chunks, b.n_chunks, b.x, b.u64, b.states);
+        // host copy of the per-problem flags goes back (counters are zero here)
+        MG_CUDA_TRY(cudaMemcpyAsync(b.states, b.states_host, b.n_fine * sizeof(MfState),
+                                    cudaMemcpyHostToDevice, s));
+        mf_refine_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.x, b.u64, b.states);
         MG_CUDA_TRY(cudaGetLastError());
         count_launches(1);
         if (prm.timeout_s > 0 && wall_time() - t0 > prm.timeout_s) {
@@ -1151,32 +1923,52 @@ int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start) {
         }
     }
     int rc = MG_OK;
-    for (int i = 0; i < b.n_probs; i++)
+    for (int i = 0; i < b.n_fine; i++)
         if (b.states_host[i].ref_status != 0) rc = b.states_host[i].ref_status;
     return rc;
 }
 
-int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_dev_all) {
+// compliance f.u per design (host) and dC/drho (unpadded, designs back to back
+// in problem order at dc_unpadded_dev) from the resident solutions
+int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded_dev) {
     cudaStream_t s = b.stream;
+    const int n0 = b.lvl_chunk_hi[0];
     if (compliance_host) {
-        mf_dot_chunks_kernel<<<b.vec_grid, kThreads, 0, s>>>(b.chunks, b.n_chunks, b.f64, b.u64, b.chunk_part);
+        mf_dot_chunks_kernel<<<std::max(1, std::min(n0, b.vec_grid)), kThreads, 0, s>>>(
+            b.chunks, n0, b.f64, b.u64, b.chunk_part);
         MG_CUDA_TRY(cudaGetLastError());
-        std::vector<double> part(b.n_chunks);
-        MG_CUDA_TRY(cudaMemcpyAsync(part.data(), b.chunk_part, b.n_chunks * 8, cudaMemcpyDeviceToHost, s));
+        std::vector<double> part(n0);
+        MG_CUDA_TRY(cudaMemcpyAsync(part.data(), b.chunk_part, n0 * 8, cudaMemcpyDeviceToHost, s));
         MG_CUDA_TRY(cudaStreamSynchronize(s));
-        for (int i = 0; i < b.n_probs; i++) {
+        for (int i = 0; i < b.n_fine; i++) {
             const MfProblem &P = b.h_probs[i];
             double c = 0;
             for (int k = 0; k < P.chunk_count; k++) c += part[P.chunk_begin + k];
             compliance_host[i] = c;
         }
     }
-    if (dc_dev_all) {
-        int64_t max_ne = 1;
-        for (auto &P : b.h_probs) max_ne = std::max<int64_t>(max_ne, (int64_t)P.nx * P.ny * P.nz);
-        dim3 grid(std::max(1u, std::min(blocks_for(max_ne, 128), 4096u)), b.n_probs);
-        mf_sens_kernel<<<grid, 128, 0, s>>>(b.probs, b.n_probs, b.dE64, b.node_fix, b.u64, b.K0, dc_dev_all);
-        MG_CUDA_TRY(cudaGetLastError());
+    if (dc_unpadded_dev) {
+        std::vector<int64_t> offs(b.n_fine);
+        int64_t o = 0, max_ne = 1;
+        for (int i = 0; i < b.n_fine; i++) {
+            const MfProblem &P = b.h_probs[i];
+            offs[i] = o;
+            o += (int64_t)P.nx * P.ny * P.nz;
+            max_ne = std::max<int64_t>(max_ne, (int64_t)P.nx * P.ny * P.nz);
+        }
+        int64_t *d_offs = nullptr;
+        MG_TRY(dev_alloc_n(&d_offs, (size_t)b.n_fine));
+        MG_CUDA_TRY(cudaMemcpyAsync(d_offs, offs.data(), b.n_fine * 8, cudaMemcpyHostToDevice, s));
+        dim3 grid(std::max(1u, std::min(blocks_for(max_ne, 128), 4096u)), b.n_fine);
+        mf_sens_kernel<<<grid, 128, 0, s>>>(b.probs, b.n_fine, b.dE64, b.node_fix, b.u64, b.K0,
+                                            d_offs, dc_unpadded_dev);
+        cudaError_t e = cudaGetLastError();
+        cudaStreamSynchronize(s);
+        dev_free(d_offs);
+        if (e != cudaSuccess) {
+            set_error("sensitivity kernel: %s", cudaGetErrorString(e));
+            return MG_ECUDA;
+        }
     }
     return MG_OK;
 }
@@ -1184,7 +1976,6 @@ int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_dev_all)
 // ----------------------------------------------------- single-problem mixed path
 struct MatfreeWork {
     MfBatch batch;
-    float *xs = nullptr, *ys = nullptr;
 };
 
 namespace {
@@ -1220,14 +2011,14 @@ int matfree_setup(mg_problem *p) {
     MatfreeWork *w = new MatfreeWork();
     MfProblem P{};
     P.nx = nx; P.ny = ny; P.nz = nz;
-    P.elem_off = -1;
+    P.share_elems = -1;
     int rc = mf_batch_init(w->batch, {P}, hx, hy, hz, p->mat.nu, p->stream);
     if (rc == MG_OK) {
         std::vector<uint8_t> nf(p->n_nodes, 0);
         for (int64_t n = 0; n < p->n_nodes; n++)
             for (int cc = 0; cc < 3; cc++)
                 if (p->h_fixed[n * 3 + cc]) nf[n] |= (uint8_t)(1u << cc);
-        rc = mf_batch_set_problem(w->batch, 0, nf.data(), p->h_F.data(), nullptr, nullptr);
+        rc = mf_batch_set_bc(w->batch, 0, nf.data(), p->h_F.data());
     }
     if (rc != MG_OK) {
         mf_batch_free(w->batch);
@@ -1243,9 +2034,9 @@ int matfree_setup(mg_problem *p) {
 int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
     MG_TRY(matfree_setup(p));
     MfBatch &b = p->mf->batch;
-    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
+    MG_TRY(mf_batch_set_moduli(b, 0, p->d_E, p->d_dE));
+    MG_TRY(mf_batch_set_u(b, 0, p->d_X));
     count_launches(1);
-    MG_CUDA_TRY(cudaMemcpyAsync(b.u64, p->d_X, p->n_dofs * 8, cudaMemcpyDeviceToDevice, p->stream));
     MfSolveParams prm;
     prm.precision = o.precision;
     prm.rtol = o.rtol;
@@ -1254,8 +2045,12 @@ int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
     prm.max_refinements = o.max_refinements;
     prm.graph_chunk = o.graph_chunk;
     prm.timeout_s = o.timeout_s;
+    prm.mg = (o.preconditioner == MG_PC_MULTIGRID) ? 1 : 0;
+    prm.smooth_deg = o.smooth_degree;
+    prm.coarse_deg = o.coarse_degree;
     int rc = mf_batch_solve(b, prm, true);
-    MG_CUDA_TRY(cudaMemcpyAsync(p->d_X, b.u64, p->n_dofs * 8, cudaMemcpyDeviceToDevice, p->stream));
+    MG_TRY(mf_batch_get_u(b, 0, p->d_X));
+    count_launches(1);
     MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
     const MfState &h = b.states_host[0];
     if (rep) {
@@ -1271,28 +2066,16 @@ int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
 int matfree_apply_debug(mg_problem *p, int precision, const double *x_host, double *y_host) {
     MG_TRY(matfree_setup(p));
     MfBatch &b = p->mf->batch;
-    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
-    MatfreeWork *w = p->mf;
-    if (!w->xs) {
-        MG_TRY(dev_alloc_n(&w->xs, (size_t)p->n_dofs));
-        MG_TRY(dev_alloc_n(&w->ys, (size_t)p->n_dofs));
-    }
-    std::vector<float> hx(p->n_dofs);
-    for (int64_t i = 0; i < p->n_dofs; i++) hx[i] = (float)x_host[i];
-    MG_CUDA_TRY(cudaMemcpyAsync(w->xs, hx.data(), p->n_dofs * 4, cudaMemcpyHostToDevice, p->stream));
-    MG_TRY(mf_apply(b, precision, w->xs, w->ys));
-    MG_CUDA_TRY(cudaMemcpyAsync(hx.data(), w->ys, p->n_dofs * 4, cudaMemcpyDeviceToHost, p->stream));
-    MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    for (int64_t i = 0; i < p->n_dofs; i++) y_host[i] = hx[i];
-    return MG_OK;
+    MG_TRY(mf_batch_set_moduli(b, 0, p->d_E, p->d_dE));
+    return mf_apply(b, precision, x_host, y_host, 0);
 }
 
 // dC/drho from the resident solution with the shared K0 (FP64)
 int matfree_sensitivity(mg_problem *p, double *dc_host) {
     MG_TRY(matfree_setup(p));
     MfBatch &b = p->mf->batch;
-    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
-    MG_CUDA_TRY(cudaMemcpyAsync(b.u64, p->d_X, p->n_dofs * 8, cudaMemcpyDeviceToDevice, p->stream));
+    MG_TRY(mf_batch_set_moduli(b, 0, p->d_E, p->d_dE));
+    MG_TRY(mf_batch_set_u(b, 0, p->d_X));
     MG_TRY(mf_batch_compliance(b, nullptr, p->d_elem_out));
     MG_CUDA_TRY(cudaMemcpyAsync(dc_host, p->d_elem_out, p->n_elems * 8, cudaMemcpyDeviceToHost, p->stream));
     MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
@@ -1312,26 +2095,12 @@ int matfree_compliance_resident(mg_problem *p, double *compliance) {
 int matfree_launch_apply(mg_problem *p, int precision, int reps) {
     MG_TRY(matfree_setup(p));
     MfBatch &b = p->mf->batch;
-    MG_TRY(mf_batch_set_problem(b, 0, nullptr, nullptr, p->d_E, p->d_dE));
-    MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
-    // nonzero search direction so that every timed launch does the full work
-    fill_f32_kernel<<<blocks_for(b.n_dofs, 256), 256, 0, b.stream>>>(b.z, 1.0f, b.n_dofs);
-    for (int i = 0; i < reps; i++) {
-        float *pold = (i & 1) ? b.p1 : b.p0, *pnew = (i & 1) ? b.p0 : b.p1;
-        if (precision == MG_MIXED_TF32)
-            launch_apply<MG_MIXED_TF32, 1>(b, nullptr, b.z, pold, pnew, b.q);
-        else
-            launch_apply<MG_MIXED_BF16, 1>(b, nullptr, b.z, pold, pnew, b.q);
-    }
-    MG_CUDA_TRY(cudaGetLastError());
-    count_launches(reps);
-    return MG_OK;
+    MG_TRY(mf_batch_set_moduli(b, 0, p->d_E, p->d_dE));
+    return mf_launch_apply(b, precision, reps);
 }
 
 void matfree_free(mg_problem *p) {
     if (!p->mf) return;
-    dev_free(p->mf->xs);
-    dev_free(p->mf->ys);
     mf_batch_free(p->mf->batch);
     delete p->mf;
     p->mf = nullptr;

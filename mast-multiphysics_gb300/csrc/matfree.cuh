@@ -3,6 +3,7 @@
 // batched solver and the request loop.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -12,26 +13,37 @@
 
 namespace mg {
 
-// Owned-node brick edge; a brick reads (kBN+2)^3 nodes and evaluates the
-// (kBN+1)^3 elements around its kBN^3 owned nodes.
+// Owned-node brick edge; a brick reads the (kBN+2)^3 node halo and evaluates
+// the (kBN+1)^3 elements around its kBN^3 owned nodes.
 constexpr int kBN = 8;
 constexpr int kBE = kBN + 1;
 constexpr int kBU = kBN + 2;
 constexpr int kNEL = kBE * kBE * kBE;          // 729 elements per brick
 constexpr int kNTILE = (kNEL + 127) / 128;     // 6 MMA tiles of 128 elements
-constexpr int kResStride = 25;                 // odd stride: conflict-free rows
-constexpr int kChunk = 4096;                   // dofs per vector-kernel chunk
+constexpr int kChunk = 1024;                   // dofs per vector-kernel chunk (one float4 per thread)
+constexpr int kMapsPerProblem = 6;             // z, p0, p1, E, mg x, mg d
+constexpr int kMaxLevels = 8;                  // multigrid levels per design
 
-// One structured problem (a design evaluation x one load case) in a batch.
+// Padded vector layout of one problem: node (i,j,k), component c lives at
+//   dof_off + (k NY + j) pitch + 3 i + c,   pitch = roundup(3 NX, 4)
+// so that every (j,k) row starts on a 16-byte boundary (TMA row strides).
+// Element moduli: elem_off + (k ny + j) pitch_e + i, pitch_e = roundup(nx, 4).
 struct MfProblem {
     int nx, ny, nz;       // elements
     int NX, NY, NZ;       // nodes
-    int64_t n_dofs;
-    int64_t dof_off;      // offset into the concatenated dof vectors
-    int64_t elem_off;     // offset into the element tables (E, dE)
-    int64_t node_off;     // offset into the node Dirichlet masks
+    int pitch, pitch_e;
+    int64_t n_dofs;       // 3 NX NY NZ
+    int64_t n_pad;        // pitch NY NZ
+    int64_t dof_off;      // offset into the concatenated padded dof vectors
+    int64_t elem_off;     // offset into the padded element tables (E32, E64, dE64)
+    int64_t node_off;     // offset into the node Dirichlet masks (unpadded)
     int brick_begin, brick_count;
     int chunk_begin, chunk_count;
+    int share_elems;      // >= 0: reuse the element tables of that problem (load cases)
+    int level;            // multigrid level (0 = the design's own grid)
+    int root;             // level-0 problem whose solver state drives this one
+    int coarse, fine;     // neighbouring levels (-1 if none)
+    int pad;
 };
 
 struct MfBrick {
@@ -42,7 +54,7 @@ struct MfBrick {
 struct MfChunkDesc {
     int prob;
     int pad;
-    int64_t begin, end;  // absolute dof range
+    int64_t begin, end;  // absolute padded dof range
 };
 
 // Per-problem solver state (device resident).
@@ -58,7 +70,7 @@ struct MfBatch {
     int n_probs = 0;
     int n_bricks = 0;
     int n_chunks = 0;
-    int64_t n_dofs = 0, n_elems = 0, n_nodes = 0;
+    int64_t n_pad = 0, n_elem_pad = 0, n_nodes = 0;
     std::vector<MfProblem> h_probs;
     std::vector<MfBrick> h_bricks;
     std::vector<MfChunkDesc> h_chunks;
@@ -67,50 +79,69 @@ struct MfBatch {
     MfChunkDesc *chunks = nullptr;
     MfState *states = nullptr;
     MfState *states_host = nullptr;  // pinned
+    CUtensorMap *tmaps = nullptr;    // kMapsPerProblem per problem
     // element / node tables
     float *E32 = nullptr;
     double *E64 = nullptr, *dE64 = nullptr;
     uint8_t *node_fix = nullptr;
-    // FP32 inner CG vectors
+    // FP32 inner CG vectors (padded layout)
     float *x = nullptr, *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr,
-          *dinv = nullptr;
-    // FP64 refinement vectors
+          *dinv = nullptr, *xdbg = nullptr;
+    // multigrid vectors (padded layout, every level): rhs, solution, Chebyshev
+    // direction, operator output, residual
+    float *mb = nullptr, *mx = nullptr, *md = nullptr, *my = nullptr, *mr = nullptr;
+    int n_fine = 0;             // level-0 problems (the designs); problems are ordered by level
+    int n_levels = 1;
+    std::vector<int> lvl_prob_lo, lvl_prob_hi, lvl_brick_lo, lvl_brick_hi, lvl_chunk_lo, lvl_chunk_hi;
+    double cheb_lmax = 0.0;     // Gershgorin bound of D^-1 A (same on every level)
+    cudaGraphExec_t graph_mg = nullptr;
+    int graph_mg_prec = -1, graph_mg_chunk = 0, graph_mg_sdeg = 0, graph_mg_cdeg = 0;
+    // FP64 refinement vectors (padded layout)
     double *u64 = nullptr, *r64 = nullptr, *f64 = nullptr;
     double *brick_part = nullptr, *chunk_part = nullptr;
     int *err = nullptr;
     // operator data
-    uint32_t *Bop_tf32 = nullptr, *Bop_bf16 = nullptr;  // K0 in the UMMA smem layout
-    double *K0 = nullptr;                               // 24x24 FP64, node-interleaved
+    uint32_t *Bop = nullptr;  // K0 in the UMMA smem layout: [tf32 hi|tf32 lo|bf16 hi|bf16 lo]
+    double *K0 = nullptr;     // 24x24 FP64, node-interleaved element order
     double hx = 1, hy = 1, hz = 1, nu = 0.3;
     cudaGraphExec_t graph = nullptr;
     int graph_prec = -1, graph_chunk = 0;
     int apply_grid = 0, vec_grid = 0;
     cudaStream_t stream = nullptr;
-    bool owns_stream = false;
 };
 
 struct MfSolveParams {
-    int precision;        // MG_MIXED_TF32 / MG_MIXED_BF16
+    int precision;        // MG_MIXED_*
     double rtol;          // FP64 outer residual target
     double inner_rtol;    // FP32 inner CG tolerance
     int max_iterations;   // inner cap per refinement
     int max_refinements;
     int graph_chunk;
     double timeout_s;
+    int mg;               // 1: geometric multigrid V-cycle preconditioner, 0: Jacobi
+    int smooth_deg;       // Chebyshev degree of the pre/post smoothers
+    int coarse_deg;       // Chebyshev degree on the coarsest level
 };
 
 // host-side element stiffness of an hx x hy x hz box at E = 1 in
 // node-interleaved element order (dof 3a + c)
 void hex8_box_stiffness(double hx, double hy, double hz, double nu, double K[576]);
 
+// shapes: the designs' own grids (level 0); max_levels > 1 adds the coarse
+// multigrid levels of every design (coarsening while all dims stay even)
 int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, double hy,
-                  double hz, double nu, cudaStream_t stream);
+                  double hz, double nu, cudaStream_t stream, int max_levels = kMaxLevels);
 void mf_batch_free(MfBatch &b);
-// per-problem Dirichlet masks, loads and moduli
-int mf_batch_set_problem(MfBatch &b, int i, const uint8_t *node_fix_host, const double *f_host,
-                         const double *E_dev, const double *dE_dev);
+// per-problem Dirichlet mask (per node, bit c = component c fixed) and load (unpadded host)
+int mf_batch_set_bc(MfBatch &b, int i, const uint8_t *node_fix_host, const double *f_host);
+// per-problem moduli from unpadded device arrays (E and dE/drho, n_elems each)
+int mf_batch_set_moduli(MfBatch &b, int i, const double *E_dev, const double *dE_dev);
 int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start);
-int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_dev_all);
-int mf_apply(MfBatch &b, int precision, const float *x, float *y);
+int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded_dev);
+// u (padded, FP64) <-> unpadded node-interleaved device vector of problem i
+int mf_batch_get_u(MfBatch &b, int i, double *u_dev);
+int mf_batch_set_u(MfBatch &b, int i, const double *u_dev);
+int mf_apply(MfBatch &b, int precision, const double *x_host, double *y_host, int prob);
+int mf_launch_apply(MfBatch &b, int precision, int reps);
 
 }  // namespace mg

@@ -82,8 +82,9 @@ def build(force=False, verbose=False):
 MG_OK, MG_EINVAL, MG_ENOMEM, MG_ENOCONV, MG_EBREAKDOWN, MG_ENAN = 0, -1, -2, -3, -4, -5
 MG_ETIMEDOUT, MG_ECUDA, MG_ENOTSUP, MG_EBUSY, MG_EBADELEM = -6, -7, -8, -9, -10
 PHYS_HEX8, PHYS_MEMBRANE, PHYS_HEAT = 0, 1, 2
-PLAIN_FP64, MIXED_TF32, MIXED_BF16 = 0, 1, 2
+PLAIN_FP64, MIXED_TF32, MIXED_BF16, MIXED_TF32X3, MIXED_BF16X3 = 0, 1, 2, 3, 4
 KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
+PC_JACOBI, PC_MULTIGRID = 0, 1
 PARAM_DENSITY, PARAM_K0, PARAM_ELEM_SCALE = 0, 1, 2
 
 _vp = ctypes.c_void_p
@@ -112,7 +113,9 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", _i32), ("krylov", _i32), ("max_iterations", _i32),
                 ("max_newton", _i32), ("rtol", _dbl), ("newton_rtol", _dbl),
                 ("consistent_jacobian", _i32), ("max_refinements", _i32), ("inner_rtol", _dbl),
-                ("timeout_s", _dbl), ("warm_start", _i32), ("graph_chunk", _i32)]
+                ("timeout_s", _dbl), ("warm_start", _i32), ("graph_chunk", _i32),
+                ("preconditioner", _i32), ("smooth_degree", _i32), ("coarse_degree", _i32),
+                ("reserved", _i32)]
 
 
 class SolveReport(ctypes.Structure):

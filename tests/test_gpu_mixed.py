@@ -15,15 +15,16 @@ import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-TOL_OP = {M.MIXED_TF32: 4e-3, M.MIXED_BF16: 3e-2}
+TOL_OP = {M.MIXED_TF32: 4e-3, M.MIXED_BF16: 3e-2, M.MIXED_TF32X3: 2e-5, M.MIXED_BF16X3: 2e-4}
+ALL = [M.MIXED_TF32, M.MIXED_BF16, M.MIXED_TF32X3, M.MIXED_BF16X3]
 
 
 def rel(a, b):
     return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
 
 
-@pytest.mark.parametrize("prec", [M.MIXED_TF32, M.MIXED_BF16])
-@pytest.mark.parametrize("shape", [(8, 4, 4), (16, 8, 8), (12, 7, 5)])
+@pytest.mark.parametrize("prec", ALL)
+@pytest.mark.parametrize("shape", [(8, 4, 4), (16, 8, 8), (12, 7, 5), (17, 9, 3)])
 def test_operator_matches_fp64_csr(prec, shape):
     nx, ny, nz = shape
     rng = np.random.default_rng(1)
@@ -40,13 +41,15 @@ def test_operator_matches_fp64_csr(prec, shape):
     assert rel(y, y_ref) < TOL_OP[prec]
 
 
-@pytest.mark.parametrize("prec", [M.MIXED_TF32, M.MIXED_BF16])
-def test_mixed_solve_matches_oracle(prec):
+@pytest.mark.parametrize("pc", [M.PC_MULTIGRID, M.PC_JACOBI])
+@pytest.mark.parametrize("prec", [M.MIXED_TF32, M.MIXED_TF32X3, M.MIXED_BF16X3])
+def test_mixed_solve_matches_oracle(prec, pc):
     nx, ny, nz = 16, 8, 8
     rho = np.random.default_rng(3).uniform(0.01, 1.0, nx * ny * nz)
     with M.simp_cantilever(nx, ny, nz) as p:
         p.set_design(rho)
-        u, rep = p.solve(M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3))
+        u, rep = p.solve(M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3,
+                                        preconditioner=pc))
         c, dc = p.compliance()
     assert rep.status == 0 and rep.relres <= 1e-8, (rep.status, rep.relres)
     _, dc_ref, r = O.simp_solve(O.simp_desc(nx, ny, nz, rtol=1e-12, maxit=10 ** 6), rho)
@@ -64,3 +67,35 @@ def test_mixed_solve_is_deterministic():
             u, rep = p.solve(M.default_opts(precision=M.MIXED_TF32, rtol=1e-8))
             outs.append((u, rep.krylov_iterations))
     assert np.array_equal(outs[0][0], outs[1][0]) and outs[0][1] == outs[1][1]
+
+
+def test_single_pass_bf16_reports_its_limit():
+    """One BF16 product per element (8-bit operand mantissa) stalls the FP64
+    refinement on this contrast (1e6); the solve must end with MG_ENOCONV and a
+    finite residual, never a hang or NaN.  MIXED_BF16X3 is the BF16 variant
+    that reaches 1e-8."""
+    nx, ny, nz = 16, 8, 8
+    rho = np.random.default_rng(3).uniform(0.01, 1.0, nx * ny * nz)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        _, rep = p.solve(M.default_opts(precision=M.MIXED_BF16, rtol=1e-8, max_refinements=8,
+                                        preconditioner=M.PC_JACOBI), raise_on_error=False)
+    assert rep.status in (M.MG_OK, M.MG_ENOCONV) and np.isfinite(rep.relres)
+
+
+@pytest.mark.parametrize("shape", [(32, 16, 16), (24, 12, 8)])
+def test_multigrid_cuts_iterations(shape):
+    """The multigrid V-cycle (Chebyshev-Jacobi smoothers, rediscretised coarse
+    grids) preconditions the same FP32 CG: same answer, far fewer iterations."""
+    nx, ny, nz = shape
+    rho = np.random.default_rng(6).uniform(0.01, 1.0, nx * ny * nz)
+    out = {}
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        for pc in (M.PC_JACOBI, M.PC_MULTIGRID):
+            u, rep = p.solve(M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8, preconditioner=pc))
+            c, _ = p.compliance(want_sens=False)
+            out[pc] = (rep.krylov_iterations, c, rep.relres)
+    assert out[M.PC_MULTIGRID][2] <= 1e-8 and out[M.PC_JACOBI][2] <= 1e-8
+    assert abs(out[M.PC_MULTIGRID][1] - out[M.PC_JACOBI][1]) / out[M.PC_JACOBI][1] < 1e-7
+    assert out[M.PC_MULTIGRID][0] * 4 < out[M.PC_JACOBI][0]
