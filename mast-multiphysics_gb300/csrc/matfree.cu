@@ -56,6 +56,7 @@ struct Prec {
     static constexpr int kCols = kTf32 ? 6 : 4;     // 16-byte core columns per A row
     static constexpr int kKsteps = kTf32 ? 3 : 2;   // MMAs per A/B pair (K = 8 / 16 each)
     static constexpr uint32_t kSbo = kCols * 128;   // bytes between 8-row groups
+    static constexpr int kStages = 2;                // tiles in flight in the MMA ring
 };
 
 // ------------------------------------------------------------------ PTX helpers
@@ -275,17 +276,23 @@ constexpr int kBoxEX = 12;
 constexpr int kBoxElemBytes = kBoxEX * kBE * kBE * 4;  // 3888
 constexpr int kResStride = 25;
 constexpr int kApplyThreads = 512;
+// the thread that issues and waits for the MMAs: warp 12 has no TMEM drain
+// role, so the draining warps are not held up by MMA issue
+constexpr int kIssuer = 384;
 
 constexpr int kOffB = 0;                                   // B: hi at 0, lo at 4096
-constexpr int kOffA = 8192;                                // 2 buffers x (hi, lo) x 12 KB
+constexpr int kOffA = 8192;                                // MMA ring: 4 x 12 KB operand slots
 constexpr int kABytes = 12288;
-constexpr int kOffBox = kOffA + 4 * kABytes;               // 57344: 2 x (z, p, E)
+constexpr int kASlots = 4;                                 // 2 stages x (hi, lo)
+constexpr int kOffBox = kOffA + kASlots * kABytes;         // 57344: 2 x (z, p, E)
 constexpr int kBoxSet = 12800 + 12800 + 3968;              // 29568 (multiple of 128)
-constexpr int kOffRes = kOffBox + 2 * kBoxSet;             // 116480
+constexpr int kOffRes = kOffBox + 2 * kBoxSet;             // 116480 (multiple of 4)
 constexpr int kOffBar = kOffRes + kNEL * kResStride * 4;   // 189380 -> aligned below
 constexpr int kOffBarA = (kOffBar + 127) / 128 * 128;
 constexpr int kApplySmem = kOffBarA + 64;
 static_assert(kOffBox % 128 == 0 && kBoxSet % 128 == 0, "TMA destinations");
+static_assert(2 * Prec<MG_MIXED_TF32X3>::kStages <= kASlots &&
+              2 * Prec<MG_MIXED_BF16X3>::kStages <= kASlots, "MMA ring slots");
 
 // offset of element-row value k (node a = k/3, component c) inside the node box,
 // relative to the element's base corner
@@ -315,8 +322,8 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
     __shared__ int sh_last;
     uint8_t *sB = smem + kOffB;
     float *sres = reinterpret_cast<float *>(smem + kOffRes);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kOffBarA);  // tma[2], mma[2]
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBarA + 48);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kOffBarA);  // tma[2], mma[4]
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBarA + 56);
     const uint32_t tma_bar0 = smem_u32(&bars[0]);
     const uint32_t mma_bar0 = smem_u32(&bars[2]);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -330,10 +337,9 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
     if (tid == 0) {
         mbar_init(tma_bar0, 1);
         mbar_init(tma_bar0 + 8, 1);
-        mbar_init(mma_bar0, 1);
-        mbar_init(mma_bar0 + 8, 1);
+        for (int k = 0; k < 4; k++) mbar_init(mma_bar0 + 8 * k, 1);
     }
-    if (warp == 0) tmem_alloc(smem_u32(tslot), 64);
+    if (warp == 0) tmem_alloc(smem_u32(tslot), 128);  // kStages x 32 accumulator columns
     {
         // B operands: [tf32 hi 768 | tf32 lo 768 | bf16 hi 512 | bf16 lo 512] words
         const uint32_t *src = Bop + (PR::kTf32 ? 0 : 1536);
@@ -374,7 +380,7 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
         obox[j] = ((oz + 1) * kBU + oy + 1) * kBoxNX + 3 * (ox + 1) + c + 1;
     }
 
-    uint32_t tma_phase[2] = {0, 0}, mma_phase[2] = {0, 0};
+    uint32_t tma_phase[2] = {0, 0}, mma_phase[4] = {0, 0, 0, 0};
     bool failed = false;
     // TMA issue for brick `b` into box set `set`
     auto issue_tma = [&](int b, int set) {
@@ -396,6 +402,7 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
         issue_tma(bi, 0);
     }
     int set = 0;
+    int run = 0;  // bricks of the current problem since the last counter update (MODE 1)
     for (; bi < n_bricks && !failed;) {
         // next usable brick of this block, prefetched into the other box set
         int nbi = bi + gridDim.x;
@@ -421,11 +428,13 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
             fence_async_smem();
             issue_tma(nbi, set ^ 1);  // the other set was released at the end of the last brick
         }
-        // ---- tiles: build A(t) | wait MMA(t-1) | barrier | MMA(t) issue, drain t-1
-        for (int t = 0; t <= kNTILE; t++) {
+        // ---- tiles through a kStages-deep MMA ring:
+        //      build A(t) | wait MMA(t-S+1) | barrier | issue MMA(t) | drain t-S+1
+        constexpr int S = PR::kStages;
+        for (int t = 0; t < kNTILE + S - 1; t++) {
             if (t < kNTILE) {
-                const int buf = t & 1;
-                uint8_t *A_hi = smem + kOffA + (buf * 2) * kABytes;
+                const int slot = t % S;
+                uint8_t *A_hi = smem + kOffA + (PR::kSplit ? 2 * slot : slot) * kABytes;
                 uint8_t *A_lo = A_hi + kABytes;
                 const int l = t * 128 + arow;
                 int base = -1;
@@ -470,48 +479,48 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
                     if (PR::kSplit) *reinterpret_cast<uint4 *>(A_lo + off) = wlo;
                 }
             }
-            // MMA(t-1) must be complete before its accumulator is drained and before
-            // A[(t+1)&1] (= A[(t-1)&1]) is rewritten in the next iteration
+            // the oldest tile in flight must be complete before it is drained and
+            // before its operand slot is rewritten in the next iteration
+            const int td = t - (S - 1);
             bool ok = true;
-            if (t >= 1 && tid == 0) {
-                const int bufp = (t - 1) & 1;
-                ok = mbar_wait_bounded(mma_bar0 + 8 * bufp, mma_phase[bufp]);
-            }
-            if (t >= 1) mma_phase[(t - 1) & 1] ^= 1u;
+            if (td >= 0 && tid == kIssuer)
+                ok = mbar_wait_bounded(mma_bar0 + 8 * (td % S), mma_phase[td % S]);
+            if (td >= 0) mma_phase[td % S] ^= 1u;
             fence_async_smem();
             fence_before();
             if (__syncthreads_or(!ok)) {
                 failed = true;
-                if (tid == 0) atomicOr(err, 1);
+                if (tid == kIssuer) atomicOr(err, 1);
                 break;
             }
             fence_after();
-            if (t < kNTILE && tid == 0) {
-                const int buf = t & 1;
-                const uint32_t a_hi = smem_u32(smem + kOffA + (buf * 2) * kABytes), a_lo = a_hi + kABytes;
-                const uint32_t d = tmem + buf * 32;
+            if (t < kNTILE && tid == kIssuer) {
+                const int slot = t % S;
+                const uint32_t a_hi = smem_u32(smem + kOffA + (PR::kSplit ? 2 * slot : slot) * kABytes);
+                const uint32_t a_lo = a_hi + kABytes;
+                const uint32_t d = tmem + slot * 32;
 #pragma unroll
-                for (int s = 0; s < PR::kKsteps; s++)
-                    umma<PR::kTf32>(d, umma_desc(a_hi + s * 256, 128, PR::kSbo),
-                                    umma_desc(b_hi + s * 256, 128, PR::kSbo), s > 0 ? 1u : 0u);
+                for (int k = 0; k < PR::kKsteps; k++)
+                    umma<PR::kTf32>(d, umma_desc(a_hi + k * 256, 128, PR::kSbo),
+                                    umma_desc(b_hi + k * 256, 128, PR::kSbo), k > 0 ? 1u : 0u);
                 if (PR::kSplit) {
 #pragma unroll
-                    for (int s = 0; s < PR::kKsteps; s++) {
-                        umma<PR::kTf32>(d, umma_desc(a_hi + s * 256, 128, PR::kSbo),
-                                        umma_desc(b_lo + s * 256, 128, PR::kSbo), 1u);
-                        umma<PR::kTf32>(d, umma_desc(a_lo + s * 256, 128, PR::kSbo),
-                                        umma_desc(b_hi + s * 256, 128, PR::kSbo), 1u);
+                    for (int k = 0; k < PR::kKsteps; k++) {
+                        umma<PR::kTf32>(d, umma_desc(a_hi + k * 256, 128, PR::kSbo),
+                                        umma_desc(b_lo + k * 256, 128, PR::kSbo), 1u);
+                        umma<PR::kTf32>(d, umma_desc(a_lo + k * 256, 128, PR::kSbo),
+                                        umma_desc(b_hi + k * 256, 128, PR::kSbo), 1u);
                     }
                 }
-                umma_commit(mma_bar0 + 8 * buf);
+                umma_commit(mma_bar0 + 8 * slot);
             }
-            if (t >= 1) {
-                // drain tile t-1 while MMA(t) runs: rows of lane group lg, 8 columns per group cg
-                const int tp = t - 1, bufp = tp & 1, lg = warp & 3, cg = warp >> 2;
+            if (td >= 0) {
+                // drain tile td: rows of lane group lg, 8 columns per column group cg
+                const int slot = td % S, lg = warp & 3, cg = warp >> 2;
                 if (cg < 3) {
-                    const int m = lg * 32 + lane, l = tp * 128 + m;
+                    const int m = lg * 32 + lane, l = td * 128 + m;
                     float v[8];
-                    tmem_ld8(tmem + bufp * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
+                    tmem_ld8(tmem + slot * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
                     if (l < kNEL) {
                         const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
                         const float e = sE[(ez * kBE + ey) * kBoxEX + ex + 3];
@@ -553,22 +562,34 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
             }
         }
         if (MODE == 1) {
-            // block sum of the brick partial (FP32 within a warp, FP64 across warps:
-            // FP64 issue is scarce on this part), then the per-problem reduction
+            // brick partial: FP32 within a warp, FP64 across warps (FP64 issue is
+            // scarce on this part)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
             if (lane == 0) red_sh[warp] = (double)part;
-            __syncthreads();
+        }
+        __syncthreads();  // box set, sres and red_sh are complete and may be reused
+        if (MODE == 1) {
+            // red_sh is rewritten only after the next brick's tile barriers
             if (tid == 0) {
                 double s = 0.0;
                 for (int w = 0; w < kApplyThreads / 32; w++) s += red_sh[w];
                 brick_part[bi] = s;
-                __threadfence();
-                const unsigned tk = atomicAdd(&st->cnt_apply, 1u);
-                sh_last = (tk == (unsigned)P.brick_count - 1);
             }
-            __syncthreads();
-            if (sh_last) {
+            // the per-problem counter is bumped once per run of consecutive
+            // bricks of one problem (one fence and one atomic per run)
+            run++;
+            const bool flush = nbi >= n_bricks || bricks[nbi].prob != br.prob;
+            if (flush) {
+                if (tid == 0) {
+                    __threadfence();
+                    const unsigned tk = atomicAdd(&st->cnt_apply, (unsigned)run);
+                    sh_last = (tk + (unsigned)run == (unsigned)P.brick_count);
+                }
+                run = 0;
+                __syncthreads();
+            }
+            if (flush && sh_last) {
                 double s = 0.0;
                 for (int k = tid; k < P.brick_count; k += kApplyThreads)
                     s += __ldcg(brick_part + P.brick_begin + k);
@@ -588,7 +609,6 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
                 }
             }
         }
-        __syncthreads();  // box set and sres are reused
         bi = nbi;
         set ^= 1;
     }
@@ -601,7 +621,7 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 64);
+    if (warp == 0) tmem_dealloc(tmem, 128);
 }
 
 // ---------------------------------------------------------------- vector phase
@@ -1779,8 +1799,10 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
 
 int build_graph_mg(MfBatch &b, int prec, int chunk, int sdeg, int cdeg, long long *launches) {
     if (b.graph_mg && b.graph_mg_prec == prec && b.graph_mg_chunk == chunk &&
-        b.graph_mg_sdeg == sdeg && b.graph_mg_cdeg == cdeg)
+        b.graph_mg_sdeg == sdeg && b.graph_mg_cdeg == cdeg) {
+        *launches = b.graph_mg_launches;
         return MG_OK;
+    }
     if (b.graph_mg) {
         cudaGraphExecDestroy(b.graph_mg);
         b.graph_mg = nullptr;
@@ -1815,6 +1837,7 @@ int build_graph_mg(MfBatch &b, int prec, int chunk, int sdeg, int cdeg, long lon
     b.graph_mg_chunk = chunk;
     b.graph_mg_sdeg = sdeg;
     b.graph_mg_cdeg = cdeg;
+    b.graph_mg_launches = n;
     *launches = n;
     return MG_OK;
 }

@@ -96,6 +96,7 @@ struct MfBatch {
     double cheb_lmax = 0.0;     // Gershgorin bound of D^-1 A (same on every level)
     cudaGraphExec_t graph_mg = nullptr;
     int graph_mg_prec = -1, graph_mg_chunk = 0, graph_mg_sdeg = 0, graph_mg_cdeg = 0;
+    long long graph_mg_launches = 0;
     // FP64 refinement vectors (padded layout)
     double *u64 = nullptr, *r64 = nullptr, *f64 = nullptr;
     double *brick_part = nullptr, *chunk_part = nullptr;
