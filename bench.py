@@ -51,7 +51,112 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=40, help="PCG iterations in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 256-design batch section")
+    ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
+    ap.add_argument("--serve-requests", type=int, default=1000, help="requests per arrival rate")
+    ap.add_argument("--kernel-only", default=None, choices=["mixed", "plain"],
+                    help="only launch the dominant kernel (tensor-core brick operator or the "
+                         "FP64 CG SpMV) --steps times after --warmup launches; for profilers")
     return ap.parse_args()
+
+
+PROFILE = os.path.join(REPO, "profiles", "mf_apply_kernel_tf32x3_128x64x64.txt")
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the brick operator from the committed ncu
+    summary (line 'dram_bytes_per_launch = N'), or None."""
+    try:
+        for line in open(PROFILE):
+            if line.strip().startswith("dram_bytes_per_launch"):
+                return int(line.split("=")[1].split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
+def kernel_only(args, M, prob, prec, rho):
+    """Launch only the dominant kernel (no solve) so that a profiler sees a
+    short, regular launch list: setup, then --warmup + --steps launches."""
+    import torch
+    prob.set_design(rho)  # the plain launch hook assembles the CSR on first use
+    p = M.PLAIN_FP64 if args.kernel_only == "plain" else prec
+    M.check(M.lib().mg_debug_launch_apply(prob.h, p, max(1, args.warmup)), "warm")
+    torch.cuda.synchronize()
+    M.check(M.lib().mg_debug_launch_apply(prob.h, p, max(1, args.steps)), "launch")
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel_only": args.kernel_only, "launches": args.warmup + args.steps}))
+
+
+def plain_time_per_size(M, sizes, rtol=1e-8):
+    """Seconds of one plain FP64 CSR Jacobi-PCG solve (one load case over the full
+    x = max, z = 0 edge, densities U[0.01,1]) per grid size, on this GPU."""
+    out = {}
+    for (nx, ny, nz) in sizes:
+        rho = np.random.default_rng(1).uniform(0.01, 1.0, nx * ny * nz)
+        with M.simp_cantilever(nx, ny, nz) as p:
+            p.set_design(rho)
+            o = M.default_opts(precision=M.PLAIN_FP64, rtol=rtol, timeout_s=600.0)
+            p.solve(o)  # assembly, graph capture
+            t0 = time.perf_counter()
+            p.solve(o)
+            p.compliance()
+            out[(nx, ny, nz)] = time.perf_counter() - t0
+    return out
+
+
+def bench_batch(M, n_designs=256, seed=0):
+    """Batched design evaluations: n_designs SIMP cantilevers of mixed sizes with
+    1-4 load cases each, all solved together (mixed form, autotuned schedule)."""
+    designs = M.batch_designs(n_designs, seed=seed)
+    b = M.Batch(designs)
+    o = M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0)
+    t0 = time.perf_counter()
+    o, trial_s = b.autotune(o, max_trials=12)
+    tune_s = time.perf_counter() - t0
+    b.solve(o)  # warm-up: graph capture
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        rc, reps = b.solve(o)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    relres = max(r.relres for r in reps)
+    # plain FP64 estimate: one solve per problem at that problem's size
+    sizes = sorted({(d["nx"], d["ny"], d["nz"]) for d in designs})
+    tp = plain_time_per_size(M, sizes)
+    t_plain = sum(tp[(d["nx"], d["ny"], d["nz"])] * len(d["spans"]) for d in designs)
+    res = {"workload": "simp_batch_%d_designs_mixed_sizes" % n_designs,
+           "n_designs": b.n_designs, "n_problems": b.n_problems, "n_dofs": b.n_dofs,
+           "seconds": t, "solves_per_s": b.n_problems / t, "designs_per_s": b.n_designs / t,
+           "dofs_per_s": b.n_dofs / t, "max_relres_fp64": relres,
+           "all_converged": all(r.status == 0 for r in reps),
+           "autotuned": {"precision": o.precision, "smooth_degree": o.smooth_degree,
+                         "coarse_degree": o.coarse_degree, "graph_chunk": o.graph_chunk,
+                         "vec_blocks_per_sm": o.vec_blocks_per_sm, "inner_rtol": o.inner_rtol,
+                         "tuning_seconds": tune_s},
+           "plain_fp64_est_solves_per_s": b.n_problems / t_plain,
+           "plain_fp64_method": "one timed plain solve per grid size x the batch's load cases",
+           "speedup_vs_plain_fp64": t_plain / t}
+    b.close()
+    return res
+
+
+def bench_serve(M, rates, n_requests, big=True, seed=0):
+    """Request loop: Poisson streams over 64 design chains (config-4 mix)."""
+    o = M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0)
+    sweep = []
+    for rate, n in zip(rates, n_requests):
+        with M.Server(o, hbm_cap_bytes=150 << 30) as s:
+            st, comp = s.run_synthetic(n, rate=rate, n_chains=64, big_fraction=0.02 if big else 0.0,
+                                       seed=seed)
+        sweep.append({"rate_req_per_s": rate, "n_requests": n, "completed": st["completed"],
+                      "failed": st["failed"], "p50_ms": st["p50_s"] * 1e3, "p99_ms": st["p99_s"] * 1e3,
+                      "mean_ms": st["mean_s"] * 1e3, "solves_per_s": st["solves_per_s"],
+                      "dofs_per_s": st["dofs_per_s"], "peak_inflight": st["peak_inflight"],
+                      "rebuilds": st["rebuilds"], "peak_resident_GB": st["peak_resident_bytes"] / 1e9})
+    return {"workload": "simp_serving_64_chains_poisson", "hbm_cap_GB": 150, "sweep": sweep}
 
 
 def dist_env():
@@ -194,6 +299,10 @@ def main():
     pc = M.PC_MULTIGRID if args.preconditioner == "multigrid" else M.PC_JACOBI
     opts = M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0,
                           preconditioner=pc)
+    if args.kernel_only:
+        kernel_only(args, M, prob, prec, rho)
+        prob.close()
+        return
 
     def step_resident():
         prob.set_design_device(d_rho.data_ptr())
@@ -242,7 +351,7 @@ def main():
     # ---------------- e2e: host buffers through the C ABI
     X0 = np.zeros(prob.n_dofs)
     e2e_ms = []
-    for i in range(max(1, args.steps)):
+    for i in range(0 if args.no_e2e else max(1, args.steps)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -250,10 +359,14 @@ def main():
         u, rep = prob.solve(opts, X=X0)
         c, dch = prob.compliance()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    if args.no_e2e:
+        c, dch = prob.compliance()
+        e2e = None
+    else:
+        e2e = {"value": world * 1e3 / (sum(e2e_ms) / len(e2e_ms)), "unit": "solves/s",
+               "h2d_bytes_per_step": int(rho.nbytes + X0.nbytes),
+               "d2h_bytes_per_step": int(X0.nbytes + NX * NY * NZ * 8 + 8)}
     dc_err = float(np.abs(dch - g["dc"]).max() / np.abs(g["dc"]).max())
-    e2e_val = world * 1e3 / (sum(e2e_ms) / len(e2e_ms))
-    h2d = rho.nbytes + X0.nbytes
-    d2h = u.nbytes + dch.nbytes + 8
 
     # ---------------- dominant kernel: tensor-core brick operator, timed alone
     n = prob.n_dofs
@@ -276,7 +389,8 @@ def main():
     roof = {"kernel": "mf_apply_kernel (tcgen05 %s brick operator, CG step)" % args.precision,
             "bound": "hbm", "achieved": alg_bytes / (k_ms * 1e-3) / 1e9, "peak": peak,
             "unit": "GB/s", "frac": alg_bytes / (k_ms * 1e-3) / 1e9 / peak,
-            "traffic": None, "bytes_per_launch": alg_bytes, "us_per_launch": k_ms * 1e3,
+            "traffic": profiled_traffic(), "traffic_source": os.path.relpath(PROFILE, REPO),
+            "bytes_per_launch": alg_bytes, "us_per_launch": k_ms * 1e3,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback"}
 
     # ---------------- plain FP64 form on the same GPU
@@ -314,6 +428,19 @@ def main():
                  "spmv_us": sp_ms * 1e3, "spmv_GBps": sp_bytes / (sp_ms * 1e-3) / 1e9,
                  "spmv_frac": sp_bytes / (sp_ms * 1e-3) / 1e9 / peak}
 
+    batch = None if args.no_batch else bench_batch(M)
+    serve = None
+    if not args.no_serve:
+        rates = [50, 200, 500, 1000, 2000]
+        serve = bench_serve(M, rates, [args.serve_requests] * len(rates))
+        plain_sz = plain_time_per_size(M, list(M.BATCH_SIZES) + [(192, 96, 96)])
+        # request mix: chain grids uniform over the five sizes, 2 % of chains on
+        # 192x96x96, 2.5 load cases on average
+        mean_t = 0.98 * sum(plain_sz[sz] for sz in M.BATCH_SIZES) / 5 + 0.02 * plain_sz[(192, 96, 96)]
+        serve["plain_fp64_est_solves_per_s"] = 1.0 / (2.5 * mean_t)
+        serve["plain_fp64_method"] = ("cold plain solve per grid size, weighted by the request mix "
+                                      "(2.5 load cases per request)")
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_sample(args.cpu_iters)
@@ -334,10 +461,10 @@ def main():
                 "iterations": reps[-1][0], "refinements": reps[-1][1],
                 "relres_fp64": reps[-1][2], "compliance_rel_err_vs_oracle": comp_err,
                 "sens_rel_err_vs_oracle": dc_err,
-                "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-                        "d2h_bytes_per_step": int(d2h)},
+                "e2e": e2e,
                 "roofline": roof, "plain_fp64": plain,
                 "speedup_vs_plain_fp64": (value / plain["solves_per_s"]) if plain else None,
+                "batch": batch, "serving": serve,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "wall_s_timed": t_wall}
         print(json.dumps(line), flush=True)

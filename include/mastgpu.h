@@ -133,7 +133,7 @@ typedef struct mg_solve_opts {
                                 the plain form is Jacobi-preconditioned */
     int32_t smooth_degree;   /* multigrid: Chebyshev degree of the smoothers (0 = 2) */
     int32_t coarse_degree;   /* multigrid: Chebyshev degree on the coarsest grid (0 = 8) */
-    int32_t reserved;
+    int32_t vec_blocks_per_sm; /* mixed form: CTAs per SM of the vector kernels (0 = 8) */
 } mg_solve_opts;
 
 #define MG_PC_JACOBI 0
@@ -228,6 +228,153 @@ int mg_debug_launch_apply(mg_problem *p, int precision, int reps);
 int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t *cols, const double *vals,
                       const double *b, double *x, double rtol, int32_t max_iterations,
                       void *stream, int32_t *iterations, double *relres);
+
+/* ---- batched design evaluations ----
+   No single counterpart in the reference: MAST evaluates one design at a time
+   (examples/structural/example_6/example_6.cpp:450-655 `evaluate`: set the
+   density field, NonlinearSystem::solve, ComplianceOutput and
+   calculate_output_adjoint_sensitivity_multiple_parameters_no_direct).  A batch
+   holds many such SIMP cantilever evaluations of uneven structured-grid sizes,
+   each with 1..MG_BATCH_MAX_CASES load cases sharing the design's stiffness, and
+   solves all of them together with the mixed-precision matrix-free form
+   (multi-problem persistent kernels driven by per-problem offset tables,
+   graph-captured CG iterations, FP64 refinement).  Every load case is one
+   problem; problems are numbered design by design, case by case. */
+#define MG_BATCH_MAX_CASES 8
+
+typedef struct mg_batch mg_batch;
+
+typedef struct mg_batch_problem {
+    int32_t nx, ny, nz;       /* unit-spaced HEX8 grid (libMesh build_cube numbering) */
+    int32_t n_cases;          /* load cases, 1..MG_BATCH_MAX_CASES */
+    const double *rho;        /* nx*ny*nz element densities in [0,1], x fastest */
+    const int32_t *span;      /* 2*n_cases: node range [j0, j1] (inclusive) of a unit -z line
+                                 load spread evenly over the nodes (nx, j, 0), j0 <= j <= j1;
+                                 nullable when F is given */
+    const double *F;          /* n_cases x 3*(nx+1)*(ny+1)*(nz+1) nodal loads, node-interleaved
+                                 (overrides span; nullable) */
+    const uint8_t *node_fix;  /* per node: bit c set = component c fixed; nullable: the x = 0
+                                 face clamped */
+} mg_batch_problem;
+
+int mg_batch_create(const mg_batch_problem *designs, int32_t n_designs,
+                    const mg_material_desc *mat, mg_batch **out);
+void mg_batch_destroy(mg_batch *b);
+/* totals: designs, problems (load cases), level-0 dofs, multigrid levels, device bytes */
+int mg_batch_info(const mg_batch *b, int32_t *n_designs, int32_t *n_problems, int64_t *n_dofs,
+                  int32_t *n_levels, int64_t *device_bytes);
+void *mg_batch_stream(mg_batch *b);
+/* replace design d's densities (host or device pointer); its solutions stay
+   resident as the next warm start */
+int mg_batch_set_design(mg_batch *b, int32_t d, const double *rho);
+int mg_batch_set_design_device(mg_batch *b, int32_t d, const double *rho_device);
+/* Solve every problem (opts->precision must be a mixed form; opts->warm_start
+   starts from the resident solutions), then form compliance f.u and dC/drho for
+   every problem.  reports (nullable) receives one entry per problem.  Returns
+   MG_OK or the first failing problem's status. */
+int mg_batch_solve(mg_batch *b, const mg_solve_opts *opts, mg_solve_report *reports);
+/* the same restricted to the problems with active[i] != 0; the others keep
+   their solutions and results */
+int mg_batch_solve_subset(mg_batch *b, const mg_solve_opts *opts, const uint8_t *active,
+                          mg_solve_report *reports);
+/* design d's results (each nullable): compliance[n_cases], dc[n_cases * n_elems],
+   u[n_cases * n_dofs] (node-interleaved) */
+int mg_batch_results(mg_batch *b, int32_t d, double *compliance, double *dc, double *u);
+/* Autotuner: times trial solves of one design per distinct grid shape over the
+   solver-schedule knobs (precision within the family of opts->precision, smoother
+   and coarse Chebyshev degrees, CG iterations per graph, inner tolerance, vector
+   kernel grid), keeps the fastest that converges, writes it into *opts and caches
+   it per shape set in the process (and in the file named by MG_TUNE_CACHE when
+   that is set).  A cache hit runs no trial.  *seconds (nullable) gets the best
+   trial time. */
+int mg_batch_autotune(mg_batch *b, mg_solve_opts *opts, int32_t max_trials, double *seconds);
+
+/* ---- request loop (continuous batching of design evaluations) ----
+   No counterpart in the reference (its design loop calls `evaluate` serially,
+   examples/structural/example_6/example_6.cpp:450-655).  A server owns one GPU
+   stream and a worker thread.  Requests belong to design chains: a chain has one
+   grid and one number of load cases; its mesh tables and last solutions stay
+   resident in device memory and every request of the chain warm-starts from the
+   chain's previous solution.  Requests that arrive while others are on the GPU
+   join the running multi-problem solve at the next step boundary (a few CG
+   iterations), so work of different requests overlaps in the same kernels.  New
+   chains are admitted against the device-memory cap (least recently used idle
+   chains are evicted when needed); a chain that cannot fit alone is rejected
+   (MG_ENOMEM in its completions). */
+typedef struct mg_server mg_server;
+
+typedef struct mg_request {
+    int32_t chain;            /* design chain id, >= 0 */
+    int32_t nx, ny, nz;       /* the chain's grid (fixed per chain) */
+    int32_t n_cases;          /* the chain's load cases (fixed per chain) */
+    int32_t reserved;
+    const double *rho;        /* nx*ny*nz densities in [0,1]; copied by mg_server_submit */
+    const int32_t *span;      /* 2*n_cases unit -z line-load node spans (as mg_batch_problem);
+                                 copied by mg_server_submit */
+    double *compliance_out;   /* n_cases, caller-owned, filled before the completion is posted
+                                 (nullable) */
+    double *dc_out;           /* n_cases * nx*ny*nz dC/drho, caller-owned (nullable) */
+    double arrival_s;         /* arrival time on the mg_server_clock() scale (<= 0: now) */
+    uint64_t tag;             /* echoed in the completion */
+} mg_request;
+
+typedef struct mg_completion {
+    uint64_t tag;
+    int32_t chain, status;
+    int32_t krylov_iterations, refinements; /* summed / maximum over the request's load cases */
+    double relres;                          /* maximum FP64 relative residual over the cases */
+    double arrival_s, admit_s, done_s;      /* mg_server_clock() times */
+} mg_completion;
+
+typedef struct mg_server_opts {
+    int64_t hbm_cap_bytes;    /* cap on the resident tables of all chains (0 = 150 GB) */
+    mg_solve_opts solve;      /* mixed-precision form, tolerances, warm starts implied */
+    int32_t max_inflight;     /* designs on the GPU at once (0 = no limit) */
+    int32_t reserved;
+} mg_server_opts;
+
+typedef struct mg_server_stats {
+    int64_t submitted, completed, failed, rebuilds, evictions;
+    int64_t resident_bytes, peak_resident_bytes;
+    int32_t resident_chains, inflight, peak_inflight, reserved;
+    double p50_s, p99_s, mean_s, max_s;   /* latency: arrival -> results posted */
+    double solves_per_s;                  /* completed / (last completion - first arrival) */
+    double dofs_per_s;                    /* solved dofs (all load cases) per second */
+} mg_server_stats;
+
+double mg_server_clock(void);
+int mg_server_create(const mg_material_desc *mat, const mg_server_opts *opts, mg_server **out);
+/* thread-safe; MG_EINVAL for a malformed request or one that contradicts its chain */
+int mg_server_submit(mg_server *s, const mg_request *req);
+/* up to max completions posted since the last poll, waiting up to timeout_s for the first */
+int mg_server_poll(mg_server *s, mg_completion *out, int32_t max, int32_t *n, double timeout_s);
+/* wait until every submitted request has completed (MG_ETIMEDOUT after timeout_s > 0) */
+int mg_server_drain(mg_server *s, double timeout_s);
+int mg_server_get_stats(mg_server *s, mg_server_stats *out);
+/* stops the worker after the submitted requests complete, frees everything */
+void mg_server_destroy(mg_server *s);
+
+/* Synthetic request stream for benchmarks: n_requests Poisson arrivals at `rate`
+   req/s over n_chains chains; chain grids drawn uniformly from sizes (3 ints
+   each), except round(big_fraction * n_chains) chains (at least one when
+   big_fraction > 0) on the big grid; 1..max_cases load cases per chain with
+   seeded spans; densities start iid U[0.01,1] and each request adds N(0, noise)
+   clipped to [0.01, 1].  All densities are generated before the clock starts;
+   a submitter thread then submits each request at its arrival time and the call
+   returns after the last completion with the server statistics of this run.
+   compliance_out (nullable): n_requests x max_cases (unused cases 0). */
+typedef struct mg_synthetic_desc {
+    int64_t n_requests;
+    double rate;
+    int32_t n_chains, n_sizes;
+    const int32_t *sizes;
+    double big_fraction;
+    int32_t big_nx, big_ny, big_nz, max_cases;
+    double noise;
+    uint64_t seed;
+} mg_synthetic_desc;
+int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *desc, double *compliance_out,
+                            mg_server_stats *stats);
 
 /* parameter kinds for mg_sensitivity_assemble */
 #define MG_PARAM_DENSITY 0      /* rho_e of element param_index (elasticity) */

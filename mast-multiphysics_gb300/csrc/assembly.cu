@@ -532,6 +532,16 @@ int compute_modulus(mg_problem *p) {
     return read_status(p, st);
 }
 
+int launch_simp_modulus(const double *d_rho, int64_t n, const mg_material_desc &mat, double *d_E,
+                        double *d_dE, int *d_status, cudaStream_t s) {
+    if (n <= 0) return MG_OK;
+    simp_modulus_kernel<<<blocks_for(n, 256), 256, 0, s>>>(d_rho, n, mat.E0, mat.Emin / mat.E0,
+                                                           mat.penal, d_E, d_dE, d_status);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return MG_OK;
+}
+
 int build_emap(mg_problem *p) {
     int *st = status_slot(p);
     MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(int), p->stream));

@@ -310,7 +310,7 @@ __device__ __forceinline__ int box_offset(int k) {
 template <int PREC, int MODE>
 __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
     const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int brick_lo,
-    int brick_hi, const CUtensorMap *__restrict__ tmaps, int in_slot, int parity,
+    int brick_hi, int sel, const CUtensorMap *__restrict__ tmaps, int in_slot, int parity,
     const uint32_t *__restrict__ Bop, const float *__restrict__ dinv,
     const float *__restrict__ rhs, float *__restrict__ p0, float *__restrict__ p1,
     float *__restrict__ y, MfState *states, double *__restrict__ brick_part, int *err) {
@@ -329,7 +329,10 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     float *p_new = (MODE == 1) ? (parity ? p0 : p1) : nullptr;
 
-    auto usable = [&](int bi) { return !states[probs[bricks[bi].prob].root].done; };
+    auto usable = [&](int bi) {
+        const MfProblem &Q = probs[bricks[bi].prob];
+        return !states[Q.root].done && (sel < 0 || sel == (Q.coarse < 0 ? 1 : 0));
+    };
     int bi = brick_lo + blockIdx.x;
     while (bi < n_bricks && !usable(bi)) bi += gridDim.x;
     if (bi >= n_bricks) return;  // uniform: no work for this block
@@ -730,8 +733,9 @@ __global__ void __launch_bounds__(kThreads) mf_dot_rz_kernel(
                     st->status = is_bad(trz) ? MG_ENAN : MG_EBREAKDOWN;
                     st->done = 1;
                 } else {
-                    st->beta = init ? 0.0 : trz / st->rz;
+                    st->beta = (init || st->first) ? 0.0 : trz / st->rz;
                     st->rz = trz;
+                    st->first = 0;
                 }
             }
         }
@@ -746,10 +750,11 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_first_kernel(
     const MfChunkDesc *__restrict__ chunks, int lo, int hi, const MfProblem *__restrict__ probs,
     const MfState *states, const float *__restrict__ rin, float *__restrict__ mr,
     float *__restrict__ md, float *__restrict__ mx, const float *__restrict__ dinv,
-    float inv_theta, int x0_zero) {
+    float inv_theta, int x0_zero, int sel) {
     for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
-        if (states[probs[C.prob].root].done) continue;
+        const MfProblem &Q = probs[C.prob];
+        if (states[Q.root].done || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 rv = *reinterpret_cast<const float4 *>(rin + i);
             const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
@@ -769,10 +774,11 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_next_kernel(
     const MfChunkDesc *__restrict__ chunks, int lo, int hi, const MfProblem *__restrict__ probs,
     const MfState *states, const float *__restrict__ my, float *__restrict__ mr,
     float *__restrict__ md, float *__restrict__ mx, const float *__restrict__ dinv, float c1,
-    float c2) {
+    float c2, int sel) {
     for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
-        if (states[probs[C.prob].root].done) continue;
+        const MfProblem &Q = probs[C.prob];
+        if (states[Q.root].done || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 yv = *reinterpret_cast<const float4 *>(my + i);
             const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
@@ -834,7 +840,7 @@ __global__ void mg_prolong_kernel(const MfProblem *__restrict__ probs, int plo,
                                   const MfState *states, float *__restrict__ mx,
                                   const float *__restrict__ dinv) {
     const MfProblem F = probs[plo + blockIdx.y];
-    if (states[F.root].done) return;
+    if (F.coarse < 0 || states[F.root].done) return;  // no coarser level: nothing to add
     const MfProblem C = probs[F.coarse];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F.n_pad;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -878,21 +884,20 @@ __global__ void mg_coarsen_kernel(const MfProblem *__restrict__ probs, int plo,
     }
 }
 
-// inner CG start: b = scale r64 (unit norm), x = 0, r = b, z = D^-1 r, p_old = 0
+// inner CG start (problems in INIT): b = scale r64 (unit norm), x = 0, r = b,
+// z = D^-1 r, p0 = p1 = 0; moves the problem to CG
 __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
     const MfChunkDesc *__restrict__ chunks, int n_chunks, const MfProblem *__restrict__ probs,
     const double *__restrict__ r64, float *__restrict__ x, float *__restrict__ r,
-    float *__restrict__ z, float *__restrict__ p_old, const float *__restrict__ dinv,
-    MfState *states, double *__restrict__ chunk_part, double inner_rtol2, int maxit) {
+    float *__restrict__ z, float *__restrict__ p0, float *__restrict__ p1,
+    const float *__restrict__ dinv, MfState *states, double *__restrict__ chunk_part,
+    double inner_rtol2, int maxit) {
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
         MfState *st = states + C.prob;
-        if (st->ref_done) {
-            if (threadIdx.x == 0) st->done = 1;  // converged problems sit out the inner loop
-            continue;
-        }
+        if (st->phase != kPhaseInit) continue;
         const double scale = st->scale;
         float rz = 0.0f, rr = 0.0f;
         for (int64_t i = C.begin + threadIdx.x; i < C.end; i += kThreads) {
@@ -901,7 +906,8 @@ __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
             r[i] = bi;
             const float zi = dinv[i] * bi;
             z[i] = zi;
-            p_old[i] = 0.0f;
+            p0[i] = 0.0f;  // either may be the first step's p_old
+            p1[i] = 0.0f;
             rz = fmaf(bi, zi, rz);
             rr = fmaf(bi, bi, rr);
         }
@@ -929,25 +935,51 @@ __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
                 st->iter = 0;
                 st->maxit = maxit;
                 st->status = 0;
+                st->first = 1;
                 st->done = (trr <= st->tol2 || trr == 0.0) ? 1 : 0;
                 if (is_bad(trr)) { st->status = MG_ENAN; st->done = 1; }
+                st->phase = kPhaseCG;
             }
         }
         __syncthreads();
     }
 }
 
-// refinement update u += x / scale (x is 0 on Dirichlet dofs and padding)
+// a problem whose inner CG has just stopped and whose correction is usable
+__device__ __forceinline__ bool inner_finished(const MfState *st) {
+    return st->phase == kPhaseCG && st->done && (st->status == 0 || st->status == MG_ENOCONV);
+}
+
+// refinement update u += x / scale (x is 0 on Dirichlet dofs and padding) for
+// the problems whose inner CG has stopped
 __global__ void mf_refine_kernel(const MfChunkDesc *__restrict__ chunks, int n_chunks,
                                  const float *__restrict__ x, double *__restrict__ u64,
                                  const MfState *states) {
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
         const MfState *st = states + C.prob;
-        if (st->ref_done || st->status != 0) continue;
+        if (!inner_finished(st)) continue;
         const double inv = 1.0 / st->scale;
         for (int64_t i = C.begin + threadIdx.x; i < C.end; i += blockDim.x)
             u64[i] = fma((double)x[i], inv, u64[i]);
+    }
+}
+
+// after the refinement update: a stopped inner CG sends its problem back to the
+// FP64 residual, or ends it on a breakdown / NaN (one thread per problem)
+__global__ void mf_phase_kernel(MfState *states, int n_fine) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_fine) return;
+    MfState *st = states + i;
+    if (st->phase != kPhaseCG || !st->done) return;
+    if (st->status != 0 && st->status != MG_ENOCONV) {
+        st->ref_status = st->status;
+        st->ref_done = 1;
+        st->phase = kPhaseFin;
+    } else {
+        st->refine += 1;
+        st->status = 0;
+        st->phase = kPhaseResid;
     }
 }
 
@@ -975,7 +1007,8 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
         const MfBrick br = bricks[bi];
         const MfProblem P = probs[br.prob];
         MfState *st = states + br.prob;
-        if (st->ref_done) continue;
+        if (st->phase != kPhaseResid) continue;
+        const bool need_ff = st->ff64 == 0.0;  // first residual of a solve: also ||f||^2
         const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
         __syncthreads();
         for (int i = threadIdx.x; i < kBU * kBU * kBU * 3; i += kThreads) {
@@ -998,7 +1031,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
             sE[l] = e;
         }
         __syncthreads();
-        double part = 0.0;
+        double part = 0.0, fpart = 0.0;
         for (int i = threadIdx.x; i < kBN * kBN * kBN * 3; i += kThreads) {
             const int node = i / 3, c = i - node * 3;
             const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
@@ -1026,14 +1059,18 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
                     }
             const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
             const int64_t gd = dof_index(P, gx, gy, gz, c);
-            double rv = f64[gd] - acc;
+            const double fv = f64[gd];
+            double rv = fv - acc;
             if ((node_fix[P.node_off + gn] >> c) & 1) rv = 0.0;
             r64[gd] = rv;
             part = fma(rv, rv, part);
+            fpart = fma(fv, fv, fpart);
         }
         const double s = block_sum(part, red_sh);
+        const double sf = need_ff ? block_sum(fpart, red_sh) : 0.0;
         if (threadIdx.x == 0) {
             brick_part[bi] = s;
+            brick_part[n_bricks + bi] = sf;
             __threadfence();
             const unsigned t = atomicAdd(&st->cnt_res, 1u);
             sh_last = (t == (unsigned)P.brick_count - 1);
@@ -1041,13 +1078,19 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
         __syncthreads();
         if (sh_last) {
             const double rr = ordered_sum(brick_part, P.brick_begin, P.brick_count);
+            const double ff = need_ff ? ordered_sum(brick_part + n_bricks, P.brick_begin, P.brick_count) : 0.0;
             if (threadIdx.x == 0) {
                 st->cnt_res = 0;
+                if (need_ff) st->ff64 = ff > 0.0 ? ff : -1.0;  // -1: zero load (u = 0)
                 st->rr64 = rr;
                 st->scale = rr > 0.0 ? 1.0 / sqrt(rr) : 1.0;
-                if (is_bad(rr)) { st->ref_status = MG_ENAN; st->ref_done = 1; }
-                else if (rr <= rtol2 * st->ff64) st->ref_done = 1;
-                else if (st->refine >= max_ref) { st->ref_status = MG_ENOCONV; st->ref_done = 1; }
+                st->phase = kPhaseFin;
+                st->ref_done = 1;
+                if (st->ff64 < 0.0) st->rr64 = 0.0;
+                else if (is_bad(rr)) st->ref_status = MG_ENAN;
+                else if (rr <= rtol2 * st->ff64) st->ref_status = 0;
+                else if (st->refine >= max_ref) st->ref_status = MG_ENOCONV;
+                else { st->ref_done = 0; st->phase = kPhaseInit; }
             }
         }
         __syncthreads();
@@ -1056,11 +1099,10 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
 
 // Jacobi inverse of the mixed operator: 1 / sum_e E_e K0[3a+c][3a+c];
 // 0 on Dirichlet dofs and padding (marks them for the vector kernels)
-__global__ void mf_diag_kernel(const MfProblem *__restrict__ probs, int n_probs,
+__global__ void mf_diag_kernel(const MfProblem *__restrict__ probs, const int *__restrict__ list,
                                const float *__restrict__ E32, const uint8_t *__restrict__ node_fix,
                                const double *__restrict__ K0, float *__restrict__ dinv) {
-    const int pi = blockIdx.y;
-    if (pi >= n_probs) return;
+    const int pi = list ? list[blockIdx.y] : (int)blockIdx.y;
     const MfProblem P = probs[pi];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_pad;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -1100,6 +1142,7 @@ __global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
     const int pi = blockIdx.y;
     if (pi >= n_probs) return;
     const MfProblem P = probs[pi];
+    if (out_off[pi] < 0) return;  // not part of this evaluation
     const int64_t ne = (int64_t)P.nx * P.ny * P.nz;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -1234,6 +1277,7 @@ struct ApplyArgs {
     int brick_lo, brick_hi, in_slot, parity;
     const float *rhs;
     float *y;
+    int sel = -1;  // -1 every problem; 0 problems with a coarser level; 1 those without
 };
 
 template <int PREC, int MODE>
@@ -1242,8 +1286,8 @@ void launch_apply(MfBatch &b, const ApplyArgs &a) {
     if (nb <= 0) return;
     const int grid = std::max(1, std::min(nb, b.apply_grid));
     mf_apply_kernel<PREC, MODE><<<grid, kApplyThreads, kApplySmem, b.stream>>>(
-        b.probs, b.bricks, a.brick_lo, a.brick_hi, b.tmaps, a.in_slot, a.parity, b.Bop, b.dinv,
-        a.rhs, b.p0, b.p1, a.y, b.states, b.brick_part, b.err);
+        b.probs, b.bricks, a.brick_lo, a.brick_hi, a.sel, b.tmaps, a.in_slot, a.parity, b.Bop,
+        b.dinv, a.rhs, b.p0, b.p1, a.y, b.states, b.brick_part, b.err);
 }
 
 template <int MODE>
@@ -1343,41 +1387,34 @@ void launch_update(MfBatch &b, float *pnew, bool mg) {
         b.chunks, n0, b.probs, b.x, b.r, b.z, pnew, b.q, b.dinv, b.states, b.chunk_part, mg ? 1 : 0);
 }
 
-int build_graph(MfBatch &b, int prec, int chunk) {
-    if (b.graph && b.graph_prec == prec && b.graph_chunk == chunk) return MG_OK;
-    if (b.graph) {
-        cudaGraphExecDestroy(b.graph);
-        b.graph = nullptr;
-    }
-    cudaGraph_t g = nullptr;
-    MG_CUDA_TRY(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
-    for (int it = 0; it < chunk; it++) {
-        const int parity = it & 1;  // p_old = p0 on even iterations
-        float *pnew = parity ? b.p0 : b.p1;
-        launch_cg_apply(b, prec, 0, parity);
-        launch_update(b, pnew, false);
-    }
-    cudaError_t e = cudaStreamEndCapture(b.stream, &g);
-    if (e != cudaSuccess) {
-        set_error("graph capture: %s", cudaGetErrorString(e));
-        return MG_ECUDA;
-    }
-    e = cudaGraphInstantiate(&b.graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
-        set_error("graph instantiate: %s", cudaGetErrorString(e));
-        return MG_ECUDA;
-    }
-    b.graph_prec = prec;
-    b.graph_chunk = chunk;
+int compute_diag(MfBatch &b) {
+    int64_t maxpad = 1;
+    for (const MfProblem &P : b.h_probs) maxpad = std::max(maxpad, P.n_pad);
+    dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 4096u)), b.n_probs);
+    mf_diag_kernel<<<grid, 256, 0, b.stream>>>(b.probs, nullptr, b.E32, b.node_fix, b.K0, b.dinv);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
     return MG_OK;
 }
 
-int compute_diag(MfBatch &b) {
-    dim3 grid(std::max(1u, std::min(blocks_for(b.n_pad, 256), 4096u)), b.n_probs);
-    mf_diag_kernel<<<grid, 256, 0, b.stream>>>(b.probs, b.n_probs, b.E32, b.node_fix, b.K0, b.dinv);
+// Jacobi inverse of the listed level-0 problems and all their coarse levels
+int compute_diag_list(MfBatch &b, const std::vector<int> &level0) {
+    std::vector<int> list;
+    int64_t maxpad = 1;
+    for (int i : level0)
+        for (int q = i; q >= 0; q = b.h_probs[q].coarse) {
+            list.push_back(q);
+            maxpad = std::max(maxpad, b.h_probs[q].n_pad);
+        }
+    if (list.empty()) return MG_OK;
+    MG_CUDA_TRY(cudaMemcpyAsync(b.diag_list, list.data(), list.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, b.stream));
+    dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 4096u)), (unsigned)list.size());
+    mf_diag_kernel<<<grid, 256, 0, b.stream>>>(b.probs, b.diag_list, b.E32, b.node_fix, b.K0, b.dinv);
     MG_CUDA_TRY(cudaGetLastError());
     count_launches(1);
+    // the list is a host temporary: finish the copy before it goes away
+    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
     return MG_OK;
 }
 
@@ -1547,9 +1584,10 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.u64, (size_t)dof));
     MG_TRY(dev_alloc_n(&b.r64, (size_t)dof));
     MG_TRY(dev_alloc_n(&b.f64, (size_t)dof));
-    MG_TRY(dev_alloc_n(&b.brick_part, (size_t)nb));
+    MG_TRY(dev_alloc_n(&b.brick_part, (size_t)2 * nb));  // operator partials | ||f||^2 partials
     MG_TRY(dev_alloc_n(&b.chunk_part, (size_t)2 * nc));
     MG_TRY(dev_alloc_n(&b.err, 1));
+    MG_TRY(dev_alloc_n(&b.diag_list, (size_t)b.n_probs));
     MG_TRY(dev_alloc_n(&b.Bop, 2560));
     MG_TRY(dev_alloc_n(&b.K0, 576));
     double K0[576];
@@ -1602,11 +1640,10 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
 void mf_batch_free(MfBatch &b) {
     if (b.stream) cudaStreamSynchronize(b.stream);
     if (b.graph) cudaGraphExecDestroy(b.graph);
-    if (b.graph_mg) cudaGraphExecDestroy(b.graph_mg);
     void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.Bop, b.K0, b.mb, b.mx, b.md,
-                    b.my, b.mr};
+                    b.my, b.mr, b.diag_list};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
     b = MfBatch();
@@ -1746,33 +1783,42 @@ Cheb cheb_coeffs(double lmax, int deg) {
     return c;
 }
 
-// one Chebyshev smoothing pass of degree deg on level l: mx (+)= S(rin)
+// one Chebyshev smoothing pass of degree deg on level l: mx (+)= S(rin), on the
+// level's problems selected by sel (see ApplyArgs)
 long long enqueue_smooth(MfBatch &b, int prec, int l, const float *rin, int x0_zero, int deg,
-                         const Cheb &cc) {
+                         const Cheb &cc, int sel) {
     const int clo = b.lvl_chunk_lo[l], chi = b.lvl_chunk_hi[l];
     const int grid = std::max(1, std::min(chi - clo, b.vec_grid));
     mg_cheb_first_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, rin,
-                                                          b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero);
+                                                          b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero, sel);
     long long n = 1;
     for (int k = 1; k < deg; k++) {
-        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 5, 0, nullptr, b.my};
+        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 5, 0, nullptr, b.my, sel};
         launch_apply_prec<3>(b, prec, a);
         mg_cheb_next_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, b.my,
-                                                             b.mr, b.md, b.mx, b.dinv, cc.c1[k], cc.c2[k]);
+                                                             b.mr, b.md, b.mx, b.dinv, cc.c1[k], cc.c2[k], sel);
         n += 2;
     }
     return n;
 }
 
-// V-cycle z = M r on every design at once (level-0 rhs = CG residual r, z = mx)
+// V-cycle z = M r on every design at once (level-0 rhs = CG residual r, z = mx).
+// A problem whose own coarsest grid is level l gets the coarse-grid smoother
+// (degree cdeg) there, whatever the depth of the other problems, so that each
+// problem's preconditioner does not depend on the batch it is solved in.
 long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
     const Cheb cs = cheb_coeffs(b.cheb_lmax, sdeg), cc = cheb_coeffs(b.cheb_lmax, cdeg);
     const int L = b.n_levels;
+    auto has_bottom = [&](int l) {  // some problem of level l has no coarser level
+        for (int pi = b.lvl_prob_lo[l]; pi < b.lvl_prob_hi[l]; pi++)
+            if (b.h_probs[pi].coarse < 0) return true;
+        return false;
+    };
     long long n = 0;
     for (int l = 0; l < L - 1; l++) {
         const float *rin = (l == 0) ? b.r : b.mb;
-        n += enqueue_smooth(b, prec, l, rin, 1, sdeg, cs);
-        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my};
+        n += enqueue_smooth(b, prec, l, rin, 1, sdeg, cs, 0);
+        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my, 0};
         launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
         const int clo = b.lvl_prob_lo[l + 1], chi = b.lvl_prob_hi[l + 1];
         int64_t maxpad = 1;
@@ -1780,8 +1826,9 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
         dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), chi - clo);
         mg_restrict_kernel<<<grid, 256, 0, b.stream>>>(b.probs, clo, b.states, b.my, b.mb, b.dinv);
         n += 2;
+        if (has_bottom(l)) n += enqueue_smooth(b, prec, l, rin, 1, cdeg, cc, 1);
     }
-    n += enqueue_smooth(b, prec, L - 1, L == 1 ? b.r : b.mb, 1, cdeg, cc);
+    n += enqueue_smooth(b, prec, L - 1, L == 1 ? b.r : b.mb, 1, cdeg, cc, -1);
     for (int l = L - 2; l >= 0; l--) {
         const float *rin = (l == 0) ? b.r : b.mb;
         const int flo = b.lvl_prob_lo[l], fhi = b.lvl_prob_hi[l];
@@ -1790,170 +1837,191 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
             if (b.h_probs[pi].coarse >= 0) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
         dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), fhi - flo);
         mg_prolong_kernel<<<grid, 256, 0, b.stream>>>(b.probs, flo, b.states, b.mx, b.dinv);
-        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my};
+        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my, 0};
         launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
-        n += 2 + enqueue_smooth(b, prec, l, b.my, 0, sdeg, cs);
+        n += 2 + enqueue_smooth(b, prec, l, b.my, 0, sdeg, cs, 0);
     }
     return n;
 }
 
-int build_graph_mg(MfBatch &b, int prec, int chunk, int sdeg, int cdeg, long long *launches) {
-    if (b.graph_mg && b.graph_mg_prec == prec && b.graph_mg_chunk == chunk &&
-        b.graph_mg_sdeg == sdeg && b.graph_mg_cdeg == cdeg) {
-        *launches = b.graph_mg_launches;
-        return MG_OK;
+// One solver step over every problem of the batch; each kernel acts only on the
+// problems in its phase, so problems advance independently:
+//   FP64 residual + stop test (RESID) | inner CG start (INIT) |
+//   [multigrid z = M r, rz, beta] | p, q = A p, alpha | x, r, stop test |
+//   u += d of stopped inner solves | phase transitions.
+long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
+    cudaStream_t s = b.stream;
+    const int n0 = b.lvl_chunk_hi[0], nb0 = b.lvl_brick_hi[0];
+    const int vg0 = std::max(1, std::min(n0, b.vec_grid));
+    const bool use_mg = prm.mg && b.n_levels > 1;
+    const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
+    const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
+    mf_residual64_kernel<<<std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s>>>(
+        b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.K0, b.r64, b.states,
+        b.brick_part, prm.rtol * prm.rtol, max_ref);
+    mf_inner_init_kernel<<<vg0, kThreads, 0, s>>>(
+        b.chunks, n0, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.p1, b.dinv, b.states, b.chunk_part,
+        prm.inner_rtol * prm.inner_rtol, maxit);
+    long long n = 2;
+    float *pnew = parity ? b.p0 : b.p1;
+    if (use_mg) {
+        const int sdeg = prm.smooth_deg > 0 ? prm.smooth_deg : 2;
+        const int cdeg = prm.coarse_deg > 0 ? prm.coarse_deg : 8;
+        n += enqueue_vcycle(b, mg_precision(prm.precision), sdeg, cdeg);
+        mf_dot_rz_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.probs, b.r, b.mx, b.states,
+                                                 b.chunk_part, 0);
+        launch_cg_apply(b, prm.precision, 4, parity);  // p = z + beta p_old, q = A p, alpha
+        launch_update(b, pnew, true);                  // x, r, stop test
+        n += 3;
+    } else {
+        launch_cg_apply(b, prm.precision, 0, parity);
+        launch_update(b, pnew, false);                 // also z = D^-1 r, beta
+        n += 2;
     }
-    if (b.graph_mg) {
-        cudaGraphExecDestroy(b.graph_mg);
-        b.graph_mg = nullptr;
+    mf_refine_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.x, b.u64, b.states);
+    mf_phase_kernel<<<(b.n_fine + 127) / 128, 128, 0, s>>>(b.states, b.n_fine);
+    return n + 2;
+}
+
+// CUDA graph of `chunk` solver steps (even: the p0/p1 roles alternate per step),
+// cached per parameter set
+int build_step_graph(MfBatch &b, const MfSolveParams &prm, int chunk) {
+    const std::vector<double> key = {(double)prm.precision, (double)chunk, (double)prm.mg,
+                                     (double)prm.smooth_deg, (double)prm.coarse_deg, prm.rtol,
+                                     prm.inner_rtol, (double)prm.max_iterations,
+                                     (double)prm.max_refinements, (double)b.vec_grid};
+    if (b.graph && b.graph_key == key) return MG_OK;
+    if (b.graph) {
+        cudaGraphExecDestroy(b.graph);
+        b.graph = nullptr;
     }
-    const int mprec = mg_precision(prec);
-    const int n0 = b.lvl_chunk_hi[0];
     long long n = 0;
     cudaGraph_t g = nullptr;
     MG_CUDA_TRY(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
-    for (int it = 0; it < chunk; it++) {
-        const int parity = it & 1;
-        float *pnew = parity ? b.p0 : b.p1;
-        launch_cg_apply(b, prec, 4, parity);  // p = z + beta p_old, q = A p, alpha
-        launch_update(b, pnew, true);         // x, r, stop test
-        n += 2 + enqueue_vcycle(b, mprec, sdeg, cdeg);
-        mf_dot_rz_kernel<<<std::max(1, std::min(n0, b.vec_grid)), kThreads, 0, b.stream>>>(
-            b.chunks, n0, b.probs, b.r, b.mx, b.states, b.chunk_part, 0);
-        n += 1;
-    }
+    for (int it = 0; it < chunk; it++) n += enqueue_step(b, prm, it & 1);
     cudaError_t e = cudaStreamEndCapture(b.stream, &g);
     if (e != cudaSuccess) {
         set_error("graph capture: %s", cudaGetErrorString(e));
         return MG_ECUDA;
     }
-    e = cudaGraphInstantiate(&b.graph_mg, g, 0);
+    e = cudaGraphInstantiate(&b.graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
+        b.graph = nullptr;
         set_error("graph instantiate: %s", cudaGetErrorString(e));
         return MG_ECUDA;
     }
-    b.graph_mg_prec = prec;
-    b.graph_mg_chunk = chunk;
-    b.graph_mg_sdeg = sdeg;
-    b.graph_mg_cdeg = cdeg;
-    b.graph_mg_launches = n;
-    *launches = n;
+    b.graph_key = key;
+    b.graph_launches = n;
     return MG_OK;
 }
 
 }  // namespace
 
-// FP64 iterative refinement around FP32 tensor-core CG:
+// FP64 iterative refinement around FP32 tensor-core CG, per problem:
 //   r = f - K u (FP64);  stop when ||r|| <= rtol ||f||;
 //   solve A d = r / ||r|| with FP32 CG to inner_rtol (Jacobi or multigrid
 //   V-cycle preconditioned);  u += ||r|| d.
-int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start) {
-    cudaStream_t s = b.stream;
-    const double t0 = wall_time();
-    const int n0 = b.lvl_chunk_hi[0];            // level-0 chunks
-    const int nb0 = b.lvl_brick_hi[0];           // level-0 bricks
-    const int vg0 = std::max(1, std::min(n0, b.vec_grid));
+// The phases run on the device (enqueue_step); the host only relaunches the
+// step graph until every active problem has finished.
+int mf_batch_prepare(MfBatch &b, const MfSolveParams &prm) {
     const bool use_mg = prm.mg && b.n_levels > 1;
-    const int sdeg = prm.smooth_deg > 0 ? prm.smooth_deg : 2;
-    const int cdeg = prm.coarse_deg > 0 ? prm.coarse_deg : 8;
-    MG_TRY(compute_diag(b));
-    if (!warm_start) MG_CUDA_TRY(cudaMemsetAsync(b.u64, 0, b.n_pad * 8, s));
-    // reset states and compute ||f||^2 per problem
-    mf_dot_chunks_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.f64, b.f64, b.chunk_part);
-    MG_CUDA_TRY(cudaGetLastError());
-    count_launches(1);
-    {
-        std::vector<double> part(n0);
-        MG_CUDA_TRY(cudaMemcpyAsync(part.data(), b.chunk_part, n0 * 8, cudaMemcpyDeviceToHost, s));
-        MG_CUDA_TRY(cudaStreamSynchronize(s));
-        std::vector<MfState> init(b.n_probs);
-        memset(init.data(), 0, init.size() * sizeof(MfState));
-        for (int i = 0; i < b.n_fine; i++) {
-            const MfProblem &P = b.h_probs[i];
-            double ff = 0;
-            for (int c = 0; c < P.chunk_count; c++) ff += part[P.chunk_begin + c];
-            init[i].ff64 = ff > 0 ? ff : 1.0;
-            if (ff == 0.0) init[i].ref_done = 1;  // zero load: u = 0
-        }
-        MG_CUDA_TRY(cudaMemcpyAsync(b.states, init.data(), b.n_probs * sizeof(MfState), cudaMemcpyHostToDevice, s));
-        MG_CUDA_TRY(cudaStreamSynchronize(s));
+    // launch shape of the vector kernels (captured in the graph)
+    int dev = 0, sms = 0;
+    MG_CUDA_TRY(cudaGetDevice(&dev));
+    MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int per_sm = prm.vec_blocks_per_sm > 0 ? std::min(prm.vec_blocks_per_sm, 64) : 8;
+    const int vg = std::max(1, std::min(b.n_chunks, per_sm * sms));
+    if (vg != b.vec_grid) {
+        b.vec_grid = vg;
+        if (b.graph) cudaGraphExecDestroy(b.graph);
+        b.graph = nullptr;
     }
     const int chunk = prm.graph_chunk > 0 ? (prm.graph_chunk + 1) / 2 * 2 : (use_mg ? 2 : 16);
-    long long per_graph = 2LL * chunk;
-    if (use_mg) MG_TRY(build_graph_mg(b, prm.precision, chunk, sdeg, cdeg, &per_graph));
-    else MG_TRY(build_graph(b, prm.precision, chunk));
-    const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
-    const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
-    for (int ref = 0;; ref++) {
-        // outer FP64 residual (also marks converged problems ref_done)
-        mf_residual64_kernel<<<std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s>>>(
-            b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.K0, b.r64, b.states,
-            b.brick_part, prm.rtol * prm.rtol, max_ref);
-        MG_CUDA_TRY(cudaGetLastError());
-        count_launches(1);
-        MG_TRY(read_states(b));
+    MfSolveParams p2 = prm;
+    p2.mg = use_mg ? 1 : 0;
+    return build_step_graph(b, p2, chunk);
+}
+
+int mf_batch_reset_states(MfBatch &b) {
+    std::vector<MfState> init(b.n_probs);
+    memset(init.data(), 0, init.size() * sizeof(MfState));
+    for (int i = 0; i < b.n_probs; i++) {
+        init[i].done = 1;
+        init[i].ref_done = 1;
+        init[i].phase = kPhaseFin;
+    }
+    MG_CUDA_TRY(cudaMemcpyAsync(b.states, init.data(), b.n_probs * sizeof(MfState), cudaMemcpyHostToDevice,
+                                b.stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));  // init is a host temporary
+    memcpy(b.states_host, init.data(), b.n_probs * sizeof(MfState));
+    return MG_OK;
+}
+
+int mf_batch_activate(MfBatch &b, const std::vector<int> &level0, bool warm_start) {
+    MG_TRY(compute_diag_list(b, level0));
+    for (int i : level0) {
+        if (i < 0 || i >= b.n_fine) return MG_EINVAL;
+        const MfProblem &P = b.h_probs[i];
+        if (!warm_start) MG_CUDA_TRY(cudaMemsetAsync(b.u64 + P.dof_off, 0, P.n_pad * 8, b.stream));
+        // the pinned host mirror entry is the staging buffer; the next
+        // read_states (later in stream order) overwrites it
+        MfState &h = b.states_host[i];
+        memset(&h, 0, sizeof(MfState));
+        h.done = 1;
+        h.phase = kPhaseResid;  // its first residual pass also forms ||f||^2
+        MG_CUDA_TRY(cudaMemcpyAsync(b.states + i, &h, sizeof(MfState), cudaMemcpyHostToDevice, b.stream));
+    }
+    return MG_OK;
+}
+
+int mf_batch_step(MfBatch &b) {
+    if (!b.graph) {
+        set_error("mf_batch_step before mf_batch_prepare");
+        return MG_EINVAL;
+    }
+    MG_CUDA_TRY(cudaGraphLaunch(b.graph, b.stream));
+    count_launches(b.graph_launches);
+    return read_states(b);  // synchronises
+}
+
+int mf_batch_finish(MfBatch &b, int i) {
+    // a zero load gives u = 0 (the residual pass marks it with ||f||^2 = -1)
+    if (b.states_host[i].ff64 < 0.0)
+        MG_CUDA_TRY(cudaMemsetAsync(b.u64 + b.h_probs[i].dof_off, 0, b.h_probs[i].n_pad * 8, b.stream));
+    return b.states_host[i].ref_status;
+}
+
+int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start) {
+    const double t0 = wall_time();
+    MG_TRY(mf_batch_prepare(b, prm));
+    MG_TRY(mf_batch_reset_states(b));
+    std::vector<int> act;
+    for (int i = 0; i < b.n_fine; i++)
+        if (!prm.active || prm.active[i]) act.push_back(i);
+    MG_TRY(mf_batch_activate(b, act, warm_start));
+    for (;;) {
+        MG_TRY(mf_batch_step(b));
         bool all_done = true;
-        for (int i = 0; i < b.n_fine; i++) all_done &= b.states_host[i].ref_done != 0;
+        for (int i : act) all_done &= b.states_host[i].phase == kPhaseFin;
         if (all_done) break;
-        // inner FP32 CG on the normalised residual
-        mf_inner_init_kernel<<<vg0, kThreads, 0, s>>>(
-            b.chunks, n0, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.dinv, b.states,
-            b.chunk_part, prm.inner_rtol * prm.inner_rtol, maxit);
-        MG_CUDA_TRY(cudaGetLastError());
-        count_launches(1);
-        if (use_mg) {
-            // z0 = M r0, rz0 (beta = 0)
-            count_launches(enqueue_vcycle(b, mg_precision(prm.precision), sdeg, cdeg));
-            mf_dot_rz_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.probs, b.r, b.mx, b.states,
-                                                     b.chunk_part, 1);
-            MG_CUDA_TRY(cudaGetLastError());
-            count_launches(1);
-        }
-        for (;;) {
-            MG_TRY(read_states(b));
-            bool inner_done = true;
-            for (int i = 0; i < b.n_fine; i++)
-                inner_done &= (b.states_host[i].done != 0 || b.states_host[i].ref_done != 0);
-            if (inner_done) break;
-            if (prm.timeout_s > 0 && wall_time() - t0 > prm.timeout_s) {
-                set_error("mixed solve exceeded %.1f s", prm.timeout_s);
-                return MG_ETIMEDOUT;
-            }
-            MG_CUDA_TRY(cudaGraphLaunch(use_mg ? b.graph_mg : b.graph, s));
-            count_launches(per_graph);
-        }
-        // a breakdown/NaN in the inner solve ends that problem's refinement
-        for (int i = 0; i < b.n_fine; i++) {
-            MfState &h = b.states_host[i];
-            if (!h.ref_done && h.status != 0 && h.status != MG_ENOCONV) {
-                h.ref_done = 1;
-                h.ref_status = h.status;
-            }
-            if (!h.ref_done) h.refine += 1;
-            h.done = h.ref_done ? 1 : 0;
-            h.status = (h.status == MG_ENOCONV) ? 0 : h.status;
-        }
-        // host copy of the per-problem flags goes back (counters are zero here)
-        MG_CUDA_TRY(cudaMemcpyAsync(b.states, b.states_host, b.n_fine * sizeof(MfState),
-                                    cudaMemcpyHostToDevice, s));
-        mf_refine_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.x, b.u64, b.states);
-        MG_CUDA_TRY(cudaGetLastError());
-        count_launches(1);
         if (prm.timeout_s > 0 && wall_time() - t0 > prm.timeout_s) {
             set_error("mixed solve exceeded %.1f s", prm.timeout_s);
             return MG_ETIMEDOUT;
         }
     }
     int rc = MG_OK;
-    for (int i = 0; i < b.n_fine; i++)
-        if (b.states_host[i].ref_status != 0) rc = b.states_host[i].ref_status;
+    for (int i : act) {
+        const int st = mf_batch_finish(b, i);
+        if (st != 0 && rc == MG_OK) rc = st;
+    }
     return rc;
 }
 
 // compliance f.u per design (host) and dC/drho (unpadded, designs back to back
 // in problem order at dc_unpadded_dev) from the resident solutions
-int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded_dev) {
+int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded_dev,
+                        const uint8_t *active) {
     cudaStream_t s = b.stream;
     const int n0 = b.lvl_chunk_hi[0];
     if (compliance_host) {
@@ -1975,7 +2043,7 @@ int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded
         int64_t o = 0, max_ne = 1;
         for (int i = 0; i < b.n_fine; i++) {
             const MfProblem &P = b.h_probs[i];
-            offs[i] = o;
+            offs[i] = (active && !active[i]) ? -1 : o;  // -1: leave this problem's output
             o += (int64_t)P.nx * P.ny * P.nz;
             max_ne = std::max<int64_t>(max_ne, (int64_t)P.nx * P.ny * P.nz);
         }
@@ -2071,6 +2139,7 @@ int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
     prm.mg = (o.preconditioner == MG_PC_MULTIGRID) ? 1 : 0;
     prm.smooth_deg = o.smooth_degree;
     prm.coarse_deg = o.coarse_degree;
+    prm.vec_blocks_per_sm = o.vec_blocks_per_sm;
     int rc = mf_batch_solve(b, prm, true);
     MG_TRY(mf_batch_get_u(b, 0, p->d_X));
     count_launches(1);
@@ -2080,7 +2149,7 @@ int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
         rep->newton_iterations = 1;
         rep->krylov_iterations = h.total_iter;
         rep->refinements = h.refine;
-        rep->relres = sqrt(h.rr64 / h.ff64);
+        rep->relres = h.ff64 > 0.0 ? sqrt(h.rr64 / h.ff64) : 0.0;
         rep->residual_norm = sqrt(h.rr64);
     }
     return rc;

@@ -57,12 +57,24 @@ struct MfChunkDesc {
     int64_t begin, end;  // absolute padded dof range
 };
 
-// Per-problem solver state (device resident).
+// Per-problem solver state (device resident).  Each level-0 problem moves
+// through the refinement phases on the device, independently of the others:
+//   RESID (FP64 r = f - K u, stop test) -> INIT (inner CG start on r/||r||)
+//   -> CG (inner iterations until the inner tolerance) -> RESID (after u += d)
+//   ... -> FIN.
+// `done` is 1 whenever the problem is not iterating its inner CG; the operator,
+// vector and multigrid kernels skip such problems.
+constexpr int kPhaseResid = 0;
+constexpr int kPhaseInit = 1;
+constexpr int kPhaseCG = 2;
+constexpr int kPhaseFin = 3;
+
 struct MfState {
     double rz, rr, pq, alpha, beta, bb, tol2;
     double rr64, ff64, scale;
     int iter, done, status, maxit;
     int total_iter, refine, ref_done, ref_status;
+    int phase, first, pad0, pad1;   // first: the next dot_rz starts the inner CG (beta = 0)
     unsigned cnt_apply, cnt_update, cnt_res, pad;
 };
 
@@ -94,19 +106,18 @@ struct MfBatch {
     int n_levels = 1;
     std::vector<int> lvl_prob_lo, lvl_prob_hi, lvl_brick_lo, lvl_brick_hi, lvl_chunk_lo, lvl_chunk_hi;
     double cheb_lmax = 0.0;     // Gershgorin bound of D^-1 A (same on every level)
-    cudaGraphExec_t graph_mg = nullptr;
-    int graph_mg_prec = -1, graph_mg_chunk = 0, graph_mg_sdeg = 0, graph_mg_cdeg = 0;
-    long long graph_mg_launches = 0;
     // FP64 refinement vectors (padded layout)
     double *u64 = nullptr, *r64 = nullptr, *f64 = nullptr;
     double *brick_part = nullptr, *chunk_part = nullptr;
     int *err = nullptr;
+    int *diag_list = nullptr;  // problem list of a partial Jacobi update
     // operator data
     uint32_t *Bop = nullptr;  // K0 in the UMMA smem layout: [tf32 hi|tf32 lo|bf16 hi|bf16 lo]
     double *K0 = nullptr;     // 24x24 FP64, node-interleaved element order
     double hx = 1, hy = 1, hz = 1, nu = 0.3;
-    cudaGraphExec_t graph = nullptr;
-    int graph_prec = -1, graph_chunk = 0;
+    cudaGraphExec_t graph = nullptr;  // solver steps (see enqueue_step)
+    std::vector<double> graph_key;    // parameters the graph was captured with
+    long long graph_launches = 0;     // kernel nodes in the graph
     int apply_grid = 0, vec_grid = 0;
     cudaStream_t stream = nullptr;
 };
@@ -122,6 +133,8 @@ struct MfSolveParams {
     int mg;               // 1: geometric multigrid V-cycle preconditioner, 0: Jacobi
     int smooth_deg;       // Chebyshev degree of the pre/post smoothers
     int coarse_deg;       // Chebyshev degree on the coarsest level
+    int vec_blocks_per_sm = 0;         // grid of the vector kernels (0 = 8 per SM)
+    const uint8_t *active = nullptr;   // per level-0 problem: 0 = leave untouched (nullable)
 };
 
 // host-side element stiffness of an hx x hy x hz box at E = 1 in
@@ -138,7 +151,20 @@ int mf_batch_set_bc(MfBatch &b, int i, const uint8_t *node_fix_host, const doubl
 // per-problem moduli from unpadded device arrays (E and dE/drho, n_elems each)
 int mf_batch_set_moduli(MfBatch &b, int i, const double *E_dev, const double *dE_dev);
 int mf_batch_solve(MfBatch &b, const MfSolveParams &prm, bool warm_start);
-int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded_dev);
+// stepping interface (mf_batch_solve and the request loop are built on it):
+// prepare captures the step graph for prm; reset puts every problem at FIN;
+// activate starts the listed level-0 problems at the FP64 residual (their
+// Jacobi inverses are refreshed; u is zeroed unless warm_start); step runs one
+// graph launch and refreshes states_host (synchronising); finish returns a
+// FIN problem's status and zeroes u of a zero-load problem.
+int mf_batch_prepare(MfBatch &b, const MfSolveParams &prm);
+int mf_batch_reset_states(MfBatch &b);
+int mf_batch_activate(MfBatch &b, const std::vector<int> &level0, bool warm_start);
+int mf_batch_step(MfBatch &b);
+int mf_batch_finish(MfBatch &b, int i);
+// active (nullable, per level-0 problem): 0 = leave that problem's dc untouched
+int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded_dev,
+                        const uint8_t *active = nullptr);
 // u (padded, FP64) <-> unpadded node-interleaved device vector of problem i
 int mf_batch_get_u(MfBatch &b, int i, double *u_dev);
 int mf_batch_set_u(MfBatch &b, int i, const double *u_dev);

@@ -129,6 +129,10 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
 int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t count,
                      double *d_Ke, double *d_fe);
 int compute_modulus(mg_problem *p);
+// SIMP E(rho), dE/drho of n elements on stream s; bit 4 of *d_status marks a
+// density outside [0,1] or NaN
+int launch_simp_modulus(const double *d_rho, int64_t n, const mg_material_desc &mat, double *d_E,
+                        double *d_dE, int *d_status, cudaStream_t s);
 int build_emap(mg_problem *p);
 int elem_sensitivity(mg_problem *p, const double *d_X, const double *d_lambda, int kind,
                      double *d_out_elem);

@@ -115,7 +115,46 @@ class SolveOpts(ctypes.Structure):
                 ("consistent_jacobian", _i32), ("max_refinements", _i32), ("inner_rtol", _dbl),
                 ("timeout_s", _dbl), ("warm_start", _i32), ("graph_chunk", _i32),
                 ("preconditioner", _i32), ("smooth_degree", _i32), ("coarse_degree", _i32),
+                ("vec_blocks_per_sm", _i32)]
+
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("hbm_cap_bytes", _i64), ("solve", SolveOpts), ("max_inflight", _i32),
                 ("reserved", _i32)]
+
+
+class BatchProblem(ctypes.Structure):
+    _fields_ = [("nx", _i32), ("ny", _i32), ("nz", _i32), ("n_cases", _i32), ("rho", _vp),
+                ("span", _vp), ("F", _vp), ("node_fix", _vp)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("chain", _i32), ("nx", _i32), ("ny", _i32), ("nz", _i32), ("n_cases", _i32),
+                ("reserved", _i32), ("rho", _vp), ("span", _vp), ("compliance_out", _vp),
+                ("dc_out", _vp), ("arrival_s", _dbl), ("tag", ctypes.c_uint64)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_uint64), ("chain", _i32), ("status", _i32),
+                ("krylov_iterations", _i32), ("refinements", _i32), ("relres", _dbl),
+                ("arrival_s", _dbl), ("admit_s", _dbl), ("done_s", _dbl)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", _i64), ("completed", _i64), ("failed", _i64), ("rebuilds", _i64),
+                ("evictions", _i64), ("resident_bytes", _i64), ("peak_resident_bytes", _i64),
+                ("resident_chains", _i32), ("inflight", _i32), ("peak_inflight", _i32),
+                ("reserved", _i32), ("p50_s", _dbl), ("p99_s", _dbl), ("mean_s", _dbl),
+                ("max_s", _dbl), ("solves_per_s", _dbl), ("dofs_per_s", _dbl)]
+
+    def as_dict(self):
+        return {f[0]: getattr(self, f[0]) for f in self._fields_ if f[0] != "reserved"}
+
+
+class SyntheticDesc(ctypes.Structure):
+    _fields_ = [("n_requests", _i64), ("rate", _dbl), ("n_chains", _i32), ("n_sizes", _i32),
+                ("sizes", _vp), ("big_fraction", _dbl), ("big_nx", _i32), ("big_ny", _i32),
+                ("big_nz", _i32), ("max_cases", _i32), ("noise", _dbl), ("seed", ctypes.c_uint64)]
 
 
 class SolveReport(ctypes.Structure):
@@ -173,6 +212,30 @@ def lib(autobuild=True):
     L.mg_debug_launch_apply.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
     L.mg_debug_fail_alloc_after.argtypes = [ctypes.c_int]
     L.mg_debug_fail_alloc_after.restype = None
+    L.mg_batch_create.argtypes = [ctypes.POINTER(BatchProblem), _i32, ctypes.POINTER(MaterialDesc),
+                                  ctypes.POINTER(_vp)]
+    L.mg_batch_destroy.argtypes = [_vp]
+    L.mg_batch_destroy.restype = None
+    L.mg_batch_info.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp]
+    L.mg_batch_stream.argtypes = [_vp]
+    L.mg_batch_stream.restype = _vp
+    L.mg_batch_set_design.argtypes = [_vp, _i32, _vp]
+    L.mg_batch_set_design_device.argtypes = [_vp, _i32, _vp]
+    L.mg_batch_solve.argtypes = [_vp, ctypes.POINTER(SolveOpts), _vp]
+    L.mg_batch_solve_subset.argtypes = [_vp, ctypes.POINTER(SolveOpts), _vp, _vp]
+    L.mg_batch_results.argtypes = [_vp, _i32, _vp, _vp, _vp]
+    L.mg_batch_autotune.argtypes = [_vp, ctypes.POINTER(SolveOpts), _i32, _vp]
+    L.mg_server_clock.restype = ctypes.c_double
+    L.mg_server_create.argtypes = [ctypes.POINTER(MaterialDesc), ctypes.POINTER(ServerOpts),
+                                   ctypes.POINTER(_vp)]
+    L.mg_server_submit.argtypes = [_vp, ctypes.POINTER(Request)]
+    L.mg_server_poll.argtypes = [_vp, _vp, _i32, _vp, ctypes.c_double]
+    L.mg_server_drain.argtypes = [_vp, ctypes.c_double]
+    L.mg_server_get_stats.argtypes = [_vp, ctypes.POINTER(ServerStats)]
+    L.mg_server_destroy.argtypes = [_vp]
+    L.mg_server_destroy.restype = None
+    L.mg_server_run_synthetic.argtypes = [_vp, ctypes.POINTER(SyntheticDesc), _vp,
+                                          ctypes.POINTER(ServerStats)]
     _lib = L
     return L
 
@@ -196,8 +259,11 @@ def _p(a):
 
 
 def default_opts(**kw):
+    """mg_default_solve_opts with the given fields replaced; the host wall-clock
+    limit defaults to 600 s here (the C default is none)."""
     o = SolveOpts()
     lib().mg_default_solve_opts(ctypes.byref(o))
+    o.timeout_s = 600.0
     for k, v in kw.items():
         setattr(o, k, v)
     return o
@@ -382,6 +448,190 @@ class Problem:
         return out
 
 
+class Batch:
+    """Batched SIMP design evaluations (mg_batch_*).  designs: list of dicts with
+    keys nx, ny, nz, rho (nx*ny*nz densities) and either spans (list of (j0, j1)
+    node ranges of the unit -z line load on the x = nx, z = 0 edge, one per load
+    case) or F (n_cases x n_dofs nodal loads); optional node_fix."""
+
+    def __init__(self, designs, material=None):
+        L = lib()
+        m = dict(SIMP_MATERIAL)
+        m.update(material or {})
+        self._mat = MaterialDesc(**m)
+        self._keep = []
+        arr = (BatchProblem * len(designs))()
+        self.shapes = []
+        for i, d in enumerate(designs):
+            nx, ny, nz = int(d["nx"]), int(d["ny"]), int(d["nz"])
+            rho = np.ascontiguousarray(d["rho"], dtype=np.float64)
+            bp = arr[i]
+            bp.nx, bp.ny, bp.nz = nx, ny, nz
+            bp.rho = rho.ctypes.data
+            self._keep.append(rho)
+            if d.get("F") is not None:
+                F = np.ascontiguousarray(d["F"], dtype=np.float64).reshape(-1)
+                nc = F.size // (3 * (nx + 1) * (ny + 1) * (nz + 1))
+                bp.F = F.ctypes.data
+                self._keep.append(F)
+            else:
+                sp = np.ascontiguousarray(np.asarray(d["spans"], dtype=np.int32).reshape(-1))
+                nc = sp.size // 2
+                bp.span = sp.ctypes.data
+                self._keep.append(sp)
+            bp.n_cases = nc
+            if d.get("node_fix") is not None:
+                nf = np.ascontiguousarray(d["node_fix"], dtype=np.uint8)
+                bp.node_fix = nf.ctypes.data
+                self._keep.append(nf)
+            self.shapes.append((nx, ny, nz, nc))
+        h = _vp()
+        check(L.mg_batch_create(arr, len(designs), ctypes.byref(self._mat), ctypes.byref(h)),
+              "mg_batch_create")
+        self._keep = []
+        self.h = h
+        nd, npb, nl = _i32(), _i32(), _i32()
+        ndof, nbytes = _i64(), _i64()
+        check(L.mg_batch_info(self.h, ctypes.byref(nd), ctypes.byref(npb), ctypes.byref(ndof),
+                              ctypes.byref(nl), ctypes.byref(nbytes)), "mg_batch_info")
+        self.n_designs, self.n_problems, self.n_dofs = nd.value, npb.value, ndof.value
+        self.n_levels, self.device_bytes = nl.value, nbytes.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return lib().mg_batch_stream(self.h)
+
+    def set_design(self, d, rho):
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        check(lib().mg_batch_set_design(self.h, d, _p(rho)), "mg_batch_set_design")
+
+    def set_design_device(self, d, ptr):
+        check(lib().mg_batch_set_design_device(self.h, d, ctypes.c_void_p(ptr)),
+              "mg_batch_set_design_device")
+
+    def solve(self, opts, active=None, raise_on_error=True):
+        reps = (SolveReport * self.n_problems)()
+        if active is None:
+            rc = lib().mg_batch_solve(self.h, ctypes.byref(opts), reps)
+        else:
+            act = np.ascontiguousarray(active, dtype=np.uint8)
+            rc = lib().mg_batch_solve_subset(self.h, ctypes.byref(opts), _p(act), reps)
+        if raise_on_error:
+            check(rc, "mg_batch_solve")
+        return rc, list(reps)
+
+    def results(self, d, want_u=False):
+        nx, ny, nz, nc = self.shapes[d]
+        ne = nx * ny * nz
+        nd = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+        comp = np.zeros(nc)
+        dc = np.zeros((nc, ne))
+        u = np.zeros((nc, nd)) if want_u else None
+        check(lib().mg_batch_results(self.h, d, _p(comp), _p(dc), _p(u)), "mg_batch_results")
+        return comp, dc, u
+
+    def autotune(self, opts, max_trials=16):
+        secs = ctypes.c_double()
+        check(lib().mg_batch_autotune(self.h, ctypes.byref(opts), max_trials, ctypes.byref(secs)),
+              "mg_batch_autotune")
+        return opts, secs.value
+
+
+class Server:
+    """Request loop (mg_server_*): continuous batching of design evaluations."""
+
+    def __init__(self, opts=None, hbm_cap_bytes=0, max_inflight=0, material=None):
+        m = dict(SIMP_MATERIAL)
+        m.update(material or {})
+        self._mat = MaterialDesc(**m)
+        so = ServerOpts()
+        so.hbm_cap_bytes = hbm_cap_bytes
+        so.solve = opts if opts is not None else default_opts(precision=MIXED_TF32X3, rtol=1e-8,
+                                                                inner_rtol=1e-3)
+        so.max_inflight = max_inflight
+        self._opts = so
+        h = _vp()
+        check(lib().mg_server_create(ctypes.byref(self._mat), ctypes.byref(so), ctypes.byref(h)),
+              "mg_server_create")
+        self.h = h
+        self._out = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, tag, chain, nx, ny, nz, rho, spans, want_dc=True, arrival_s=0.0):
+        """Returns (compliance, dc) output arrays, filled when the completion posts."""
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        sp = np.ascontiguousarray(np.asarray(spans, dtype=np.int32).reshape(-1))
+        nc = sp.size // 2
+        comp = np.zeros(nc)
+        dc = np.zeros((nc, nx * ny * nz)) if want_dc else None
+        q = Request(chain=chain, nx=nx, ny=ny, nz=nz, n_cases=nc, rho=rho.ctypes.data,
+                    span=sp.ctypes.data, compliance_out=comp.ctypes.data,
+                    dc_out=None if dc is None else dc.ctypes.data, arrival_s=arrival_s, tag=tag)
+        self._out[tag] = (comp, dc)  # keep the output buffers alive until posted
+        check(lib().mg_server_submit(self.h, ctypes.byref(q)), "mg_server_submit")
+        return comp, dc
+
+    def poll(self, max_n=1024, timeout_s=0.0):
+        buf = (Completion * max_n)()
+        n = _i32()
+        check(lib().mg_server_poll(self.h, buf, max_n, ctypes.byref(n), timeout_s), "mg_server_poll")
+        return [buf[i] for i in range(n.value)]
+
+    def drain(self, timeout_s=0.0):
+        check(lib().mg_server_drain(self.h, timeout_s), "mg_server_drain")
+
+    def stats(self):
+        st = ServerStats()
+        check(lib().mg_server_get_stats(self.h, ctypes.byref(st)), "mg_server_get_stats")
+        return st.as_dict()
+
+    def run_synthetic(self, n_requests, rate, n_chains=64, sizes=None, big=(192, 96, 96),
+                      big_fraction=0.02, max_cases=4, noise=0.02, seed=0):
+        sizes = BATCH_SIZES if sizes is None else sizes
+        sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.int32).reshape(-1))
+        d = SyntheticDesc(n_requests=n_requests, rate=rate, n_chains=n_chains, n_sizes=sz.size // 3,
+                          sizes=sz.ctypes.data, big_fraction=big_fraction, big_nx=big[0],
+                          big_ny=big[1], big_nz=big[2], max_cases=max_cases, noise=noise, seed=seed)
+        comp = np.zeros((n_requests, max_cases))
+        st = ServerStats()
+        check(lib().mg_server_run_synthetic(self.h, ctypes.byref(d), _p(comp), ctypes.byref(st)),
+              "mg_server_run_synthetic")
+        return st.as_dict(), comp
+
+
 # ------------------------------------------------------------------ benchmark problems
 SIMP_MATERIAL = dict(E0=1.0, Emin=1e-9, nu=0.3, penal=3.0, thickness=1.0, k0=0.0, k_beta=0.0)
 
@@ -401,6 +651,28 @@ def simp_cantilever(nx, ny, nz, load_y0=0, load_y1=None, material=None):
     load_vals = np.full(ys.shape[0], -1.0 / ys.shape[0])
     return Problem(PHYS_HEX8, coords, conn, material or SIMP_MATERIAL, fixed_dofs=fixed,
                    load_dofs=load_dofs, load_values=load_vals, grid=(nx, ny, nz))
+
+
+BATCH_SIZES = ((16, 8, 8), (32, 16, 16), (48, 24, 24), (64, 32, 32), (96, 48, 48))
+
+
+def batch_designs(n, seed=0, sizes=BATCH_SIZES, max_cases=4):
+    """Seeded batch of SIMP cantilever designs: grid drawn uniformly from `sizes`,
+    densities iid U[0.01, 1], 1..max_cases load cases, each a unit -z line load on
+    the x = max, z = 0 edge over a random contiguous node span along y."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nx, ny, nz = sizes[int(rng.integers(len(sizes)))]
+        rho = rng.uniform(0.01, 1.0, nx * ny * nz)
+        nc = int(rng.integers(1, max_cases + 1))
+        spans = []
+        for _ in range(nc):
+            j0 = int(rng.integers(0, ny + 1))
+            j1 = int(rng.integers(j0, ny + 1))
+            spans.append((j0, j1))
+        out.append(dict(nx=nx, ny=ny, nz=nz, rho=rho, spans=spans))
+    return out
 
 
 def heat_square(nx=200, ny=200, k0=1.0, beta=0.01, h=1.0, hc=10.0, Tinf=0.0, q=1.0,

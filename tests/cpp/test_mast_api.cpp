@@ -1,0 +1,306 @@
+// Tests of the C++ mirror of MAST's API (mast_api.hpp), written the way MAST's
+// own tests are (tests/material/mast_isotropic_material.cpp,
+// tests/element/structural/...): build the property cards, disciplines and
+// boundary conditions, assemble or solve, compare with the truth.  The truth
+// here is the FP64 oracle (oracle/mast_oracle.h), itself pinned to the
+// reference's known answers by tests/test_oracle_pins.py.
+#include <cmath>
+#include <random>
+#include <vector>
+
+#include "mast_api.hpp"
+#include "mast_oracle.h"
+#include "mini_catch.hpp"
+
+using MAST::Real;
+
+static bool have_gpu() {
+    char name[64];
+    int sm = 0, ma = 0, mi = 0;
+    return mg_device_info(name, 64, &sm, &ma, &mi) == MG_OK;
+}
+
+TEST_CASE("constant_isotropic_structural_material_3d", "[cpu],[isotropic],[material],[3D]") {
+    MAST::Parameter E("E_param", 72.0e9), nu("nu_param", 0.33);
+    MAST::ConstantFieldFunction E_f("E", E), nu_f("nu", nu);
+    MAST::IsotropicMaterialPropertyCard material;
+    material.add(E_f);
+    material.add(nu_f);
+    REQUIRE(material.contains("E"));
+    REQUIRE(material.contains("nu"));
+    const MAST::FieldFunction<MAST::RealMatrixX> &mat_stiff = material.stiffness_matrix(3);
+    MAST::RealMatrixX D;
+    mat_stiff(MAST::Point(2.3, 3.1, 5.2), 2.34, D);
+    double truth[36];
+    or_iso_stiffness_3d(72.0e9, 0.33, truth);
+    REQUIRE(D.rows() == 6 && D.cols() == 6);
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 6; j++) {
+            CHECK(D(i, j) == Approx(truth[6 * i + j]).margin(1e-6));
+            CHECK(D(i, j) == Approx(D(j, i)));
+        }
+    // dC/dE with nu held: C(E = 1)
+    MAST::RealMatrixX dD;
+    mat_stiff.derivative(E, MAST::Point(), 0.0, dD);
+    or_iso_stiffness_3d(1.0, 0.33, truth);
+    for (int i = 0; i < 36; i++) CHECK(dD.data()[i] == Approx(truth[i]));
+}
+
+TEST_CASE("constant_isotropic_structural_material_2d", "[cpu],[isotropic],[material],[2D]") {
+    MAST::Parameter E("E_param", 72.0e9), nu("nu_param", 0.33);
+    MAST::ConstantFieldFunction E_f("E", E), nu_f("nu", nu);
+    MAST::IsotropicMaterialPropertyCard material;
+    material.add(E_f);
+    material.add(nu_f);
+    for (int strain = 0; strain < 2; strain++) {
+        MAST::RealMatrixX D;
+        material.stiffness_matrix(2, strain == 1)(MAST::Point(), 0.0, D);
+        double truth[9];
+        or_iso_stiffness_2d(72.0e9, 0.33, strain == 0, truth);
+        for (int i = 0; i < 9; i++) CHECK(D.data()[i] == Approx(truth[i]).margin(1e-6));
+    }
+}
+
+TEST_CASE("constant_isotropic_thermal_conductance", "[cpu],[isotropic],[material],[thermal]") {
+    MAST::Parameter k("k_param", 237.0);
+    MAST::ConstantFieldFunction k_f("k_th", k);
+    MAST::IsotropicMaterialPropertyCard material;
+    material.add(k_f);
+    for (int dim = 1; dim <= 3; dim++) {
+        MAST::RealMatrixX K;
+        material.conductance_matrix(dim)(MAST::Point(), 0.0, K);
+        for (int i = 0; i < dim; i++)
+            for (int j = 0; j < dim; j++) CHECK(K(i, j) == Approx(i == j ? 237.0 : 0.0));
+    }
+}
+
+TEST_CASE("build_cube_numbering_and_boundary_ids", "[cpu],[mesh]") {
+    MAST::Mesh mesh;
+    MAST::MeshTools::Generation::build_cube(mesh, 4, 3, 2, 0, 4, 0, 3, 0, 2);
+    std::vector<double> c(5 * 4 * 3 * 3);
+    std::vector<int32_t> e(4 * 3 * 2 * 8);
+    or_grid_hex8(4, 3, 2, 4, 3, 2, c.data(), e.data());
+    REQUIRE(mesh.coords.size() == c.size() && mesh.conn.size() == e.size());
+    for (size_t i = 0; i < c.size(); i++) CHECK(mesh.coords[i] == Approx(c[i]));
+    for (size_t i = 0; i < e.size(); i++) CHECK(mesh.conn[i] == e[i]);
+    CHECK(mesh.boundary_nodes(4).size() == 4 * 3);  // x = 0 face
+    CHECK(mesh.boundary_nodes(2).size() == 4 * 3);  // x = max face
+    CHECK(mesh.boundary_nodes(0).size() == 5 * 4);  // z = 0 face
+    MAST::Mesh sq;
+    MAST::MeshTools::Generation::build_square(sq, 5, 4, 0, 1, 0, 1);
+    CHECK(sq.boundary_sides(1).size() == 4);  // x = 1 edge
+    CHECK(sq.boundary_nodes(3).size() == 5);  // x = 0 edge
+}
+
+TEST_CASE("misuse_is_reported", "[cpu],[errors]") {
+    REQUIRE_THROWS(MAST::PointLoadCondition(MAST::DIRICHLET));
+    MAST::NonlinearImplicitAssembly assembly;
+    REQUIRE_THROWS(assembly.problem());  // no discipline and system
+    MAST::IsotropicMaterialPropertyCard material;
+    REQUIRE_THROWS(material.value("E"));
+    if (!have_gpu()) {
+        // a complete set-up on a host without a GPU: the library's status surfaces
+        MAST::Mesh mesh;
+        MAST::MeshTools::Generation::build_cube(mesh, 2, 1, 1, 0, 2, 0, 1, 0, 1);
+        MAST::Parameter E("E_param", 1.0), nu("nu_param", 0.3);
+        MAST::ConstantFieldFunction E_f("E", E), nu_f("nu", nu);
+        material.add(E_f);
+        material.add(nu_f);
+        MAST::Solid3DSectionElementPropertyCard section;
+        section.set_material(material);
+        MAST::StructuralDiscipline discipline;
+        discipline.set_property_for_subdomain(0, section);
+        MAST::NonlinearSystem sys;
+        MAST::StructuralSystemInitialization init(sys, mesh);
+        MAST::StructuralNonlinearAssemblyElemOperations ops;
+        assembly.set_discipline_and_system(discipline, init, ops);
+        bool ecuda = false;
+        try {
+            assembly.problem();
+        } catch (const MAST::Error &e) {
+            ecuda = (e.status == MG_ECUDA || e.status == MG_ENOMEM);
+        }
+        REQUIRE(ecuda);
+    }
+}
+
+// config 0, written as a MAST driver: clamp x = 0, -z unit load over the x = max,
+// z = 0 edge, SIMP densities, Jacobi-PCG to 1e-10, compliance and dC/drho by adjoint
+TEST_CASE("hex8_simp_cantilever", "[gpu],[structural],[3D]") {
+    const int nx = 24, ny = 12, nz = 12;
+    MAST::Mesh mesh;
+    MAST::MeshTools::Generation::build_cube(mesh, nx, ny, nz, 0, nx, 0, ny, 0, nz);
+    MAST::Parameter E("E_param", 1.0), nu("nu_param", 0.3);
+    MAST::ConstantFieldFunction E_f("E", E), nu_f("nu", nu);
+    MAST::IsotropicMaterialPropertyCard material;
+    material.add(E_f);
+    material.add(nu_f);
+    MAST::Solid3DSectionElementPropertyCard section;
+    section.set_material(material);
+    MAST::StructuralDiscipline discipline;
+    discipline.set_property_for_subdomain(0, section);
+    MAST::DirichletBoundaryCondition clamp;
+    clamp.init(4, {0, 1, 2});
+    discipline.add_dirichlet_bc(4, clamp);
+    MAST::PointLoadCondition load(MAST::POINT_LOAD);
+    int n_load = 0;
+    for (int64_t n : mesh.boundary_nodes(2))
+        if (mesh.point(n).z == 0.0) {
+            load.add_node(n);
+            n_load++;
+        }
+    load.set_load({0.0, 0.0, -1.0 / n_load});
+    discipline.add_point_load(load);
+    MAST::NonlinearSystem sys;
+    MAST::StructuralSystemInitialization init(sys, mesh);
+    MAST::StructuralNonlinearAssemblyElemOperations ops;
+    MAST::NonlinearImplicitAssembly assembly;
+    assembly.set_discipline_and_system(discipline, init, ops);
+    std::mt19937_64 rng(7);
+    std::uniform_real_distribution<double> U(0.01, 1.0);
+    std::vector<Real> rho(mesh.n_elem());
+    for (auto &r : rho) r = U(rng);
+    assembly.set_simp(rho, 1e-9, 3.0);
+    sys.opts.rtol = 1e-10;
+    sys.solve(ops, assembly);
+    REQUIRE(sys.last_report.status == MG_OK);
+    REQUIRE(sys.last_report.relres <= 1e-10);
+    MAST::ComplianceOutput compliance;
+    assembly.calculate_output(sys.solution, false, compliance);
+    MAST::Vector adjoint;
+    sys.adjoint_solve(sys.solution, false, ops, compliance, assembly, adjoint);
+    std::vector<std::unique_ptr<MAST::Parameter>> params;
+    std::vector<const MAST::FunctionBase *> p_vec;
+    for (int64_t e = 0; e < mesh.n_elem(); e += 37) {
+        params.emplace_back(new MAST::Parameter(MAST::NonlinearImplicitAssembly::elem_param_name("rho", e), rho[e]));
+        p_vec.push_back(params.back().get());
+    }
+    std::vector<Real> sens;
+    assembly.calculate_output_adjoint_sensitivity_multiple_parameters_no_direct(sys.solution, false, adjoint, p_vec,
+                                                                              ops, compliance, sens);
+    // oracle
+    or_simp_desc d{nx, ny, nz, 1.0, 1e-9, 0.3, 3.0, 0, ny, 1.0, 1e-12, 1000000};
+    std::vector<double> u((size_t)3 * (nx + 1) * (ny + 1) * (nz + 1)), dc(mesh.n_elem());
+    or_simp_report rep;
+    REQUIRE(or_simp_solve(&d, rho.data(), u.data(), dc.data(), &rep) == 0);
+    CHECK(compliance.output_total() == Approx(rep.compliance).epsilon(1e-10));
+    for (size_t i = 0; i < p_vec.size(); i++) CHECK(sens[i] == Approx(dc[(size_t)i * 37]).epsilon(1e-9));
+    // the general adjoint path (lambda . dR/drho_e) agrees with the compliance shortcut
+    MAST::Vector dR;
+    assembly.sensitivity_assemble(sys.solution, false, *p_vec[3], dR);
+    Real s = 0;
+    for (size_t k = 0; k < dR.size(); k++) s += adjoint(k) * dR(k);
+    CHECK(s == Approx(sens[3]).epsilon(1e-9));
+}
+
+// dR/drho_e from sensitivity_assemble against a central difference of the
+// residual assembled by residual_and_jacobian
+TEST_CASE("structural_sensitivity_assemble_matches_fd", "[gpu],[structural],[3D]") {
+    const int nx = 4, ny = 3, nz = 2;
+    MAST::Mesh mesh;
+    MAST::MeshTools::Generation::build_cube(mesh, nx, ny, nz, 0, nx, 0, ny, 0, nz);
+    MAST::Parameter E("E_param", 1.0), nu("nu_param", 0.3);
+    MAST::ConstantFieldFunction E_f("E", E), nu_f("nu", nu);
+    MAST::IsotropicMaterialPropertyCard material;
+    material.add(E_f);
+    material.add(nu_f);
+    MAST::Solid3DSectionElementPropertyCard section;
+    section.set_material(material);
+    MAST::StructuralDiscipline discipline;
+    discipline.set_property_for_subdomain(0, section);
+    MAST::NonlinearSystem sys;
+    MAST::StructuralSystemInitialization init(sys, mesh);
+    MAST::StructuralNonlinearAssemblyElemOperations ops;
+    MAST::NonlinearImplicitAssembly assembly;
+    assembly.set_discipline_and_system(discipline, init, ops);
+    std::vector<Real> rho(mesh.n_elem(), 0.6);
+    assembly.set_simp(rho, 1e-9, 3.0);
+    std::mt19937_64 rng(3);
+    std::normal_distribution<double> N(0.0, 1.0);
+    MAST::Vector X(3 * mesh.n_nodes());
+    for (size_t i = 0; i < X.size(); i++) X(i) = 1e-2 * N(rng);
+    const int64_t e = 7;
+    MAST::Parameter p(MAST::NonlinearImplicitAssembly::elem_param_name("rho", e), rho[e]);
+    MAST::Vector dR;
+    assembly.sensitivity_assemble(X, false, p, dR);
+    const double h = 1e-6;
+    MAST::Vector Rp, Rm;
+    rho[e] = 0.6 + h;
+    assembly.set_simp(rho, 1e-9, 3.0);
+    assembly.residual_and_jacobian(X, &Rp, nullptr, sys);
+    rho[e] = 0.6 - h;
+    assembly.set_simp(rho, 1e-9, 3.0);
+    assembly.residual_and_jacobian(X, &Rm, nullptr, sys);
+    double err = 0, ref = 0;
+    for (size_t i = 0; i < X.size(); i++) {
+        const double fd = (Rp(i) - Rm(i)) / (2 * h);
+        err = std::max(err, std::fabs(fd - dR(i)));
+        ref = std::max(ref, std::fabs(dR(i)));
+    }
+    REQUIRE(ref > 0);
+    CHECK(err <= 1e-7 * ref);
+}
+
+// config 1 on a coarser grid: k(T) = k0 (1 + 0.01 T), q = 1 on [0.25, 0.75]^2,
+// T = 0 at x = 0, convection h = 10, T_inf = 0 at x = 1
+TEST_CASE("quad4_nonlinear_conduction", "[gpu],[heat],[2D]") {
+    const int n = 40;
+    MAST::Mesh mesh;
+    MAST::MeshTools::Generation::build_square(mesh, n, n, 0, 1, 0, 1);
+    MAST::Parameter k("k_param", 1.0), beta("beta_param", 0.01), h("h_param", 1.0);
+    MAST::ConstantFieldFunction k_f("k_th", k), b_f("k_beta", beta), h_f("h", h);
+    MAST::IsotropicMaterialPropertyCard material;
+    material.add(k_f);
+    material.add(b_f);
+    MAST::Solid2DSectionElementPropertyCard section;
+    section.set_material(material);
+    section.add(h_f);
+    MAST::HeatConductionDiscipline discipline;
+    discipline.set_property_for_subdomain(0, section);
+    MAST::DirichletBoundaryCondition left;
+    left.init(3, {0});
+    discipline.add_dirichlet_bc(3, left);
+    MAST::Parameter hc("hc", 10.0), Tinf("Tinf", 0.0), q("q", 1.0);
+    MAST::ConstantFieldFunction hc_f("convection_coeff", hc), Tinf_f("ambient_temperature", Tinf), q_f("heat_source", q);
+    MAST::BoundaryConditionBase conv(MAST::CONVECTION_HEAT_FLUX), src(MAST::HEAT_SOURCE);
+    conv.add(hc_f);
+    conv.add(Tinf_f);
+    src.add(q_f);
+    discipline.add_side_load(1, conv);
+    discipline.add_volume_load(1, src);
+    MAST::NonlinearSystem sys;
+    MAST::HeatConductionSystemInitialization init(sys, mesh);
+    MAST::HeatConductionNonlinearAssemblyElemOperations ops;
+    MAST::NonlinearImplicitAssembly assembly;
+    std::vector<double> qe(mesh.n_elem(), 0.0);
+    assembly._subdomain.assign(mesh.n_elem(), 0);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+            const double xc = (i + 0.5) / n, yc = (j + 0.5) / n;
+            if (xc > 0.25 && xc < 0.75 && yc > 0.25 && yc < 0.75) {
+                assembly._subdomain[i + n * j] = 1;
+                qe[i + n * j] = 1.0;
+            }
+        }
+    assembly.set_discipline_and_system(discipline, init, ops);
+    sys.opts.rtol = 1e-10;
+    sys.opts.newton_rtol = 1e-10;
+    sys.opts.consistent_jacobian = 1;
+    sys.solve(ops, assembly);
+    REQUIRE(sys.last_report.status == MG_OK);
+    MAST::AverageTemperatureOutput Tbar;
+    assembly.calculate_output(sys.solution, false, Tbar);
+    or_heat_desc d{n, n, 1.0, 1.0, 1.0, 0.01, 1.0, 10.0, 0.0, 1e-12, 1e-12, 100000, 30, 1, 0};
+    std::vector<double> T((size_t)(n + 1) * (n + 1)), s(mesh.n_elem(), 1.0), dq(mesh.n_elem());
+    or_heat_report rep;
+    REQUIRE(or_heat_solve(&d, s.data(), qe.data(), T.data(), dq.data(), &rep) == 0);
+    CHECK(Tbar.output_total() == Approx(rep.mean_temperature).epsilon(1e-9));
+    for (size_t i = 0; i < T.size(); i++) CHECK(sys.solution(i) == Approx(T[i]).epsilon(1e-8).margin(1e-12));
+    // total dq/dk0 through the library's adjoint (mg_mean_temperature)
+    mg_solve_opts o = sys.opts;
+    double qv = 0, dk0 = 0;
+    MAST::check(mg_mean_temperature(assembly.problem(), sys.solution.data(), &o, &qv, &dk0, nullptr), "mean T");
+    CHECK(dk0 == Approx(rep.dq_dk0).epsilon(1e-7));
+}
+
+MINI_CATCH_MAIN

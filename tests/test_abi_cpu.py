@@ -60,3 +60,42 @@ def test_problem_create_without_gpu_fails_cleanly():
         assert e.status in (M.MG_ECUDA, M.MG_ENOMEM)
     else:  # pragma: no cover - only on a GPU host
         p.close()
+
+
+def test_batch_create_validates_before_touching_the_gpu():
+    """Malformed designs are rejected with MG_EINVAL before any CUDA call; a
+    well-formed batch on a host without a GPU reports MG_ECUDA."""
+    import torch
+    rho = np.full(8 * 4 * 4, 0.5)
+    bad = [
+        dict(nx=8, ny=4, nz=4, rho=np.full(128, 1.5), spans=[(0, 4)]),  # density > 1
+        dict(nx=8, ny=4, nz=4, rho=rho, spans=[(3, 1)]),                # inverted span
+        dict(nx=8, ny=4, nz=4, rho=rho, spans=[(0, 5)]),                # span beyond the edge
+        dict(nx=0, ny=4, nz=4, rho=rho, spans=[(0, 4)]),                # empty grid
+        dict(nx=8, ny=4, nz=4, rho=rho, spans=[]),                      # no load case
+    ]
+    for d in bad:
+        try:
+            M.Batch([d])
+        except M.MastGpuError as e:
+            assert e.status == M.MG_EINVAL, (d, e)
+        else:  # pragma: no cover
+            raise AssertionError("accepted %r" % (d,))
+    if torch.cuda.is_available():
+        return
+    try:
+        M.Batch([dict(nx=8, ny=4, nz=4, rho=rho, spans=[(0, 4)])])
+    except M.MastGpuError as e:
+        assert e.status in (M.MG_ECUDA, M.MG_ENOMEM)
+
+
+def test_batch_designs_generator_is_seeded_and_in_range():
+    a = M.batch_designs(12, seed=3)
+    b = M.batch_designs(12, seed=3)
+    for x, y in zip(a, b):
+        assert (x["nx"], x["ny"], x["nz"]) == (y["nx"], y["ny"], y["nz"])
+        assert np.array_equal(x["rho"], y["rho"]) and x["spans"] == y["spans"]
+        assert (x["nx"], x["ny"], x["nz"]) in M.BATCH_SIZES
+        assert 1 <= len(x["spans"]) <= 4
+        assert all(0 <= j0 <= j1 <= x["ny"] for j0, j1 in x["spans"])
+        assert x["rho"].min() >= 0.01 and x["rho"].max() <= 1.0
