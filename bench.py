@@ -106,6 +106,61 @@ def plain_time_per_size(M, sizes, rtol=1e-8):
     return out
 
 
+def bench_small_configs(M, with_cpu=True):
+    """Configs 0 and 1 through the plain FP64 form (GPU), beside the oracle on the
+    host cores: config 0 = 24x12x12 HEX8 cantilever, rho = 0.5, Jacobi-PCG to 1e-10,
+    compliance and dC/drho; config 1 = QUAD4 200x200 k(T) conduction, Newton with
+    Jacobi-PCG to 1e-10, mean temperature and its adjoint sensitivities."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    out = {}
+    rho = np.full(24 * 12 * 12, 0.5)
+    with M.simp_cantilever(24, 12, 12) as p:
+        o = M.default_opts(precision=M.PLAIN_FP64, rtol=1e-10)
+        p.set_design(rho)
+        p.solve(o)
+        p.compliance()
+        ts = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            p.set_design(rho)
+            u, rep = p.solve(o)
+            c, dc = p.compliance()
+            ts.append(time.perf_counter() - t0)
+    g = {"gpu_ms_per_solve": 1e3 * min(ts), "iterations": rep.krylov_iterations, "relres": rep.relres,
+         "compliance": c}
+    if with_cpu:
+        t0 = time.perf_counter()
+        _, dc_ref, r = O.simp_solve(O.simp_desc(24, 12, 12, rtol=1e-10), rho)
+        g["cpu_ms_per_solve"] = 1e3 * (time.perf_counter() - t0)
+        g["cpu_threads"] = O.max_threads()
+        g["compliance_rel_err_vs_oracle"] = abs(c - r.compliance) / r.compliance
+        g["sens_rel_err_vs_oracle"] = float(np.abs(dc - dc_ref).max() / np.abs(dc_ref).max())
+    out["config0_hex8_24x12x12"] = g
+    with M.heat_square() as p:
+        o = M.default_opts(precision=M.PLAIN_FP64, rtol=1e-10, newton_rtol=1e-10, krylov=M.KRYLOV_CG)
+        oa = M.default_opts(precision=M.PLAIN_FP64, rtol=1e-10, krylov=M.KRYLOV_BICGSTAB)  # adjoint
+        p.solve(o, X=np.zeros(p.n_dofs))
+        p.mean_temperature(opts=oa)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            T, rep = p.solve(o, X=np.zeros(p.n_dofs))
+            q, dk0, ds = p.mean_temperature(opts=oa)
+            ts.append(time.perf_counter() - t0)
+    h = {"gpu_ms_per_solve": 1e3 * min(ts), "newton_iterations": rep.newton_iterations,
+         "krylov_iterations": rep.krylov_iterations, "mean_temperature": q}
+    if with_cpu:
+        t0 = time.perf_counter()
+        _, ds_ref, r = O.heat_solve(O.heat_desc(krylov=0), q_elem=O.heat_source_field(200, 200))
+        h["cpu_ms_per_solve"] = 1e3 * (time.perf_counter() - t0)
+        h["mean_temperature_rel_err_vs_oracle"] = abs(q - r.mean_temperature) / abs(r.mean_temperature)
+        h["dq_dk0_rel_err_vs_oracle"] = abs(dk0 - r.dq_dk0) / abs(r.dq_dk0)
+        h["dq_ds_rel_err_vs_oracle"] = float(np.abs(ds - ds_ref).max() / np.abs(ds_ref).max())
+    out["config1_quad4_heat_200x200"] = h
+    return out
+
+
 def bench_batch(M, n_designs=256, seed=0):
     """Batched design evaluations: n_designs SIMP cantilevers of mixed sizes with
     1-4 load cases each, all solved together (mixed form, autotuned schedule)."""
@@ -428,6 +483,7 @@ def main():
                  "spmv_us": sp_ms * 1e3, "spmv_GBps": sp_bytes / (sp_ms * 1e-3) / 1e9,
                  "spmv_frac": sp_bytes / (sp_ms * 1e-3) / 1e9 / peak}
 
+    small = bench_small_configs(M, with_cpu=not args.no_cpu)
     batch = None if args.no_batch else bench_batch(M)
     serve = None
     if not args.no_serve:
@@ -464,7 +520,7 @@ def main():
                 "e2e": e2e,
                 "roofline": roof, "plain_fp64": plain,
                 "speedup_vs_plain_fp64": (value / plain["solves_per_s"]) if plain else None,
-                "batch": batch, "serving": serve,
+                "small_configs": small, "batch": batch, "serving": serve,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "wall_s_timed": t_wall}
         print(json.dumps(line), flush=True)

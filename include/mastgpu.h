@@ -376,6 +376,28 @@ typedef struct mg_synthetic_desc {
 int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *desc, double *compliance_out,
                             mg_server_stats *stats);
 
+/* ---- density filter ----
+   MAST::FilterBase (src/level_set/filter_base.cpp): x_filtered_i =
+   sum_j w_ij x_j over the points j within `radius` of point i, w_ij = (radius -
+   d_ij) / sum_k (radius - d_ik) (`_init` :378-437, `_init2` :275-359); points
+   not flagged in dv_mask keep their value (compute_filtered_values :58-95).
+   transpose = 1 applies F^T: the chain rule of a design gradient taken with
+   respect to the filtered field (examples/structural/example_6/example_6.cpp:661-697). */
+typedef struct mg_filter mg_filter;
+/* element centroids of a structured grid with spacings hx, hy, hz (nz = 0: 2D
+   grid); dv_mask nullable (every element is a design variable) */
+int mg_filter_create_grid(int32_t nx, int32_t ny, int32_t nz, double hx, double hy, double hz,
+                          double radius, const uint8_t *dv_mask, mg_filter **out);
+/* arbitrary points (n x dim coordinates, dim 1..3) */
+int mg_filter_create_points(int64_t n, int32_t dim, const double *xyz, double radius,
+                            const uint8_t *dv_mask, mg_filter **out);
+int mg_filter_info(const mg_filter *f, int64_t *n, int64_t *nnz);
+int mg_filter_apply(mg_filter *f, const double *in, double *out, int32_t transpose);
+/* device pointers (in != out), on `stream` (NULL: the filter's own stream; no sync) */
+int mg_filter_apply_device(mg_filter *f, const double *in_dev, double *out_dev, int32_t transpose,
+                           void *stream);
+void mg_filter_destroy(mg_filter *f);
+
 /* parameter kinds for mg_sensitivity_assemble */
 #define MG_PARAM_DENSITY 0      /* rho_e of element param_index (elasticity) */
 #define MG_PARAM_K0 1           /* conductivity k0 (heat) */

@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
 
     auto usable = [&](int bi) {
         const MfProblem &Q = probs[bricks[bi].prob];
-        return !states[Q.root].done && (sel < 0 || sel == (Q.coarse < 0 ? 1 : 0));
+        return !states[Q.root].done && !Q.bottom && (sel < 0 || sel == (Q.coarse < 0 ? 1 : 0));
     };
     int bi = brick_lo + blockIdx.x;
     while (bi < n_bricks && !usable(bi)) bi += gridDim.x;
@@ -418,6 +418,13 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
         const float *sZ = reinterpret_cast<const float *>(smem + kOffBox + set * kBoxSet);
         const float *sP = sZ + 12800 / 4;
         const float *sE = sZ + 25600 / 4;
+        // live elements: those touching an owned node inside the grid (a brick at
+        // the high end of a dimension owns fewer than kBN nodes there); only their
+        // tiles are multiplied.  Row l of the live box is element (lx, ly, lz).
+        const int ex_n = min(kBN, P.NX - gx0) + 1, ey_n = min(kBN, P.NY - gy0) + 1,
+                  ez_n = min(kBN, P.NZ - gz0) + 1;
+        const int n_live = ex_n * ey_n * ez_n;
+        const int n_tiles = (n_live + 127) >> 7;
         // one thread waits for the halo; the barrier releases the others
         bool tma_ok = true;
         if (tid == 0) tma_ok = mbar_wait_bounded(tma_bar0 + 8 * set, tma_phase[set]);
@@ -434,15 +441,15 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
         // ---- tiles through a kStages-deep MMA ring:
         //      build A(t) | wait MMA(t-S+1) | barrier | issue MMA(t) | drain t-S+1
         constexpr int S = PR::kStages;
-        for (int t = 0; t < kNTILE + S - 1; t++) {
-            if (t < kNTILE) {
+        for (int t = 0; t < n_tiles + S - 1; t++) {
+            if (t < n_tiles) {
                 const int slot = t % S;
                 uint8_t *A_hi = smem + kOffA + (PR::kSplit ? 2 * slot : slot) * kABytes;
                 uint8_t *A_lo = A_hi + kABytes;
                 const int l = t * 128 + arow;
                 int base = -1;
-                if (l < kNEL) {
-                    const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+                if (l < n_live) {
+                    const int ex = l % ex_n, ey = (l / ex_n) % ey_n, ez = l / (ex_n * ey_n);
                     base = (ez * kBU + ey) * kBoxNX + 3 * ex + 1;
                 }
 #pragma unroll
@@ -497,7 +504,7 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
                 break;
             }
             fence_after();
-            if (t < kNTILE && tid == kIssuer) {
+            if (t < n_tiles && tid == kIssuer) {
                 const int slot = t % S;
                 const uint32_t a_hi = smem_u32(smem + kOffA + (PR::kSplit ? 2 * slot : slot) * kABytes);
                 const uint32_t a_lo = a_hi + kABytes;
@@ -524,11 +531,13 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
                     const int m = lg * 32 + lane, l = td * 128 + m;
                     float v[8];
                     tmem_ld8(tmem + slot * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
-                    if (l < kNEL) {
-                        const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
+                    if (l < n_live) {
+                        // results are kept at the element's place in the full 9^3 box
+                        const int ex = l % ex_n, ey = (l / ex_n) % ey_n, ez = l / (ex_n * ey_n);
+                        const int lp = (ez * kBE + ey) * kBE + ex;
                         const float e = sE[(ez * kBE + ey) * kBoxEX + ex + 3];
 #pragma unroll
-                        for (int n = 0; n < 8; n++) sres[l * kResStride + cg * 8 + n] = e * v[n];
+                        for (int n = 0; n < 8; n++) sres[lp * kResStride + cg * 8 + n] = e * v[n];
                     }
                 }
                 fence_before();
@@ -754,7 +763,7 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_first_kernel(
     for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
         const MfProblem &Q = probs[C.prob];
-        if (states[Q.root].done || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
+        if (states[Q.root].done || Q.bottom || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 rv = *reinterpret_cast<const float4 *>(rin + i);
             const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
@@ -778,7 +787,7 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_next_kernel(
     for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
         const MfProblem &Q = probs[C.prob];
-        if (states[Q.root].done || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
+        if (states[Q.root].done || Q.bottom || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 yv = *reinterpret_cast<const float4 *>(my + i);
             const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
@@ -804,6 +813,7 @@ __global__ void mg_restrict_kernel(const MfProblem *__restrict__ probs, int plo,
     const MfProblem C = probs[plo + blockIdx.y];
     if (states[C.root].done) return;
     const MfProblem F = probs[C.fine];
+    if (F.bottom) return;  // inside a bottom chain: restricted by the bottom kernel
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < C.n_pad;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t row = i / C.pitch;
@@ -840,7 +850,7 @@ __global__ void mg_prolong_kernel(const MfProblem *__restrict__ probs, int plo,
                                   const MfState *states, float *__restrict__ mx,
                                   const float *__restrict__ dinv) {
     const MfProblem F = probs[plo + blockIdx.y];
-    if (F.coarse < 0 || states[F.root].done) return;  // no coarser level: nothing to add
+    if (F.coarse < 0 || F.bottom || states[F.root].done) return;  // nothing to add here
     const MfProblem C = probs[F.coarse];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F.n_pad;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -881,6 +891,212 @@ __global__ void mg_coarsen_kernel(const MfProblem *__restrict__ probs, int plo,
                 for (int dx = 0; dx < 2; dx++)
                     s += E32[F.elem_off + ((int64_t)(2 * ez + dz) * F.ny + 2 * ey + dy) * F.pitch_e + 2 * ex + dx];
         E32[C.elem_off + ((int64_t)ez * C.ny + ey) * C.pitch_e + ex] = 0.25f * s;
+    }
+}
+
+// ------------------------------------------------------ bottom V-cycle (one CTA)
+// The small coarse levels of a design (from its chain head down to its
+// coarsest grid) are solved by one CTA per chain, entirely in shared memory,
+// in FP32 on the CUDA cores: the same Chebyshev-Jacobi smoothers, residuals,
+// restriction and prolongation as the level-by-level launches above, without
+// one launch per level operation.  Per level the shared memory holds x, b, r,
+// d, y, D^-1 (per dof, compact node-interleaved order) and E (per element).
+constexpr int kBottomThreads = 512;
+constexpr int kBottomMaxLevels = 6;
+constexpr int kBottomSmemMax = 200 * 1024;  // per chain: 576 + sum over levels (18 NN + ne) floats
+
+struct BottomLevel {
+    int NX, NY, NZ, nx, ny, nz;
+    float *x, *b, *r, *d, *y, *dinv, *E;
+};
+
+// y = A in on level L (0 on Dirichlet dofs; `in` is 0 there): node-centric
+// gather over the node's elements in a fixed order
+__device__ void bottom_apply(const BottomLevel &L, const float *sK, const float *in, float *out) {
+    const int nn = L.NX * L.NY * L.NZ;
+    for (int n = threadIdx.x; n < nn; n += kBottomThreads) {
+        const int i = n % L.NX, j = (n / L.NX) % L.NY, k = n / (L.NX * L.NY);
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        for (int dz = 0; dz < 2; dz++)
+            for (int dy = 0; dy < 2; dy++)
+                for (int dx = 0; dx < 2; dx++) {
+                    const int ex = i - dx, ey = j - dy, ez = k - dz;
+                    if (ex < 0 || ey < 0 || ez < 0 || ex >= L.nx || ey >= L.ny || ez >= L.nz) continue;
+                    const float e = L.E[ex + L.nx * (ey + L.ny * ez)];
+                    const float *K = sK + 3 * corner_index(dx, dy, dz) * 24;
+                    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+                    for (int bc = 0; bc < 8; bc++) {
+                        int bx, by, bz;
+                        corner_bits(bc, bx, by, bz);
+                        const float *u = in + 3 * ((ex + bx) + L.NX * ((ey + by) + L.NY * (ez + bz)));
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            s0 = fmaf(K[3 * bc + c], u[c], s0);
+                            s1 = fmaf(K[24 + 3 * bc + c], u[c], s1);
+                            s2 = fmaf(K[48 + 3 * bc + c], u[c], s2);
+                        }
+                    }
+                    a0 = fmaf(e, s0, a0);
+                    a1 = fmaf(e, s1, a1);
+                    a2 = fmaf(e, s2, a2);
+                }
+        out[3 * n] = L.dinv[3 * n] == 0.0f ? 0.0f : a0;
+        out[3 * n + 1] = L.dinv[3 * n + 1] == 0.0f ? 0.0f : a1;
+        out[3 * n + 2] = L.dinv[3 * n + 2] == 0.0f ? 0.0f : a2;
+    }
+}
+
+// x (+)= Chebyshev-Jacobi smoothing of degree deg for rhs rin (r, d, y scratch)
+__device__ void bottom_smooth(const BottomLevel &L, const float *sK, const float *rin, bool x0_zero, int deg,
+                              float inv_theta, const float *c1, const float *c2) {
+    const int nd = 3 * L.NX * L.NY * L.NZ;
+    for (int q = threadIdx.x; q < nd; q += kBottomThreads) {
+        const float rv = rin[q], dv = L.dinv[q] * rv * inv_theta;
+        L.r[q] = rv;
+        L.d[q] = dv;
+        L.x[q] = x0_zero ? dv : L.x[q] + dv;
+    }
+    __syncthreads();
+    for (int k = 1; k < deg; k++) {
+        bottom_apply(L, sK, L.d, L.y);
+        __syncthreads();
+        for (int q = threadIdx.x; q < nd; q += kBottomThreads) {
+            const float rv = L.r[q] - L.y[q];
+            const float dv = fmaf(c1[k], L.d[q], c2[k] * L.dinv[q] * rv);
+            L.r[q] = rv;
+            L.d[q] = dv;
+            L.x[q] += dv;
+        }
+        __syncthreads();
+    }
+}
+
+// r = b - A x  (0 on Dirichlet dofs)
+__device__ void bottom_residual(const BottomLevel &L, const float *sK) {
+    bottom_apply(L, sK, L.x, L.y);
+    __syncthreads();
+    const int nd = 3 * L.NX * L.NY * L.NZ;
+    for (int q = threadIdx.x; q < nd; q += kBottomThreads) L.r[q] = L.dinv[q] == 0.0f ? 0.0f : L.b[q] - L.y[q];
+    __syncthreads();
+}
+
+struct BottomCheb {
+    float inv_theta_s, inv_theta_c;
+    float c1s[32], c2s[32], c1c[32], c2c[32];
+};
+
+__global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
+    const MfProblem *__restrict__ probs, const int *__restrict__ heads, const MfState *states,
+    const float *__restrict__ E32, const float *__restrict__ dinv_g, const float *__restrict__ mb,
+    float *__restrict__ mx, const double *__restrict__ K0, BottomCheb cc, int sdeg, int cdeg) {
+    extern __shared__ __align__(16) float sbm[];
+    const int head = heads[blockIdx.x];
+    const MfProblem H = probs[head];
+    if (states[H.root].done) return;
+    float *sK = sbm;  // 576
+    for (int i = threadIdx.x; i < 576; i += kBottomThreads) sK[i] = (float)K0[i];
+    // carve the levels of the chain
+    BottomLevel Lv[kBottomMaxLevels];
+    int pl[kBottomMaxLevels];
+    int m = 0;
+    float *p = sbm + 576;
+    for (int q = head; q >= 0 && m < kBottomMaxLevels; q = probs[q].coarse) {
+        const MfProblem P = probs[q];
+        BottomLevel &L = Lv[m];
+        L.NX = P.NX; L.NY = P.NY; L.NZ = P.NZ;
+        L.nx = P.nx; L.ny = P.ny; L.nz = P.nz;
+        const int nd = 3 * P.NX * P.NY * P.NZ, ne = P.nx * P.ny * P.nz;
+        L.x = p; p += nd;
+        L.b = p; p += nd;
+        L.r = p; p += nd;
+        L.d = p; p += nd;
+        L.y = p; p += nd;
+        L.dinv = p; p += nd;
+        L.E = p; p += ne;
+        pl[m] = q;
+        m++;
+    }
+    // load E, D^-1 (and the rhs of the head) from the padded global layout
+    for (int l = 0; l < m; l++) {
+        const MfProblem P = probs[pl[l]];
+        BottomLevel &L = Lv[l];
+        const int ne = P.nx * P.ny * P.nz, nn = P.NX * P.NY * P.NZ;
+        for (int e = threadIdx.x; e < ne; e += kBottomThreads) {
+            const int ex = e % P.nx, ey = (e / P.nx) % P.ny, ez = e / (P.nx * P.ny);
+            L.E[e] = E32[P.elem_off + ((int64_t)ez * P.ny + ey) * P.pitch_e + ex];
+        }
+        for (int q = threadIdx.x; q < 3 * nn; q += kBottomThreads) {
+            const int n = q / 3, c = q - 3 * n;
+            const int i = n % P.NX, j = (n / P.NX) % P.NY, k = n / (P.NX * P.NY);
+            const int64_t g = dof_index(P, i, j, k, c);
+            L.dinv[q] = dinv_g[g];
+            if (l == 0) L.b[q] = L.dinv[q] == 0.0f ? 0.0f : mb[g];
+        }
+    }
+    __syncthreads();
+    // down: smooth, residual, restrict
+    for (int l = 0; l < m - 1; l++) {
+        bottom_smooth(Lv[l], sK, Lv[l].b, true, sdeg, cc.inv_theta_s, cc.c1s, cc.c2s);
+        bottom_residual(Lv[l], sK);
+        const BottomLevel &F = Lv[l], &C = Lv[l + 1];
+        const int ncd = 3 * C.NX * C.NY * C.NZ;
+        for (int q = threadIdx.x; q < ncd; q += kBottomThreads) {
+            const int n = q / 3, c = q - 3 * n;
+            const int I = n % C.NX, J = (n / C.NX) % C.NY, K = n / (C.NX * C.NY);
+            float out = 0.0f;
+            if (C.dinv[q] != 0.0f)
+                for (int dz = -1; dz <= 1; dz++) {
+                    const int kk = 2 * K + dz;
+                    if (kk < 0 || kk >= F.NZ) continue;
+                    for (int dy = -1; dy <= 1; dy++) {
+                        const int jj = 2 * J + dy;
+                        if (jj < 0 || jj >= F.NY) continue;
+                        for (int dx = -1; dx <= 1; dx++) {
+                            const int ii = 2 * I + dx;
+                            if (ii < 0 || ii >= F.NX) continue;
+                            const float w = (dx ? 0.5f : 1.0f) * (dy ? 0.5f : 1.0f) * (dz ? 0.5f : 1.0f);
+                            out = fmaf(w, F.r[3 * (ii + F.NX * (jj + F.NY * kk)) + c], out);
+                        }
+                    }
+                }
+            C.b[q] = out;
+        }
+        __syncthreads();
+    }
+    // coarsest grid of the chain
+    bottom_smooth(Lv[m - 1], sK, Lv[m - 1].b, true, cdeg, cc.inv_theta_c, cc.c1c, cc.c2c);
+    // up: prolong, residual, post-smooth
+    for (int l = m - 2; l >= 0; l--) {
+        const BottomLevel &F = Lv[l], &C = Lv[l + 1];
+        const int nfd = 3 * F.NX * F.NY * F.NZ;
+        for (int q = threadIdx.x; q < nfd; q += kBottomThreads) {
+            if (F.dinv[q] == 0.0f) continue;
+            const int n = q / 3, c = q - 3 * n;
+            const int ii = n % F.NX, jj = (n / F.NX) % F.NY, kk = n / (F.NX * F.NY);
+            const int Is[2] = {ii >> 1, (ii + 1) >> 1}, Js[2] = {jj >> 1, (jj + 1) >> 1}, Ks[2] = {kk >> 1, (kk + 1) >> 1};
+            const float w = ((ii & 1) ? 0.5f : 1.0f) * ((jj & 1) ? 0.5f : 1.0f) * ((kk & 1) ? 0.5f : 1.0f);
+            float acc = 0.0f;
+            for (int a = 0; a < ((kk & 1) ? 2 : 1); a++)
+                for (int bb = 0; bb < ((jj & 1) ? 2 : 1); bb++)
+                    for (int cc2 = 0; cc2 < ((ii & 1) ? 2 : 1); cc2++)
+                        acc = fmaf(w, C.x[3 * (Is[cc2] + C.NX * (Js[bb] + C.NY * Ks[a])) + c], acc);
+            F.x[q] += acc;
+        }
+        __syncthreads();
+        bottom_residual(Lv[l], sK);
+        // post-smoothing on the residual: x += S(r) (the smoother starts from r in place)
+        bottom_smooth(Lv[l], sK, Lv[l].r, false, sdeg, cc.inv_theta_s, cc.c1s, cc.c2s);
+    }
+    // the head's correction back to the padded global layout
+    {
+        const MfProblem P = probs[head];
+        const int nn = P.NX * P.NY * P.NZ;
+        for (int q = threadIdx.x; q < 3 * nn; q += kBottomThreads) {
+            const int n = q / 3, c = q - 3 * n;
+            const int i = n % P.NX, j = (n / P.NX) % P.NY, k = n / (P.NX * P.NY);
+            mx[dof_index(P, i, j, k, c)] = Lv[0].x[q];
+        }
     }
 }
 
@@ -1326,6 +1542,8 @@ int configure_kernels() {
     MG_TRY(set_apply_attrs<MG_MIXED_BF16X3>());
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_residual64_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kResidSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mg_bottom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kBottomSmemMax));
     done = true;
     return MG_OK;
 }
@@ -1563,6 +1781,27 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     b.n_pad = dof;
     b.n_elem_pad = el;
     b.n_nodes = nd;
+    // bottom chains: for every design, the first level below the finest whose
+    // chain (it and all coarser levels) fits the bottom kernel's shared memory
+    b.h_heads.clear();
+    b.bottom_smem = 0;
+    for (int r = 0; r < b.n_fine; r++) {
+        for (int q = b.h_probs[r].coarse; q >= 0; q = b.h_probs[q].coarse) {
+            int64_t floats = 576, depth = 0;
+            for (int t = q; t >= 0; t = b.h_probs[t].coarse, depth++) {
+                const MfProblem &T = b.h_probs[t];
+                // x, b, r, d, y, D^-1 per dof and E per element
+                floats += 18LL * T.NX * T.NY * T.NZ + (int64_t)T.nx * T.ny * T.nz;
+            }
+            const int64_t bytes = floats * 4;
+            if (depth <= kBottomMaxLevels && bytes <= kBottomSmemMax) {
+                b.h_heads.push_back(q);
+                b.bottom_smem = std::max(b.bottom_smem, (int)bytes);
+                for (int t = q; t >= 0; t = b.h_probs[t].coarse) b.h_probs[t].bottom = 1;
+                break;
+            }
+        }
+    }
     int dev = 0, sms = 0;
     MG_CUDA_TRY(cudaGetDevice(&dev));
     MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1588,6 +1827,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.chunk_part, (size_t)2 * nc));
     MG_TRY(dev_alloc_n(&b.err, 1));
     MG_TRY(dev_alloc_n(&b.diag_list, (size_t)b.n_probs));
+    MG_TRY(dev_alloc_n(&b.heads, std::max<size_t>(1, b.h_heads.size())));
     MG_TRY(dev_alloc_n(&b.Bop, 2560));
     MG_TRY(dev_alloc_n(&b.K0, 576));
     double K0[576];
@@ -1622,6 +1862,9 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.Bop, bop.data(), bop.size() * 4, cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
+    if (!b.h_heads.empty())
+        MG_CUDA_TRY(cudaMemcpyAsync(b.heads, b.h_heads.data(), b.h_heads.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), s));
     MG_CUDA_TRY(cudaMemsetAsync(b.err, 0, sizeof(int), s));
     MG_CUDA_TRY(cudaMemsetAsync(b.u64, 0, dof * 8, s));
@@ -1643,7 +1886,7 @@ void mf_batch_free(MfBatch &b) {
     void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.Bop, b.K0, b.mb, b.mx, b.md,
-                    b.my, b.mr, b.diag_list};
+                    b.my, b.mr, b.diag_list, b.heads};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
     b = MfBatch();
@@ -1805,17 +2048,25 @@ long long enqueue_smooth(MfBatch &b, int prec, int l, const float *rin, int x0_z
 // V-cycle z = M r on every design at once (level-0 rhs = CG residual r, z = mx).
 // A problem whose own coarsest grid is level l gets the coarse-grid smoother
 // (degree cdeg) there, whatever the depth of the other problems, so that each
-// problem's preconditioner does not depend on the batch it is solved in.
+// problem's preconditioner does not depend on the batch it is solved in.  The
+// small levels of each chain (MfProblem::bottom) are done by one CTA per chain
+// (mg_bottom_kernel) between the down and the up sweep.
 long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
     const Cheb cs = cheb_coeffs(b.cheb_lmax, sdeg), cc = cheb_coeffs(b.cheb_lmax, cdeg);
     const int L = b.n_levels;
-    auto has_bottom = [&](int l) {  // some problem of level l has no coarser level
+    auto any_level = [&](int l) {  // some problem of level l is solved level by level
         for (int pi = b.lvl_prob_lo[l]; pi < b.lvl_prob_hi[l]; pi++)
-            if (b.h_probs[pi].coarse < 0) return true;
+            if (!b.h_probs[pi].bottom) return true;
+        return false;
+    };
+    auto own_coarsest = [&](int l) {  // ... and has no coarser level
+        for (int pi = b.lvl_prob_lo[l]; pi < b.lvl_prob_hi[l]; pi++)
+            if (!b.h_probs[pi].bottom && b.h_probs[pi].coarse < 0) return true;
         return false;
     };
     long long n = 0;
     for (int l = 0; l < L - 1; l++) {
+        if (!any_level(l)) continue;
         const float *rin = (l == 0) ? b.r : b.mb;
         n += enqueue_smooth(b, prec, l, rin, 1, sdeg, cs, 0);
         ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my, 0};
@@ -1826,10 +2077,23 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
         dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), chi - clo);
         mg_restrict_kernel<<<grid, 256, 0, b.stream>>>(b.probs, clo, b.states, b.my, b.mb, b.dinv);
         n += 2;
-        if (has_bottom(l)) n += enqueue_smooth(b, prec, l, rin, 1, cdeg, cc, 1);
+        if (own_coarsest(l)) n += enqueue_smooth(b, prec, l, rin, 1, cdeg, cc, 1);
     }
-    n += enqueue_smooth(b, prec, L - 1, L == 1 ? b.r : b.mb, 1, cdeg, cc, -1);
+    if (any_level(L - 1)) n += enqueue_smooth(b, prec, L - 1, L == 1 ? b.r : b.mb, 1, cdeg, cc, -1);
+    if (!b.h_heads.empty()) {
+        BottomCheb bc{};
+        bc.inv_theta_s = cs.inv_theta;
+        bc.inv_theta_c = cc.inv_theta;
+        for (int k = 0; k < 32; k++) {
+            bc.c1s[k] = cs.c1[k]; bc.c2s[k] = cs.c2[k];
+            bc.c1c[k] = cc.c1[k]; bc.c2c[k] = cc.c2[k];
+        }
+        mg_bottom_kernel<<<(unsigned)b.h_heads.size(), kBottomThreads, b.bottom_smem, b.stream>>>(
+            b.probs, b.heads, b.states, b.E32, b.dinv, b.mb, b.mx, b.K0, bc, sdeg, cdeg);
+        n += 1;
+    }
     for (int l = L - 2; l >= 0; l--) {
+        if (!any_level(l)) continue;
         const float *rin = (l == 0) ? b.r : b.mb;
         const int flo = b.lvl_prob_lo[l], fhi = b.lvl_prob_hi[l];
         int64_t maxpad = 1;

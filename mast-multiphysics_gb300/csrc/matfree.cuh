@@ -43,7 +43,7 @@ struct MfProblem {
     int level;            // multigrid level (0 = the design's own grid)
     int root;             // level-0 problem whose solver state drives this one
     int coarse, fine;     // neighbouring levels (-1 if none)
-    int pad;
+    int bottom;           // 1: solved inside the one-CTA bottom V-cycle of its chain
 };
 
 struct MfBrick {
@@ -106,6 +106,10 @@ struct MfBatch {
     int n_levels = 1;
     std::vector<int> lvl_prob_lo, lvl_prob_hi, lvl_brick_lo, lvl_brick_hi, lvl_chunk_lo, lvl_chunk_hi;
     double cheb_lmax = 0.0;     // Gershgorin bound of D^-1 A (same on every level)
+    // bottom V-cycle: the head (first bottom level) of every chain that has one
+    std::vector<int> h_heads;
+    int *heads = nullptr;
+    int bottom_smem = 0;        // dynamic shared memory of the bottom kernel
     // FP64 refinement vectors (padded layout)
     double *u64 = nullptr, *r64 = nullptr, *f64 = nullptr;
     double *brick_part = nullptr, *chunk_part = nullptr;

@@ -225,6 +225,13 @@ def lib(autobuild=True):
     L.mg_batch_solve_subset.argtypes = [_vp, ctypes.POINTER(SolveOpts), _vp, _vp]
     L.mg_batch_results.argtypes = [_vp, _i32, _vp, _vp, _vp]
     L.mg_batch_autotune.argtypes = [_vp, ctypes.POINTER(SolveOpts), _i32, _vp]
+    L.mg_filter_create_grid.argtypes = [_i32, _i32, _i32, _dbl, _dbl, _dbl, _dbl, _vp, ctypes.POINTER(_vp)]
+    L.mg_filter_create_points.argtypes = [_i64, _i32, _vp, _dbl, _vp, ctypes.POINTER(_vp)]
+    L.mg_filter_info.argtypes = [_vp, _vp, _vp]
+    L.mg_filter_apply.argtypes = [_vp, _vp, _vp, _i32]
+    L.mg_filter_apply_device.argtypes = [_vp, _vp, _vp, _i32, _vp]
+    L.mg_filter_destroy.argtypes = [_vp]
+    L.mg_filter_destroy.restype = None
     L.mg_server_clock.restype = ctypes.c_double
     L.mg_server_create.argtypes = [ctypes.POINTER(MaterialDesc), ctypes.POINTER(ServerOpts),
                                    ctypes.POINTER(_vp)]
@@ -552,6 +559,54 @@ class Batch:
         check(lib().mg_batch_autotune(self.h, ctypes.byref(opts), max_trials, ctypes.byref(secs)),
               "mg_batch_autotune")
         return opts, secs.value
+
+
+class Filter:
+    """Density filter (mg_filter_*): Filter.grid(nx, ny, nz, radius) over element
+    centroids, or Filter(points, radius) over arbitrary points."""
+
+    def __init__(self, points=None, radius=1.5, dv=None, _grid=None):
+        h = _vp()
+        self._dv = None if dv is None else np.ascontiguousarray(dv, dtype=np.uint8)
+        if _grid is not None:
+            nx, ny, nz, hx, hy, hz = _grid
+            check(lib().mg_filter_create_grid(nx, ny, nz, hx, hy, hz, radius, _p(self._dv), ctypes.byref(h)),
+                  "mg_filter_create_grid")
+        else:
+            pts = np.ascontiguousarray(points, dtype=np.float64)
+            check(lib().mg_filter_create_points(pts.shape[0], pts.shape[1], _p(pts), radius, _p(self._dv),
+                                                ctypes.byref(h)), "mg_filter_create_points")
+        self.h = h
+        n, nnz = _i64(), _i64()
+        check(lib().mg_filter_info(self.h, ctypes.byref(n), ctypes.byref(nnz)), "mg_filter_info")
+        self.n, self.nnz = n.value, nnz.value
+
+    @classmethod
+    def grid(cls, nx, ny, nz, radius, dv=None, h=(1.0, 1.0, 1.0)):
+        return cls(radius=radius, dv=dv, _grid=(nx, ny, nz, h[0], h[1], h[2]))
+
+    def apply(self, x, transpose=False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.n)
+        check(lib().mg_filter_apply(self.h, _p(x), _p(y), int(transpose)), "mg_filter_apply")
+        return y
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mg_filter_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Server:

@@ -1067,3 +1067,77 @@ int or_heat_solve(const or_heat_desc *d, const double *s_elem, const double *q_e
     free(ce); free(cs); free(R); free(dT); free(dqdT); free(rpt); free(ct); free(vt); free(lam);
     return st;
 }
+
+/* ------------------------------------------------------------------ density filter
+   MAST::FilterBase (src/level_set/filter_base.cpp): the weights of point i are
+   w_ij = (r - d_ij) / sum_k (r - d_ik) over every point j with d_ij <= r
+   (`_init`, the linear search, :378-437, normalised at :429-435); the
+   filtered value of a design-variable point is sum_j w_ij x_j, any other point
+   keeps its input value (compute_filtered_values, :58-95).  Plain O(n^2)
+   search over the points, as the reference's linear search does. */
+int or_filter_points(int64_t n, int dim, const double *xyz, double r, const uint8_t *dv,
+                     const double *in, double *out, int transpose) {
+    if (n <= 0 || r <= 0.0) return -1;
+    double *S = (double *)calloc((size_t)n, sizeof(double));
+    if (!S) return -2;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        double s = 0.0;
+        for (int64_t j = 0; j < n; j++) {
+            double d2 = 0.0;
+            for (int c = 0; c < dim; c++) {
+                const double t = xyz[i * dim + c] - xyz[j * dim + c];
+                d2 += t * t;
+            }
+            if (d2 <= r * r) s += r - sqrt(d2);
+        }
+        S[i] = s;
+    }
+    if (!transpose) {
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; i++) {
+            if (dv && !dv[i]) { out[i] = in[i]; continue; }
+            double acc = 0.0;
+            for (int64_t j = 0; j < n; j++) {
+                double d2 = 0.0;
+                for (int c = 0; c < dim; c++) {
+                    const double t = xyz[i * dim + c] - xyz[j * dim + c];
+                    d2 += t * t;
+                }
+                if (d2 <= r * r) acc += (r - sqrt(d2)) / S[i] * in[j];
+            }
+            out[i] = acc;
+        }
+    } else {
+        /* out_j = sum_i [dv_i] w_ij in_i + [!dv_j] in_j */
+#pragma omp parallel for schedule(static)
+        for (int64_t j = 0; j < n; j++) {
+            double acc = (dv && !dv[j]) ? in[j] : 0.0;
+            for (int64_t i = 0; i < n; i++) {
+                if (dv && !dv[i]) continue;
+                double d2 = 0.0;
+                for (int c = 0; c < dim; c++) {
+                    const double t = xyz[i * dim + c] - xyz[j * dim + c];
+                    d2 += t * t;
+                }
+                if (d2 <= r * r) acc += (r - sqrt(d2)) / S[i] * in[i];
+            }
+            out[j] = acc;
+        }
+    }
+    free(S);
+    return 0;
+}
+
+/* element centroids of a structured grid (spacing hx, hy, hz; nz = 0: 2D) */
+void or_grid_centroids(int nx, int ny, int nz, double hx, double hy, double hz, double *xyz) {
+    const int dim = nz > 0 ? 3 : 2, NZ = nz > 0 ? nz : 1;
+    int64_t e = 0;
+    for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++, e++) {
+                xyz[e * dim] = (i + 0.5) * hx;
+                xyz[e * dim + 1] = (j + 0.5) * hy;
+                if (dim == 3) xyz[e * dim + 2] = (k + 0.5) * hz;
+            }
+}

@@ -150,6 +150,12 @@ typedef struct {
 int or_heat_solve(const or_heat_desc *d, const double *s_elem, const double *q_elem,
                   double *T, double *dq_ds, or_heat_report *rep);
 
+/* density filter of MAST::FilterBase over points (transpose = 1: the chain
+   rule F^T); element centroids of a structured grid */
+int or_filter_points(int64_t n, int dim, const double *xyz, double r, const uint8_t *dv,
+                     const double *in, double *out, int transpose);
+void or_grid_centroids(int nx, int ny, int nz, double hx, double hy, double hz, double *xyz);
+
 /* bounded-sample timers used by the CPU baseline */
 double or_wtime(void);
 int or_max_threads(void);

@@ -97,6 +97,8 @@ def lib():
         L.or_simp_modulus.argtypes = [ctypes.POINTER(SimpDesc), i64, _f64p, vp, vp]
         L.or_heat_solve.argtypes = [ctypes.POINTER(HeatDesc), vp, vp, _f64p, vp,
                                     ctypes.POINTER(HeatReport)]
+        L.or_filter_points.argtypes = [i64, i32, _f64p, d, vp, _f64p, _f64p, i32]
+        L.or_grid_centroids.argtypes = [i32, i32, i32, d, d, d, _f64p]
         L.or_wtime.restype = d
         L.or_max_threads.restype = i32
         L.or_set_threads.argtypes = [i32]
@@ -335,3 +337,23 @@ def set_threads(n):
 
 def max_threads():
     return lib().or_max_threads()
+
+
+def grid_centroids(nx, ny, nz, hx=1.0, hy=1.0, hz=1.0):
+    dim = 3 if nz > 0 else 2
+    xyz = np.zeros(nx * ny * max(nz, 1) * dim)
+    lib().or_grid_centroids(nx, ny, nz, hx, hy, hz, xyz)
+    return xyz.reshape(-1, dim)
+
+
+def filter_points(xyz, radius, x, dv=None, transpose=False):
+    """MAST::FilterBase weights over points (O(n^2) search): F x, or F^T x."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    n, dim = xyz.shape
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros(n)
+    dvm = None if dv is None else np.ascontiguousarray(dv, dtype=np.uint8)
+    rc = lib().or_filter_points(n, dim, xyz.reshape(-1), radius, _ptr(dvm), x, out, int(transpose))
+    if rc:
+        raise RuntimeError("oracle filter failed (%d)" % rc)
+    return out
