@@ -425,6 +425,14 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
                   ez_n = min(kBN, P.NZ - gz0) + 1;
         const int n_live = ex_n * ey_n * ez_n;
         const int n_tiles = (n_live + 127) >> 7;
+        const bool full = (n_live == kNEL);  // constant divisors on the common path
+        auto live_xyz = [&](int l, int &ex, int &ey, int &ez) {
+            if (full) {
+                ex = l % kBE; ey = (l / kBE) % kBE; ez = l / (kBE * kBE);
+            } else {
+                ex = l % ex_n; ey = (l / ex_n) % ey_n; ez = l / (ex_n * ey_n);
+            }
+        };
         // one thread waits for the halo; the barrier releases the others
         bool tma_ok = true;
         if (tid == 0) tma_ok = mbar_wait_bounded(tma_bar0 + 8 * set, tma_phase[set]);
@@ -449,7 +457,8 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
                 const int l = t * 128 + arow;
                 int base = -1;
                 if (l < n_live) {
-                    const int ex = l % ex_n, ey = (l / ex_n) % ey_n, ez = l / (ex_n * ey_n);
+                    int ex, ey, ez;
+                    live_xyz(l, ex, ey, ez);
                     base = (ez * kBU + ey) * kBoxNX + 3 * ex + 1;
                 }
 #pragma unroll
@@ -533,7 +542,8 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
                     tmem_ld8(tmem + slot * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
                     if (l < n_live) {
                         // results are kept at the element's place in the full 9^3 box
-                        const int ex = l % ex_n, ey = (l / ex_n) % ey_n, ez = l / (ex_n * ey_n);
+                        int ex, ey, ez;
+                        live_xyz(l, ex, ey, ez);
                         const int lp = (ez * kBE + ey) * kBE + ex;
                         const float e = sE[(ez * kBE + ey) * kBoxEX + ex + 3];
 #pragma unroll
