@@ -646,6 +646,330 @@ __global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
     if (warp == 0) tmem_dealloc(tmem, 128);
 }
 
+// ----------------------------------------------------------- column operator
+// y = sum_e E_e P_e^T K0 P_e x by columns of owned nodes (kCX x kCY nodes in x,
+// y; up to kCZ node planes in z), streamed plane by plane.  The A operand of
+// the tensor-core MMA is never assembled: the halo nodes of each plane are
+// converted once into 16-byte node records (x, y, z, 0 in TF32; x, y, z and five
+// zeros in BF16), and the MMA reads them in place.  An element plane holds 8 x 16
+// elements, one M = 128 tile: row r = ey * 8 + ex; the eight rows of a core
+// matrix are eight x-consecutive elements (nodes 16 bytes apart), the 16 row
+// groups are the 16 element rows (stride of a node row).  One MMA per corner
+// pair (dx = 0, 1 at fixed dy, dz) uses K chunks 16 bytes apart (the node and
+// its x-neighbour), so the element operator is 4 MMAs per product (3 products
+// in the split forms) against four B tiles cut from K0.
+constexpr int kColThreads = 256;
+constexpr int kCPX = kCX + 2;                 // 9 nodes per plane row
+constexpr int kCPY = kCY + 2;                 // 17 node rows per plane
+constexpr int kCPN = kCPX * kCPY;             // 153 nodes per plane
+constexpr int kCPB = kCPN * 16;               // 2448 bytes per converted plane (one part)
+constexpr int kCRing = 4;                     // planes in flight
+constexpr int kCRawX = 32;                    // TMA node box: 32 floats x 17 rows x 1 plane
+constexpr int kCRawNode = kCRawX * kCPY * 4;  // 2176
+constexpr int kCRawE = 12 * 16 * 4;           // E box: 12 elements x 16 rows x 1 plane = 768
+constexpr int kCRawSlot = 2 * kCRawNode + kCRawE;  // 5120 (z, p_old, E)
+constexpr int kCResStride = 25;
+// issuer of the MMAs and waiter on them (warp 7 has one drain task)
+constexpr int kColIssuer = 224;
+
+constexpr int kC_OffB = 0;                                      // 4 B tiles x 1 KB, hi | lo
+constexpr int kC_OffConv = 8192;                                // kCRing x (hi, lo) converted planes
+constexpr int kC_OffU = kC_OffConv + kCRing * 2 * kCPB;         // 27776: FP32 u of the planes
+constexpr int kC_OffE = kC_OffU + kCRing * kCPN * 3 * 4;        // 35120: E of the element planes
+constexpr int kC_OffRaw = (kC_OffE + kCRing * 128 * 4 + 127) / 128 * 128;  // 37248: TMA ring
+constexpr int kC_OffR = kC_OffRaw + kCRing * kCRawSlot;         // 57728: drained plane results
+constexpr int kC_OffBar = (kC_OffR + 2 * 128 * kCResStride * 4 + 127) / 128 * 128;  // 83328
+constexpr int kColSmem = kC_OffBar + 64;
+static_assert(kC_OffRaw % 128 == 0 && kCRawSlot % 128 == 0 && kCRawNode % 128 == 0, "TMA destinations");
+static_assert(kC_OffConv % 16 == 0 && kCPB % 16 == 0, "operand alignment");
+
+// Columns col_lo .. col_hi-1; the same modes as mf_apply_kernel.
+template <int PREC, int MODE>
+__global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
+    const MfProblem *__restrict__ probs, const MfCol *__restrict__ cols, int col_lo, int col_hi, int sel,
+    const CUtensorMap *__restrict__ tmaps, int in_slot, int parity, const uint32_t *__restrict__ Bop2,
+    const float *__restrict__ dinv, const float *__restrict__ rhs, float *__restrict__ p0,
+    float *__restrict__ p1, float *__restrict__ y, MfState *states, double *__restrict__ col_part,
+    int *err) {
+    using PR = Prec<PREC>;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ double red_sh[kColThreads / 32];
+    __shared__ double tree[kColThreads];
+    __shared__ int sh_last;
+    uint32_t *convHi = reinterpret_cast<uint32_t *>(smem + kC_OffConv);  // slot s: + s * 2 * kCPB
+    float *sU = reinterpret_cast<float *>(smem + kC_OffU);
+    float *sE = reinterpret_cast<float *>(smem + kC_OffE);
+    float *sR = reinterpret_cast<float *>(smem + kC_OffR);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kC_OffBar);  // tma[4], mma[2]
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kC_OffBar + 56);
+    const uint32_t tma_bar0 = smem_u32(&bars[0]);
+    const uint32_t mma_bar0 = smem_u32(&bars[4]);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float *p_new = (MODE == 1) ? (parity ? p0 : p1) : nullptr;
+
+    auto usable = [&](int ci) {
+        const MfProblem &Q = probs[cols[ci].prob];
+        return !states[Q.root].done && !Q.bottom && (sel < 0 || sel == (Q.coarse < 0 ? 1 : 0));
+    };
+    int ci = col_lo + blockIdx.x;
+    while (ci < col_hi && !usable(ci)) ci += gridDim.x;
+    if (ci >= col_hi) return;  // uniform: no work for this block
+
+    if (tid == 0) {
+        for (int k = 0; k < kCRing; k++) mbar_init(tma_bar0 + 8 * k, 1);
+        for (int k = 0; k < 2; k++) mbar_init(mma_bar0 + 8 * k, 1);
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tslot), 64);  // 2 accumulator slots x 32 columns
+    {
+        // B tiles: [tf32 hi 1024 | tf32 lo 1024 | bf16 hi 1024 | bf16 lo 1024] words
+        const uint32_t *src = Bop2 + (PR::kTf32 ? 0 : 2048);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(smem + kC_OffB);
+        for (int i = tid; i < 2048; i += kColThreads) dst[i] = src[i];
+        // node records: the unused lanes stay 0 (B has zero rows there; 0 x NaN is NaN)
+        for (int i = tid; i < kCRing * 2 * kCPB / 4; i += kColThreads) convHi[i] = 0u;
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t b_base = smem_u32(smem + kC_OffB), conv_base = smem_u32(smem + kC_OffConv);
+
+    uint32_t tma_phase[kCRing] = {0, 0, 0, 0}, mma_phase[2] = {0, 0};
+    uint32_t tma_issued = 0;  // bit k: a TMA into raw slot k is outstanding
+    bool failed = false;
+    int run = 0;  // columns of the current problem since the last counter update (MODE 1)
+    for (; ci < col_hi && !failed;) {
+        int nci = ci + gridDim.x;
+        while (nci < col_hi && !usable(nci)) nci += gridDim.x;
+        const MfCol cl = cols[ci];
+        const MfProblem P = probs[cl.prob];
+        MfState *st = states + cl.prob;
+        const float beta = (MODE == 1) ? (float)st->beta : 0.0f;
+        const int x0 = cl.cx * kCX, y0 = cl.cy * kCY, z0 = cl.cz * P.col_z;
+        const int z1 = min(z0 + P.col_z, P.NZ);
+        const int S = z1 - z0 + 1;                     // element planes z0-1 .. z1-1
+        const int xs = (3 * (x0 - 1)) & ~3, ox = 3 * (x0 - 1) - xs;  // 16-byte aligned box starts
+        const int xe = (x0 - 1) & ~3, oe = (x0 - 1) - xe;
+        const CUtensorMap *maps = tmaps + (size_t)cl.prob * kMapsPerProblem + 6;
+        // TMA of node plane p (nz = z0 - 1 + p) and, for p < S, element plane p
+        auto issue = [&](int p) {
+            const int slot = p % kCRing;
+            uint8_t *raw = smem + kC_OffRaw + slot * kCRawSlot;
+            const uint32_t bar = tma_bar0 + 8 * slot;
+            const uint32_t bytes = (MODE == 1 ? 2 : 1) * kCRawNode + (p < S ? kCRawE : 0);
+            mbar_expect_tx(bar, bytes);
+            tma_load_3d(smem_u32(raw), maps + in_slot, xs, y0 - 1, z0 - 1 + p, bar);
+            if (MODE == 1) tma_load_3d(smem_u32(raw + kCRawNode), maps + 1 + parity, xs, y0 - 1, z0 - 1 + p, bar);
+            if (p < S) tma_load_3d(smem_u32(raw + 2 * kCRawNode), maps + 3, xe, y0 - 1, z0 - 1 + p, bar);
+        };
+        // wait for plane p and convert it into the operand records, u and E
+        auto convert = [&](int p) -> bool {
+            const int slot = p % kCRing;
+            bool ok = true;
+            if (tid == 0) ok = mbar_wait_bounded(tma_bar0 + 8 * slot, tma_phase[slot]);
+            if (__syncthreads_or(!ok)) return false;
+            tma_phase[slot] ^= 1u;
+            tma_issued &= ~(1u << slot);
+            const float *rz = reinterpret_cast<const float *>(smem + kC_OffRaw + slot * kCRawSlot);
+            const float *rp = rz + kCRawNode / 4;
+            const float *re = rz + 2 * kCRawNode / 4;
+            uint32_t *hi = convHi + slot * (2 * kCPB / 4);
+            uint32_t *lo = hi + kCPB / 4;
+            float *u = sU + slot * kCPN * 3;
+            for (int i = tid; i < kCPN * 3; i += kColThreads) {
+                const int n = i / 3, c = i - 3 * n;
+                const int nx = n % kCPX, ny = n / kCPX;
+                const int bo = ny * kCRawX + ox + 3 * nx + c;
+                const float v = (MODE == 1) ? fmaf(beta, rp[bo], rz[bo]) : rz[bo];
+                u[i] = v;
+                if (PR::kTf32) {
+                    const uint32_t h = to_tf32(v);
+                    hi[n * 4 + c] = h;
+                    if (PR::kSplit) lo[n * 4 + c] = __float_as_uint(v - __uint_as_float(h));
+                } else {
+                    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                    reinterpret_cast<__nv_bfloat16 *>(hi)[n * 8 + c] = h;
+                    if (PR::kSplit)
+                        reinterpret_cast<__nv_bfloat16 *>(lo)[n * 8 + c] = __float2bfloat16_rn(v - __bfloat162float(h));
+                }
+            }
+            if (p < S)
+                for (int e = tid; e < 128; e += kColThreads) sE[slot * 128 + e] = re[(e >> 3) * 12 + oe + (e & 7)];
+            fence_async_smem();  // the records are read by the tensor core (async proxy)
+            return true;
+        };
+        // MMA of element plane s into accumulator slot s % 2
+        auto mma = [&](int s) {
+            const uint32_t d = tmem + (s & 1) * 32;
+            uint32_t acc = 0u;
+            const int nprod = PR::kSplit ? 3 : 1;
+            for (int prod = 0; prod < nprod; prod++) {
+                const uint32_t apart = (prod == 2) ? kCPB : 0u;         // lo records
+                const uint32_t bpart = (prod == 1) ? 4096u : 0u;        // lo B
+#pragma unroll
+                for (int st4 = 0; st4 < 4; st4++) {
+                    const int dy = st4 & 1, dz = st4 >> 1;
+                    const uint32_t a = conv_base + ((s + dz) % kCRing) * 2 * kCPB + apart + dy * kCPX * 16;
+                    umma<PR::kTf32>(d, umma_desc(a, 16, kCPX * 16), umma_desc(b_base + bpart + st4 * 1024, 128, 256),
+                                    acc);
+                    acc = 1u;
+                }
+            }
+            umma_commit(mma_bar0 + 8 * (s & 1));
+        };
+
+        // ---- prologue: planes 0, 1 converted, 2 and 3 in flight, MMA(0) issued
+        if (tid == 0) {
+            fence_async_smem();
+            for (int p = 0; p <= min(3, S); p++) issue(p);
+        }
+        for (int p = 0; p <= min(3, S); p++) tma_issued |= 1u << (p % kCRing);
+        if (!convert(0) || !convert(1)) {
+            failed = true;
+            if (tid == 0) atomicOr(err, 2);
+            break;
+        }
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (tid == kColIssuer) mma(0);
+        float part = 0.0f;
+        for (int s = 0; s < S && !failed; s++) {
+            // (a) convert plane s + 2; the TMA ring slot of plane s is then free for s + 4
+            if (s + 2 <= S && !convert(s + 2)) {
+                failed = true;
+                if (tid == 0) atomicOr(err, 2);
+                break;
+            }
+            fence_before();
+            __syncthreads();
+            fence_after();
+            if (s + 4 <= S) {
+                if (tid == 0) {
+                    fence_async_smem();
+                    issue(s + 4);
+                }
+                tma_issued |= 1u << ((s + 4) % kCRing);
+            }
+            // (b) MMA(s + 1) overlaps the drain of plane s
+            if (tid == kColIssuer && s + 1 < S) mma(s + 1);
+            // (c) wait for MMA(s)
+            bool ok = true;
+            if (tid == kColIssuer) ok = mbar_wait_bounded(mma_bar0 + 8 * (s & 1), mma_phase[s & 1]);
+            mma_phase[s & 1] ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                if (tid == kColIssuer) atomicOr(err, 1);
+                break;
+            }
+            fence_after();
+            // (d) drain element plane s: rows of lane group w % 4, columns 8 cg .. 8 cg + 7
+            {
+                const float *Es = sE + (s % kCRing) * 128;
+                float *R = sR + (s & 1) * 128 * kCResStride;
+                for (int task = warp; task < 12; task += kColThreads / 32) {
+                    const int lg = task & 3, cg = task >> 2;
+                    const int r = lg * 32 + lane;
+                    float v[8];
+                    tmem_ld8(tmem + (s & 1) * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
+                    const float e = Es[r];
+#pragma unroll
+                    for (int n = 0; n < 8; n++) R[r * kCResStride + cg * 8 + n] = e * v[n];
+                }
+            }
+            fence_before();
+            __syncthreads();
+            // (e) node sums of node plane nz = z0 - 1 + s (owned planes z0 .. z1-1)
+            const int nz = z0 - 1 + s;
+            if (s >= 1 && nz < z1) {
+                const float *R0 = sR + (s & 1) * 128 * kCResStride;         // element plane nz (dz = 0)
+                const float *R1 = sR + ((s - 1) & 1) * 128 * kCResStride;   // element plane nz - 1 (dz = 1)
+                const float *u = sU + (s % kCRing) * kCPN * 3;
+                for (int i = tid; i < kCX * kCY * 3; i += kColThreads) {
+                    const int n = i / 3, c = i - 3 * n;
+                    const int oxn = n % kCX, oyn = n / kCX;
+                    const int gx = x0 + oxn, gy = y0 + oyn;
+                    if (gx >= P.NX || gy >= P.NY) continue;
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int a = 0; a < 8; a++) {
+                        int dx, dy, dz;
+                        corner_bits(a, dx, dy, dz);
+                        const int r = (oyn + 1 - dy) * 8 + (oxn + 1 - dx);
+                        acc += (dz ? R1 : R0)[r * kCResStride + 3 * a + c];
+                    }
+                    const int64_t gd = dof_index(P, gx, gy, nz, c);
+                    if (MODE == 1) {
+                        const float pv = u[((oyn + 1) * kCPX + oxn + 1) * 3 + c];
+                        y[gd] = acc;
+                        p_new[gd] = pv;
+                        part = fmaf(pv, acc, part);
+                    } else if (MODE == 2) {
+                        y[gd] = (dinv[gd] == 0.0f) ? 0.0f : rhs[gd] - acc;
+                    } else {
+                        y[gd] = (dinv[gd] == 0.0f) ? 0.0f : acc;
+                    }
+                }
+            }
+        }
+        if (failed) break;
+        if (MODE == 1) {
+            // column partial: FP32 within a warp, FP64 across warps
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            if (lane == 0) red_sh[warp] = (double)part;
+        }
+        __syncthreads();  // all of this column's shared data may be reused
+        if (MODE == 1) {
+            if (tid == 0) {
+                double sum = 0.0;
+                for (int w = 0; w < kColThreads / 32; w++) sum += red_sh[w];
+                col_part[ci] = sum;
+            }
+            run++;
+            const bool flush = nci >= col_hi || cols[nci].prob != cl.prob;
+            if (flush) {
+                if (tid == 0) {
+                    __threadfence();
+                    const unsigned tk = atomicAdd(&st->cnt_apply, (unsigned)run);
+                    sh_last = (tk + (unsigned)run == (unsigned)P.col_count);
+                }
+                run = 0;
+                __syncthreads();
+            }
+            if (flush && sh_last) {
+                double sum = 0.0;
+                for (int k = tid; k < P.col_count; k += kColThreads) sum += __ldcg(col_part + P.col_begin + k);
+                tree[tid] = sum;
+                __syncthreads();
+                for (int w = kColThreads / 2; w > 0; w >>= 1) {
+                    if (tid < w) tree[tid] += tree[tid + w];
+                    __syncthreads();
+                }
+                if (tid == 0) {
+                    const double pq = tree[0];
+                    st->cnt_apply = 0;
+                    st->pq = pq;
+                    if (is_bad(pq)) { st->status = MG_ENAN; st->done = 1; }
+                    else if (!(pq > 0.0)) { st->status = MG_EBREAKDOWN; st->done = 1; }
+                    else st->alpha = st->rz / pq;
+                }
+                __syncthreads();
+            }
+        }
+        ci = nci;
+    }
+    // after a failed wait, give the outstanding halo loads a bounded chance to land
+    if (failed)
+        for (int k = 0; k < kCRing; k++)
+            if (tma_issued & (1u << k)) (void)mbar_wait_bounded(tma_bar0 + 8 * k, tma_phase[k]);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
 // ---------------------------------------------------------------- vector phase
 // x += alpha p; r -= alpha q (r stays 0 on Dirichlet dofs, D^-1 = 0 there);
 // z = D^-1 r; rz, rr -> beta, stop test.  float4 over 16-byte aligned chunks.
@@ -1499,8 +1823,64 @@ void pack_b_operand(const double *K0, std::vector<uint32_t> &out) {
     }
 }
 
+// B tiles of the column operator: tile t = dy + 2 dz holds the K0 columns of the
+// corners (0, dy, dz) and (1, dy, dz) (K chunk dx: x, y, z, 0 in TF32; x, y, z
+// and five zeros in BF16) for the 32 N rows n = 3 a + c (libMesh corner a; rows
+// 24..31 zero), in the no-swizzle K-major layout: core matrix (n / 8, dx) at
+// ((n / 8) * 2 + dx) * 128 bytes.  [tf32 hi | tf32 lo | bf16 hi | bf16 lo], 1024
+// words each.
+void pack_b_columns(const double *K0, std::vector<uint32_t> &out) {
+    auto tf32_round = [](float x) -> float {
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;  // nearest, ties away
+        float r;
+        memcpy(&r, &u, 4);
+        return r;
+    };
+    auto bf16_bits = [](float x) -> uint32_t {
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        return ((u + 0x7fffu + ((u >> 16) & 1u)) >> 16) & 0xffffu;  // nearest even
+    };
+    auto bits_of = [](uint32_t h) -> float {
+        const uint32_t u = h << 16;
+        float r;
+        memcpy(&r, &u, 4);
+        return r;
+    };
+    auto fbits = [](float x) -> uint32_t {
+        uint32_t u;
+        memcpy(&u, &x, 4);
+        return u;
+    };
+    out.assign(4096, 0u);
+    for (int t = 0; t < 4; t++) {
+        const int dy = t & 1, dz = t >> 1;
+        for (int n = 0; n < 32; n++)
+            for (int dx = 0; dx < 2; dx++) {
+                const int a = corner_index(dx, dy, dz);
+                const int core = (n / 8) * 2 + dx;
+                for (int c = 0; c < 3; c++) {
+                    const double v = (n < 24) ? K0[n * 24 + 3 * a + c] : 0.0;
+                    // TF32: 4 words per row
+                    const int w = t * 256 + core * 32 + (n % 8) * 4 + c;
+                    const float h = tf32_round((float)v);
+                    out[w] = fbits(h);
+                    out[1024 + w] = fbits(tf32_round((float)(v - (double)h)));
+                    // BF16: 8 halves per row (x, y, z, 0, 0, 0, 0, 0)
+                    const int wb = 2048 + t * 256 + core * 32 + (n % 8) * 4 + c / 2;
+                    const uint32_t hb = bf16_bits((float)v);
+                    const uint32_t lb = bf16_bits((float)(v - (double)bits_of(hb)));
+                    out[wb] |= hb << (16 * (c & 1));
+                    out[1024 + wb] |= lb << (16 * (c & 1));
+                }
+            }
+    }
+}
+
 struct ApplyArgs {
-    int brick_lo, brick_hi, in_slot, parity;
+    int col_lo, col_hi, in_slot, parity;  // column range
     const float *rhs;
     float *y;
     int sel = -1;  // -1 every problem; 0 problems with a coarser level; 1 those without
@@ -1508,12 +1888,12 @@ struct ApplyArgs {
 
 template <int PREC, int MODE>
 void launch_apply(MfBatch &b, const ApplyArgs &a) {
-    const int nb = a.brick_hi - a.brick_lo;
-    if (nb <= 0) return;
-    const int grid = std::max(1, std::min(nb, b.apply_grid));
-    mf_apply_kernel<PREC, MODE><<<grid, kApplyThreads, kApplySmem, b.stream>>>(
-        b.probs, b.bricks, a.brick_lo, a.brick_hi, a.sel, b.tmaps, a.in_slot, a.parity, b.Bop,
-        b.dinv, a.rhs, b.p0, b.p1, a.y, b.states, b.brick_part, b.err);
+    const int nc = a.col_hi - a.col_lo;
+    if (nc <= 0) return;
+    const int grid = std::max(1, std::min(nc, b.col_grid));
+    mf_col_kernel<PREC, MODE><<<grid, kColThreads, kColSmem, b.stream>>>(
+        b.probs, b.cols, a.col_lo, a.col_hi, a.sel, b.tmaps, a.in_slot, a.parity, b.Bop2, b.dinv,
+        a.rhs, b.p0, b.p1, a.y, b.states, b.col_part, b.err);
 }
 
 template <int MODE>
@@ -1528,18 +1908,15 @@ void launch_apply_prec(MfBatch &b, int prec, const ApplyArgs &a) {
 
 // CG step on the level-0 bricks (z from map in_slot)
 void launch_cg_apply(MfBatch &b, int prec, int in_slot, int parity) {
-    ApplyArgs a{b.lvl_brick_lo[0], b.lvl_brick_hi[0], in_slot, parity, nullptr, b.q};
+    ApplyArgs a{b.lvl_col_lo[0], b.lvl_col_hi[0], in_slot, parity, nullptr, b.q};
     launch_apply_prec<1>(b, prec, a);
 }
 
 template <int PREC>
 int set_apply_attrs() {
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<PREC, 1>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<PREC, 2>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_apply_kernel<PREC, 3>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kApplySmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
     return MG_OK;
 }
 
@@ -1688,6 +2065,9 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(configure_kernels());
     EncodeTiledFn enc = nullptr;
     MG_TRY(encode_fn(&enc));
+    int dev = 0, sms = 0;
+    MG_CUDA_TRY(cudaGetDevice(&dev));
+    MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     b.stream = stream;
     b.hx = hx; b.hy = hy; b.hz = hz; b.nu = nu;
     // level 0: the designs; then every design's coarse levels, ordered by level
@@ -1766,6 +2146,18 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
                 for (int i = 0; i < bx; i++)
                     b.h_bricks.push_back(MfBrick{(int)pi, (int16_t)i, (int16_t)j, (int16_t)k, 0});
         nb += P.brick_count;
+        // columns of the tensor-core operator: at most kCZ node planes each, fewer
+        // (at least 4) when that gives a small grid more columns than SM slots
+        const int cx = (P.NX + kCX - 1) / kCX, cy = (P.NY + kCY - 1) / kCY;
+        const int64_t slots = 2 * (int64_t)sms;
+        P.col_z = (int)std::min<int64_t>(kCZ, std::max<int64_t>(4, (P.NZ * (int64_t)cx * cy + slots - 1) / slots));
+        const int cz = (P.NZ + P.col_z - 1) / P.col_z;
+        P.col_begin = (int)b.h_cols.size();
+        P.col_count = cx * cy * cz;
+        for (int k = 0; k < cz; k++)
+            for (int j = 0; j < cy; j++)
+                for (int i = 0; i < cx; i++)
+                    b.h_cols.push_back(MfCol{(int)pi, (int16_t)i, (int16_t)j, (int16_t)k, 0});
         P.chunk_begin = nc;
         P.chunk_count = (int)((P.n_pad + kChunk - 1) / kChunk);
         for (int c = 0; c < P.chunk_count; c++) {
@@ -1780,11 +2172,15 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     }
     b.n_bricks = nb;
     b.n_chunks = nc;
+    b.n_cols = (int)b.h_cols.size();
     b.lvl_brick_lo.clear(); b.lvl_brick_hi.clear(); b.lvl_chunk_lo.clear(); b.lvl_chunk_hi.clear();
+    b.lvl_col_lo.clear(); b.lvl_col_hi.clear();
     for (int l = 0; l < b.n_levels; l++) {
         const MfProblem &A = b.h_probs[b.lvl_prob_lo[l]], &Z = b.h_probs[b.lvl_prob_hi[l] - 1];
         b.lvl_brick_lo.push_back(A.brick_begin);
         b.lvl_brick_hi.push_back(Z.brick_begin + Z.brick_count);
+        b.lvl_col_lo.push_back(A.col_begin);
+        b.lvl_col_hi.push_back(Z.col_begin + Z.col_count);
         b.lvl_chunk_lo.push_back(A.chunk_begin);
         b.lvl_chunk_hi.push_back(Z.chunk_begin + Z.chunk_count);
     }
@@ -1812,13 +2208,14 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
             }
         }
     }
-    int dev = 0, sms = 0;
-    MG_CUDA_TRY(cudaGetDevice(&dev));
-    MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     b.apply_grid = std::max(1, std::min(nb, sms));
+    b.col_grid = std::max(1, std::min(b.n_cols, 2 * sms));  // two column CTAs per SM
     b.vec_grid = std::max(1, std::min(nc, 8 * sms));
     MG_TRY(dev_alloc_n(&b.probs, b.h_probs.size()));
     MG_TRY(dev_alloc_n(&b.bricks, b.h_bricks.size()));
+    MG_TRY(dev_alloc_n(&b.cols, b.h_cols.size()));
+    MG_TRY(dev_alloc_n(&b.col_part, b.h_cols.size()));
+    MG_TRY(dev_alloc_n(&b.Bop2, 4096));
     MG_TRY(dev_alloc_n(&b.chunks, b.h_chunks.size()));
     MG_TRY(dev_alloc_n(&b.states, (size_t)b.n_probs));
     MG_TRY(dev_alloc_n(&b.tmaps, (size_t)b.n_probs * kMapsPerProblem));
@@ -1864,11 +2261,25 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
                             (uint64_t)P.pitch * P.NY * 4, kBoxNX, kBU, kBU));
         MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 3], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
                         (uint64_t)P.pitch_e * 4, (uint64_t)P.pitch_e * P.ny * 4, kBoxEX, kBE, kBE));
+        // column operator: one node plane {32 floats, 17 rows} / element plane {12, 16}
+        for (int k = 0; k < 5; k++)
+            MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 6 + slot[k]], vecs[k] + P.dof_off,
+                            3 * (uint64_t)P.NX, P.NY, P.NZ, (uint64_t)P.pitch * 4,
+                            (uint64_t)P.pitch * P.NY * 4, kCRawX, kCPY, 1));
+        MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 6 + 3], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
+                        (uint64_t)P.pitch_e * 4, (uint64_t)P.pitch_e * P.ny * 4, 12, 16, 1));
     }
     cudaStream_t s = b.stream;
     MG_CUDA_TRY(cudaMemcpyAsync(b.tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.probs, b.h_probs.data(), b.h_probs.size() * sizeof(MfProblem), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.bricks, b.h_bricks.data(), b.h_bricks.size() * sizeof(MfBrick), cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.cols, b.h_cols.data(), b.h_cols.size() * sizeof(MfCol), cudaMemcpyHostToDevice, s));
+    {
+        std::vector<uint32_t> bop2;
+        pack_b_columns(K0, bop2);
+        MG_CUDA_TRY(cudaMemcpyAsync(b.Bop2, bop2.data(), bop2.size() * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA_TRY(cudaStreamSynchronize(s));  // bop2 is a host temporary
+    }
     MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.Bop, bop.data(), bop.size() * 4, cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
@@ -1896,7 +2307,7 @@ void mf_batch_free(MfBatch &b) {
     void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.Bop, b.K0, b.mb, b.mx, b.md,
-                    b.my, b.mr, b.diag_list, b.heads};
+                    b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
     b = MfBatch();
@@ -1981,7 +2392,7 @@ int mf_apply(MfBatch &b, int precision, const double *x_host, double *y_host, in
         for (int64_t k = 0; k < 3 * P.NX; k++) pad[row * P.pitch + k] = (float)x_host[row * 3 * P.NX + k];
     MG_CUDA_TRY(cudaMemcpyAsync(b.mx + P.dof_off, pad.data(), P.n_pad * 4, cudaMemcpyHostToDevice, b.stream));
     MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
-    ApplyArgs a{P.brick_begin, P.brick_begin + P.brick_count, 4, 0, nullptr, b.my};
+    ApplyArgs a{P.col_begin, P.col_begin + P.col_count, 4, 0, nullptr, b.my};
     launch_apply_prec<3>(b, precision, a);
     MG_CUDA_TRY(cudaGetLastError());
     MG_CUDA_TRY(cudaMemcpyAsync(pad.data(), b.my + P.dof_off, P.n_pad * 4, cudaMemcpyDeviceToHost, b.stream));
@@ -2046,7 +2457,7 @@ long long enqueue_smooth(MfBatch &b, int prec, int l, const float *rin, int x0_z
                                                           b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero, sel);
     long long n = 1;
     for (int k = 1; k < deg; k++) {
-        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 5, 0, nullptr, b.my, sel};
+        ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], 5, 0, nullptr, b.my, sel};
         launch_apply_prec<3>(b, prec, a);
         mg_cheb_next_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, b.my,
                                                              b.mr, b.md, b.mx, b.dinv, cc.c1[k], cc.c2[k], sel);
@@ -2079,7 +2490,7 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
         if (!any_level(l)) continue;
         const float *rin = (l == 0) ? b.r : b.mb;
         n += enqueue_smooth(b, prec, l, rin, 1, sdeg, cs, 0);
-        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my, 0};
+        ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], 4, 0, rin, b.my, 0};
         launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
         const int clo = b.lvl_prob_lo[l + 1], chi = b.lvl_prob_hi[l + 1];
         int64_t maxpad = 1;
@@ -2111,7 +2522,7 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
             if (b.h_probs[pi].coarse >= 0) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
         dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), fhi - flo);
         mg_prolong_kernel<<<grid, 256, 0, b.stream>>>(b.probs, flo, b.states, b.mx, b.dinv);
-        ApplyArgs a{b.lvl_brick_lo[l], b.lvl_brick_hi[l], 4, 0, rin, b.my, 0};
+        ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], 4, 0, rin, b.my, 0};
         launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
         n += 2 + enqueue_smooth(b, prec, l, b.my, 0, sdeg, cs, 0);
     }

@@ -21,7 +21,13 @@ constexpr int kBU = kBN + 2;
 constexpr int kNEL = kBE * kBE * kBE;          // 729 elements per brick
 constexpr int kNTILE = (kNEL + 127) / 128;     // 6 MMA tiles of 128 elements
 constexpr int kChunk = 1024;                   // dofs per vector-kernel chunk (one float4 per thread)
-constexpr int kMapsPerProblem = 6;             // z, p0, p1, E, mg x, mg d
+constexpr int kMapsPerProblem = 12;            // z, p0, p1, E, mg x, mg d: brick boxes, then column boxes
+// Column operator: a column owns kCX x kCY nodes in x, y and up to kCZ node
+// planes in z; it streams through its element planes (8 x 16 elements each,
+// one M = 128 tensor-core tile per plane).
+constexpr int kCX = 7;
+constexpr int kCY = 15;
+constexpr int kCZ = 16;   // most node planes per column
 constexpr int kMaxLevels = 8;                  // multigrid levels per design
 
 // Padded vector layout of one problem: node (i,j,k), component c lives at
@@ -39,6 +45,8 @@ struct MfProblem {
     int64_t node_off;     // offset into the node Dirichlet masks (unpadded)
     int brick_begin, brick_count;
     int chunk_begin, chunk_count;
+    int col_begin, col_count;
+    int col_z;            // node planes per column (kCZ or fewer for small grids)
     int share_elems;      // >= 0: reuse the element tables of that problem (load cases)
     int level;            // multigrid level (0 = the design's own grid)
     int root;             // level-0 problem whose solver state drives this one
@@ -49,6 +57,11 @@ struct MfProblem {
 struct MfBrick {
     int prob;
     int16_t bx, by, bz, pad;
+};
+
+struct MfCol {
+    int prob;
+    int16_t cx, cy, cz, pad;
 };
 
 struct MfChunkDesc {
@@ -88,6 +101,12 @@ struct MfBatch {
     std::vector<MfChunkDesc> h_chunks;
     MfProblem *probs = nullptr;
     MfBrick *bricks = nullptr;
+    MfCol *cols = nullptr;
+    std::vector<MfCol> h_cols;
+    int n_cols = 0;
+    std::vector<int> lvl_col_lo, lvl_col_hi;
+    double *col_part = nullptr;   // per-column partial of p.q
+    uint32_t *Bop2 = nullptr;     // K0 as the column operator's four (dy, dz) B tiles
     MfChunkDesc *chunks = nullptr;
     MfState *states = nullptr;
     MfState *states_host = nullptr;  // pinned
@@ -122,7 +141,7 @@ struct MfBatch {
     cudaGraphExec_t graph = nullptr;  // solver steps (see enqueue_step)
     std::vector<double> graph_key;    // parameters the graph was captured with
     long long graph_launches = 0;     // kernel nodes in the graph
-    int apply_grid = 0, vec_grid = 0;
+    int apply_grid = 0, vec_grid = 0, col_grid = 0;
     cudaStream_t stream = nullptr;
 };
 
