@@ -56,16 +56,16 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
     ap.add_argument("--serve-requests", type=int, default=1000, help="requests per arrival rate")
     ap.add_argument("--kernel-only", default=None, choices=["mixed", "plain"],
-                    help="only launch the dominant kernel (tensor-core brick operator or the "
+                    help="only launch the dominant kernel (tensor-core column operator or the "
                          "FP64 CG SpMV) --steps times after --warmup launches; for profilers")
     return ap.parse_args()
 
 
-PROFILE = os.path.join(REPO, "profiles", "mf_apply_kernel_tf32x3_128x64x64.txt")
+PROFILE = os.path.join(REPO, "profiles", "mf_col_kernel_tf32x3_128x64x64.txt")
 
 
 def profiled_traffic():
-    """DRAM bytes per launch of the brick operator from the committed ncu
+    """DRAM bytes per launch of the column operator from the committed ncu
     summary (line 'dram_bytes_per_launch = N'), or None."""
     try:
         for line in open(PROFILE):
@@ -423,7 +423,7 @@ def main():
                "d2h_bytes_per_step": int(X0.nbytes + NX * NY * NZ * 8 + 8)}
     dc_err = float(np.abs(dch - g["dc"]).max() / np.abs(g["dc"]).max())
 
-    # ---------------- dominant kernel: tensor-core brick operator, timed alone
+    # ---------------- dominant kernel: tensor-core column operator, timed alone
     n = prob.n_dofs
     n_el = NX * NY * NZ
     reps_k = 50
@@ -441,7 +441,7 @@ def main():
     alg_bytes = 16 * n + 4 * n_el + n // 3
     pk = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
-    roof = {"kernel": "mf_apply_kernel (tcgen05 %s brick operator, CG step)" % args.precision,
+    roof = {"kernel": "mf_col_kernel (tcgen05 %s column operator, CG step)" % args.precision,
             "bound": "hbm", "achieved": alg_bytes / (k_ms * 1e-3) / 1e9, "peak": peak,
             "unit": "GB/s", "frac": alg_bytes / (k_ms * 1e-3) / 1e9 / peak,
             "traffic": profiled_traffic(), "traffic_source": os.path.relpath(PROFILE, REPO),

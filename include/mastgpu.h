@@ -204,7 +204,7 @@ const double *mg_sensitivities_device(mg_problem *p);
 long long mg_launch_count(void);
 /* Enqueues `reps` launches of the dominant Krylov kernel on the handle's stream
    without synchronising (for event timing): the fused CSR SpMV of the CG step
-   (MG_PLAIN_FP64) or the tensor-core brick operator (MG_MIXED_*). */
+   (MG_PLAIN_FP64) or the tensor-core column operator (MG_MIXED_*). */
 int mg_debug_launch_apply(mg_problem *p, int precision, int reps);
 
 /* ---- allocation-free solve ---- */

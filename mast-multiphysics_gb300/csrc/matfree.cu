@@ -266,386 +266,6 @@ __device__ __forceinline__ double ordered_sum(const double *part, int begin, int
 
 __device__ __forceinline__ bool is_bad(double x) { return !isfinite(x); }
 
-// ------------------------------------------------------------------ apply
-// TMA boxes: nodes {32 floats, 10, 10} starting one float before the x
-// component of node gx0-1 (a 16-byte aligned start: 3(8b-1)-1 = 24b-4);
-// elements {12, 9, 9} starting at element gx0-4.
-constexpr int kBoxNX = 32;
-constexpr int kBoxNodeBytes = kBoxNX * kBU * kBU * 4;  // 12800
-constexpr int kBoxEX = 12;
-constexpr int kBoxElemBytes = kBoxEX * kBE * kBE * 4;  // 3888
-constexpr int kResStride = 25;
-constexpr int kApplyThreads = 512;
-// the thread that issues and waits for the MMAs: warp 12 has no TMEM drain
-// role, so the draining warps are not held up by MMA issue
-constexpr int kIssuer = 384;
-
-constexpr int kOffB = 0;                                   // B: hi at 0, lo at 4096
-constexpr int kOffA = 8192;                                // MMA ring: 4 x 12 KB operand slots
-constexpr int kABytes = 12288;
-constexpr int kASlots = 4;                                 // 2 stages x (hi, lo)
-constexpr int kOffBox = kOffA + kASlots * kABytes;         // 57344: 2 x (z, p, E)
-constexpr int kBoxSet = 12800 + 12800 + 3968;              // 29568 (multiple of 128)
-constexpr int kOffRes = kOffBox + 2 * kBoxSet;             // 116480 (multiple of 4)
-constexpr int kOffBar = kOffRes + kNEL * kResStride * 4;   // 189380 -> aligned below
-constexpr int kOffBarA = (kOffBar + 127) / 128 * 128;
-constexpr int kApplySmem = kOffBarA + 64;
-static_assert(kOffBox % 128 == 0 && kBoxSet % 128 == 0, "TMA destinations");
-static_assert(2 * Prec<MG_MIXED_TF32X3>::kStages <= kASlots &&
-              2 * Prec<MG_MIXED_BF16X3>::kStages <= kASlots, "MMA ring slots");
-
-// offset of element-row value k (node a = k/3, component c) inside the node box,
-// relative to the element's base corner
-__device__ __forceinline__ int box_offset(int k) {
-    const int a = (k * 11) >> 5, c = k - 3 * a;  // k / 3 for k < 24
-    int dx, dy, dz;
-    corner_bits(a, dx, dy, dz);
-    return (dz * kBU + dy) * kBoxNX + 3 * dx + c;
-}
-
-// Bricks brick_lo .. brick_hi-1; the input vector is tensor map `in_slot`.
-// MODE 1: CG step, gathered u = z + beta p_old (z = in_slot, p_old = map 1 +
-//         parity), p_new (owned) = u, q = A u, per-problem alpha = rz / (p.q).
-// MODE 2: y = rhs - A x.   MODE 3: y = A x.   (Both 0 on Dirichlet dofs.)
-template <int PREC, int MODE>
-__global__ void __launch_bounds__(kApplyThreads, 1) mf_apply_kernel(
-    const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int brick_lo,
-    int brick_hi, int sel, const CUtensorMap *__restrict__ tmaps, int in_slot, int parity,
-    const uint32_t *__restrict__ Bop, const float *__restrict__ dinv,
-    const float *__restrict__ rhs, float *__restrict__ p0, float *__restrict__ p1,
-    float *__restrict__ y, MfState *states, double *__restrict__ brick_part, int *err) {
-    const int n_bricks = brick_hi;
-    using PR = Prec<PREC>;
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ double red_sh[kApplyThreads / 32];
-    __shared__ double tree[kApplyThreads];
-    __shared__ int sh_last;
-    uint8_t *sB = smem + kOffB;
-    float *sres = reinterpret_cast<float *>(smem + kOffRes);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kOffBarA);  // tma[2], mma[4]
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBarA + 56);
-    const uint32_t tma_bar0 = smem_u32(&bars[0]);
-    const uint32_t mma_bar0 = smem_u32(&bars[2]);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    float *p_new = (MODE == 1) ? (parity ? p0 : p1) : nullptr;
-
-    auto usable = [&](int bi) {
-        const MfProblem &Q = probs[bricks[bi].prob];
-        return !states[Q.root].done && !Q.bottom && (sel < 0 || sel == (Q.coarse < 0 ? 1 : 0));
-    };
-    int bi = brick_lo + blockIdx.x;
-    while (bi < n_bricks && !usable(bi)) bi += gridDim.x;
-    if (bi >= n_bricks) return;  // uniform: no work for this block
-
-    if (tid == 0) {
-        mbar_init(tma_bar0, 1);
-        mbar_init(tma_bar0 + 8, 1);
-        for (int k = 0; k < 4; k++) mbar_init(mma_bar0 + 8 * k, 1);
-    }
-    if (warp == 0) tmem_alloc(smem_u32(tslot), 128);  // kStages x 32 accumulator columns
-    {
-        // B operands: [tf32 hi 768 | tf32 lo 768 | bf16 hi 512 | bf16 lo 512] words
-        const uint32_t *src = Bop + (PR::kTf32 ? 0 : 1536);
-        const int words = PR::kTf32 ? 768 : 512;
-        uint32_t *dst = reinterpret_cast<uint32_t *>(sB);
-        for (int i = tid; i < 2 * words; i += kApplyThreads) dst[(i / words) * 1024 + i % words] = src[i];
-    }
-    fence_async_smem();
-    fence_before();
-    __syncthreads();
-    fence_after();
-    const uint32_t tmem = *tslot;
-    const uint32_t b_hi = smem_u32(sB), b_lo = b_hi + 4096;
-
-    // A-build roles: row r = tid / 4 of each 128-row tile, chunks q, q + 4 (q = tid % 4)
-    const int arow = tid >> 2, aq = tid & 3;
-    constexpr int kPer = PR::kTf32 ? 4 : 8;   // operand values per 16-byte chunk
-    int aoff[2][kPer];
-    bool achunk[2];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int kc = aq + 4 * h;
-        achunk[h] = kc < PR::kCols;
-#pragma unroll
-        for (int j = 0; j < kPer; j++) {
-            const int k = kc * kPer + j;
-            aoff[h][j] = (achunk[h] && k < 24) ? box_offset(k) : -1;
-        }
-    }
-    // output roles: dofs i = tid + 512 j, j < 3 (512 owned nodes x 3)
-    int obase[3], obox[3];
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        const int i = tid + j * kApplyThreads;
-        const int node = i / 3, c = i - node * 3;
-        const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
-        obase[j] = ((ox + 1) + kBE * ((oy + 1) + kBE * (oz + 1))) * kResStride + c;
-        obox[j] = ((oz + 1) * kBU + oy + 1) * kBoxNX + 3 * (ox + 1) + c + 1;
-    }
-
-    uint32_t tma_phase[2] = {0, 0}, mma_phase[4] = {0, 0, 0, 0};
-    bool failed = false;
-    // TMA issue for brick `b` into box set `set`
-    auto issue_tma = [&](int b, int set) {
-        const MfBrick br = bricks[b];
-        const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
-        const CUtensorMap *maps = tmaps + (size_t)br.prob * kMapsPerProblem;
-        uint8_t *box = smem + kOffBox + set * kBoxSet;
-        const uint32_t bar = tma_bar0 + 8 * set;
-        const uint32_t bytes = (MODE == 1 ? 2 : 1) * kBoxNodeBytes + kBoxElemBytes;
-        mbar_expect_tx(bar, bytes);
-        const int xn = 3 * (gx0 - 1) - 1;
-        tma_load_3d(smem_u32(box), maps + in_slot, xn, gy0 - 1, gz0 - 1, bar);
-        if (MODE == 1)
-            tma_load_3d(smem_u32(box + 12800), maps + 1 + parity, xn, gy0 - 1, gz0 - 1, bar);
-        tma_load_3d(smem_u32(box + 25600), maps + 3, gx0 - 4, gy0 - 1, gz0 - 1, bar);
-    };
-    if (tid == 0) {
-        fence_async_smem();
-        issue_tma(bi, 0);
-    }
-    int set = 0;
-    int run = 0;  // bricks of the current problem since the last counter update (MODE 1)
-    for (; bi < n_bricks && !failed;) {
-        // next usable brick of this block, prefetched into the other box set
-        int nbi = bi + gridDim.x;
-        while (nbi < n_bricks && !usable(nbi)) nbi += gridDim.x;
-        const MfBrick br = bricks[bi];
-        const MfProblem P = probs[br.prob];
-        MfState *st = states + br.prob;
-        const float beta = (MODE == 1) ? (float)st->beta : 0.0f;
-        const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
-        const float *sZ = reinterpret_cast<const float *>(smem + kOffBox + set * kBoxSet);
-        const float *sP = sZ + 12800 / 4;
-        const float *sE = sZ + 25600 / 4;
-        // live elements: those touching an owned node inside the grid (a brick at
-        // the high end of a dimension owns fewer than kBN nodes there); only their
-        // tiles are multiplied.  Row l of the live box is element (lx, ly, lz).
-        const int ex_n = min(kBN, P.NX - gx0) + 1, ey_n = min(kBN, P.NY - gy0) + 1,
-                  ez_n = min(kBN, P.NZ - gz0) + 1;
-        const int n_live = ex_n * ey_n * ez_n;
-        const int n_tiles = (n_live + 127) >> 7;
-        const bool full = (n_live == kNEL);  // constant divisors on the common path
-        auto live_xyz = [&](int l, int &ex, int &ey, int &ez) {
-            if (full) {
-                ex = l % kBE; ey = (l / kBE) % kBE; ez = l / (kBE * kBE);
-            } else {
-                ex = l % ex_n; ey = (l / ex_n) % ey_n; ez = l / (ex_n * ey_n);
-            }
-        };
-        // one thread waits for the halo; the barrier releases the others
-        bool tma_ok = true;
-        if (tid == 0) tma_ok = mbar_wait_bounded(tma_bar0 + 8 * set, tma_phase[set]);
-        tma_phase[set] ^= 1u;
-        if (__syncthreads_or(!tma_ok)) {
-            failed = true;
-            if (tid == 0) atomicOr(err, 2);
-            break;
-        }
-        if (tid == 0 && nbi < n_bricks) {
-            fence_async_smem();
-            issue_tma(nbi, set ^ 1);  // the other set was released at the end of the last brick
-        }
-        // ---- tiles through a kStages-deep MMA ring:
-        //      build A(t) | wait MMA(t-S+1) | barrier | issue MMA(t) | drain t-S+1
-        constexpr int S = PR::kStages;
-        for (int t = 0; t < n_tiles + S - 1; t++) {
-            if (t < n_tiles) {
-                const int slot = t % S;
-                uint8_t *A_hi = smem + kOffA + (PR::kSplit ? 2 * slot : slot) * kABytes;
-                uint8_t *A_lo = A_hi + kABytes;
-                const int l = t * 128 + arow;
-                int base = -1;
-                if (l < n_live) {
-                    int ex, ey, ez;
-                    live_xyz(l, ex, ey, ez);
-                    base = (ez * kBU + ey) * kBoxNX + 3 * ex + 1;
-                }
-#pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    if (!achunk[h]) continue;
-                    const int kc = aq + 4 * h;
-                    float f[kPer];
-#pragma unroll
-                    for (int j = 0; j < kPer; j++) {
-                        const int o = aoff[h][j];
-                        float v = 0.0f;
-                        if (base >= 0 && o >= 0)
-                            v = (MODE == 1) ? fmaf(beta, sP[base + o], sZ[base + o]) : sZ[base + o];
-                        f[j] = v;
-                    }
-                    uint4 whi, wlo;
-                    if (PR::kTf32) {
-                        uint32_t hb[4], lb[4];
-#pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            hb[j] = to_tf32(f[j]);
-                            lb[j] = PR::kSplit ? to_tf32(f[j] - __uint_as_float(hb[j])) : 0u;
-                        }
-                        whi = make_uint4(hb[0], hb[1], hb[2], hb[3]);
-                        wlo = make_uint4(lb[0], lb[1], lb[2], lb[3]);
-                    } else {
-                        float g[kPer];
-#pragma unroll
-                        for (int j = 0; j < kPer; j++) g[j] = PR::kSplit ? f[j] - bf16_round(f[j]) : 0.0f;
-                        whi = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
-                                         pack_bf16(f[4 % kPer], f[5 % kPer]), pack_bf16(f[6 % kPer], f[7 % kPer]));
-                        wlo = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]),
-                                         pack_bf16(g[4 % kPer], g[5 % kPer]), pack_bf16(g[6 % kPer], g[7 % kPer]));
-                    }
-                    const int off = ((arow >> 3) * PR::kCols + kc) * 128 + (arow & 7) * 16;
-                    *reinterpret_cast<uint4 *>(A_hi + off) = whi;
-                    if (PR::kSplit) *reinterpret_cast<uint4 *>(A_lo + off) = wlo;
-                }
-            }
-            // the oldest tile in flight must be complete before it is drained and
-            // before its operand slot is rewritten in the next iteration
-            const int td = t - (S - 1);
-            bool ok = true;
-            if (td >= 0 && tid == kIssuer)
-                ok = mbar_wait_bounded(mma_bar0 + 8 * (td % S), mma_phase[td % S]);
-            if (td >= 0) mma_phase[td % S] ^= 1u;
-            fence_async_smem();
-            fence_before();
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                if (tid == kIssuer) atomicOr(err, 1);
-                break;
-            }
-            fence_after();
-            if (t < n_tiles && tid == kIssuer) {
-                const int slot = t % S;
-                const uint32_t a_hi = smem_u32(smem + kOffA + (PR::kSplit ? 2 * slot : slot) * kABytes);
-                const uint32_t a_lo = a_hi + kABytes;
-                const uint32_t d = tmem + slot * 32;
-#pragma unroll
-                for (int k = 0; k < PR::kKsteps; k++)
-                    umma<PR::kTf32>(d, umma_desc(a_hi + k * 256, 128, PR::kSbo),
-                                    umma_desc(b_hi + k * 256, 128, PR::kSbo), k > 0 ? 1u : 0u);
-                if (PR::kSplit) {
-#pragma unroll
-                    for (int k = 0; k < PR::kKsteps; k++) {
-                        umma<PR::kTf32>(d, umma_desc(a_hi + k * 256, 128, PR::kSbo),
-                                        umma_desc(b_lo + k * 256, 128, PR::kSbo), 1u);
-                        umma<PR::kTf32>(d, umma_desc(a_lo + k * 256, 128, PR::kSbo),
-                                        umma_desc(b_hi + k * 256, 128, PR::kSbo), 1u);
-                    }
-                }
-                umma_commit(mma_bar0 + 8 * slot);
-            }
-            if (td >= 0) {
-                // drain tile td: rows of lane group lg, 8 columns per column group cg
-                const int slot = td % S, lg = warp & 3, cg = warp >> 2;
-                if (cg < 3) {
-                    const int m = lg * 32 + lane, l = td * 128 + m;
-                    float v[8];
-                    tmem_ld8(tmem + slot * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
-                    if (l < n_live) {
-                        // results are kept at the element's place in the full 9^3 box
-                        int ex, ey, ez;
-                        live_xyz(l, ex, ey, ez);
-                        const int lp = (ez * kBE + ey) * kBE + ex;
-                        const float e = sE[(ez * kBE + ey) * kBoxEX + ex + 3];
-#pragma unroll
-                        for (int n = 0; n < 8; n++) sres[lp * kResStride + cg * 8 + n] = e * v[n];
-                    }
-                }
-                fence_before();
-            }
-        }
-        if (failed) break;
-        __syncthreads();  // sres complete
-        // ---- node sums over the 8 surrounding elements (fixed order) and outputs
-        float part = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            const int i = tid + j * kApplyThreads;
-            const int node = i / 3, c = i - node * 3;
-            const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
-            const int gx = gx0 + ox, gy = gy0 + oy, gz = gz0 + oz;
-            float acc = 0.0f;
-#pragma unroll
-            for (int a = 0; a < 8; a++) {
-                int dx, dy, dz;
-                corner_bits(a, dx, dy, dz);
-                acc += sres[obase[j] - (dx + kBE * dy + kBE * kBE * dz) * kResStride + 3 * a];
-            }
-            if (gx >= P.NX || gy >= P.NY || gz >= P.NZ) continue;
-            const int64_t gd = dof_index(P, gx, gy, gz, c);
-            if (MODE == 1) {
-                const float pv = fmaf(beta, sP[obox[j]], sZ[obox[j]]);
-                y[gd] = acc;
-                p_new[gd] = pv;
-                part = fmaf(pv, acc, part);
-            } else if (MODE == 2) {
-                y[gd] = (dinv[gd] == 0.0f) ? 0.0f : rhs[gd] - acc;
-            } else {
-                y[gd] = (dinv[gd] == 0.0f) ? 0.0f : acc;
-            }
-        }
-        if (MODE == 1) {
-            // brick partial: FP32 within a warp, FP64 across warps (FP64 issue is
-            // scarce on this part)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-            if (lane == 0) red_sh[warp] = (double)part;
-        }
-        __syncthreads();  // box set, sres and red_sh are complete and may be reused
-        if (MODE == 1) {
-            // red_sh is rewritten only after the next brick's tile barriers
-            if (tid == 0) {
-                double s = 0.0;
-                for (int w = 0; w < kApplyThreads / 32; w++) s += red_sh[w];
-                brick_part[bi] = s;
-            }
-            // the per-problem counter is bumped once per run of consecutive
-            // bricks of one problem (one fence and one atomic per run)
-            run++;
-            const bool flush = nbi >= n_bricks || bricks[nbi].prob != br.prob;
-            if (flush) {
-                if (tid == 0) {
-                    __threadfence();
-                    const unsigned tk = atomicAdd(&st->cnt_apply, (unsigned)run);
-                    sh_last = (tk + (unsigned)run == (unsigned)P.brick_count);
-                }
-                run = 0;
-                __syncthreads();
-            }
-            if (flush && sh_last) {
-                double s = 0.0;
-                for (int k = tid; k < P.brick_count; k += kApplyThreads)
-                    s += __ldcg(brick_part + P.brick_begin + k);
-                tree[tid] = s;
-                __syncthreads();
-                for (int w = kApplyThreads / 2; w > 0; w >>= 1) {
-                    if (tid < w) tree[tid] += tree[tid + w];
-                    __syncthreads();
-                }
-                if (tid == 0) {
-                    const double pq = tree[0];
-                    st->cnt_apply = 0;
-                    st->pq = pq;
-                    if (is_bad(pq)) { st->status = MG_ENAN; st->done = 1; }
-                    else if (!(pq > 0.0)) { st->status = MG_EBREAKDOWN; st->done = 1; }
-                    else st->alpha = st->rz / pq;
-                }
-            }
-        }
-        bi = nbi;
-        set ^= 1;
-    }
-    // after a failed wait, give an outstanding halo prefetch a bounded chance to land
-    if (failed) {
-        int nb2 = bi + gridDim.x;
-        while (nb2 < n_bricks && !usable(nb2)) nb2 += gridDim.x;
-        if (nb2 < n_bricks) (void)mbar_wait_bounded(tma_bar0 + 8 * (set ^ 1), tma_phase[set ^ 1]);
-    }
-    fence_before();
-    __syncthreads();
-    fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 128);
-}
-
 // ----------------------------------------------------------- column operator
 // y = sum_e E_e P_e^T K0 P_e x by columns of owned nodes (kCX x kCY nodes in x,
 // y; up to kCZ node planes in z), streamed plane by plane.  The A operand of
@@ -663,7 +283,9 @@ constexpr int kCPX = kCX + 2;                 // 9 nodes per plane row
 constexpr int kCPY = kCY + 2;                 // 17 node rows per plane
 constexpr int kCPN = kCPX * kCPY;             // 153 nodes per plane
 constexpr int kCPB = kCPN * 16;               // 2448 bytes per converted plane (one part)
-constexpr int kCRing = 4;                     // planes in flight
+constexpr int kCRaw = 3;                      // TMA ring: plane being converted + 2 in flight
+constexpr int kCConv = 3;                     // operand records: planes s+1, s+2 of MMA(s+1) + the next
+constexpr int kCU = 4;                        // FP32 u and E of the planes (read after the next conversion)
 constexpr int kCRawX = 32;                    // TMA node box: 32 floats x 17 rows x 1 plane
 constexpr int kCRawNode = kCRawX * kCPY * 4;  // 2176
 constexpr int kCRawE = 12 * 16 * 4;           // E box: 12 elements x 16 rows x 1 plane = 768
@@ -673,19 +295,22 @@ constexpr int kCResStride = 25;
 constexpr int kColIssuer = 224;
 
 constexpr int kC_OffB = 0;                                      // 4 B tiles x 1 KB, hi | lo
-constexpr int kC_OffConv = 8192;                                // kCRing x (hi, lo) converted planes
-constexpr int kC_OffU = kC_OffConv + kCRing * 2 * kCPB;         // 27776: FP32 u of the planes
-constexpr int kC_OffE = kC_OffU + kCRing * kCPN * 3 * 4;        // 35120: E of the element planes
-constexpr int kC_OffRaw = (kC_OffE + kCRing * 128 * 4 + 127) / 128 * 128;  // 37248: TMA ring
-constexpr int kC_OffR = kC_OffRaw + kCRing * kCRawSlot;         // 57728: drained plane results
-constexpr int kC_OffBar = (kC_OffR + 2 * 128 * kCResStride * 4 + 127) / 128 * 128;  // 83328
-constexpr int kColSmem = kC_OffBar + 64;
+constexpr int kC_OffConv = 8192;                                // kCConv x (hi, lo) converted planes
+constexpr int kC_OffU = kC_OffConv + kCConv * 2 * kCPB;         // 22880: FP32 u of the planes
+constexpr int kC_OffE = kC_OffU + kCU * kCPN * 3 * 4;           // 30224: E of the element planes
+constexpr int kC_OffRaw = (kC_OffE + kCU * 128 * 4 + 127) / 128 * 128;  // 32256: TMA ring
+constexpr int kC_OffR = kC_OffRaw + kCRaw * kCRawSlot;          // 47616: drained plane results
+constexpr int kC_OffBar = (kC_OffR + 2 * 128 * kCResStride * 4 + 127) / 128 * 128;  // 73216
+constexpr int kColSmem = kC_OffBar + 64;                        // three CTAs per SM
 static_assert(kC_OffRaw % 128 == 0 && kCRawSlot % 128 == 0 && kCRawNode % 128 == 0, "TMA destinations");
 static_assert(kC_OffConv % 16 == 0 && kCPB % 16 == 0, "operand alignment");
 
-// Columns col_lo .. col_hi-1; the same modes as mf_apply_kernel.
+// Columns col_lo .. col_hi-1; the input vector is tensor map `in_slot`.
+// MODE 1: CG step, gathered u = z + beta p_old (z = in_slot, p_old = map 1 +
+//         parity), p_new (owned) = u, q = A u, per-problem alpha = rz / (p.q).
+// MODE 2: y = rhs - A x.   MODE 3: y = A x.   (Both 0 on Dirichlet dofs.)
 template <int PREC, int MODE>
-__global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
+__global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
     const MfProblem *__restrict__ probs, const MfCol *__restrict__ cols, int col_lo, int col_hi, int sel,
     const CUtensorMap *__restrict__ tmaps, int in_slot, int parity, const uint32_t *__restrict__ Bop2,
     const float *__restrict__ dinv, const float *__restrict__ rhs, float *__restrict__ p0,
@@ -700,10 +325,10 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
     float *sU = reinterpret_cast<float *>(smem + kC_OffU);
     float *sE = reinterpret_cast<float *>(smem + kC_OffE);
     float *sR = reinterpret_cast<float *>(smem + kC_OffR);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kC_OffBar);  // tma[4], mma[2]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kC_OffBar);  // tma[3], mma[2]
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kC_OffBar + 56);
     const uint32_t tma_bar0 = smem_u32(&bars[0]);
-    const uint32_t mma_bar0 = smem_u32(&bars[4]);
+    const uint32_t mma_bar0 = smem_u32(&bars[3]);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     float *p_new = (MODE == 1) ? (parity ? p0 : p1) : nullptr;
 
@@ -716,7 +341,7 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
     if (ci >= col_hi) return;  // uniform: no work for this block
 
     if (tid == 0) {
-        for (int k = 0; k < kCRing; k++) mbar_init(tma_bar0 + 8 * k, 1);
+        for (int k = 0; k < kCRaw; k++) mbar_init(tma_bar0 + 8 * k, 1);
         for (int k = 0; k < 2; k++) mbar_init(mma_bar0 + 8 * k, 1);
     }
     if (warp == 0) tmem_alloc(smem_u32(tslot), 64);  // 2 accumulator slots x 32 columns
@@ -726,7 +351,7 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
         uint32_t *dst = reinterpret_cast<uint32_t *>(smem + kC_OffB);
         for (int i = tid; i < 2048; i += kColThreads) dst[i] = src[i];
         // node records: the unused lanes stay 0 (B has zero rows there; 0 x NaN is NaN)
-        for (int i = tid; i < kCRing * 2 * kCPB / 4; i += kColThreads) convHi[i] = 0u;
+        for (int i = tid; i < kCConv * 2 * kCPB / 4; i += kColThreads) convHi[i] = 0u;
     }
     fence_async_smem();
     fence_before();
@@ -735,7 +360,7 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
     const uint32_t tmem = *tslot;
     const uint32_t b_base = smem_u32(smem + kC_OffB), conv_base = smem_u32(smem + kC_OffConv);
 
-    uint32_t tma_phase[kCRing] = {0, 0, 0, 0}, mma_phase[2] = {0, 0};
+    uint32_t tma_phase[kCRaw] = {0, 0, 0}, mma_phase[2] = {0, 0};
     uint32_t tma_issued = 0;  // bit k: a TMA into raw slot k is outstanding
     bool failed = false;
     int run = 0;  // columns of the current problem since the last counter update (MODE 1)
@@ -751,10 +376,10 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
         const int S = z1 - z0 + 1;                     // element planes z0-1 .. z1-1
         const int xs = (3 * (x0 - 1)) & ~3, ox = 3 * (x0 - 1) - xs;  // 16-byte aligned box starts
         const int xe = (x0 - 1) & ~3, oe = (x0 - 1) - xe;
-        const CUtensorMap *maps = tmaps + (size_t)cl.prob * kMapsPerProblem + 6;
+        const CUtensorMap *maps = tmaps + (size_t)cl.prob * kMapsPerProblem;
         // TMA of node plane p (nz = z0 - 1 + p) and, for p < S, element plane p
         auto issue = [&](int p) {
-            const int slot = p % kCRing;
+            const int slot = p % kCRaw;
             uint8_t *raw = smem + kC_OffRaw + slot * kCRawSlot;
             const uint32_t bar = tma_bar0 + 8 * slot;
             const uint32_t bytes = (MODE == 1 ? 2 : 1) * kCRawNode + (p < S ? kCRawE : 0);
@@ -763,20 +388,19 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
             if (MODE == 1) tma_load_3d(smem_u32(raw + kCRawNode), maps + 1 + parity, xs, y0 - 1, z0 - 1 + p, bar);
             if (p < S) tma_load_3d(smem_u32(raw + 2 * kCRawNode), maps + 3, xe, y0 - 1, z0 - 1 + p, bar);
         };
-        // wait for plane p and convert it into the operand records, u and E
+        // wait for plane p (every thread polls the barrier) and convert it into the
+        // operand records, u and E; returns this thread's wait status
         auto convert = [&](int p) -> bool {
-            const int slot = p % kCRing;
-            bool ok = true;
-            if (tid == 0) ok = mbar_wait_bounded(tma_bar0 + 8 * slot, tma_phase[slot]);
-            if (__syncthreads_or(!ok)) return false;
+            const int slot = p % kCRaw, cs = p % kCConv, us = p % kCU;
+            const bool ok = mbar_wait_bounded(tma_bar0 + 8 * slot, tma_phase[slot]);
             tma_phase[slot] ^= 1u;
             tma_issued &= ~(1u << slot);
             const float *rz = reinterpret_cast<const float *>(smem + kC_OffRaw + slot * kCRawSlot);
             const float *rp = rz + kCRawNode / 4;
             const float *re = rz + 2 * kCRawNode / 4;
-            uint32_t *hi = convHi + slot * (2 * kCPB / 4);
+            uint32_t *hi = convHi + cs * (2 * kCPB / 4);
             uint32_t *lo = hi + kCPB / 4;
-            float *u = sU + slot * kCPN * 3;
+            float *u = sU + us * kCPN * 3;
             for (int i = tid; i < kCPN * 3; i += kColThreads) {
                 const int n = i / 3, c = i - 3 * n;
                 const int nx = n % kCPX, ny = n / kCPX;
@@ -795,9 +419,9 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
                 }
             }
             if (p < S)
-                for (int e = tid; e < 128; e += kColThreads) sE[slot * 128 + e] = re[(e >> 3) * 12 + oe + (e & 7)];
+                for (int e = tid; e < 128; e += kColThreads) sE[us * 128 + e] = re[(e >> 3) * 12 + oe + (e & 7)];
             fence_async_smem();  // the records are read by the tensor core (async proxy)
-            return true;
+            return ok;
         };
         // MMA of element plane s into accumulator slot s % 2
         auto mma = [&](int s) {
@@ -810,7 +434,7 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
 #pragma unroll
                 for (int st4 = 0; st4 < 4; st4++) {
                     const int dy = st4 & 1, dz = st4 >> 1;
-                    const uint32_t a = conv_base + ((s + dz) % kCRing) * 2 * kCPB + apart + dy * kCPX * 16;
+                    const uint32_t a = conv_base + ((s + dz) % kCConv) * 2 * kCPB + apart + dy * kCPX * 16;
                     umma<PR::kTf32>(d, umma_desc(a, 16, kCPX * 16), umma_desc(b_base + bpart + st4 * 1024, 128, 256),
                                     acc);
                     acc = 1u;
@@ -822,51 +446,56 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
         // ---- prologue: planes 0, 1 converted, 2 and 3 in flight, MMA(0) issued
         if (tid == 0) {
             fence_async_smem();
-            for (int p = 0; p <= min(3, S); p++) issue(p);
+            for (int p = 0; p <= min(2, S); p++) issue(p);
         }
-        for (int p = 0; p <= min(3, S); p++) tma_issued |= 1u << (p % kCRing);
-        if (!convert(0) || !convert(1)) {
-            failed = true;
-            if (tid == 0) atomicOr(err, 2);
-            break;
-        }
-        fence_before();
-        __syncthreads();
-        fence_after();
-        if (tid == kColIssuer) mma(0);
-        float part = 0.0f;
-        for (int s = 0; s < S && !failed; s++) {
-            // (a) convert plane s + 2; the TMA ring slot of plane s is then free for s + 4
-            if (s + 2 <= S && !convert(s + 2)) {
+        for (int p = 0; p <= min(2, S); p++) tma_issued |= 1u << (p % kCRaw);
+        {
+            bool ok = convert(0);
+            ok = convert(1) && ok;
+            fence_before();
+            if (__syncthreads_or(!ok)) {
                 failed = true;
                 if (tid == 0) atomicOr(err, 2);
                 break;
             }
+            fence_after();
+        }
+        if (S >= 3) {
+            if (tid == 0) {
+                fence_async_smem();
+                issue(3);  // into the slot of plane 0
+            }
+            tma_issued |= 1u << (3 % kCRaw);
+        }
+        if (tid == kColIssuer) mma(0);
+        float part = 0.0f;
+        // ---- one element plane per step, two CTA barriers per step:
+        //      (a) convert plane s+2 | barrier | TMA(s+4), MMA(s+1)
+        //      (c) wait MMA(s), drain plane s | barrier | (d) node sums of node plane s
+        for (int s = 0; s < S && !failed; s++) {
+            bool ok = true;
+            if (s + 2 <= S) ok = convert(s + 2);
             fence_before();
-            __syncthreads();
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                if (tid == 0) atomicOr(err, 2);
+                break;
+            }
             fence_after();
             if (s + 4 <= S) {
                 if (tid == 0) {
                     fence_async_smem();
-                    issue(s + 4);
+                    issue(s + 4);  // into the slot of plane s + 1, converted a step ago
                 }
-                tma_issued |= 1u << ((s + 4) % kCRing);
+                tma_issued |= 1u << ((s + 4) % kCRaw);
             }
-            // (b) MMA(s + 1) overlaps the drain of plane s
             if (tid == kColIssuer && s + 1 < S) mma(s + 1);
-            // (c) wait for MMA(s)
-            bool ok = true;
-            if (tid == kColIssuer) ok = mbar_wait_bounded(mma_bar0 + 8 * (s & 1), mma_phase[s & 1]);
+            // (c) every thread waits for MMA(s), then drains its TMEM quarter
+            const bool mok = mbar_wait_bounded(mma_bar0 + 8 * (s & 1), mma_phase[s & 1]);
             mma_phase[s & 1] ^= 1u;
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                if (tid == kColIssuer) atomicOr(err, 1);
-                break;
-            }
             fence_after();
-            // (d) drain element plane s: rows of lane group w % 4, columns 8 cg .. 8 cg + 7
             {
-                const float *Es = sE + (s % kCRing) * 128;
+                const float *Es = sE + (s % kCU) * 128;
                 float *R = sR + (s & 1) * 128 * kCResStride;
                 for (int task = warp; task < 12; task += kColThreads / 32) {
                     const int lg = task & 3, cg = task >> 2;
@@ -879,13 +508,17 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
                 }
             }
             fence_before();
-            __syncthreads();
-            // (e) node sums of node plane nz = z0 - 1 + s (owned planes z0 .. z1-1)
+            if (__syncthreads_or(!mok)) {
+                failed = true;
+                if (tid == kColIssuer) atomicOr(err, 1);
+                break;
+            }
+            // (d) node sums of node plane nz = z0 - 1 + s (owned planes z0 .. z1-1)
             const int nz = z0 - 1 + s;
             if (s >= 1 && nz < z1) {
                 const float *R0 = sR + (s & 1) * 128 * kCResStride;         // element plane nz (dz = 0)
                 const float *R1 = sR + ((s - 1) & 1) * 128 * kCResStride;   // element plane nz - 1 (dz = 1)
-                const float *u = sU + (s % kCRing) * kCPN * 3;
+                const float *u = sU + (s % kCU) * kCPN * 3;
                 for (int i = tid; i < kCX * kCY * 3; i += kColThreads) {
                     const int n = i / 3, c = i - 3 * n;
                     const int oxn = n % kCX, oyn = n / kCX;
@@ -962,7 +595,7 @@ __global__ void __launch_bounds__(kColThreads, 2) mf_col_kernel(
     }
     // after a failed wait, give the outstanding halo loads a bounded chance to land
     if (failed)
-        for (int k = 0; k < kCRing; k++)
+        for (int k = 0; k < kCRaw; k++)
             if (tma_issued & (1u << k)) (void)mbar_wait_bounded(tma_bar0 + 8 * k, tma_phase[k]);
     fence_before();
     __syncthreads();
@@ -1774,55 +1407,6 @@ inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) /
 
 // K0 in the UMMA K-major no-swizzle layout (B operand, N = 32 rows, zero padded):
 // [tf32 hi 768 | tf32 lo 768 | bf16 hi 512 | bf16 lo 512] 32-bit words
-void pack_b_operand(const double *K0, std::vector<uint32_t> &out) {
-    auto tf32_round = [](float x) -> float {
-        uint32_t u;
-        memcpy(&u, &x, 4);
-        if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;  // nearest, ties away
-        float r;
-        memcpy(&r, &u, 4);
-        return r;
-    };
-    auto bf16_round_h = [](float x) -> float {
-        uint32_t u;
-        memcpy(&u, &x, 4);
-        u = (u + 0x7fffu + ((u >> 16) & 1u)) & 0xffff0000u;  // nearest even
-        float r;
-        memcpy(&r, &u, 4);
-        return r;
-    };
-    auto bits = [](float x) -> uint32_t {
-        uint32_t u;
-        memcpy(&u, &x, 4);
-        return u;
-    };
-    out.assign(2560, 0u);
-    for (int n = 0; n < 32; n++) {
-        const int rg = n / 8, rr = n % 8;
-        for (int kc = 0; kc < 6; kc++)
-            for (int j = 0; j < 4; j++) {
-                const int k = kc * 4 + j;
-                const float v = (n < 24) ? (float)K0[n * 24 + k] : 0.0f;
-                const float h = tf32_round(v);
-                const int w = ((rg * 6 + kc) * 128 + rr * 16) / 4 + j;
-                out[w] = bits(h);
-                out[768 + w] = bits(tf32_round((n < 24) ? (float)(K0[n * 24 + k] - (double)h) : 0.0f));
-            }
-        for (int kc = 0; kc < 4; kc++)
-            for (int j = 0; j < 8; j += 2) {
-                const int k = kc * 8 + j;
-                const double v0 = (n < 24 && k < 24) ? K0[n * 24 + k] : 0.0;
-                const double v1 = (n < 24 && k + 1 < 24) ? K0[n * 24 + k + 1] : 0.0;
-                const float h0 = bf16_round_h((float)v0), h1 = bf16_round_h((float)v1);
-                const float l0 = bf16_round_h((float)(v0 - (double)h0));
-                const float l1 = bf16_round_h((float)(v1 - (double)h1));
-                const int w = ((rg * 4 + kc) * 128 + rr * 16) / 4 + j / 2;
-                out[1536 + w] = (bits(h0) >> 16) | (bits(h1) & 0xffff0000u);
-                out[2048 + w] = (bits(l0) >> 16) | (bits(l1) & 0xffff0000u);
-            }
-    }
-}
-
 // B tiles of the column operator: tile t = dy + 2 dz holds the K0 columns of the
 // corners (0, dy, dz) and (1, dy, dz) (K chunk dx: x, y, z, 0 in TF32; x, y, z
 // and five zeros in BF16) for the 32 N rows n = 3 a + c (libMesh corner a; rows
@@ -1917,6 +1501,10 @@ int set_apply_attrs() {
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
+    // all of the unified L1/shared storage as shared memory: three CTAs per SM
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 2>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_col_kernel<PREC, 3>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     return MG_OK;
 }
 
@@ -2149,7 +1737,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         // columns of the tensor-core operator: at most kCZ node planes each, fewer
         // (at least 4) when that gives a small grid more columns than SM slots
         const int cx = (P.NX + kCX - 1) / kCX, cy = (P.NY + kCY - 1) / kCY;
-        const int64_t slots = 2 * (int64_t)sms;
+        const int64_t slots = 3 * (int64_t)sms;
         P.col_z = (int)std::min<int64_t>(kCZ, std::max<int64_t>(4, (P.NZ * (int64_t)cx * cy + slots - 1) / slots));
         const int cz = (P.NZ + P.col_z - 1) / P.col_z;
         P.col_begin = (int)b.h_cols.size();
@@ -2209,7 +1797,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         }
     }
     b.apply_grid = std::max(1, std::min(nb, sms));
-    b.col_grid = std::max(1, std::min(b.n_cols, 2 * sms));  // two column CTAs per SM
+    b.col_grid = std::max(1, std::min(b.n_cols, 3 * sms));  // three column CTAs per SM
     b.vec_grid = std::max(1, std::min(nc, 8 * sms));
     MG_TRY(dev_alloc_n(&b.probs, b.h_probs.size()));
     MG_TRY(dev_alloc_n(&b.bricks, b.h_bricks.size()));
@@ -2235,7 +1823,6 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.err, 1));
     MG_TRY(dev_alloc_n(&b.diag_list, (size_t)b.n_probs));
     MG_TRY(dev_alloc_n(&b.heads, std::max<size_t>(1, b.h_heads.size())));
-    MG_TRY(dev_alloc_n(&b.Bop, 2560));
     MG_TRY(dev_alloc_n(&b.K0, 576));
     double K0[576];
     hex8_box_stiffness(hx, hy, hz, nu, K0);
@@ -2247,26 +1834,18 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         for (int j = 0; j < 24; j++) sabs += fabs(K0[i * 24 + j]);
         b.cheb_lmax = std::max(b.cheb_lmax, sabs / K0[i * 24 + i]);
     }
-    std::vector<uint32_t> bop;
-    pack_b_operand(K0, bop);
     // tensor maps: z, p0, p1, E, debug x per problem
     std::vector<CUtensorMap> maps(b.n_probs * kMapsPerProblem);
     for (int pi = 0; pi < b.n_probs; pi++) {
         const MfProblem &P = b.h_probs[pi];
         float *vecs[5] = {b.z, b.p0, b.p1, b.mx, b.md};
         const int slot[5] = {0, 1, 2, 4, 5};
+        // column operator: one node plane {32 floats, 17 rows} / element plane {12, 16}
         for (int k = 0; k < 5; k++)
             MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + slot[k]], vecs[k] + P.dof_off,
                             3 * (uint64_t)P.NX, P.NY, P.NZ, (uint64_t)P.pitch * 4,
-                            (uint64_t)P.pitch * P.NY * 4, kBoxNX, kBU, kBU));
-        MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 3], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
-                        (uint64_t)P.pitch_e * 4, (uint64_t)P.pitch_e * P.ny * 4, kBoxEX, kBE, kBE));
-        // column operator: one node plane {32 floats, 17 rows} / element plane {12, 16}
-        for (int k = 0; k < 5; k++)
-            MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 6 + slot[k]], vecs[k] + P.dof_off,
-                            3 * (uint64_t)P.NX, P.NY, P.NZ, (uint64_t)P.pitch * 4,
                             (uint64_t)P.pitch * P.NY * 4, kCRawX, kCPY, 1));
-        MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 6 + 3], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
+        MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 3], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
                         (uint64_t)P.pitch_e * 4, (uint64_t)P.pitch_e * P.ny * 4, 12, 16, 1));
     }
     cudaStream_t s = b.stream;
@@ -2281,7 +1860,6 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         MG_CUDA_TRY(cudaStreamSynchronize(s));  // bop2 is a host temporary
     }
     MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
-    MG_CUDA_TRY(cudaMemcpyAsync(b.Bop, bop.data(), bop.size() * 4, cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
     if (!b.h_heads.empty())
         MG_CUDA_TRY(cudaMemcpyAsync(b.heads, b.h_heads.data(), b.h_heads.size() * sizeof(int),
@@ -2306,7 +1884,7 @@ void mf_batch_free(MfBatch &b) {
     if (b.graph) cudaGraphExecDestroy(b.graph);
     void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
-                    b.f64, b.brick_part, b.chunk_part, b.err, b.Bop, b.K0, b.mb, b.mx, b.md,
+                    b.f64, b.brick_part, b.chunk_part, b.err, b.K0, b.mb, b.mx, b.md,
                     b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);

@@ -21,7 +21,7 @@ constexpr int kBU = kBN + 2;
 constexpr int kNEL = kBE * kBE * kBE;          // 729 elements per brick
 constexpr int kNTILE = (kNEL + 127) / 128;     // 6 MMA tiles of 128 elements
 constexpr int kChunk = 1024;                   // dofs per vector-kernel chunk (one float4 per thread)
-constexpr int kMapsPerProblem = 12;            // z, p0, p1, E, mg x, mg d: brick boxes, then column boxes
+constexpr int kMapsPerProblem = 6;             // z, p0, p1, E, mg x, mg d (column operator boxes)
 // Column operator: a column owns kCX x kCY nodes in x, y and up to kCZ node
 // planes in z; it streams through its element planes (8 x 16 elements each,
 // one M = 128 tensor-core tile per plane).
@@ -135,7 +135,6 @@ struct MfBatch {
     int *err = nullptr;
     int *diag_list = nullptr;  // problem list of a partial Jacobi update
     // operator data
-    uint32_t *Bop = nullptr;  // K0 in the UMMA smem layout: [tf32 hi|tf32 lo|bf16 hi|bf16 lo]
     double *K0 = nullptr;     // 24x24 FP64, node-interleaved element order
     double hx = 1, hy = 1, hz = 1, nu = 0.3;
     cudaGraphExec_t graph = nullptr;  // solver steps (see enqueue_step)
