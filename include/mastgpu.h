@@ -338,7 +338,7 @@ typedef struct mg_server_stats {
     int64_t resident_bytes, peak_resident_bytes;
     int32_t resident_chains, inflight, peak_inflight, reserved;
     double p50_s, p99_s, mean_s, max_s;   /* latency: arrival -> results posted */
-    double solves_per_s;                  /* completed / (last completion - first arrival) */
+    double solves_per_s;                  /* completed requests / (last completion - first arrival) */
     double dofs_per_s;                    /* solved dofs (all load cases) per second */
 } mg_server_stats;
 
