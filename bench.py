@@ -55,9 +55,10 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-design batch section")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
     ap.add_argument("--serve-requests", type=int, default=1000, help="requests per arrival rate")
-    ap.add_argument("--kernel-only", default=None, choices=["mixed", "plain"],
-                    help="only launch the dominant kernel (tensor-core column operator or the "
-                         "FP64 CG SpMV) --steps times after --warmup launches; for profilers")
+    ap.add_argument("--kernel-only", default=None, choices=["mixed", "plain", "factored"],
+                    help="only launch one kernel (tensor-core column operator, FP64 CG SpMV or the "
+                         "factored multigrid level operator) --steps times after --warmup "
+                         "launches; for profilers")
     return ap.parse_args()
 
 
@@ -81,7 +82,7 @@ def kernel_only(args, M, prob, prec, rho):
     short, regular launch list: setup, then --warmup + --steps launches."""
     import torch
     prob.set_design(rho)  # the plain launch hook assembles the CSR on first use
-    p = M.PLAIN_FP64 if args.kernel_only == "plain" else prec
+    p = {"plain": M.PLAIN_FP64, "factored": M.OPERATOR_FACTORED_FP32}.get(args.kernel_only, prec)
     M.check(M.lib().mg_debug_launch_apply(prob.h, p, max(1, args.warmup)), "warm")
     torch.cuda.synchronize()
     M.check(M.lib().mg_debug_launch_apply(prob.h, p, max(1, args.steps)), "launch")
@@ -447,6 +448,20 @@ def main():
             "traffic": profiled_traffic(), "traffic_source": os.path.relpath(PROFILE, REPO),
             "bytes_per_launch": alg_bytes, "us_per_launch": k_ms * 1e3,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback"}
+    # the multigrid level operator (factored FP32, CUDA cores) on the same grid: y = A x,
+    # read x, D^-1 (4 B per dof each), E (4 B per element), write y
+    M.check(M.lib().mg_debug_launch_apply(prob.h, M.OPERATOR_FACTORED_FP32, 5), "warm")
+    torch.cuda.synchronize()
+    k0.record(stream)
+    M.check(M.lib().mg_debug_launch_apply(prob.h, M.OPERATOR_FACTORED_FP32, reps_k), "apply")
+    k1.record(stream)
+    torch.cuda.synchronize()
+    f_ms = k0.elapsed_time(k1) / reps_k
+    f_bytes = 12 * n + 4 * n_el
+    roof_fac = {"kernel": "mf_fac_kernel<3> (factored FP32 multigrid level operator, y = A x)",
+                "bound": "hbm", "achieved": f_bytes / (f_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": f_bytes / (f_ms * 1e-3) / 1e9 / peak, "bytes_per_launch": f_bytes,
+                "us_per_launch": f_ms * 1e3}
 
     # ---------------- plain FP64 form on the same GPU
     plain = None
@@ -518,7 +533,7 @@ def main():
                 "relres_fp64": reps[-1][2], "compliance_rel_err_vs_oracle": comp_err,
                 "sens_rel_err_vs_oracle": dc_err,
                 "e2e": e2e,
-                "roofline": roof, "plain_fp64": plain,
+                "roofline": roof, "roofline_level_operator": roof_fac, "plain_fp64": plain,
                 "speedup_vs_plain_fp64": (value / plain["solves_per_s"]) if plain else None,
                 "small_configs": small, "batch": batch, "serving": serve,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),

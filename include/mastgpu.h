@@ -134,7 +134,14 @@ typedef struct mg_solve_opts {
     int32_t smooth_degree;   /* multigrid: Chebyshev degree of the smoothers (0 = 2) */
     int32_t coarse_degree;   /* multigrid: Chebyshev degree on the coarsest grid (0 = 8) */
     int32_t vec_blocks_per_sm; /* mixed form: CTAs per SM of the vector kernels (0 = 8) */
+    int32_t smoother_operator; /* multigrid level operator: MG_SMOOTHER_FACTORED (0, default:
+                                  FP32 on the CUDA cores, factored element stiffness) or
+                                  MG_SMOOTHER_TENSOR (the tensor-core operator, single pass
+                                  of the CG operator's input type) */
 } mg_solve_opts;
+
+#define MG_SMOOTHER_FACTORED 0
+#define MG_SMOOTHER_TENSOR 1
 
 #define MG_PC_JACOBI 0
 #define MG_PC_MULTIGRID 1
@@ -192,7 +199,10 @@ int mg_mean_temperature(mg_problem *p, const double *T, const mg_solve_opts *opt
    the library reports MG_ENOMEM (-1 disables).  No GPU fault is involved. */
 void mg_debug_fail_alloc_after(int countdown);
 /* One application of the mixed-precision matrix-free operator y = A x
-   (precision MG_MIXED_TF32 / MG_MIXED_BF16; x must be zero on Dirichlet dofs). */
+   (precision MG_MIXED_TF32 / MG_MIXED_BF16 / MG_MIXED_TF32X3 / MG_MIXED_BF16X3: the
+   tensor-core operator; MG_OPERATOR_FACTORED_FP32: the factored FP32 CUDA-core
+   operator of the multigrid levels; x must be zero on Dirichlet dofs). */
+#define MG_OPERATOR_FACTORED_FP32 100
 int mg_debug_matfree_apply(mg_problem *p, int precision, const double *x, double *y);
 
 /* ---- device-resident outputs and diagnostics ---- */

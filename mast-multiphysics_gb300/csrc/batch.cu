@@ -85,6 +85,7 @@ MfSolveParams params_from(const mg_solve_opts &o) {
     prm.smooth_deg = o.smooth_degree;
     prm.coarse_deg = o.coarse_degree;
     prm.vec_blocks_per_sm = o.vec_blocks_per_sm;
+    prm.mg_operator = o.smoother_operator == MG_SMOOTHER_TENSOR ? 1 : 0;
     prm.active = nullptr;
     return prm;
 }
@@ -137,6 +138,7 @@ namespace {
 struct TuneEntry {
     int precision, smooth, coarse, chunk, vec_blocks;
     double inner_rtol, seconds;
+    int smoother = MG_SMOOTHER_FACTORED;
 };
 
 std::mutex g_tune_mu;
@@ -169,8 +171,8 @@ void tune_file_load() {
     if (!f) return;
     char key[4096];
     TuneEntry e;
-    while (fscanf(f, "%4095s %d %d %d %d %d %lf %lf", key, &e.precision, &e.smooth, &e.coarse,
-                  &e.chunk, &e.vec_blocks, &e.inner_rtol, &e.seconds) == 8)
+    while (fscanf(f, "%4095s %d %d %d %d %d %lf %lf %d", key, &e.precision, &e.smooth, &e.coarse,
+                  &e.chunk, &e.vec_blocks, &e.inner_rtol, &e.seconds, &e.smoother) == 9)
         g_tune_cache[key] = e;
     fclose(f);
 }
@@ -181,9 +183,9 @@ void tune_file_save() {
     FILE *f = fopen(path, "w");
     if (!f) return;
     for (auto &kv : g_tune_cache)
-        fprintf(f, "%s %d %d %d %d %d %.3e %.6e\n", kv.first.c_str(), kv.second.precision,
+        fprintf(f, "%s %d %d %d %d %d %.3e %.6e %d\n", kv.first.c_str(), kv.second.precision,
                 kv.second.smooth, kv.second.coarse, kv.second.chunk, kv.second.vec_blocks,
-                kv.second.inner_rtol, kv.second.seconds);
+                kv.second.inner_rtol, kv.second.seconds, kv.second.smoother);
     fclose(f);
 }
 
@@ -194,6 +196,7 @@ void apply_entry(const TuneEntry &e, mg_solve_opts &o) {
     o.graph_chunk = e.chunk;
     o.vec_blocks_per_sm = e.vec_blocks;
     o.inner_rtol = e.inner_rtol;
+    o.smoother_operator = e.smoother;
 }
 
 }  // namespace
@@ -427,7 +430,8 @@ int mg_batch_autotune(mg_batch *b, mg_solve_opts *opts, int32_t max_trials, doub
                   opts->coarse_degree > 0 ? opts->coarse_degree : 8,
                   opts->graph_chunk > 0 ? opts->graph_chunk : 2,
                   opts->vec_blocks_per_sm > 0 ? opts->vec_blocks_per_sm : 8,
-                  opts->inner_rtol > 0 ? opts->inner_rtol : 1e-3, 0.0};
+                  opts->inner_rtol > 0 ? opts->inner_rtol : 1e-3, 0.0,
+                  opts->smoother_operator == MG_SMOOTHER_TENSOR ? MG_SMOOTHER_TENSOR : MG_SMOOTHER_FACTORED};
     int trials = 0;
     const int cap = max_trials > 0 ? max_trials : 16;
     auto run = [&](const TuneEntry &e) -> double {
@@ -457,8 +461,9 @@ int mg_batch_autotune(mg_batch *b, mg_solve_opts *opts, int32_t max_trials, doub
     const int chunks[3] = {2, 4, 8};
     const int vecs[3] = {4, 8, 16};
     const double inners[3] = {1e-2, 1e-3, 1e-4};
-    for (int knob = 0; knob < 6 && trials < cap; knob++) {
-        const int nvals = (knob == 0) ? 2 : 3;
+    const int smoothers[2] = {MG_SMOOTHER_FACTORED, MG_SMOOTHER_TENSOR};
+    for (int knob = 0; knob < 7 && trials < cap; knob++) {
+        const int nvals = (knob == 0 || knob == 6) ? 2 : 3;
         for (int v = 0; v < nvals && trials < cap; v++) {
             TuneEntry t = cur;
             switch (knob) {
@@ -467,10 +472,12 @@ int mg_batch_autotune(mg_batch *b, mg_solve_opts *opts, int32_t max_trials, doub
                 case 2: t.coarse = coarses[v]; break;
                 case 3: t.chunk = chunks[v]; break;
                 case 4: t.vec_blocks = vecs[v]; break;
-                default: t.inner_rtol = inners[v]; break;
+                case 5: t.inner_rtol = inners[v]; break;
+                default: t.smoother = smoothers[v]; break;
             }
             if (t.precision == cur.precision && t.smooth == cur.smooth && t.coarse == cur.coarse &&
-                t.chunk == cur.chunk && t.vec_blocks == cur.vec_blocks && t.inner_rtol == cur.inner_rtol)
+                t.chunk == cur.chunk && t.vec_blocks == cur.vec_blocks && t.inner_rtol == cur.inner_rtol &&
+                t.smoother == cur.smoother)
                 continue;
             t.seconds = run(t);
             if (t.seconds < cur.seconds) cur = t;

@@ -778,7 +778,8 @@ int mg_debug_launch_apply(mg_problem *p, int precision, int reps) {
 // host FP64 buffers); Dirichlet entries of x must be zero.
 int mg_debug_matfree_apply(mg_problem *p, int precision, const double *x, double *y) {
     if (!p || !x || !y) return MG_EINVAL;
-    if (precision < MG_MIXED_TF32 || precision > MG_MIXED_BF16X3) return MG_EINVAL;
+    if ((precision < MG_MIXED_TF32 || precision > MG_MIXED_BF16X3) && precision != MG_OPERATOR_FACTORED_FP32)
+        return MG_EINVAL;
     return matfree_apply_debug(p, precision, x, y);
 }
 

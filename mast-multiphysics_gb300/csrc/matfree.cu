@@ -603,6 +603,159 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
     if (warp == 0) tmem_dealloc(tmem, 64);
 }
 
+// ------------------------------------------------- factored CUDA-core operator
+// y = sum_e E_e P_e^T K0 P_e x in FP32 on the CUDA cores with the factored
+// element stiffness (hex8_factored.cuh: 2 x 72 butterfly additions + 45 FMA per
+// element instead of 576 FMA).  A tile owns kFNX x kFNY nodes in x, y and
+// P.fac_z node planes in z and streams through its element planes: one thread
+// per element of the (kFNX + 1) x (kFNY + 1) element plane around the owned
+// nodes (the halo elements are recomputed by the neighbouring tiles).  Per
+// element plane: the thread gathers its 24 corner values from the two node
+// planes in shared memory, applies the factored stiffness scaled by E_e and
+// stores the corner results; after one barrier each owned node sums the four
+// bottom-corner results of this element plane onto the four top-corner results
+// of the previous one (kept in registers), in a fixed order (deterministic,
+// atomic-free).  The next node plane is prefetched into registers while the
+// current plane is computed; corner results are double-buffered, so one
+// barrier per element plane suffices.
+constexpr int kFEX = 32, kFEY = 8;                 // elements per tile plane
+constexpr int kFNX = kFEX - 1, kFNY = kFEY - 1;    // owned nodes per tile plane
+constexpr int kFPX = kFEX + 1, kFPY = kFEY + 1;    // tile node plane (with halo)
+constexpr int kFThreads = kFEX * kFEY;             // 256
+constexpr int kFPlane = kFPX * kFPY * 3;           // 891 floats
+constexpr int kFPlaneLd = (kFPlane + kFThreads - 1) / kFThreads;  // 4
+constexpr int kFMinZ = 8, kFMaxZ = 32;
+constexpr int kFPlaneSlot = (kFPlane + 3) / 4 * 4;                 // 892
+constexpr int kFSmem = (3 * kFPlaneSlot + 2 * 24 * kFThreads) * 4;  // 59,856 B: three CTAs per SM
+
+// MODE 2: y = rhs - A x.  MODE 3: y = A x.  (Both 0 where dinv = 0.)
+template <int MODE>
+__global__ void __launch_bounds__(kFThreads, 3) mf_fac_kernel(
+    const MfProblem *__restrict__ probs, const MfCol *__restrict__ tiles, int t_lo, int t_hi, int sel,
+    const FacK<float> K, const float *__restrict__ x, const float *__restrict__ rhs,
+    const float *__restrict__ E32, const float *__restrict__ dinv, float *__restrict__ y,
+    const MfState *__restrict__ states) {
+    extern __shared__ __align__(16) float fsm[];
+    float(*sN)[kFPlaneSlot] = reinterpret_cast<float(*)[kFPlaneSlot]>(fsm);
+    // corner results [buffer][(corner b) * 3 + c][element]
+    float(*sY)[24][kFThreads] = reinterpret_cast<float(*)[24][kFThreads]>(fsm + 3 * kFPlaneSlot);
+    const int tid = threadIdx.x, tx = tid & (kFEX - 1), ty = tid / kFEX;
+    for (int ti = t_lo + blockIdx.x; ti < t_hi; ti += gridDim.x) {
+        const MfCol T = tiles[ti];
+        const MfProblem P = probs[T.prob];
+        if (states[P.root].done || P.bottom || (sel >= 0 && sel != (P.coarse < 0 ? 1 : 0))) continue;
+        const int x0 = T.cx * kFNX, y0 = T.cy * kFNY, z0 = T.cz * P.fac_z;
+        const int z1 = min(z0 + P.fac_z, P.NZ);
+        const int S = z1 - z0 + 1;  // element planes z0-1 .. z1-1
+        const float *xp = x + P.dof_off;
+        // node plane nz of the tile: row py holds 3 kFPX floats from node x0-1
+        auto load_plane = [&](int nz, float (&r)[kFPlaneLd]) {
+#pragma unroll
+            for (int k = 0; k < kFPlaneLd; k++) {
+                const int i = tid + k * kFThreads;
+                const int py = i / (3 * kFPX), o = i - py * 3 * kFPX;
+                const int gy = y0 - 1 + py, gxc = 3 * (x0 - 1) + o;
+                float v = 0.0f;
+                if (i < kFPlane && nz >= 0 && nz < P.NZ && gy >= 0 && gy < P.NY && gxc >= 0 && gxc < 3 * P.NX)
+                    v = xp[((int64_t)nz * P.NY + gy) * P.pitch + gxc];
+                r[k] = v;
+            }
+        };
+        auto store_plane = [&](int slot, const float (&r)[kFPlaneLd]) {
+#pragma unroll
+            for (int k = 0; k < kFPlaneLd; k++) {
+                const int i = tid + k * kFThreads;
+                if (i < kFPlane) sN[slot][i] = r[k];
+            }
+        };
+        const int gex = x0 - 1 + tx, gey = y0 - 1 + ty;
+        const bool ex_in = gex >= 0 && gex < P.nx && gey >= 0 && gey < P.ny;
+        auto load_E = [&](int ez) {
+            return (ex_in && ez >= 0 && ez < P.nz) ? E32[P.elem_off + ((int64_t)ez * P.ny + gey) * P.pitch_e + gex]
+                                                    : 0.0f;
+        };
+        const int gx = x0 + tx, gy = y0 + ty;
+        const bool owner = tx < kFNX && ty < kFNY && gx < P.NX && gy < P.NY;
+        __syncthreads();  // the previous tile's readers of sN and sY are done
+        {
+            float r[kFPlaneLd];
+            load_plane(z0 - 1, r);
+            store_plane(0, r);
+            load_plane(z0, r);
+            store_plane(1, r);
+        }
+        float e_cur = load_E(z0 - 1);
+        float pt0 = 0.0f, pt1 = 0.0f, pt2 = 0.0f;  // top-corner sums of the previous element plane
+        __syncthreads();
+        for (int s = 0; s < S; s++) {
+            const int ez = z0 - 1 + s;
+            float rn[kFPlaneLd];
+            if (s + 1 < S) load_plane(ez + 2, rn);  // node plane of the next element plane's top
+            const float e_next = (s + 1 < S) ? load_E(ez + 1) : 0.0f;
+            // node-phase inputs of node plane ez (owned planes z0 .. z1-1)
+            float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f;
+            int64_t gd = 0;
+            if (s >= 1 && owner) {
+                gd = P.dof_off + ((int64_t)ez * P.NY + gy) * P.pitch + 3 * gx;
+                d0 = dinv[gd]; d1 = dinv[gd + 1]; d2 = dinv[gd + 2];
+                if (MODE == 2) { b0 = rhs[gd]; b1 = rhs[gd + 1]; b2 = rhs[gd + 2]; }
+            }
+            // element phase
+            {
+                float v[3][8];
+                const float *n0 = sN[s % 3], *n1 = sN[(s + 1) % 3];
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
+                    const float *src = (bz ? n1 : n0) + ((ty + by) * kFPX + tx + bx) * 3;
+                    v[0][b] = src[0]; v[1][b] = src[1]; v[2][b] = src[2];
+                }
+                if (e_cur != 0.0f) {
+                    hex8_factored_apply(K, e_cur, v);
+                } else {
+#pragma unroll
+                    for (int b = 0; b < 8; b++) { v[0][b] = 0.0f; v[1][b] = 0.0f; v[2][b] = 0.0f; }
+                }
+                float(*Y)[kFThreads] = sY[s & 1];
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    Y[b * 3][tid] = v[0][b];
+                    Y[b * 3 + 1][tid] = v[1][b];
+                    Y[b * 3 + 2][tid] = v[2][b];
+                }
+            }
+            if (s + 1 < S) store_plane((s + 2) % 3, rn);
+            __syncthreads();
+            // node phase: node (gx, gy, ez) is corner (dx, dy) of elements
+            // (tx + 1 - dx, ty + 1 - dy) of this plane (bottom) and of the previous (top)
+            if (owner) {
+                const float(*Y)[kFThreads] = sY[s & 1];
+                float a0 = pt0, a1 = pt1, a2 = pt2, t0 = 0.0f, t1 = 0.0f, t2 = 0.0f;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int dx = q & 1, dy = q >> 1;
+                    const int el = (ty + 1 - dy) * kFEX + tx + 1 - dx;
+                    a0 += Y[q * 3][el]; a1 += Y[q * 3 + 1][el]; a2 += Y[q * 3 + 2][el];
+                    t0 += Y[(q + 4) * 3][el]; t1 += Y[(q + 4) * 3 + 1][el]; t2 += Y[(q + 4) * 3 + 2][el];
+                }
+                if (s >= 1) {
+                    if (MODE == 2) {
+                        y[gd] = d0 == 0.0f ? 0.0f : b0 - a0;
+                        y[gd + 1] = d1 == 0.0f ? 0.0f : b1 - a1;
+                        y[gd + 2] = d2 == 0.0f ? 0.0f : b2 - a2;
+                    } else {
+                        y[gd] = d0 == 0.0f ? 0.0f : a0;
+                        y[gd + 1] = d1 == 0.0f ? 0.0f : a1;
+                        y[gd + 2] = d2 == 0.0f ? 0.0f : a2;
+                    }
+                }
+                pt0 = t0; pt1 = t1; pt2 = t2;
+            }
+            e_cur = e_next;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- vector phase
 // x += alpha p; r -= alpha q (r stays 0 on Dirichlet dofs, D^-1 = 0 there);
 // z = D^-1 r; rz, rr -> beta, stop test.  float4 over 16-byte aligned chunks.
@@ -1162,39 +1315,48 @@ __global__ void mf_phase_kernel(MfState *states, int n_fine) {
     } else {
         st->refine += 1;
         st->status = 0;
+        st->u_zero = 0;  // u has been corrected
         st->phase = kPhaseResid;
     }
 }
 
-// FP64 outer residual r = f - K u (CUDA-core FP64, node-centric: each owned dof
-// sums E_e K0[row, :] u_e over its 8 elements), per-problem ||r||^2 -> scale
+// FP64 outer residual r = f - K u (CUDA-core FP64, factored element stiffness,
+// hex8_factored.cuh), per-problem ||r||^2 -> scale.  A brick of kBN^3 owned
+// nodes evaluates its (kBN+1)^3 surrounding elements in three groups of kBE/3
+// element layers: each element's 24 corner results go to shared memory, then
+// every owned node adds the results of its elements in that group to register
+// accumulators, in a fixed order (deterministic, atomic-free).
+constexpr int kRGroupLayers = kBE / 3;                      // 3 element layers per group
+constexpr int kRGroupEl = kBE * kBE * kRGroupLayers;        // 243 elements
+constexpr int kRNodesPerThread = (kBN * kBN * kBN + kThreads - 1) / kThreads;  // 2
 constexpr int kOffU64 = 0;
-constexpr int kOffK64 = kBU * kBU * kBU * 3 * 8;            // 24000
-constexpr int kOffE64 = kOffK64 + 576 * 8;                   // +4608
-constexpr int kResidSmem = kOffE64 + kNEL * 8;               // +5832
+constexpr int kOffE64 = kBU * kBU * kBU * 3 * 8;            // 24000
+constexpr int kOffY64 = kOffE64 + kNEL * 8;                 // +5832
+constexpr int kResidSmem = kOffY64 + 24 * kRGroupEl * 8;    // +46656
+static_assert(kBE % 3 == 0 && kRGroupEl <= kThreads, "one element per thread and group");
 
 __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
     const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int n_bricks,
     const double *__restrict__ E64, const uint8_t *__restrict__ node_fix,
-    const double *__restrict__ u64, const double *__restrict__ f64, const double *__restrict__ K0,
+    const double *__restrict__ u64, const double *__restrict__ f64, const FacK<double> K,
     double *__restrict__ r64, MfState *states, double *__restrict__ brick_part, double rtol2,
     int max_ref) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
     double *su = reinterpret_cast<double *>(smem + kOffU64);
-    double *sK = reinterpret_cast<double *>(smem + kOffK64);
     double *sE = reinterpret_cast<double *>(smem + kOffE64);
-    for (int i = threadIdx.x; i < 576; i += kThreads) sK[i] = K0[i];
+    double(*sY)[kRGroupEl] = reinterpret_cast<double(*)[kRGroupEl]>(smem + kOffY64);  // [b * 3 + c][element]
     for (int bi = blockIdx.x; bi < n_bricks; bi += gridDim.x) {
         const MfBrick br = bricks[bi];
         const MfProblem P = probs[br.prob];
         MfState *st = states + br.prob;
         if (st->phase != kPhaseResid) continue;
         const bool need_ff = st->ff64 == 0.0;  // first residual of a solve: also ||f||^2
+        const bool u_zero = st->u_zero != 0;    // cold start: r = f, no operator pass
         const int gx0 = br.bx * kBN, gy0 = br.by * kBN, gz0 = br.bz * kBN;
         __syncthreads();
-        for (int i = threadIdx.x; i < kBU * kBU * kBU * 3; i += kThreads) {
+        for (int i = threadIdx.x; i < (u_zero ? 0 : kBU * kBU * kBU * 3); i += kThreads) {
             const int node = i / 3, c = i - node * 3;
             const int ux = node % kBU, uy = (node / kBU) % kBU, uz = node / (kBU * kBU);
             const int gx = gx0 - 1 + ux, gy = gy0 - 1 + uy, gz = gz0 - 1 + uz;
@@ -1205,7 +1367,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
             }
             su[i] = v;
         }
-        for (int l = threadIdx.x; l < kNEL; l += kThreads) {
+        for (int l = threadIdx.x; l < (u_zero ? 0 : kNEL); l += kThreads) {
             const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
             const int gx = gx0 - 1 + ex, gy = gy0 - 1 + ey, gz = gz0 - 1 + ez;
             double e = 0.0;
@@ -1213,41 +1375,72 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
                 e = E64[P.elem_off + ((int64_t)gz * P.ny + gy) * P.pitch_e + gx];
             sE[l] = e;
         }
-        __syncthreads();
+        double acc[kRNodesPerThread][3];
+#pragma unroll
+        for (int k = 0; k < kRNodesPerThread; k++) acc[k][0] = acc[k][1] = acc[k][2] = 0.0;
+        for (int g = 0; g < (u_zero ? 0 : 3); g++) {
+            __syncthreads();  // su / sE loaded; the previous group's readers of sY are done
+            const int l = threadIdx.x;
+            if (l < kRGroupEl) {
+                const int ex = l % kBE, ey = (l / kBE) % kBE, ez = g * kRGroupLayers + l / (kBE * kBE);
+                const double e = sE[ex + kBE * (ey + kBE * ez)];
+                double v[3][8];
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    const double *ub = su + (((ez + (b >> 2)) * kBU + ey + ((b >> 1) & 1)) * kBU + ex + (b & 1)) * 3;
+                    v[0][b] = ub[0]; v[1][b] = ub[1]; v[2][b] = ub[2];
+                }
+                if (e != 0.0) {
+                    hex8_factored_apply(K, e, v);
+                } else {
+#pragma unroll
+                    for (int b = 0; b < 8; b++) v[0][b] = v[1][b] = v[2][b] = 0.0;
+                }
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    sY[b * 3][l] = v[0][b];
+                    sY[b * 3 + 1][l] = v[1][b];
+                    sY[b * 3 + 2][l] = v[2][b];
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < kRNodesPerThread; k++) {
+                const int node = threadIdx.x + k * kThreads;
+                if (node >= kBN * kBN * kBN) continue;
+                const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
+#pragma unroll
+                for (int b = 0; b < 8; b++) {  // the node is corner b of element (o + 1 - d)
+                    const int dx = b & 1, dy = (b >> 1) & 1, dz = b >> 2;
+                    const int lz = oz + 1 - dz - g * kRGroupLayers;
+                    if (lz < 0 || lz >= kRGroupLayers) continue;
+                    const int el = (ox + 1 - dx) + kBE * ((oy + 1 - dy) + kBE * lz);
+                    acc[k][0] += sY[b * 3][el];
+                    acc[k][1] += sY[b * 3 + 1][el];
+                    acc[k][2] += sY[b * 3 + 2][el];
+                }
+            }
+        }
         double part = 0.0, fpart = 0.0;
-        for (int i = threadIdx.x; i < kBN * kBN * kBN * 3; i += kThreads) {
-            const int node = i / 3, c = i - node * 3;
+#pragma unroll
+        for (int k = 0; k < kRNodesPerThread; k++) {
+            const int node = threadIdx.x + k * kThreads;
+            if (node >= kBN * kBN * kBN) continue;
             const int ox = node % kBN, oy = (node / kBN) % kBN, oz = node / (kBN * kBN);
             const int gx = gx0 + ox, gy = gy0 + oy, gz = gz0 + oz;
             if (gx >= P.NX || gy >= P.NY || gz >= P.NZ) continue;
-            double acc = 0.0;
-            for (int dz = 0; dz < 2; dz++)
-                for (int dy = 0; dy < 2; dy++)
-                    for (int dx = 0; dx < 2; dx++) {
-                        const int ex = ox + 1 - dx, ey = oy + 1 - dy, ez = oz + 1 - dz;
-                        const double e = sE[ex + kBE * (ey + kBE * ez)];
-                        if (e == 0.0) continue;
-                        const double *Krow = sK + (3 * corner_index(dx, dy, dz) + c) * 24;
-                        double s = 0.0;
-#pragma unroll
-                        for (int b = 0; b < 8; b++) {
-                            int bx, by, bz;
-                            corner_bits(b, bx, by, bz);
-                            const double *ub = su + (((ez + bz) * kBU + ey + by) * kBU + ex + bx) * 3;
-                            s = fma(Krow[3 * b], ub[0], s);
-                            s = fma(Krow[3 * b + 1], ub[1], s);
-                            s = fma(Krow[3 * b + 2], ub[2], s);
-                        }
-                        acc = fma(e, s, acc);
-                    }
             const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
-            const int64_t gd = dof_index(P, gx, gy, gz, c);
-            const double fv = f64[gd];
-            double rv = fv - acc;
-            if ((node_fix[P.node_off + gn] >> c) & 1) rv = 0.0;
-            r64[gd] = rv;
-            part = fma(rv, rv, part);
-            fpart = fma(fv, fv, fpart);
+            const uint8_t fix = node_fix[P.node_off + gn];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int64_t gd = dof_index(P, gx, gy, gz, c);
+                const double fv = f64[gd];
+                double rv = fv - acc[k][c];
+                if ((fix >> c) & 1) rv = 0.0;
+                r64[gd] = rv;
+                part = fma(rv, rv, part);
+                fpart = fma(fv, fv, fpart);
+            }
         }
         const double s = block_sum(part, red_sh);
         const double sf = need_ff ? block_sum(fpart, red_sh) : 0.0;
@@ -1490,6 +1683,24 @@ void launch_apply_prec(MfBatch &b, int prec, const ApplyArgs &a) {
     }
 }
 
+// level operator of the multigrid (MODE 2: y = rhs - A x, MODE 3: y = A x) on
+// level l: the factored CUDA-core operator (fac) or the tensor-core column
+// operator in precision prec (x is the vector of map in_slot there)
+template <int MODE>
+void launch_level_op(MfBatch &b, bool fac, int prec, int l, int in_slot, const float *x, const float *rhs,
+                     float *y, int sel) {
+    if (fac) {
+        const int lo = b.lvl_fac_lo[l], hi = b.lvl_fac_hi[l];
+        if (hi <= lo) return;
+        const int grid = std::max(1, std::min(hi - lo, b.fac_grid));
+        mf_fac_kernel<MODE><<<grid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, lo, hi, sel, b.fac32, x, rhs,
+                                                              b.E32, b.dinv, y, b.states);
+    } else {
+        ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], in_slot, 0, rhs, y, sel};
+        launch_apply_prec<MODE>(b, prec, a);
+    }
+}
+
 // CG step on the level-0 bricks (z from map in_slot)
 void launch_cg_apply(MfBatch &b, int prec, int in_slot, int parity) {
     ApplyArgs a{b.lvl_col_lo[0], b.lvl_col_hi[0], in_slot, parity, nullptr, b.q};
@@ -1517,6 +1728,8 @@ int configure_kernels() {
     MG_TRY(set_apply_attrs<MG_MIXED_BF16X3>());
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_residual64_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kResidSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
     MG_CUDA_TRY(cudaFuncSetAttribute(mg_bottom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kBottomSmemMax));
     done = true;
@@ -1698,6 +1911,8 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     int nb = 0, nc = 0;
     b.h_bricks.clear();
     b.h_chunks.clear();
+    b.h_cols.clear();
+    b.h_fac_tiles.clear();
     for (size_t pi = 0; pi < b.h_probs.size(); pi++) {
         MfProblem &P = b.h_probs[pi];
         if (P.nx <= 0 || P.ny <= 0 || P.nz <= 0 || P.nx >= 32767 * kBN || P.ny >= 32767 * kBN ||
@@ -1746,6 +1961,19 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
             for (int j = 0; j < cy; j++)
                 for (int i = 0; i < cx; i++)
                     b.h_cols.push_back(MfCol{(int)pi, (int16_t)i, (int16_t)j, (int16_t)k, 0});
+        // tiles of the factored operator: kFNX x kFNY owned nodes, fac_z node
+        // planes (kFMinZ .. kFMaxZ, sized for about three tiles per SM slot)
+        {
+            const int tx = (P.NX + kFNX - 1) / kFNX, ty = (P.NY + kFNY - 1) / kFNY;
+            P.fac_z = (int)std::min<int64_t>(kFMaxZ, std::max<int64_t>(kFMinZ, (P.NZ * (int64_t)tx * ty + slots - 1) / slots));
+            const int tz = (P.NZ + P.fac_z - 1) / P.fac_z;
+            P.fac_begin = (int)b.h_fac_tiles.size();
+            P.fac_count = tx * ty * tz;
+            for (int k = 0; k < tz; k++)
+                for (int j = 0; j < ty; j++)
+                    for (int i = 0; i < tx; i++)
+                        b.h_fac_tiles.push_back(MfCol{(int)pi, (int16_t)i, (int16_t)j, (int16_t)k, 0});
+        }
         P.chunk_begin = nc;
         P.chunk_count = (int)((P.n_pad + kChunk - 1) / kChunk);
         for (int c = 0; c < P.chunk_count; c++) {
@@ -1763,12 +1991,15 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     b.n_cols = (int)b.h_cols.size();
     b.lvl_brick_lo.clear(); b.lvl_brick_hi.clear(); b.lvl_chunk_lo.clear(); b.lvl_chunk_hi.clear();
     b.lvl_col_lo.clear(); b.lvl_col_hi.clear();
+    b.lvl_fac_lo.clear(); b.lvl_fac_hi.clear();
     for (int l = 0; l < b.n_levels; l++) {
         const MfProblem &A = b.h_probs[b.lvl_prob_lo[l]], &Z = b.h_probs[b.lvl_prob_hi[l] - 1];
         b.lvl_brick_lo.push_back(A.brick_begin);
         b.lvl_brick_hi.push_back(Z.brick_begin + Z.brick_count);
         b.lvl_col_lo.push_back(A.col_begin);
         b.lvl_col_hi.push_back(Z.col_begin + Z.col_count);
+        b.lvl_fac_lo.push_back(A.fac_begin);
+        b.lvl_fac_hi.push_back(Z.fac_begin + Z.fac_count);
         b.lvl_chunk_lo.push_back(A.chunk_begin);
         b.lvl_chunk_hi.push_back(Z.chunk_begin + Z.chunk_count);
     }
@@ -1796,13 +2027,15 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
             }
         }
     }
-    b.apply_grid = std::max(1, std::min(nb, sms));
+    b.apply_grid = std::max(1, std::min(nb, 2 * sms));  // FP64 residual: two CTAs per SM
     b.col_grid = std::max(1, std::min(b.n_cols, 3 * sms));  // three column CTAs per SM
+    b.fac_grid = 3 * sms;                                     // three factored-operator CTAs per SM
     b.vec_grid = std::max(1, std::min(nc, 8 * sms));
     MG_TRY(dev_alloc_n(&b.probs, b.h_probs.size()));
     MG_TRY(dev_alloc_n(&b.bricks, b.h_bricks.size()));
     MG_TRY(dev_alloc_n(&b.cols, b.h_cols.size()));
     MG_TRY(dev_alloc_n(&b.col_part, b.h_cols.size()));
+    MG_TRY(dev_alloc_n(&b.fac_tiles, std::max<size_t>(1, b.h_fac_tiles.size())));
     MG_TRY(dev_alloc_n(&b.Bop2, 4096));
     MG_TRY(dev_alloc_n(&b.chunks, b.h_chunks.size()));
     MG_TRY(dev_alloc_n(&b.states, (size_t)b.n_probs));
@@ -1826,6 +2059,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.K0, 576));
     double K0[576];
     hex8_box_stiffness(hx, hy, hz, nu, K0);
+    if (!hex8_factored_build(K0, b.fac64, b.fac32)) return MG_EINVAL;
     // Gershgorin bound of D^-1 A: every assembled row is a positive combination
     // of K0 rows, so max_i sum_j |K0_ij| / K0_ii bounds it on every level
     b.cheb_lmax = 0.0;
@@ -1853,6 +2087,9 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_CUDA_TRY(cudaMemcpyAsync(b.probs, b.h_probs.data(), b.h_probs.size() * sizeof(MfProblem), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.bricks, b.h_bricks.data(), b.h_bricks.size() * sizeof(MfBrick), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.cols, b.h_cols.data(), b.h_cols.size() * sizeof(MfCol), cudaMemcpyHostToDevice, s));
+    if (!b.h_fac_tiles.empty())
+        MG_CUDA_TRY(cudaMemcpyAsync(b.fac_tiles, b.h_fac_tiles.data(), b.h_fac_tiles.size() * sizeof(MfCol),
+                                    cudaMemcpyHostToDevice, s));
     {
         std::vector<uint32_t> bop2;
         pack_b_columns(K0, bop2);
@@ -1885,7 +2122,7 @@ void mf_batch_free(MfBatch &b) {
     void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.K0, b.mb, b.mx, b.md,
-                    b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2};
+                    b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
     b = MfBatch();
@@ -1970,8 +2207,15 @@ int mf_apply(MfBatch &b, int precision, const double *x_host, double *y_host, in
         for (int64_t k = 0; k < 3 * P.NX; k++) pad[row * P.pitch + k] = (float)x_host[row * 3 * P.NX + k];
     MG_CUDA_TRY(cudaMemcpyAsync(b.mx + P.dof_off, pad.data(), P.n_pad * 4, cudaMemcpyHostToDevice, b.stream));
     MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
-    ApplyArgs a{P.col_begin, P.col_begin + P.col_count, 4, 0, nullptr, b.my};
-    launch_apply_prec<3>(b, precision, a);
+    if (precision == MG_OPERATOR_FACTORED_FP32) {
+        const int grid = std::max(1, std::min(P.fac_count, b.fac_grid));
+        mf_fac_kernel<3><<<grid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, P.fac_begin,
+                                                               P.fac_begin + P.fac_count, -1, b.fac32, b.mx,
+                                                               nullptr, b.E32, b.dinv, b.my, b.states);
+    } else {
+        ApplyArgs a{P.col_begin, P.col_begin + P.col_count, 4, 0, nullptr, b.my};
+        launch_apply_prec<3>(b, precision, a);
+    }
     MG_CUDA_TRY(cudaGetLastError());
     MG_CUDA_TRY(cudaMemcpyAsync(pad.data(), b.my + P.dof_off, P.n_pad * 4, cudaMemcpyDeviceToHost, b.stream));
     MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
@@ -1992,7 +2236,13 @@ int mf_launch_apply(MfBatch &b, int precision, int reps) {
     MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
     // nonzero search direction (zero on Dirichlet dofs) so every launch does the full work
     fill_f32_kernel<<<blocks_for(b.n_pad, 256), 256, 0, b.stream>>>(b.z, b.dinv, 1.0f, b.n_pad);
-    for (int i = 0; i < reps; i++) launch_cg_apply(b, precision, 0, i & 1);
+    if (precision == MG_OPERATOR_FACTORED_FP32) {
+        // the multigrid level operator y = A x on level 0 (mx, my)
+        fill_f32_kernel<<<blocks_for(b.n_pad, 256), 256, 0, b.stream>>>(b.mx, b.dinv, 1.0f, b.n_pad);
+        for (int i = 0; i < reps; i++) launch_level_op<3>(b, true, 0, 0, 4, b.mx, nullptr, b.my, -1);
+    } else {
+        for (int i = 0; i < reps; i++) launch_cg_apply(b, precision, 0, i & 1);
+    }
     MG_CUDA_TRY(cudaGetLastError());
     count_launches(reps + 2);
     return MG_OK;
@@ -2027,7 +2277,7 @@ Cheb cheb_coeffs(double lmax, int deg) {
 
 // one Chebyshev smoothing pass of degree deg on level l: mx (+)= S(rin), on the
 // level's problems selected by sel (see ApplyArgs)
-long long enqueue_smooth(MfBatch &b, int prec, int l, const float *rin, int x0_zero, int deg,
+long long enqueue_smooth(MfBatch &b, bool fac, int prec, int l, const float *rin, int x0_zero, int deg,
                          const Cheb &cc, int sel) {
     const int clo = b.lvl_chunk_lo[l], chi = b.lvl_chunk_hi[l];
     const int grid = std::max(1, std::min(chi - clo, b.vec_grid));
@@ -2035,8 +2285,7 @@ long long enqueue_smooth(MfBatch &b, int prec, int l, const float *rin, int x0_z
                                                           b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero, sel);
     long long n = 1;
     for (int k = 1; k < deg; k++) {
-        ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], 5, 0, nullptr, b.my, sel};
-        launch_apply_prec<3>(b, prec, a);
+        launch_level_op<3>(b, fac, prec, l, 5, b.md, nullptr, b.my, sel);
         mg_cheb_next_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, b.my,
                                                              b.mr, b.md, b.mx, b.dinv, cc.c1[k], cc.c2[k], sel);
         n += 2;
@@ -2050,7 +2299,7 @@ long long enqueue_smooth(MfBatch &b, int prec, int l, const float *rin, int x0_z
 // problem's preconditioner does not depend on the batch it is solved in.  The
 // small levels of each chain (MfProblem::bottom) are done by one CTA per chain
 // (mg_bottom_kernel) between the down and the up sweep.
-long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
+long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
     const Cheb cs = cheb_coeffs(b.cheb_lmax, sdeg), cc = cheb_coeffs(b.cheb_lmax, cdeg);
     const int L = b.n_levels;
     auto any_level = [&](int l) {  // some problem of level l is solved level by level
@@ -2067,18 +2316,17 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
     for (int l = 0; l < L - 1; l++) {
         if (!any_level(l)) continue;
         const float *rin = (l == 0) ? b.r : b.mb;
-        n += enqueue_smooth(b, prec, l, rin, 1, sdeg, cs, 0);
-        ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], 4, 0, rin, b.my, 0};
-        launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
+        n += enqueue_smooth(b, fac, prec, l, rin, 1, sdeg, cs, 0);
+        launch_level_op<2>(b, fac, prec, l, 4, b.mx, rin, b.my, 0);  // my = rin - A mx
         const int clo = b.lvl_prob_lo[l + 1], chi = b.lvl_prob_hi[l + 1];
         int64_t maxpad = 1;
         for (int pi = clo; pi < chi; pi++) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
         dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), chi - clo);
         mg_restrict_kernel<<<grid, 256, 0, b.stream>>>(b.probs, clo, b.states, b.my, b.mb, b.dinv);
         n += 2;
-        if (own_coarsest(l)) n += enqueue_smooth(b, prec, l, rin, 1, cdeg, cc, 1);
+        if (own_coarsest(l)) n += enqueue_smooth(b, fac, prec, l, rin, 1, cdeg, cc, 1);
     }
-    if (any_level(L - 1)) n += enqueue_smooth(b, prec, L - 1, L == 1 ? b.r : b.mb, 1, cdeg, cc, -1);
+    if (any_level(L - 1)) n += enqueue_smooth(b, fac, prec, L - 1, L == 1 ? b.r : b.mb, 1, cdeg, cc, -1);
     if (!b.h_heads.empty()) {
         BottomCheb bc{};
         bc.inv_theta_s = cs.inv_theta;
@@ -2100,9 +2348,8 @@ long long enqueue_vcycle(MfBatch &b, int prec, int sdeg, int cdeg) {
             if (b.h_probs[pi].coarse >= 0) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
         dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), fhi - flo);
         mg_prolong_kernel<<<grid, 256, 0, b.stream>>>(b.probs, flo, b.states, b.mx, b.dinv);
-        ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], 4, 0, rin, b.my, 0};
-        launch_apply_prec<2>(b, prec, a);  // my = rin - A mx
-        n += 2 + enqueue_smooth(b, prec, l, b.my, 0, sdeg, cs, 0);
+        launch_level_op<2>(b, fac, prec, l, 4, b.mx, rin, b.my, 0);  // my = rin - A mx
+        n += 2 + enqueue_smooth(b, fac, prec, l, b.my, 0, sdeg, cs, 0);
     }
     return n;
 }
@@ -2120,7 +2367,7 @@ long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
     const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
     const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
     mf_residual64_kernel<<<std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s>>>(
-        b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.K0, b.r64, b.states,
+        b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.fac64, b.r64, b.states,
         b.brick_part, prm.rtol * prm.rtol, max_ref);
     mf_inner_init_kernel<<<vg0, kThreads, 0, s>>>(
         b.chunks, n0, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.p1, b.dinv, b.states, b.chunk_part,
@@ -2130,7 +2377,7 @@ long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
     if (use_mg) {
         const int sdeg = prm.smooth_deg > 0 ? prm.smooth_deg : 2;
         const int cdeg = prm.coarse_deg > 0 ? prm.coarse_deg : 8;
-        n += enqueue_vcycle(b, mg_precision(prm.precision), sdeg, cdeg);
+        n += enqueue_vcycle(b, prm.mg_operator == 0, mg_precision(prm.precision), sdeg, cdeg);
         mf_dot_rz_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.probs, b.r, b.mx, b.states,
                                                  b.chunk_part, 0);
         launch_cg_apply(b, prm.precision, 4, parity);  // p = z + beta p_old, q = A p, alpha
@@ -2152,7 +2399,8 @@ int build_step_graph(MfBatch &b, const MfSolveParams &prm, int chunk) {
     const std::vector<double> key = {(double)prm.precision, (double)chunk, (double)prm.mg,
                                      (double)prm.smooth_deg, (double)prm.coarse_deg, prm.rtol,
                                      prm.inner_rtol, (double)prm.max_iterations,
-                                     (double)prm.max_refinements, (double)b.vec_grid};
+                                     (double)prm.max_refinements, (double)b.vec_grid,
+                                     (double)prm.mg_operator};
     if (b.graph && b.graph_key == key) return MG_OK;
     if (b.graph) {
         cudaGraphExecDestroy(b.graph);
@@ -2233,6 +2481,7 @@ int mf_batch_activate(MfBatch &b, const std::vector<int> &level0, bool warm_star
         memset(&h, 0, sizeof(MfState));
         h.done = 1;
         h.phase = kPhaseResid;  // its first residual pass also forms ||f||^2
+        h.u_zero = warm_start ? 0 : 1;
         MG_CUDA_TRY(cudaMemcpyAsync(b.states + i, &h, sizeof(MfState), cudaMemcpyHostToDevice, b.stream));
     }
     return MG_OK;
@@ -2403,6 +2652,7 @@ int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
     prm.smooth_deg = o.smooth_degree;
     prm.coarse_deg = o.coarse_degree;
     prm.vec_blocks_per_sm = o.vec_blocks_per_sm;
+    prm.mg_operator = o.smoother_operator == MG_SMOOTHER_TENSOR ? 1 : 0;
     int rc = mf_batch_solve(b, prm, true);
     MG_TRY(mf_batch_get_u(b, 0, p->d_X));
     count_launches(1);

@@ -9,6 +9,7 @@
 
 #include <vector>
 
+#include "hex8_factored.cuh"
 #include "mg_internal.h"
 
 namespace mg {
@@ -47,6 +48,8 @@ struct MfProblem {
     int chunk_begin, chunk_count;
     int col_begin, col_count;
     int col_z;            // node planes per column (kCZ or fewer for small grids)
+    int fac_begin, fac_count;
+    int fac_z;            // node planes per tile of the factored CUDA-core operator
     int share_elems;      // >= 0: reuse the element tables of that problem (load cases)
     int level;            // multigrid level (0 = the design's own grid)
     int root;             // level-0 problem whose solver state drives this one
@@ -87,7 +90,8 @@ struct MfState {
     double rr64, ff64, scale;
     int iter, done, status, maxit;
     int total_iter, refine, ref_done, ref_status;
-    int phase, first, pad0, pad1;   // first: the next dot_rz starts the inner CG (beta = 0)
+    int phase, first, u_zero, pad1; // first: the next dot_rz starts the inner CG (beta = 0);
+                                    // u_zero: u is still 0 (the residual is f)
     unsigned cnt_apply, cnt_update, cnt_res, pad;
 };
 
@@ -107,6 +111,11 @@ struct MfBatch {
     std::vector<int> lvl_col_lo, lvl_col_hi;
     double *col_part = nullptr;   // per-column partial of p.q
     uint32_t *Bop2 = nullptr;     // K0 as the column operator's four (dy, dz) B tiles
+    MfCol *fac_tiles = nullptr;   // tiles of the factored CUDA-core operator (cx, cy, cz)
+    std::vector<MfCol> h_fac_tiles;
+    std::vector<int> lvl_fac_lo, lvl_fac_hi;
+    FacK<float> fac32{};          // K0 in the per-axis sum/difference basis
+    FacK<double> fac64{};
     MfChunkDesc *chunks = nullptr;
     MfState *states = nullptr;
     MfState *states_host = nullptr;  // pinned
@@ -140,7 +149,7 @@ struct MfBatch {
     cudaGraphExec_t graph = nullptr;  // solver steps (see enqueue_step)
     std::vector<double> graph_key;    // parameters the graph was captured with
     long long graph_launches = 0;     // kernel nodes in the graph
-    int apply_grid = 0, vec_grid = 0, col_grid = 0;
+    int apply_grid = 0, vec_grid = 0, col_grid = 0, fac_grid = 0;
     cudaStream_t stream = nullptr;
 };
 
@@ -155,6 +164,7 @@ struct MfSolveParams {
     int mg;               // 1: geometric multigrid V-cycle preconditioner, 0: Jacobi
     int smooth_deg;       // Chebyshev degree of the pre/post smoothers
     int coarse_deg;       // Chebyshev degree on the coarsest level
+    int mg_operator = 0;  // multigrid level operator: 0 factored FP32 (CUDA cores), 1 tensor cores
     int vec_blocks_per_sm = 0;         // grid of the vector kernels (0 = 8 per SM)
     const uint8_t *active = nullptr;   // per level-0 problem: 0 = leave untouched (nullable)
 };

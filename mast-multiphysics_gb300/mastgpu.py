@@ -85,6 +85,8 @@ PHYS_HEX8, PHYS_MEMBRANE, PHYS_HEAT = 0, 1, 2
 PLAIN_FP64, MIXED_TF32, MIXED_BF16, MIXED_TF32X3, MIXED_BF16X3 = 0, 1, 2, 3, 4
 KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
 PC_JACOBI, PC_MULTIGRID = 0, 1
+SMOOTHER_FACTORED, SMOOTHER_TENSOR = 0, 1
+OPERATOR_FACTORED_FP32 = 100  # mg_debug_matfree_apply / mg_debug_launch_apply: factored FP32 operator
 PARAM_DENSITY, PARAM_K0, PARAM_ELEM_SCALE = 0, 1, 2
 
 _vp = ctypes.c_void_p
@@ -115,7 +117,7 @@ class SolveOpts(ctypes.Structure):
                 ("consistent_jacobian", _i32), ("max_refinements", _i32), ("inner_rtol", _dbl),
                 ("timeout_s", _dbl), ("warm_start", _i32), ("graph_chunk", _i32),
                 ("preconditioner", _i32), ("smooth_degree", _i32), ("coarse_degree", _i32),
-                ("vec_blocks_per_sm", _i32)]
+                ("vec_blocks_per_sm", _i32), ("smoother_operator", _i32)]
 
 
 class ServerOpts(ctypes.Structure):

@@ -15,12 +15,49 @@ import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-TOL_OP = {M.MIXED_TF32: 4e-3, M.MIXED_BF16: 3e-2, M.MIXED_TF32X3: 2e-5, M.MIXED_BF16X3: 2e-4}
+TOL_OP = {M.MIXED_TF32: 4e-3, M.MIXED_BF16: 3e-2, M.MIXED_TF32X3: 2e-5, M.MIXED_BF16X3: 2e-4,
+          M.OPERATOR_FACTORED_FP32: 2e-6}
 ALL = [M.MIXED_TF32, M.MIXED_BF16, M.MIXED_TF32X3, M.MIXED_BF16X3]
 
 
 def rel(a, b):
     return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+@pytest.mark.parametrize("shape", [(8, 4, 4), (16, 8, 8), (12, 7, 5), (17, 9, 3), (40, 9, 10)])
+def test_factored_level_operator_matches_fp64_csr(shape):
+    """The multigrid level operator (FP32, CUDA cores, factored element
+    stiffness; tiles of 31 x 7 owned nodes, so the 40 x 9 grid spans several)
+    against the FP64 CSR product: FP32 rounding only."""
+    nx, ny, nz = shape
+    rng = np.random.default_rng(2)
+    rho = rng.uniform(0.01, 1.0, nx * ny * nz)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        x = rng.standard_normal(p.n_dofs)
+        fixed = O.simp_fixed_mask(O.simp_desc(nx, ny, nz))
+        x[fixed == 1] = 0.0
+        p.residual_and_jacobian(np.zeros(p.n_dofs), want_R=False)
+        y_ref = p.spmv(x)
+        y = p.matfree_apply(x, M.OPERATOR_FACTORED_FP32)
+    y_ref[fixed == 1] = 0.0
+    assert rel(y, y_ref) < TOL_OP[M.OPERATOR_FACTORED_FP32]
+    assert np.all(y[fixed == 1] == 0.0)
+
+
+@pytest.mark.parametrize("smoother", [M.SMOOTHER_FACTORED, M.SMOOTHER_TENSOR])
+def test_both_smoother_operators_converge(smoother):
+    nx, ny, nz = 32, 16, 16
+    rho = np.random.default_rng(7).uniform(0.01, 1.0, nx * ny * nz)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        _, rep = p.solve(M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8, inner_rtol=1e-3,
+                                        smoother_operator=smoother))
+        c, dc = p.compliance()
+    assert rep.status == 0 and rep.relres <= 1e-8, (rep.status, rep.relres)
+    _, dc_ref, r = O.simp_solve(O.simp_desc(nx, ny, nz, rtol=1e-12, maxit=10 ** 6), rho)
+    assert abs(c - r.compliance) / r.compliance < 1e-6
+    assert np.abs(dc - dc_ref).max() / np.abs(dc_ref).max() < 1e-6
 
 
 @pytest.mark.parametrize("prec", ALL)
