@@ -624,21 +624,38 @@ constexpr int kFPX = kFEX + 1, kFPY = kFEY + 1;    // tile node plane (with halo
 constexpr int kFThreads = kFEX * kFEY;             // 256
 constexpr int kFPlane = kFPX * kFPY * 3;           // 891 floats
 constexpr int kFPlaneLd = (kFPlane + kFThreads - 1) / kFThreads;  // 4
-constexpr int kFMinZ = 8, kFMaxZ = 32;
+constexpr int kFMinZ = 4, kFMaxZ = 32;
+constexpr int kFRing = 4;                          // node / modulus planes in flight
 constexpr int kFPlaneSlot = (kFPlane + 3) / 4 * 4;                 // 892
-constexpr int kFSmem = (3 * kFPlaneSlot + 2 * 24 * kFThreads) * 4;  // 59,856 B: three CTAs per SM
+constexpr int kFSmem = (kFRing * (kFPlaneSlot + kFThreads) + 2 * 24 * kFThreads) * 4;  // 67,456 B
+
+// 4-byte asynchronous global -> shared copy; src_bytes = 0 fills zero (no read)
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+                 "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 // MODE 2: y = rhs - A x.  MODE 3: y = A x.  (Both 0 where dinv = 0.)
+// MODE 4: one Chebyshev step on direction x = d: r -= A d; y = d' = c1 d +
+//         c2 D^-1 r; xs += d' (the sequence of mg_cheb_next_kernel, fused).
 template <int MODE>
 __global__ void __launch_bounds__(kFThreads, 3) mf_fac_kernel(
     const MfProblem *__restrict__ probs, const MfCol *__restrict__ tiles, int t_lo, int t_hi, int sel,
     const FacK<float> K, const float *__restrict__ x, const float *__restrict__ rhs,
     const float *__restrict__ E32, const float *__restrict__ dinv, float *__restrict__ y,
-    const MfState *__restrict__ states) {
+    const MfState *__restrict__ states, float *__restrict__ r, float *__restrict__ xs, float c1, float c2) {
     extern __shared__ __align__(16) float fsm[];
-    float(*sN)[kFPlaneSlot] = reinterpret_cast<float(*)[kFPlaneSlot]>(fsm);
+    float(*sN)[kFPlaneSlot] = reinterpret_cast<float(*)[kFPlaneSlot]>(fsm);            // node planes
+    float(*sE)[kFThreads] = reinterpret_cast<float(*)[kFThreads]>(fsm + kFRing * kFPlaneSlot);  // moduli
     // corner results [buffer][(corner b) * 3 + c][element]
-    float(*sY)[24][kFThreads] = reinterpret_cast<float(*)[24][kFThreads]>(fsm + 3 * kFPlaneSlot);
+    float(*sY)[24][kFThreads] =
+        reinterpret_cast<float(*)[24][kFThreads]>(fsm + kFRing * (kFPlaneSlot + kFThreads));
     const int tid = threadIdx.x, tx = tid & (kFEX - 1), ty = tid / kFEX;
     for (int ti = t_lo + blockIdx.x; ti < t_hi; ti += gridDim.x) {
         const MfCol T = tiles[ti];
@@ -646,72 +663,87 @@ __global__ void __launch_bounds__(kFThreads, 3) mf_fac_kernel(
         if (states[P.root].done || P.bottom || (sel >= 0 && sel != (P.coarse < 0 ? 1 : 0))) continue;
         const int x0 = T.cx * kFNX, y0 = T.cy * kFNY, z0 = T.cz * P.fac_z;
         const int z1 = min(z0 + P.fac_z, P.NZ);
-        const int S = z1 - z0 + 1;  // element planes z0-1 .. z1-1
+        const int S = z1 - z0 + 1;  // element planes z0-1 .. z1-1; node planes z0-1 .. z1
         const float *xp = x + P.dof_off;
-        // node plane nz of the tile: row py holds 3 kFPX floats from node x0-1
-        auto load_plane = [&](int nz, float (&r)[kFPlaneLd]) {
+        const int64_t plane_stride = (int64_t)P.NY * P.pitch;
+        // this thread's part of a tile node plane: row py holds 3 kFPX floats from
+        // node x0-1; off < 0 marks a position outside the grid
+        int off[kFPlaneLd];
 #pragma unroll
-            for (int k = 0; k < kFPlaneLd; k++) {
-                const int i = tid + k * kFThreads;
-                const int py = i / (3 * kFPX), o = i - py * 3 * kFPX;
-                const int gy = y0 - 1 + py, gxc = 3 * (x0 - 1) + o;
-                float v = 0.0f;
-                if (i < kFPlane && nz >= 0 && nz < P.NZ && gy >= 0 && gy < P.NY && gxc >= 0 && gxc < 3 * P.NX)
-                    v = xp[((int64_t)nz * P.NY + gy) * P.pitch + gxc];
-                r[k] = v;
-            }
-        };
-        auto store_plane = [&](int slot, const float (&r)[kFPlaneLd]) {
-#pragma unroll
-            for (int k = 0; k < kFPlaneLd; k++) {
-                const int i = tid + k * kFThreads;
-                if (i < kFPlane) sN[slot][i] = r[k];
-            }
-        };
+        for (int k = 0; k < kFPlaneLd; k++) {
+            const int i = tid + k * kFThreads;
+            const int py = i / (3 * kFPX), o = i - py * 3 * kFPX;
+            const int gy = y0 - 1 + py, gxc = 3 * (x0 - 1) + o;
+            off[k] = (i < kFPlane && gy >= 0 && gy < P.NY && gxc >= 0 && gxc < 3 * P.NX) ? gy * P.pitch + gxc : -1;
+        }
         const int gex = x0 - 1 + tx, gey = y0 - 1 + ty;
         const bool ex_in = gex >= 0 && gex < P.nx && gey >= 0 && gey < P.ny;
-        auto load_E = [&](int ez) {
-            return (ex_in && ez >= 0 && ez < P.nz) ? E32[P.elem_off + ((int64_t)ez * P.ny + gey) * P.pitch_e + gex]
-                                                    : 0.0f;
+        const float *Ep = E32 + P.elem_off + (ex_in ? (int64_t)gey * P.pitch_e + gex : 0);
+        // node plane p (nz = z0 - 1 + p) and element plane p's moduli into ring slot p % kFRing
+        auto issue = [&](int p) {
+            const int nz = z0 - 1 + p, slot = p % kFRing;
+            const bool zin = nz >= 0 && nz < P.NZ;
+#pragma unroll
+            for (int k = 0; k < kFPlaneLd; k++) {
+                const int i = tid + k * kFThreads;
+                if (i < kFPlane) {
+                    const bool v = zin && off[k] >= 0;
+                    cp_async4(&sN[slot][i], v ? xp + nz * plane_stride + off[k] : xp, v ? 4 : 0);
+                }
+            }
+            const bool ev = ex_in && nz >= 0 && nz < P.nz && p < S;
+            cp_async4(&sE[slot][tid], ev ? Ep + (int64_t)nz * P.ny * P.pitch_e : E32, ev ? 4 : 0);
+            cp_async_commit();
         };
         const int gx = x0 + tx, gy = y0 + ty;
         const bool owner = tx < kFNX && ty < kFNY && gx < P.NX && gy < P.NY;
-        __syncthreads();  // the previous tile's readers of sN and sY are done
-        {
-            float r[kFPlaneLd];
-            load_plane(z0 - 1, r);
-            store_plane(0, r);
-            load_plane(z0, r);
-            store_plane(1, r);
-        }
-        float e_cur = load_E(z0 - 1);
-        float pt0 = 0.0f, pt1 = 0.0f, pt2 = 0.0f;  // top-corner sums of the previous element plane
+        __syncthreads();  // the previous tile's readers of sN, sE and sY are done
+        issue(0);
+        issue(1);
+        issue(2);
+        cp_async_wait<1>();  // planes 0 and 1
         __syncthreads();
+        float pt0 = 0.0f, pt1 = 0.0f, pt2 = 0.0f;  // top-corner sums of the previous element plane
+        // node-phase inputs of node plane s (owned planes z0 .. z1-1), one step ahead
+        // (MODE 2: b = rhs; MODE 4: b = r and w = xs)
+        float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, w0 = 0.0f, w1 = 0.0f, w2 = 0.0f;
+        int64_t gd = P.dof_off + ((int64_t)(z0 - 1) * P.NY + gy) * P.pitch + 3 * gx;
         for (int s = 0; s < S; s++) {
             const int ez = z0 - 1 + s;
-            float rn[kFPlaneLd];
-            if (s + 1 < S) load_plane(ez + 2, rn);  // node plane of the next element plane's top
-            const float e_next = (s + 1 < S) ? load_E(ez + 1) : 0.0f;
-            // node-phase inputs of node plane ez (owned planes z0 .. z1-1)
-            float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f;
-            int64_t gd = 0;
-            if (s >= 1 && owner) {
-                gd = P.dof_off + ((int64_t)ez * P.NY + gy) * P.pitch + 3 * gx;
-                d0 = dinv[gd]; d1 = dinv[gd + 1]; d2 = dinv[gd + 2];
-                if (MODE == 2) { b0 = rhs[gd]; b1 = rhs[gd + 1]; b2 = rhs[gd + 2]; }
+            // plane s + 3 into the slot of plane s - 1 (read in step s - 1, before its barrier)
+            if (s + 3 <= S) issue(s + 3);
+            else cp_async_commit();  // keep one group per step
+            float nd0 = 0.0f, nd1 = 0.0f, nd2 = 0.0f, nb0 = 0.0f, nb1 = 0.0f, nb2 = 0.0f;
+            float nw0 = 0.0f, nw1 = 0.0f, nw2 = 0.0f;
+            if (s + 1 < S && owner) {
+                const int64_t g1 = gd + plane_stride;
+                nd0 = dinv[g1]; nd1 = dinv[g1 + 1]; nd2 = dinv[g1 + 2];
+                if (MODE == 2) { nb0 = rhs[g1]; nb1 = rhs[g1 + 1]; nb2 = rhs[g1 + 2]; }
+                if (MODE == 4) {
+                    nb0 = r[g1]; nb1 = r[g1 + 1]; nb2 = r[g1 + 2];
+                    nw0 = xs[g1]; nw1 = xs[g1 + 1]; nw2 = xs[g1 + 2];
+                }
+            }
+            // MODE 4: the direction at this thread's node (node plane s), read before
+            // the barrier (its ring slot is refilled in the next step)
+            float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f;
+            if (MODE == 4 && owner) {
+                const float *un = sN[s % kFRing] + ((ty + 1) * kFPX + tx + 1) * 3;
+                u0 = un[0]; u1 = un[1]; u2 = un[2];
             }
             // element phase
             {
                 float v[3][8];
-                const float *n0 = sN[s % 3], *n1 = sN[(s + 1) % 3];
+                const float *n0 = sN[s % kFRing], *n1 = sN[(s + 1) % kFRing];
 #pragma unroll
                 for (int b = 0; b < 8; b++) {
                     const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
                     const float *src = (bz ? n1 : n0) + ((ty + by) * kFPX + tx + bx) * 3;
                     v[0][b] = src[0]; v[1][b] = src[1]; v[2][b] = src[2];
                 }
-                if (e_cur != 0.0f) {
-                    hex8_factored_apply(K, e_cur, v);
+                const float e = sE[s % kFRing][tid];
+                if (e != 0.0f) {
+                    hex8_factored_apply(K, e, v);
                 } else {
 #pragma unroll
                     for (int b = 0; b < 8; b++) { v[0][b] = 0.0f; v[1][b] = 0.0f; v[2][b] = 0.0f; }
@@ -724,7 +756,7 @@ __global__ void __launch_bounds__(kFThreads, 3) mf_fac_kernel(
                     Y[b * 3 + 2][tid] = v[2][b];
                 }
             }
-            if (s + 1 < S) store_plane((s + 2) % 3, rn);
+            cp_async_wait<1>();  // plane s + 2 (the next step's top plane) has landed
             __syncthreads();
             // node phase: node (gx, gy, ez) is corner (dx, dy) of elements
             // (tx + 1 - dx, ty + 1 - dy) of this plane (bottom) and of the previous (top)
@@ -743,6 +775,14 @@ __global__ void __launch_bounds__(kFThreads, 3) mf_fac_kernel(
                         y[gd] = d0 == 0.0f ? 0.0f : b0 - a0;
                         y[gd + 1] = d1 == 0.0f ? 0.0f : b1 - a1;
                         y[gd + 2] = d2 == 0.0f ? 0.0f : b2 - a2;
+                    } else if (MODE == 4) {
+                        const float r0 = b0 - (d0 == 0.0f ? 0.0f : a0), r1 = b1 - (d1 == 0.0f ? 0.0f : a1),
+                                    r2 = b2 - (d2 == 0.0f ? 0.0f : a2);
+                        const float e0 = fmaf(c1, u0, c2 * d0 * r0), e1 = fmaf(c1, u1, c2 * d1 * r1),
+                                    e2 = fmaf(c1, u2, c2 * d2 * r2);
+                        r[gd] = r0; r[gd + 1] = r1; r[gd + 2] = r2;
+                        y[gd] = e0; y[gd + 1] = e1; y[gd + 2] = e2;
+                        xs[gd] = w0 + e0; xs[gd + 1] = w1 + e1; xs[gd + 2] = w2 + e2;
                     } else {
                         y[gd] = d0 == 0.0f ? 0.0f : a0;
                         y[gd + 1] = d1 == 0.0f ? 0.0f : a1;
@@ -751,8 +791,10 @@ __global__ void __launch_bounds__(kFThreads, 3) mf_fac_kernel(
                 }
                 pt0 = t0; pt1 = t1; pt2 = t2;
             }
-            e_cur = e_next;
+            d0 = nd0; d1 = nd1; d2 = nd2; b0 = nb0; b1 = nb1; b2 = nb2; w0 = nw0; w1 = nw1; w2 = nw2;
+            gd += plane_stride;
         }
+        cp_async_wait<0>();
     }
 }
 
@@ -1024,6 +1066,7 @@ __global__ void mg_coarsen_kernel(const MfProblem *__restrict__ probs, int plo,
 constexpr int kBottomThreads = 512;
 constexpr int kBottomMaxLevels = 6;
 constexpr int kBottomSmemMax = 200 * 1024;  // per chain: 576 + sum over levels (18 NN + ne) floats
+constexpr int kBottomMaxHeadNodes = 2 * kBottomThreads;
 
 struct BottomLevel {
     int NX, NY, NZ, nx, ny, nz;
@@ -1694,7 +1737,8 @@ void launch_level_op(MfBatch &b, bool fac, int prec, int l, int in_slot, const f
         if (hi <= lo) return;
         const int grid = std::max(1, std::min(hi - lo, b.fac_grid));
         mf_fac_kernel<MODE><<<grid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, lo, hi, sel, b.fac32, x, rhs,
-                                                              b.E32, b.dinv, y, b.states);
+                                                              b.E32, b.dinv, y, b.states, nullptr, nullptr,
+                                                              0.0f, 0.0f);
     } else {
         ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], in_slot, 0, rhs, y, sel};
         launch_apply_prec<MODE>(b, prec, a);
@@ -1730,6 +1774,7 @@ int configure_kernels() {
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kResidSmem));
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
     MG_CUDA_TRY(cudaFuncSetAttribute(mg_bottom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kBottomSmemMax));
     done = true;
@@ -2006,8 +2051,10 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     b.n_pad = dof;
     b.n_elem_pad = el;
     b.n_nodes = nd;
-    // bottom chains: for every design, the first level below the finest whose
-    // chain (it and all coarser levels) fits the bottom kernel's shared memory
+    // bottom chains: for every design, the first level below the finest with at
+    // most kBottomMaxHeadNodes nodes whose chain (it and all coarser levels) fits
+    // the bottom kernel's shared memory; larger levels run level by level on the
+    // whole GPU (the one-CTA kernel is bound by one SM's shared-memory pipe there)
     b.h_heads.clear();
     b.bottom_smem = 0;
     for (int r = 0; r < b.n_fine; r++) {
@@ -2019,7 +2066,9 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
                 floats += 18LL * T.NX * T.NY * T.NZ + (int64_t)T.nx * T.ny * T.nz;
             }
             const int64_t bytes = floats * 4;
-            if (depth <= kBottomMaxLevels && bytes <= kBottomSmemMax) {
+            const MfProblem &Hd = b.h_probs[q];
+            if (depth <= kBottomMaxLevels && bytes <= kBottomSmemMax &&
+                (int64_t)Hd.NX * Hd.NY * Hd.NZ <= kBottomMaxHeadNodes) {
                 b.h_heads.push_back(q);
                 b.bottom_smem = std::max(b.bottom_smem, (int)bytes);
                 for (int t = q; t >= 0; t = b.h_probs[t].coarse) b.h_probs[t].bottom = 1;
@@ -2211,7 +2260,8 @@ int mf_apply(MfBatch &b, int precision, const double *x_host, double *y_host, in
         const int grid = std::max(1, std::min(P.fac_count, b.fac_grid));
         mf_fac_kernel<3><<<grid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, P.fac_begin,
                                                                P.fac_begin + P.fac_count, -1, b.fac32, b.mx,
-                                                               nullptr, b.E32, b.dinv, b.my, b.states);
+                                                               nullptr, b.E32, b.dinv, b.my, b.states,
+                                                               nullptr, nullptr, 0.0f, 0.0f);
     } else {
         ApplyArgs a{P.col_begin, P.col_begin + P.col_count, 4, 0, nullptr, b.my};
         launch_apply_prec<3>(b, precision, a);
@@ -2284,6 +2334,20 @@ long long enqueue_smooth(MfBatch &b, bool fac, int prec, int l, const float *rin
     mg_cheb_first_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, rin,
                                                           b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero, sel);
     long long n = 1;
+    if (fac) {
+        // fused Chebyshev steps; the direction alternates between md and my
+        const int lo = b.lvl_fac_lo[l], hi = b.lvl_fac_hi[l];
+        const int fgrid = std::max(1, std::min(hi - lo, b.fac_grid));
+        float *din = b.md, *dout = b.my;
+        for (int k = 1; k < deg && hi > lo; k++) {
+            mf_fac_kernel<4><<<fgrid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, lo, hi, sel, b.fac32,
+                                                                    din, nullptr, b.E32, b.dinv, dout, b.states,
+                                                                    b.mr, b.mx, cc.c1[k], cc.c2[k]);
+            std::swap(din, dout);
+            n += 1;
+        }
+        return n;
+    }
     for (int k = 1; k < deg; k++) {
         launch_level_op<3>(b, fac, prec, l, 5, b.md, nullptr, b.my, sel);
         mg_cheb_next_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, b.my,
