@@ -167,6 +167,91 @@ __device__ __forceinline__ void hex8_factored_apply(const FacK<T> &K, T e, T (&v
         for (int b = 0; b < 8; b++) v[c][b] = yh[c][b];
     }
 }
+
+// Two elements at once in packed FP32x2 arithmetic (each component of a
+// float2 is one element; per component the same operations, in the same
+// order and rounding, as hex8_factored_apply<float>)
+struct FacK2 {
+    float2 v[kFacN];  // (k, k) pairs of FacK<float>
+};
+
+__device__ __forceinline__ void hex8_factored_apply2(const FacK2 &K, float2 e, float2 (&v)[3][8]) {
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int t = 1; t < 8; t <<= 1)
+#pragma unroll
+            for (int b = 0; b < 8; b++)
+                if (!(b & t)) {
+                    const float2 lo = v[c][b], hi = v[c][b | t];
+                    v[c][b] = __fadd2_rn(lo, hi);
+                    v[c][b | t] = __ffma2_rn(lo, m1, hi);  // hi - lo
+                }
+    float2 yh[3][8];
+    yh[0][1] = __fmul2_rn(K.v[0], v[0][1]);
+    yh[0][1] = __ffma2_rn(K.v[1], v[1][2], yh[0][1]);
+    yh[0][1] = __ffma2_rn(K.v[2], v[2][4], yh[0][1]);
+    yh[0][2] = __fmul2_rn(K.v[3], v[0][2]);
+    yh[0][2] = __ffma2_rn(K.v[4], v[1][1], yh[0][2]);
+    yh[0][3] = __fmul2_rn(K.v[5], v[0][3]);
+    yh[0][3] = __ffma2_rn(K.v[6], v[2][6], yh[0][3]);
+    yh[0][4] = __fmul2_rn(K.v[7], v[0][4]);
+    yh[0][4] = __ffma2_rn(K.v[8], v[2][1], yh[0][4]);
+    yh[0][5] = __fmul2_rn(K.v[9], v[0][5]);
+    yh[0][5] = __ffma2_rn(K.v[10], v[1][6], yh[0][5]);
+    yh[0][6] = __fmul2_rn(K.v[11], v[0][6]);
+    yh[0][6] = __ffma2_rn(K.v[12], v[1][5], yh[0][6]);
+    yh[0][6] = __ffma2_rn(K.v[13], v[2][3], yh[0][6]);
+    yh[0][7] = __fmul2_rn(K.v[14], v[0][7]);
+    yh[1][1] = __fmul2_rn(K.v[15], v[0][2]);
+    yh[1][1] = __ffma2_rn(K.v[16], v[1][1], yh[1][1]);
+    yh[1][2] = __fmul2_rn(K.v[17], v[0][1]);
+    yh[1][2] = __ffma2_rn(K.v[18], v[1][2], yh[1][2]);
+    yh[1][2] = __ffma2_rn(K.v[19], v[2][4], yh[1][2]);
+    yh[1][3] = __fmul2_rn(K.v[20], v[1][3]);
+    yh[1][3] = __ffma2_rn(K.v[21], v[2][5], yh[1][3]);
+    yh[1][4] = __fmul2_rn(K.v[22], v[1][4]);
+    yh[1][4] = __ffma2_rn(K.v[23], v[2][2], yh[1][4]);
+    yh[1][5] = __fmul2_rn(K.v[24], v[0][6]);
+    yh[1][5] = __ffma2_rn(K.v[25], v[1][5], yh[1][5]);
+    yh[1][5] = __ffma2_rn(K.v[26], v[2][3], yh[1][5]);
+    yh[1][6] = __fmul2_rn(K.v[27], v[0][5]);
+    yh[1][6] = __ffma2_rn(K.v[28], v[1][6], yh[1][6]);
+    yh[1][7] = __fmul2_rn(K.v[29], v[1][7]);
+    yh[2][1] = __fmul2_rn(K.v[30], v[0][4]);
+    yh[2][1] = __ffma2_rn(K.v[31], v[2][1], yh[2][1]);
+    yh[2][2] = __fmul2_rn(K.v[32], v[1][4]);
+    yh[2][2] = __ffma2_rn(K.v[33], v[2][2], yh[2][2]);
+    yh[2][3] = __fmul2_rn(K.v[34], v[0][6]);
+    yh[2][3] = __ffma2_rn(K.v[35], v[1][5], yh[2][3]);
+    yh[2][3] = __ffma2_rn(K.v[36], v[2][3], yh[2][3]);
+    yh[2][4] = __fmul2_rn(K.v[37], v[0][1]);
+    yh[2][4] = __ffma2_rn(K.v[38], v[1][2], yh[2][4]);
+    yh[2][4] = __ffma2_rn(K.v[39], v[2][4], yh[2][4]);
+    yh[2][5] = __fmul2_rn(K.v[40], v[1][3]);
+    yh[2][5] = __ffma2_rn(K.v[41], v[2][5], yh[2][5]);
+    yh[2][6] = __fmul2_rn(K.v[42], v[0][3]);
+    yh[2][6] = __ffma2_rn(K.v[43], v[2][6], yh[2][6]);
+    yh[2][7] = __fmul2_rn(K.v[44], v[2][7]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+#pragma unroll
+        for (int m = 1; m < 8; m++) yh[c][m] = __fmul2_rn(yh[c][m], e);
+        yh[c][0] = make_float2(0.0f, 0.0f);  // mode 0 is zero
+#pragma unroll
+        for (int t = 1; t < 8; t <<= 1)
+#pragma unroll
+            for (int b = 0; b < 8; b++)
+                if (!(b & t)) {
+                    const float2 a = yh[c][b], bb = yh[c][b | t];
+                    yh[c][b] = __ffma2_rn(bb, m1, a);  // a - bb
+                    yh[c][b | t] = __fadd2_rn(a, bb);
+                }
+#pragma unroll
+        for (int b = 0; b < 8; b++) v[c][b] = yh[c][b];
+    }
+}
 #endif
 
 }  // namespace mg

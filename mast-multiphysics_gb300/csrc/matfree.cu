@@ -606,196 +606,255 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
 // ------------------------------------------------- factored CUDA-core operator
 // y = sum_e E_e P_e^T K0 P_e x in FP32 on the CUDA cores with the factored
 // element stiffness (hex8_factored.cuh: 2 x 72 butterfly additions + 45 FMA per
-// element instead of 576 FMA).  A tile owns kFNX x kFNY nodes in x, y and
-// P.fac_z node planes in z and streams through its element planes: one thread
-// per element of the (kFNX + 1) x (kFNY + 1) element plane around the owned
-// nodes (the halo elements are recomputed by the neighbouring tiles).  Per
-// element plane: the thread gathers its 24 corner values from the two node
-// planes in shared memory, applies the factored stiffness scaled by E_e and
-// stores the corner results; after one barrier each owned node sums the four
-// bottom-corner results of this element plane onto the four top-corner results
-// of the previous one (kept in registers), in a fixed order (deterministic,
-// atomic-free).  The next node plane is prefetched into registers while the
-// current plane is computed; corner results are double-buffered, so one
-// barrier per element plane suffices.
-constexpr int kFEX = 32, kFEY = 8;                 // elements per tile plane
+// element instead of 576 FMA), two elements per thread in packed FP32x2
+// arithmetic.  A tile owns kFNX x kFNY nodes in x, y and P.fac_z node planes
+// in z and streams through its element planes.  Warp w holds element rows 2w
+// and 2w+1 of the kFEX x kFEY element plane around the owned nodes (lane = x;
+// halo elements are recomputed by the neighbouring tiles).  The node planes
+// (input, D^-1 and the per-mode node vectors) and the moduli plane arrive by
+// TMA two planes ahead into a four-slot ring.  Per element plane: gather the
+// corner values from the two node planes, apply the factored stiffness scaled
+// by E_e, then sum the corner results into the owned nodes: along x with a warp
+// shuffle (left element + right element), along y inside the thread (rows 2w,
+// 2w+1) or through shared memory (row 2w+1 with the next warp's row 2w+2),
+// along z through registers (the top corners of plane z-1 + the bottom corners
+// of plane z).  Every node's sum has the same fixed order (deterministic and
+// independent of the tiling).
+constexpr int kFEX = 32, kFEY = 16;                // elements per tile plane
 constexpr int kFNX = kFEX - 1, kFNY = kFEY - 1;    // owned nodes per tile plane
 constexpr int kFPX = kFEX + 1, kFPY = kFEY + 1;    // tile node plane (with halo)
-constexpr int kFThreads = kFEX * kFEY;             // 256
-constexpr int kFPlane = kFPX * kFPY * 3;           // 891 floats
-constexpr int kFPlaneLd = (kFPlane + kFThreads - 1) / kFThreads;  // 4
+constexpr int kFThreads = 256;                     // 8 warps x 2 element rows
 constexpr int kFMinZ = 4, kFMaxZ = 32;
-constexpr int kFRing = 4;                          // node / modulus planes in flight
-constexpr int kFPlaneSlot = (kFPlane + 3) / 4 * 4;                 // 892
-constexpr int kFSmem = (kFRing * (kFPlaneSlot + kFThreads) + 2 * 24 * kFThreads) * 4;  // 67,456 B
+constexpr int kFRing = 4;                          // 2 planes read, 2 in flight
+constexpr int kFBoxX = 104;                        // TMA node box: 104 floats (3 kFPX + alignment) x kFPY rows
+constexpr int kFPlaneF = 1792;                     // floats per node plane in the ring (7168 B, 128 B aligned)
+constexpr int kFBoxE = 36;                         // TMA moduli box: 36 elements x kFEY rows
+constexpr int kFModF = kFBoxE * kFEY;              // 576 floats
+constexpr int kFXch = 6 * kFThreads;               // row exchange: 6 floats per thread
+static_assert(kFBoxX * kFPY <= kFPlaneF && kFBoxX >= 3 + 3 * kFPX && kFBoxE >= 3 + kFEX, "boxes");
+static_assert(kFThreads == 32 * (kFEY / 2) && kFEX == 32, "warp = element row pair, lane = x");
+// tensor maps per problem for this kernel: node vectors with the 104 x 17 x 1 box
+// and the moduli with the 36 x 16 x 1 box
+enum FacMap { kFMapMx = 0, kFMapMd, kFMapMy, kFMapMb, kFMapR, kFMapDinv, kFMapMr, kFMapE, kFacMaps };
+// node planes per ring slot: the input, D^-1 and (MODE 2 rhs, MODE 4 r, MODE 5 the iterate)
+__host__ __device__ constexpr int fac_planes(int mode) { return mode == 3 ? 2 : 3; }
+__host__ __device__ constexpr int fac_slot(int mode) { return fac_planes(mode) * kFPlaneF + kFModF; }
+__host__ __device__ constexpr int fac_smem(int mode) { return (kFRing * fac_slot(mode) + 2 * kFXch) * 4 + 128; }
+// MODE 3: 77,696 B; MODE 2, 4, 5: 106,368 B: two CTAs per SM
 
-// 4-byte asynchronous global -> shared copy; src_bytes = 0 fills zero (no read)
-__device__ __forceinline__ void cp_async4(float *dst, const float *src, int src_bytes) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
-                 "r"(src_bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
+struct FacArgs {
+    int in_map, b_map;  // tensor maps (FacMap) of the input and of the third node plane
+    float *y;           // MODE 2, 3: output; MODE 4, 5: the new direction
+    float *r, *xs;      // MODE 4, 5: Chebyshev residual and iterate
+    float c1, c2, inv_theta;
+    int x0_zero;        // MODE 5: the iterate starts at 0 (its plane is not loaded)
+};
 
 // MODE 2: y = rhs - A x.  MODE 3: y = A x.  (Both 0 where dinv = 0.)
 // MODE 4: one Chebyshev step on direction x = d: r -= A d; y = d' = c1 d +
-//         c2 D^-1 r; xs += d' (the sequence of mg_cheb_next_kernel, fused).
+//         c2 D^-1 r; xs += d' (mg_cheb_next_kernel's sequence, fused).
+// MODE 5: the first two Chebyshev steps on rhs x = b: d = D^-1 b / theta,
+//         xs (+)= d, r = b - A d, y = d' = c1 d + c2 D^-1 r, xs += d'
+//         (mg_cheb_first_kernel's and mg_cheb_next_kernel's sequence, fused).
+// A TMA wait that exceeds its bound sets bit 4 of *err and ends the block.
 template <int MODE>
-__global__ void __launch_bounds__(kFThreads, 3) mf_fac_kernel(
+__global__ void __launch_bounds__(kFThreads, 2) mf_fac_kernel(
     const MfProblem *__restrict__ probs, const MfCol *__restrict__ tiles, int t_lo, int t_hi, int sel,
-    const FacK<float> K, const float *__restrict__ x, const float *__restrict__ rhs,
-    const float *__restrict__ E32, const float *__restrict__ dinv, float *__restrict__ y,
-    const MfState *__restrict__ states, float *__restrict__ r, float *__restrict__ xs, float c1, float c2) {
-    extern __shared__ __align__(16) float fsm[];
-    float(*sN)[kFPlaneSlot] = reinterpret_cast<float(*)[kFPlaneSlot]>(fsm);            // node planes
-    float(*sE)[kFThreads] = reinterpret_cast<float(*)[kFThreads]>(fsm + kFRing * kFPlaneSlot);  // moduli
-    // corner results [buffer][(corner b) * 3 + c][element]
-    float(*sY)[24][kFThreads] =
-        reinterpret_cast<float(*)[24][kFThreads]>(fsm + kFRing * (kFPlaneSlot + kFThreads));
-    const int tid = threadIdx.x, tx = tid & (kFEX - 1), ty = tid / kFEX;
-    for (int ti = t_lo + blockIdx.x; ti < t_hi; ti += gridDim.x) {
+    const FacK2 K, const CUtensorMap *__restrict__ fmaps, const MfState *__restrict__ states, const FacArgs A,
+    int *err) {
+    extern __shared__ __align__(128) float fsm[];
+    __shared__ __align__(8) uint64_t bars[kFRing];
+    constexpr int NP = fac_planes(MODE);
+    // slot k: [input plane | D^-1 plane | third plane (NP = 3) | moduli]
+    auto plane_of = [&](int slot, int part) { return fsm + slot * fac_slot(MODE) + part * kFPlaneF; };
+    auto mod_of = [&](int slot) { return fsm + slot * fac_slot(MODE) + NP * kFPlaneF; };
+    float(*sX)[6][kFThreads] = reinterpret_cast<float(*)[6][kFThreads]>(fsm + kFRing * fac_slot(MODE));
+    const int tid = threadIdx.x, tx = tid & 31, w = tid >> 5;
+    const uint32_t bar0 = smem_u32(&bars[0]);
+    if (tid == 0)
+        for (int k = 0; k < kFRing; k++) mbar_init(bar0 + 8 * k, 1);
+    __syncthreads();
+    uint32_t phase = 0;   // bit k: parity of slot k's next completion
+    uint32_t issued = 0;  // bit k: a load into slot k is outstanding (thread 0)
+    bool failed = false;
+    const bool third = MODE == 2 || MODE == 4 || (MODE == 5 && !A.x0_zero);
+    for (int ti = t_lo + blockIdx.x; ti < t_hi && !failed; ti += gridDim.x) {
         const MfCol T = tiles[ti];
         const MfProblem P = probs[T.prob];
         if (states[P.root].done || P.bottom || (sel >= 0 && sel != (P.coarse < 0 ? 1 : 0))) continue;
         const int x0 = T.cx * kFNX, y0 = T.cy * kFNY, z0 = T.cz * P.fac_z;
         const int z1 = min(z0 + P.fac_z, P.NZ);
         const int S = z1 - z0 + 1;  // element planes z0-1 .. z1-1; node planes z0-1 .. z1
-        const float *xp = x + P.dof_off;
+        // 16-byte aligned box starts and the offsets of the tile inside the boxes
+        const int xs = (3 * (x0 - 1)) & ~3, ox = 3 * (x0 - 1) - xs;
+        const int xe = (x0 - 1) & ~3, oe = (x0 - 1) - xe;
+        const CUtensorMap *maps = fmaps + (size_t)T.prob * kFacMaps;
         const int64_t plane_stride = (int64_t)P.NY * P.pitch;
-        // this thread's part of a tile node plane: row py holds 3 kFPX floats from
-        // node x0-1; off < 0 marks a position outside the grid
-        int off[kFPlaneLd];
-#pragma unroll
-        for (int k = 0; k < kFPlaneLd; k++) {
-            const int i = tid + k * kFThreads;
-            const int py = i / (3 * kFPX), o = i - py * 3 * kFPX;
-            const int gy = y0 - 1 + py, gxc = 3 * (x0 - 1) + o;
-            off[k] = (i < kFPlane && gy >= 0 && gy < P.NY && gxc >= 0 && gxc < 3 * P.NX) ? gy * P.pitch + gxc : -1;
-        }
-        const int gex = x0 - 1 + tx, gey = y0 - 1 + ty;
-        const bool ex_in = gex >= 0 && gex < P.nx && gey >= 0 && gey < P.ny;
-        const float *Ep = E32 + P.elem_off + (ex_in ? (int64_t)gey * P.pitch_e + gex : 0);
-        // node plane p (nz = z0 - 1 + p) and element plane p's moduli into ring slot p % kFRing
+        const uint32_t bytes = (uint32_t)(((third ? 3 : 2) * kFBoxX * kFPY + kFModF) * 4);
+        // node planes p (nz = z0 - 1 + p) and element plane p's moduli into slot p % kFRing
         auto issue = [&](int p) {
-            const int nz = z0 - 1 + p, slot = p % kFRing;
-            const bool zin = nz >= 0 && nz < P.NZ;
-#pragma unroll
-            for (int k = 0; k < kFPlaneLd; k++) {
-                const int i = tid + k * kFThreads;
-                if (i < kFPlane) {
-                    const bool v = zin && off[k] >= 0;
-                    cp_async4(&sN[slot][i], v ? xp + nz * plane_stride + off[k] : xp, v ? 4 : 0);
-                }
-            }
-            const bool ev = ex_in && nz >= 0 && nz < P.nz && p < S;
-            cp_async4(&sE[slot][tid], ev ? Ep + (int64_t)nz * P.ny * P.pitch_e : E32, ev ? 4 : 0);
-            cp_async_commit();
+            const int slot = p % kFRing;
+            const uint32_t bar = bar0 + 8 * slot;
+            fence_async_smem();
+            mbar_expect_tx(bar, bytes);
+            tma_load_3d(smem_u32(plane_of(slot, 0)), maps + A.in_map, xs, y0 - 1, z0 - 1 + p, bar);
+            tma_load_3d(smem_u32(plane_of(slot, 1)), maps + kFMapDinv, xs, y0 - 1, z0 - 1 + p, bar);
+            if (third) tma_load_3d(smem_u32(plane_of(slot, 2)), maps + A.b_map, xs, y0 - 1, z0 - 1 + p, bar);
+            tma_load_3d(smem_u32(mod_of(slot)), maps + kFMapE, xe, y0 - 1, z0 - 1 + p, bar);
         };
-        const int gx = x0 + tx, gy = y0 + ty;
-        const bool owner = tx < kFNX && ty < kFNY && gx < P.NX && gy < P.NY;
-        __syncthreads();  // the previous tile's readers of sN, sE and sY are done
-        issue(0);
-        issue(1);
-        issue(2);
-        cp_async_wait<1>();  // planes 0 and 1
-        __syncthreads();
-        float pt0 = 0.0f, pt1 = 0.0f, pt2 = 0.0f;  // top-corner sums of the previous element plane
-        // node-phase inputs of node plane s (owned planes z0 .. z1-1), one step ahead
-        // (MODE 2: b = rhs; MODE 4: b = r and w = xs)
-        float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, w0 = 0.0f, w1 = 0.0f, w2 = 0.0f;
-        int64_t gd = P.dof_off + ((int64_t)(z0 - 1) * P.NY + gy) * P.pitch + 3 * gx;
+        // every thread waits for slot p's loads; false after the bound
+        auto arrive = [&](int p) {
+            const int slot = p % kFRing;
+            const bool ok = mbar_wait_bounded(bar0 + 8 * slot, (phase >> slot) & 1u);
+            phase ^= 1u << slot;
+            if (tid == 0) issued &= ~(1u << slot);
+            return ok;
+        };
+        // owned nodes: x = x0 + tx; rows y0 + 2w (row 2w+1 of the tile plane) and
+        // y0 + 2w + 1 (row 2w+2, warps 0..6)
+        const int gx = x0 + tx, gy1 = y0 + 2 * w, gy2 = gy1 + 1;
+        const bool own1 = tx < kFNX && gx < P.NX && gy1 < P.NY;
+        const bool own2 = tx < kFNX && w < kFEY / 2 - 1 && gx < P.NX && gy2 < P.NY;
+        __syncthreads();  // the previous tile's readers of the ring and the exchange are done
+        if (tid == 0) {
+            for (int p = 0; p < 3 && p <= S; p++) {
+                issue(p);
+                issued |= 1u << (p % kFRing);
+            }
+        }
+        bool ok = arrive(0);
+        ok = arrive(1) && ok;
+        float pt[2][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};  // top-corner sums of the previous plane
+        int64_t g1 = P.dof_off + ((int64_t)(z0 - 1) * P.NY + gy1) * P.pitch + 3 * gx;
         for (int s = 0; s < S; s++) {
-            const int ez = z0 - 1 + s;
-            // plane s + 3 into the slot of plane s - 1 (read in step s - 1, before its barrier)
-            if (s + 3 <= S) issue(s + 3);
-            else cp_async_commit();  // keep one group per step
-            float nd0 = 0.0f, nd1 = 0.0f, nd2 = 0.0f, nb0 = 0.0f, nb1 = 0.0f, nb2 = 0.0f;
-            float nw0 = 0.0f, nw1 = 0.0f, nw2 = 0.0f;
-            if (s + 1 < S && owner) {
-                const int64_t g1 = gd + plane_stride;
-                nd0 = dinv[g1]; nd1 = dinv[g1 + 1]; nd2 = dinv[g1 + 2];
-                if (MODE == 2) { nb0 = rhs[g1]; nb1 = rhs[g1 + 1]; nb2 = rhs[g1 + 2]; }
-                if (MODE == 4) {
-                    nb0 = r[g1]; nb1 = r[g1 + 1]; nb2 = r[g1 + 2];
-                    nw0 = xs[g1]; nw1 = xs[g1 + 1]; nw2 = xs[g1 + 2];
-                }
+            // plane s + 3 into the slot of plane s - 1, whose readers (the element phases
+            // of steps s - 2, s - 1 and the node-phase reads of step s - 1) are behind
+            // the barrier of step s - 1
+            if (tid == 0 && s + 3 <= S) {
+                issue(s + 3);
+                issued |= 1u << ((s + 3) % kFRing);
             }
-            // MODE 4: the direction at this thread's node (node plane s), read before
-            // the barrier (its ring slot is refilled in the next step)
-            float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f;
-            if (MODE == 4 && owner) {
-                const float *un = sN[s % kFRing] + ((ty + 1) * kFPX + tx + 1) * 3;
-                u0 = un[0]; u1 = un[1]; u2 = un[2];
-            }
-            // element phase
+            // element phase: corner values of the element pair, packed (A in .x, B in .y)
+            float2 v[3][8];
             {
-                float v[3][8];
-                const float *n0 = sN[s % kFRing], *n1 = sN[(s + 1) % kFRing];
+                const float *n0 = plane_of(s % kFRing, 0) + ox, *n1 = plane_of((s + 1) % kFRing, 0) + ox;
+                const float *m0 = plane_of(s % kFRing, 1) + ox, *m1 = plane_of((s + 1) % kFRing, 1) + ox;
+                float nv[2][3][2][3];  // [bz][row 2w + 0..2][bx][c]
+#pragma unroll
+                for (int bz = 0; bz < 2; bz++)
+#pragma unroll
+                    for (int r3 = 0; r3 < 3; r3++)
+#pragma unroll
+                        for (int bx = 0; bx < 2; bx++) {
+                            const int o = (2 * w + r3) * kFBoxX + 3 * (tx + bx);
+#pragma unroll
+                            for (int c = 0; c < 3; c++) {
+                                float val = (bz ? n1 : n0)[o + c];
+                                if (MODE == 5) val = (bz ? m1 : m0)[o + c] * val * A.inv_theta;
+                                nv[bz][r3][bx][c] = val;
+                            }
+                        }
 #pragma unroll
                 for (int b = 0; b < 8; b++) {
                     const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
-                    const float *src = (bz ? n1 : n0) + ((ty + by) * kFPX + tx + bx) * 3;
-                    v[0][b] = src[0]; v[1][b] = src[1]; v[2][b] = src[2];
-                }
-                const float e = sE[s % kFRing][tid];
-                if (e != 0.0f) {
-                    hex8_factored_apply(K, e, v);
-                } else {
 #pragma unroll
-                    for (int b = 0; b < 8; b++) { v[0][b] = 0.0f; v[1][b] = 0.0f; v[2][b] = 0.0f; }
-                }
-                float(*Y)[kFThreads] = sY[s & 1];
-#pragma unroll
-                for (int b = 0; b < 8; b++) {
-                    Y[b * 3][tid] = v[0][b];
-                    Y[b * 3 + 1][tid] = v[1][b];
-                    Y[b * 3 + 2][tid] = v[2][b];
+                    for (int c = 0; c < 3; c++) v[c][b] = make_float2(nv[bz][by][bx][c], nv[bz][by + 1][bx][c]);
                 }
             }
-            cp_async_wait<1>();  // plane s + 2 (the next step's top plane) has landed
-            __syncthreads();
-            // node phase: node (gx, gy, ez) is corner (dx, dy) of elements
-            // (tx + 1 - dx, ty + 1 - dy) of this plane (bottom) and of the previous (top)
-            if (owner) {
-                const float(*Y)[kFThreads] = sY[s & 1];
-                float a0 = pt0, a1 = pt1, a2 = pt2, t0 = 0.0f, t1 = 0.0f, t2 = 0.0f;
+            const float *Es = mod_of(s % kFRing) + oe + tx;
+            const float2 e2 = make_float2(Es[2 * w * kFBoxE], Es[(2 * w + 1) * kFBoxE]);
+            hex8_factored_apply2(K, e2, v);  // E = 0 (outside the grid) gives exact zeros
+            // along x: node x0 + tx = corner dx = 1 of this lane's element + dx = 0 of the next lane's
+            float2 xsum[3][2][2];  // [c][by][bz]
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int dx = q & 1, dy = q >> 1;
-                    const int el = (ty + 1 - dy) * kFEX + tx + 1 - dx;
-                    a0 += Y[q * 3][el]; a1 += Y[q * 3 + 1][el]; a2 += Y[q * 3 + 2][el];
-                    t0 += Y[(q + 4) * 3][el]; t1 += Y[(q + 4) * 3 + 1][el]; t2 += Y[(q + 4) * 3 + 2][el];
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int by = 0; by < 2; by++)
+#pragma unroll
+                    for (int bz = 0; bz < 2; bz++) {
+                        const float2 lo = v[c][2 * by + 4 * bz], hi = v[c][1 + 2 * by + 4 * bz];
+                        float2 nb;
+                        nb.x = __shfl_down_sync(0xffffffffu, lo.x, 1);
+                        nb.y = __shfl_down_sync(0xffffffffu, lo.y, 1);
+                        xsum[c][by][bz] = __fadd2_rn(hi, nb);
+                    }
+            // along y: row 2w of this warp (element 2w at by = 0) goes to the warp above
+            float(*X)[kFThreads] = sX[s & 1];
+#pragma unroll
+            for (int bz = 0; bz < 2; bz++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) X[bz * 3 + c][tid] = xsum[c][0][bz].x;
+            // node-phase inputs at the owned nodes of node plane s (its slot is refilled
+            // in the next step): the input in un, D^-1 in dv, the third plane in bv
+            float un[2][3], dv[2][3], bv[2][3];
+#pragma unroll
+            for (int rr = 0; rr < 2; rr++) {
+                const int o = ox + (2 * w + 1 + rr) * kFBoxX + 3 * (tx + 1);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    un[rr][c] = plane_of(s % kFRing, 0)[o + c];
+                    dv[rr][c] = plane_of(s % kFRing, 1)[o + c];
+                    bv[rr][c] = third ? plane_of(s % kFRing, 2)[o + c] : 0.0f;
                 }
-                if (s >= 1) {
-                    if (MODE == 2) {
-                        y[gd] = d0 == 0.0f ? 0.0f : b0 - a0;
-                        y[gd + 1] = d1 == 0.0f ? 0.0f : b1 - a1;
-                        y[gd + 2] = d2 == 0.0f ? 0.0f : b2 - a2;
-                    } else if (MODE == 4) {
-                        const float r0 = b0 - (d0 == 0.0f ? 0.0f : a0), r1 = b1 - (d1 == 0.0f ? 0.0f : a1),
-                                    r2 = b2 - (d2 == 0.0f ? 0.0f : a2);
-                        const float e0 = fmaf(c1, u0, c2 * d0 * r0), e1 = fmaf(c1, u1, c2 * d1 * r1),
-                                    e2 = fmaf(c1, u2, c2 * d2 * r2);
-                        r[gd] = r0; r[gd + 1] = r1; r[gd + 2] = r2;
-                        y[gd] = e0; y[gd + 1] = e1; y[gd + 2] = e2;
-                        xs[gd] = w0 + e0; xs[gd + 1] = w1 + e1; xs[gd + 2] = w2 + e2;
-                    } else {
-                        y[gd] = d0 == 0.0f ? 0.0f : a0;
-                        y[gd + 1] = d1 == 0.0f ? 0.0f : a1;
-                        y[gd + 2] = d2 == 0.0f ? 0.0f : a2;
+            }
+            // the next step's top plane (s + 2) has landed
+            bool sok = true;
+            if (s + 2 <= S) sok = arrive(s + 2);
+            if (__syncthreads_or(!(sok && ok))) {
+                failed = true;
+                if (tid == 0) atomicOr(err, 4);
+                break;
+            }
+            float nn[2][2][3];  // [row][bz][c]; node plane z0 - 1 + s gets its bottom-corner sums now
+#pragma unroll
+            for (int bz = 0; bz < 2; bz++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    nn[0][bz][c] = xsum[c][1][bz].x + xsum[c][0][bz].y;  // element 2w (by = 1) + 2w+1 (by = 0)
+                    nn[1][bz][c] = xsum[c][1][bz].y + (w < kFEY / 2 - 1 ? X[bz * 3 + c][tid + 32] : 0.0f);
+                }
+#pragma unroll
+            for (int rr = 0; rr < 2; rr++) {
+                const bool own = rr ? own2 : own1;
+                if (own && s >= 1) {
+                    const int64_t g = g1 + (rr ? P.pitch : 0);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float a = pt[rr][c] + nn[rr][0][c];
+                        if (MODE == 2) {
+                            A.y[g + c] = dv[rr][c] == 0.0f ? 0.0f : bv[rr][c] - a;
+                        } else if (MODE == 3) {
+                            A.y[g + c] = dv[rr][c] == 0.0f ? 0.0f : a;
+                        } else if (MODE == 4) {
+                            const float rv = bv[rr][c] - (dv[rr][c] == 0.0f ? 0.0f : a);
+                            const float dn2 = fmaf(A.c1, un[rr][c], A.c2 * dv[rr][c] * rv);
+                            A.r[g + c] = rv;
+                            A.y[g + c] = dn2;
+                            A.xs[g + c] += dn2;
+                        } else {
+                            // d = D^-1 b / theta at the node, its iterate, residual and next direction
+                            const float dd = dv[rr][c], bb = un[rr][c];
+                            const float d0 = dd * bb * A.inv_theta;
+                            const float xv = A.x0_zero ? d0 : bv[rr][c] + d0;
+                            const float rv = bb - (dd == 0.0f ? 0.0f : a);
+                            const float dn2 = fmaf(A.c1, d0, A.c2 * dd * rv);
+                            A.r[g + c] = rv;
+                            A.y[g + c] = dn2;
+                            A.xs[g + c] = xv + dn2;
+                        }
                     }
                 }
-                pt0 = t0; pt1 = t1; pt2 = t2;
+#pragma unroll
+                for (int c = 0; c < 3; c++) pt[rr][c] = nn[rr][1][c];
             }
-            d0 = nd0; d1 = nd1; d2 = nd2; b0 = nb0; b1 = nb1; b2 = nb2; w0 = nw0; w1 = nw1; w2 = nw2;
-            gd += plane_stride;
+            g1 += plane_stride;
         }
-        cp_async_wait<0>();
     }
+    // after a failed wait, give the outstanding loads a bounded chance to land
+    if (failed && tid == 0)
+        for (int k = 0; k < kFRing; k++)
+            if (issued & (1u << k)) (void)mbar_wait_bounded(bar0 + 8 * k, (phase >> k) & 1u);
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------- vector phase
@@ -1729,16 +1788,32 @@ void launch_apply_prec(MfBatch &b, int prec, const ApplyArgs &a) {
 // level operator of the multigrid (MODE 2: y = rhs - A x, MODE 3: y = A x) on
 // level l: the factored CUDA-core operator (fac) or the tensor-core column
 // operator in precision prec (x is the vector of map in_slot there)
+// the factored kernel's tensor map of a batch vector
+int fac_map_of(const MfBatch &b, const float *v) {
+    if (v == b.mx) return kFMapMx;
+    if (v == b.md) return kFMapMd;
+    if (v == b.my) return kFMapMy;
+    if (v == b.mb) return kFMapMb;
+    if (v == b.r) return kFMapR;
+    if (v == b.mr) return kFMapMr;
+    return -1;
+}
+
+template <int MODE>
+void launch_fac(MfBatch &b, int lo, int hi, int sel, const FacArgs &a) {
+    if (hi <= lo || a.in_map < 0) return;
+    const int grid = std::max(1, std::min(hi - lo, b.fac_grid));
+    mf_fac_kernel<MODE><<<grid, kFThreads, fac_smem(MODE), b.stream>>>(b.probs, b.fac_tiles, lo, hi, sel, b.fac2,
+                                                                      b.fac_maps, b.states, a, b.err);
+}
+
 template <int MODE>
 void launch_level_op(MfBatch &b, bool fac, int prec, int l, int in_slot, const float *x, const float *rhs,
                      float *y, int sel) {
     if (fac) {
-        const int lo = b.lvl_fac_lo[l], hi = b.lvl_fac_hi[l];
-        if (hi <= lo) return;
-        const int grid = std::max(1, std::min(hi - lo, b.fac_grid));
-        mf_fac_kernel<MODE><<<grid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, lo, hi, sel, b.fac32, x, rhs,
-                                                              b.E32, b.dinv, y, b.states, nullptr, nullptr,
-                                                              0.0f, 0.0f);
+        launch_fac<MODE>(b, b.lvl_fac_lo[l], b.lvl_fac_hi[l], sel,
+                         FacArgs{fac_map_of(b, x), rhs ? fac_map_of(b, rhs) : -1, y, nullptr, nullptr, 0.0f, 0.0f,
+                                 0.0f, 0});
     } else {
         ApplyArgs a{b.lvl_col_lo[l], b.lvl_col_hi[l], in_slot, 0, rhs, y, sel};
         launch_apply_prec<MODE>(b, prec, a);
@@ -1772,9 +1847,10 @@ int configure_kernels() {
     MG_TRY(set_apply_attrs<MG_MIXED_BF16X3>());
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_residual64_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kResidSmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
-    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, fac_smem(2)));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, fac_smem(3)));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, fac_smem(4)));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, fac_smem(5)));
     MG_CUDA_TRY(cudaFuncSetAttribute(mg_bottom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kBottomSmemMax));
     done = true;
@@ -2007,10 +2083,11 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
                 for (int i = 0; i < cx; i++)
                     b.h_cols.push_back(MfCol{(int)pi, (int16_t)i, (int16_t)j, (int16_t)k, 0});
         // tiles of the factored operator: kFNX x kFNY owned nodes, fac_z node
-        // planes (kFMinZ .. kFMaxZ, sized for about three tiles per SM slot)
+        // planes (kFMinZ .. kFMaxZ): as deep as one wave of resident tiles allows
         {
             const int tx = (P.NX + kFNX - 1) / kFNX, ty = (P.NY + kFNY - 1) / kFNY;
-            P.fac_z = (int)std::min<int64_t>(kFMaxZ, std::max<int64_t>(kFMinZ, (P.NZ * (int64_t)tx * ty + slots - 1) / slots));
+            const int64_t fac_slots = 2 * (int64_t)sms, per_col = std::max<int64_t>(1, fac_slots / (tx * ty));
+            P.fac_z = (int)std::min<int64_t>(kFMaxZ, std::max<int64_t>(kFMinZ, (P.NZ + per_col - 1) / per_col));
             const int tz = (P.NZ + P.fac_z - 1) / P.fac_z;
             P.fac_begin = (int)b.h_fac_tiles.size();
             P.fac_count = tx * ty * tz;
@@ -2078,7 +2155,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     }
     b.apply_grid = std::max(1, std::min(nb, 2 * sms));  // FP64 residual: two CTAs per SM
     b.col_grid = std::max(1, std::min(b.n_cols, 3 * sms));  // three column CTAs per SM
-    b.fac_grid = 3 * sms;                                     // three factored-operator CTAs per SM
+    b.fac_grid = 2 * sms;                                     // two factored-operator CTAs per SM
     b.vec_grid = std::max(1, std::min(nc, 8 * sms));
     MG_TRY(dev_alloc_n(&b.probs, b.h_probs.size()));
     MG_TRY(dev_alloc_n(&b.bricks, b.h_bricks.size()));
@@ -2089,6 +2166,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.chunks, b.h_chunks.size()));
     MG_TRY(dev_alloc_n(&b.states, (size_t)b.n_probs));
     MG_TRY(dev_alloc_n(&b.tmaps, (size_t)b.n_probs * kMapsPerProblem));
+    MG_TRY(dev_alloc_n(&b.fac_maps, (size_t)b.n_probs * kFacMaps));
     MG_CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&b.states_host), b.n_probs * sizeof(MfState)));
     MG_TRY(dev_alloc_n(&b.E32, (size_t)el + 4));
     MG_TRY(dev_alloc_n(&b.E64, (size_t)el + 4));
@@ -2109,6 +2187,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     double K0[576];
     hex8_box_stiffness(hx, hy, hz, nu, K0);
     if (!hex8_factored_build(K0, b.fac64, b.fac32)) return MG_EINVAL;
+    for (int k = 0; k < kFacN; k++) b.fac2.v[k] = make_float2(b.fac32.v[k], b.fac32.v[k]);
     // Gershgorin bound of D^-1 A: every assembled row is a positive combination
     // of K0 rows, so max_i sum_j |K0_ij| / K0_ii bounds it on every level
     b.cheb_lmax = 0.0;
@@ -2131,8 +2210,20 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         MG_TRY(make_map(enc, &maps[pi * kMapsPerProblem + 3], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
                         (uint64_t)P.pitch_e * 4, (uint64_t)P.pitch_e * P.ny * 4, 12, 16, 1));
     }
+    // factored level operator: node planes {104 floats, 17 rows}, moduli planes {36, 16}
+    std::vector<CUtensorMap> fmaps((size_t)b.n_probs * kFacMaps);
+    for (int pi = 0; pi < b.n_probs; pi++) {
+        const MfProblem &P = b.h_probs[pi];
+        float *vecs[kFMapE] = {b.mx, b.md, b.my, b.mb, b.r, b.dinv, b.mr};
+        for (int k = 0; k < kFMapE; k++)
+            MG_TRY(make_map(enc, &fmaps[(size_t)pi * kFacMaps + k], vecs[k] + P.dof_off, 3 * (uint64_t)P.NX, P.NY,
+                            P.NZ, (uint64_t)P.pitch * 4, (uint64_t)P.pitch * P.NY * 4, kFBoxX, kFPY, 1));
+        MG_TRY(make_map(enc, &fmaps[(size_t)pi * kFacMaps + kFMapE], b.E32 + P.elem_off, P.nx, P.ny, P.nz,
+                        (uint64_t)P.pitch_e * 4, (uint64_t)P.pitch_e * P.ny * 4, kFBoxE, kFEY, 1));
+    }
     cudaStream_t s = b.stream;
     MG_CUDA_TRY(cudaMemcpyAsync(b.tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.fac_maps, fmaps.data(), fmaps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.probs, b.h_probs.data(), b.h_probs.size() * sizeof(MfProblem), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.bricks, b.h_bricks.data(), b.h_bricks.size() * sizeof(MfBrick), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.cols, b.h_cols.data(), b.h_cols.size() * sizeof(MfCol), cudaMemcpyHostToDevice, s));
@@ -2171,7 +2262,7 @@ void mf_batch_free(MfBatch &b) {
     void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.K0, b.mb, b.mx, b.md,
-                    b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles};
+                    b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles, b.fac_maps};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
     b = MfBatch();
@@ -2258,10 +2349,8 @@ int mf_apply(MfBatch &b, int precision, const double *x_host, double *y_host, in
     MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
     if (precision == MG_OPERATOR_FACTORED_FP32) {
         const int grid = std::max(1, std::min(P.fac_count, b.fac_grid));
-        mf_fac_kernel<3><<<grid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, P.fac_begin,
-                                                               P.fac_begin + P.fac_count, -1, b.fac32, b.mx,
-                                                               nullptr, b.E32, b.dinv, b.my, b.states,
-                                                               nullptr, nullptr, 0.0f, 0.0f);
+        launch_fac<3>(b, P.fac_begin, P.fac_begin + P.fac_count, -1,
+                      FacArgs{kFMapMx, -1, b.my, nullptr, nullptr, 0.0f, 0.0f, 0.0f, 0});
     } else {
         ApplyArgs a{P.col_begin, P.col_begin + P.col_count, 4, 0, nullptr, b.my};
         launch_apply_prec<3>(b, precision, a);
@@ -2331,23 +2420,25 @@ long long enqueue_smooth(MfBatch &b, bool fac, int prec, int l, const float *rin
                          const Cheb &cc, int sel) {
     const int clo = b.lvl_chunk_lo[l], chi = b.lvl_chunk_hi[l];
     const int grid = std::max(1, std::min(chi - clo, b.vec_grid));
-    mg_cheb_first_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, rin,
-                                                          b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero, sel);
-    long long n = 1;
-    if (fac) {
-        // fused Chebyshev steps; the direction alternates between md and my
+    if (fac && deg >= 2) {
+        // fused: the first two steps in one launch (direction into md, which is
+        // never rin), then one launch per step, the direction alternating md / my
         const int lo = b.lvl_fac_lo[l], hi = b.lvl_fac_hi[l];
-        const int fgrid = std::max(1, std::min(hi - lo, b.fac_grid));
+        launch_fac<5>(b, lo, hi, sel,
+                      FacArgs{fac_map_of(b, rin), kFMapMx, b.md, b.mr, b.mx, cc.c1[1], cc.c2[1], cc.inv_theta, x0_zero});
         float *din = b.md, *dout = b.my;
-        for (int k = 1; k < deg && hi > lo; k++) {
-            mf_fac_kernel<4><<<fgrid, kFThreads, kFSmem, b.stream>>>(b.probs, b.fac_tiles, lo, hi, sel, b.fac32,
-                                                                    din, nullptr, b.E32, b.dinv, dout, b.states,
-                                                                    b.mr, b.mx, cc.c1[k], cc.c2[k]);
+        long long n = 1;
+        for (int k = 2; k < deg; k++) {
+            launch_fac<4>(b, lo, hi, sel,
+                          FacArgs{fac_map_of(b, din), kFMapMr, dout, b.mr, b.mx, cc.c1[k], cc.c2[k], 0.0f, 0});
             std::swap(din, dout);
             n += 1;
         }
         return n;
     }
+    mg_cheb_first_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, rin,
+                                                          b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero, sel);
+    long long n = 1;
     for (int k = 1; k < deg; k++) {
         launch_level_op<3>(b, fac, prec, l, 5, b.md, nullptr, b.my, sel);
         mg_cheb_next_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, b.my,

@@ -112,10 +112,12 @@ struct MfBatch {
     double *col_part = nullptr;   // per-column partial of p.q
     uint32_t *Bop2 = nullptr;     // K0 as the column operator's four (dy, dz) B tiles
     MfCol *fac_tiles = nullptr;   // tiles of the factored CUDA-core operator (cx, cy, cz)
+    CUtensorMap *fac_maps = nullptr;  // its tensor maps per problem (node vectors, moduli)
     std::vector<MfCol> h_fac_tiles;
     std::vector<int> lvl_fac_lo, lvl_fac_hi;
     FacK<float> fac32{};          // K0 in the per-axis sum/difference basis
     FacK<double> fac64{};
+    FacK2 fac2{};                 // fac32 as (k, k) pairs for the packed FP32x2 kernels
     MfChunkDesc *chunks = nullptr;
     MfState *states = nullptr;
     MfState *states_host = nullptr;  // pinned
