@@ -624,7 +624,7 @@ constexpr int kFEX = 32, kFEY = 16;                // elements per tile plane
 constexpr int kFNX = kFEX - 1, kFNY = kFEY - 1;    // owned nodes per tile plane
 constexpr int kFPX = kFEX + 1, kFPY = kFEY + 1;    // tile node plane (with halo)
 constexpr int kFThreads = 256;                     // 8 warps x 2 element rows
-constexpr int kFMinZ = 4, kFMaxZ = 32;
+constexpr int kFMinZ = 1, kFMaxZ = 32;
 constexpr int kFRing = 4;                          // 2 planes read, 2 in flight
 constexpr int kFBoxX = 104;                        // TMA node box: 104 floats (3 kFPX + alignment) x kFPY rows
 constexpr int kFPlaneF = 1792;                     // floats per node plane in the ring (7168 B, 128 B aligned)
@@ -1035,33 +1035,34 @@ __global__ void mg_restrict_kernel(const MfProblem *__restrict__ probs, int plo,
     if (states[C.root].done) return;
     const MfProblem F = probs[C.fine];
     if (F.bottom) return;  // inside a bottom chain: restricted by the bottom kernel
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < C.n_pad;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t row = i / C.pitch;
-        const int xin = (int)(i - row * C.pitch);
-        float out = 0.0f;
-        const int64_t o = C.dof_off + i;
-        if (xin < 3 * C.NX && dinv[o] != 0.0f) {
-            const int I = xin / 3, c = xin - 3 * I;
-            const int J = (int)(row % C.NY), K = (int)(row / C.NY);
-            for (int dz = -1; dz <= 1; dz++) {
-                const int k = 2 * K + dz;
-                if (k < 0 || k >= F.NZ) continue;
-                const float wz = dz ? 0.5f : 1.0f;
-                for (int dy = -1; dy <= 1; dy++) {
-                    const int j = 2 * J + dy;
-                    if (j < 0 || j >= F.NY) continue;
-                    const float wy = wz * (dy ? 0.5f : 1.0f);
-                    const float *rowp = my + F.dof_off + ((int64_t)k * F.NY + j) * F.pitch;
-                    for (int dx = -1; dx <= 1; dx++) {
-                        const int ii = 2 * I + dx;
-                        if (ii < 0 || ii >= F.NX) continue;
-                        out = fmaf(wy * (dx ? 0.5f : 1.0f), rowp[3 * ii + c], out);
+    // one coarse node row (J, K) per block iteration, its padded dofs across the threads
+    for (int row = blockIdx.x; row < C.NY * C.NZ; row += gridDim.x) {
+        const int J = row % C.NY, K = row / C.NY;
+        const int64_t base = C.dof_off + (int64_t)row * C.pitch;
+        for (int xin = threadIdx.x; xin < C.pitch; xin += blockDim.x) {
+            const int64_t o = base + xin;
+            float out = 0.0f;
+            if (xin < 3 * C.NX && dinv[o] != 0.0f) {
+                const int I = xin / 3, c = xin - 3 * I;
+                for (int dz = -1; dz <= 1; dz++) {
+                    const int k = 2 * K + dz;
+                    if (k < 0 || k >= F.NZ) continue;
+                    const float wz = dz ? 0.5f : 1.0f;
+                    for (int dy = -1; dy <= 1; dy++) {
+                        const int j = 2 * J + dy;
+                        if (j < 0 || j >= F.NY) continue;
+                        const float wy = wz * (dy ? 0.5f : 1.0f);
+                        const float *rowp = my + F.dof_off + ((int64_t)k * F.NY + j) * F.pitch;
+                        for (int dx = -1; dx <= 1; dx++) {
+                            const int ii = 2 * I + dx;
+                            if (ii < 0 || ii >= F.NX) continue;
+                            out = fmaf(wy * (dx ? 0.5f : 1.0f), rowp[3 * ii + c], out);
+                        }
                     }
                 }
             }
+            mb[o] = out;
         }
-        mb[o] = out;
     }
 }
 
@@ -1073,25 +1074,28 @@ __global__ void mg_prolong_kernel(const MfProblem *__restrict__ probs, int plo,
     const MfProblem F = probs[plo + blockIdx.y];
     if (F.coarse < 0 || F.bottom || states[F.root].done) return;  // nothing to add here
     const MfProblem C = probs[F.coarse];
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F.n_pad;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t row = i / F.pitch;
-        const int xin = (int)(i - row * F.pitch);
-        const int64_t o = F.dof_off + i;
-        if (xin >= 3 * F.NX || dinv[o] == 0.0f) continue;
-        const int ii = xin / 3, c = xin - 3 * ii;
-        const int j = (int)(row % F.NY), k = (int)(row / F.NY);
-        const int I0 = ii >> 1, I1 = (ii + 1) >> 1, J0 = j >> 1, J1 = (j + 1) >> 1, K0 = k >> 1,
-                  K1 = (k + 1) >> 1;
-        const float wx = (ii & 1) ? 0.5f : 1.0f, wy = (j & 1) ? 0.5f : 1.0f, wz = (k & 1) ? 0.5f : 1.0f;
-        float acc = 0.0f;
-        const int Is[2] = {I0, I1}, Js[2] = {J0, J1}, Ks[2] = {K0, K1};
-        for (int a = 0; a < ((k & 1) ? 2 : 1); a++)
-            for (int bb = 0; bb < ((j & 1) ? 2 : 1); bb++)
-                for (int cc = 0; cc < ((ii & 1) ? 2 : 1); cc++)
-                    acc = fmaf(wx * wy * wz,
-                               mx[C.dof_off + ((int64_t)Ks[a] * C.NY + Js[bb]) * C.pitch + 3 * Is[cc] + c], acc);
-        mx[o] += acc;
+    // one fine node row (j, k) per block iteration, its dofs across the threads
+    for (int row = blockIdx.x; row < F.NY * F.NZ; row += gridDim.x) {
+        const int j = row % F.NY, k = row / F.NY;
+        const int J0 = j >> 1, J1 = (j + 1) >> 1, K0 = k >> 1, K1 = (k + 1) >> 1;
+        const float wy = (j & 1) ? 0.5f : 1.0f, wz = (k & 1) ? 0.5f : 1.0f;
+        const int Js[2] = {J0, J1}, Ks[2] = {K0, K1};
+        const int64_t base = F.dof_off + (int64_t)row * F.pitch;
+        for (int xin = threadIdx.x; xin < 3 * F.NX; xin += blockDim.x) {
+            const int64_t o = base + xin;
+            if (dinv[o] == 0.0f) continue;
+            const int ii = xin / 3, c = xin - 3 * ii;
+            const int I0 = ii >> 1, I1 = (ii + 1) >> 1;
+            const float wx = (ii & 1) ? 0.5f : 1.0f;
+            const int Is[2] = {I0, I1};
+            float acc = 0.0f;
+            for (int a = 0; a < ((k & 1) ? 2 : 1); a++)
+                for (int bb = 0; bb < ((j & 1) ? 2 : 1); bb++)
+                    for (int cc = 0; cc < ((ii & 1) ? 2 : 1); cc++)
+                        acc = fmaf(wx * wy * wz,
+                                   mx[C.dof_off + ((int64_t)Ks[a] * C.NY + Js[bb]) * C.pitch + 3 * Is[cc] + c], acc);
+            mx[o] += acc;
+        }
     }
 }
 
@@ -2034,6 +2038,8 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     b.h_chunks.clear();
     b.h_cols.clear();
     b.h_fac_tiles.clear();
+    std::vector<int64_t> level_count(b.n_levels + 1, 0);  // problems per multigrid level
+    for (const MfProblem &P : b.h_probs) level_count[P.level]++;
     for (size_t pi = 0; pi < b.h_probs.size(); pi++) {
         MfProblem &P = b.h_probs[pi];
         if (P.nx <= 0 || P.ny <= 0 || P.nz <= 0 || P.nx >= 32767 * kBN || P.ny >= 32767 * kBN ||
@@ -2086,7 +2092,8 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         // planes (kFMinZ .. kFMaxZ): as deep as one wave of resident tiles allows
         {
             const int tx = (P.NX + kFNX - 1) / kFNX, ty = (P.NY + kFNY - 1) / kFNY;
-            const int64_t fac_slots = 2 * (int64_t)sms, per_col = std::max<int64_t>(1, fac_slots / (tx * ty));
+            const int64_t fac_slots = 2 * (int64_t)sms;
+            const int64_t per_col = std::max<int64_t>(1, fac_slots / ((int64_t)tx * ty * level_count[P.level]));
             P.fac_z = (int)std::min<int64_t>(kFMaxZ, std::max<int64_t>(kFMinZ, (P.NZ + per_col - 1) / per_col));
             const int tz = (P.NZ + P.fac_z - 1) / P.fac_z;
             P.fac_begin = (int)b.h_fac_tiles.size();
@@ -2474,9 +2481,9 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
         n += enqueue_smooth(b, fac, prec, l, rin, 1, sdeg, cs, 0);
         launch_level_op<2>(b, fac, prec, l, 4, b.mx, rin, b.my, 0);  // my = rin - A mx
         const int clo = b.lvl_prob_lo[l + 1], chi = b.lvl_prob_hi[l + 1];
-        int64_t maxpad = 1;
-        for (int pi = clo; pi < chi; pi++) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
-        dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), chi - clo);
+        int64_t maxrows = 1;
+        for (int pi = clo; pi < chi; pi++) maxrows = std::max<int64_t>(maxrows, (int64_t)b.h_probs[pi].NY * b.h_probs[pi].NZ);
+        dim3 grid((unsigned)std::min<int64_t>(maxrows, std::max(1, b.vec_grid / (chi - clo))), chi - clo);
         mg_restrict_kernel<<<grid, 256, 0, b.stream>>>(b.probs, clo, b.states, b.my, b.mb, b.dinv);
         n += 2;
         if (own_coarsest(l)) n += enqueue_smooth(b, fac, prec, l, rin, 1, cdeg, cc, 1);
@@ -2498,10 +2505,11 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
         if (!any_level(l)) continue;
         const float *rin = (l == 0) ? b.r : b.mb;
         const int flo = b.lvl_prob_lo[l], fhi = b.lvl_prob_hi[l];
-        int64_t maxpad = 1;
+        int64_t maxrows = 1;
         for (int pi = flo; pi < fhi; pi++)
-            if (b.h_probs[pi].coarse >= 0) maxpad = std::max(maxpad, b.h_probs[pi].n_pad);
-        dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 2048u)), fhi - flo);
+            if (b.h_probs[pi].coarse >= 0)
+                maxrows = std::max<int64_t>(maxrows, (int64_t)b.h_probs[pi].NY * b.h_probs[pi].NZ);
+        dim3 grid((unsigned)std::min<int64_t>(maxrows, std::max(1, b.vec_grid / (fhi - flo))), fhi - flo);
         mg_prolong_kernel<<<grid, 256, 0, b.stream>>>(b.probs, flo, b.states, b.mx, b.dinv);
         launch_level_op<2>(b, fac, prec, l, 4, b.mx, rin, b.my, 0);  // my = rin - A mx
         n += 2 + enqueue_smooth(b, fac, prec, l, b.my, 0, sdeg, cs, 0);
