@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-design batch section")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="solve the headline problem with the default schedule instead of the autotuned one")
     ap.add_argument("--serve-requests", type=int, default=1000, help="requests per arrival rate")
     ap.add_argument("--kernel-only", default=None, choices=["mixed", "plain", "factored"],
                     help="only launch one kernel (tensor-core column operator, FP64 CG SpMV or the "
@@ -329,6 +331,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def tune_schedule(M, opts, rho):
+    """The solver schedule (smoother and coarse degrees, smoother operator, CG
+    steps per graph, vector-kernel CTAs, inner tolerance) that the library's
+    autotuner picks for this grid: a one-design batch of the same cantilever,
+    tuned once before the timed region."""
+    b = M.Batch([dict(nx=NX, ny=NY, nz=NZ, rho=rho, spans=[(0, NY)])])
+    t0 = time.perf_counter()
+    o, _ = b.autotune(opts, max_trials=14)
+    secs = time.perf_counter() - t0
+    b.close()
+    sched = {"smooth_degree": o.smooth_degree, "coarse_degree": o.coarse_degree,
+             "smoother_operator": "factored" if o.smoother_operator == M.SMOOTHER_FACTORED else "tensor",
+             "graph_chunk": o.graph_chunk, "vec_blocks_per_sm": o.vec_blocks_per_sm,
+             "inner_rtol": o.inner_rtol, "precision": o.precision, "tuning_seconds": secs}
+    return o, sched
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -359,6 +378,10 @@ def main():
         kernel_only(args, M, prob, prec, rho)
         prob.close()
         return
+    schedule = {"autotuned": False}
+    if not args.no_autotune:
+        opts, schedule = tune_schedule(M, opts, rho)
+        schedule["autotuned"] = True
 
     def step_resident():
         prob.set_design_device(d_rho.data_ptr())
@@ -524,8 +547,8 @@ def main():
                 else "f32 (BF16 tensor-core operator) / f64 refinement",
                 "data": "synthetic (seeded U[0.01,1] densities, default_rng(0))",
                 "config": {"workload": WORKLOAD, "n_dofs": n, "n_elems": n_el, "rtol": 1e-8,
-                           "precision": args.precision, "inner_rtol": 1e-3,
-                           "preconditioner": args.preconditioner,
+                           "precision": args.precision, "inner_rtol": opts.inner_rtol,
+                           "preconditioner": args.preconditioner, "schedule": schedule,
                            "l2": "flushed between steps (512 MB write)",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "dof_per_s": value * n,

@@ -875,6 +875,7 @@ __global__ void __launch_bounds__(kThreads) mf_update_kernel(
         if (st->done) continue;
         const float alpha = (float)st->alpha;
         float rz = 0.0f, rr = 0.0f;
+#pragma unroll 4
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 pv = *reinterpret_cast<const float4 *>(p + i);
             const float4 qv = *reinterpret_cast<const float4 *>(q + i);
@@ -940,6 +941,7 @@ __global__ void __launch_bounds__(kThreads) mf_dot_rz_kernel(
         MfState *st = states + C.prob;
         if (st->done) continue;
         float rz = 0.0f;
+#pragma unroll 4
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 rv = *reinterpret_cast<const float4 *>(r + i);
             const float4 zv = *reinterpret_cast<const float4 *>(z + i);
@@ -985,6 +987,7 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_first_kernel(
         const MfChunkDesc C = chunks[ci];
         const MfProblem &Q = probs[C.prob];
         if (states[Q.root].done || Q.bottom || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
+#pragma unroll 4
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 rv = *reinterpret_cast<const float4 *>(rin + i);
             const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
@@ -1009,6 +1012,7 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_next_kernel(
         const MfChunkDesc C = chunks[ci];
         const MfProblem &Q = probs[C.prob];
         if (states[Q.root].done || Q.bottom || (sel >= 0 && sel != (Q.coarse < 0 ? 1 : 0))) continue;
+#pragma unroll 4
         for (int64_t i = C.begin + 4 * threadIdx.x; i < C.end; i += 4 * kThreads) {
             const float4 yv = *reinterpret_cast<const float4 *>(my + i);
             const float4 dv = *reinterpret_cast<const float4 *>(dinv + i);
@@ -1028,73 +1032,81 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_next_kernel(
 
 // restriction (transpose of trilinear interpolation) into the coarse problems
 // plo..phi-1: mb_c[I] = sum_d w(d) my_f[2I + d], d in {-1,0,1}^3, w = prod (1 - |d|/2)
-__global__ void mg_restrict_kernel(const MfProblem *__restrict__ probs, int plo,
-                                   const MfState *states, const float *__restrict__ my,
-                                   float *__restrict__ mb, const float *__restrict__ dinv) {
+__global__ void __launch_bounds__(256) mg_restrict_kernel(const MfProblem *__restrict__ probs, int plo,
+                                                          const MfState *states, const float *__restrict__ my,
+                                                          float *__restrict__ mb, const float *__restrict__ dinv) {
     const MfProblem C = probs[plo + blockIdx.y];
     if (states[C.root].done) return;
     const MfProblem F = probs[C.fine];
     if (F.bottom) return;  // inside a bottom chain: restricted by the bottom kernel
-    // one coarse node row (J, K) per block iteration, its padded dofs across the threads
-    for (int row = blockIdx.x; row < C.NY * C.NZ; row += gridDim.x) {
-        const int J = row % C.NY, K = row / C.NY;
-        const int64_t base = C.dof_off + (int64_t)row * C.pitch;
-        for (int xin = threadIdx.x; xin < C.pitch; xin += blockDim.x) {
-            const int64_t o = base + xin;
+    // one coarse node (3 dofs) per thread: its 27 fine neighbours' loads are all
+    // issued before the sums (independent, predicated on the grid bounds)
+    const int nn = C.NX * C.NY * C.NZ;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
+        const int I = n % C.NX, JK = n / C.NX, J = JK % C.NY, K = JK / C.NY;
+        const int64_t o = C.dof_off + ((int64_t)K * C.NY + J) * C.pitch + 3 * I;
+        float v[27][3];
+#pragma unroll
+        for (int q = 0; q < 27; q++) {
+            const int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = q / 9 - 1;
+            const int ii = 2 * I + dx, j = 2 * J + dy, k = 2 * K + dz;
+            const bool in = ii >= 0 && ii < F.NX && j >= 0 && j < F.NY && k >= 0 && k < F.NZ;
+            const float *src = my + F.dof_off + (in ? ((int64_t)k * F.NY + j) * F.pitch + 3 * ii : 0);
+#pragma unroll
+            for (int c = 0; c < 3; c++) v[q][c] = in ? src[c] : 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            // the order of the sums: dz outermost, then dy, then dx (as the transpose of prolongation)
             float out = 0.0f;
-            if (xin < 3 * C.NX && dinv[o] != 0.0f) {
-                const int I = xin / 3, c = xin - 3 * I;
-                for (int dz = -1; dz <= 1; dz++) {
-                    const int k = 2 * K + dz;
-                    if (k < 0 || k >= F.NZ) continue;
-                    const float wz = dz ? 0.5f : 1.0f;
-                    for (int dy = -1; dy <= 1; dy++) {
-                        const int j = 2 * J + dy;
-                        if (j < 0 || j >= F.NY) continue;
-                        const float wy = wz * (dy ? 0.5f : 1.0f);
-                        const float *rowp = my + F.dof_off + ((int64_t)k * F.NY + j) * F.pitch;
-                        for (int dx = -1; dx <= 1; dx++) {
-                            const int ii = 2 * I + dx;
-                            if (ii < 0 || ii >= F.NX) continue;
-                            out = fmaf(wy * (dx ? 0.5f : 1.0f), rowp[3 * ii + c], out);
-                        }
-                    }
-                }
+#pragma unroll
+            for (int q = 0; q < 27; q++) {
+                const int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = q / 9 - 1;
+                const float w = (dz ? 0.5f : 1.0f) * (dy ? 0.5f : 1.0f) * (dx ? 0.5f : 1.0f);
+                out = fmaf(w, v[q][c], out);
             }
-            mb[o] = out;
+            mb[o + c] = dinv[o + c] != 0.0f ? out : 0.0f;
         }
     }
 }
 
 // prolongation (trilinear) from the coarse levels into the fine problems
 // plo..phi-1: mx_f[i] += sum_I w mx_c[I] (skips Dirichlet dofs and padding)
-__global__ void mg_prolong_kernel(const MfProblem *__restrict__ probs, int plo,
-                                  const MfState *states, float *__restrict__ mx,
-                                  const float *__restrict__ dinv) {
+__global__ void __launch_bounds__(256) mg_prolong_kernel(const MfProblem *__restrict__ probs, int plo,
+                                                         const MfState *states, float *__restrict__ mx,
+                                                         const float *__restrict__ dinv) {
     const MfProblem F = probs[plo + blockIdx.y];
     if (F.coarse < 0 || F.bottom || states[F.root].done) return;  // nothing to add here
     const MfProblem C = probs[F.coarse];
-    // one fine node row (j, k) per block iteration, its dofs across the threads
-    for (int row = blockIdx.x; row < F.NY * F.NZ; row += gridDim.x) {
-        const int j = row % F.NY, k = row / F.NY;
-        const int J0 = j >> 1, J1 = (j + 1) >> 1, K0 = k >> 1, K1 = (k + 1) >> 1;
-        const float wy = (j & 1) ? 0.5f : 1.0f, wz = (k & 1) ? 0.5f : 1.0f;
-        const int Js[2] = {J0, J1}, Ks[2] = {K0, K1};
-        const int64_t base = F.dof_off + (int64_t)row * F.pitch;
-        for (int xin = threadIdx.x; xin < 3 * F.NX; xin += blockDim.x) {
-            const int64_t o = base + xin;
-            if (dinv[o] == 0.0f) continue;
-            const int ii = xin / 3, c = xin - 3 * ii;
-            const int I0 = ii >> 1, I1 = (ii + 1) >> 1;
-            const float wx = (ii & 1) ? 0.5f : 1.0f;
-            const int Is[2] = {I0, I1};
+    // one fine node (3 dofs) per thread; its 1, 2, 4 or 8 coarse parents' loads are
+    // issued together (the unused ones predicated off)
+    const int nn = F.NX * F.NY * F.NZ;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
+        const int ii = n % F.NX, jk = n / F.NX, j = jk % F.NY, k = jk / F.NY;
+        const int64_t o = F.dof_off + ((int64_t)k * F.NY + j) * F.pitch + 3 * ii;
+        const float wx = (ii & 1) ? 0.5f : 1.0f, wy = (j & 1) ? 0.5f : 1.0f, wz = (k & 1) ? 0.5f : 1.0f;
+        const float w = wx * wy * wz;
+        float v[8][3];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int a = q >> 2, bb = (q >> 1) & 1, cc = q & 1;
+            const bool use = (a == 0 || (k & 1)) && (bb == 0 || (j & 1)) && (cc == 0 || (ii & 1));
+            const int I = (ii + cc) >> 1, J = (j + bb) >> 1, K = (k + a) >> 1;
+            const float *src = mx + C.dof_off + (use ? ((int64_t)K * C.NY + J) * C.pitch + 3 * I : 0);
+#pragma unroll
+            for (int c = 0; c < 3; c++) v[q][c] = use ? src[c] : 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (dinv[o + c] == 0.0f) continue;
             float acc = 0.0f;
-            for (int a = 0; a < ((k & 1) ? 2 : 1); a++)
-                for (int bb = 0; bb < ((j & 1) ? 2 : 1); bb++)
-                    for (int cc = 0; cc < ((ii & 1) ? 2 : 1); cc++)
-                        acc = fmaf(wx * wy * wz,
-                                   mx[C.dof_off + ((int64_t)Ks[a] * C.NY + Js[bb]) * C.pitch + 3 * Is[cc] + c], acc);
-            mx[o] += acc;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int a = q >> 2, bb = (q >> 1) & 1, cc = q & 1;
+                const bool use = (a == 0 || (k & 1)) && (bb == 0 || (j & 1)) && (cc == 0 || (ii & 1));
+                if (use) acc = fmaf(w, v[q][c], acc);
+            }
+            mx[o + c] += acc;
         }
     }
 }
@@ -1137,9 +1149,56 @@ struct BottomLevel {
 };
 
 // y = A in on level L (0 on Dirichlet dofs; `in` is 0 there): node-centric
-// gather over the node's elements in a fixed order
+// gather over the node's elements in a fixed order.  Levels of at most
+// kBottomLaneNodes nodes use eight lanes per node instead (lane d = dx + 2 dy +
+// 4 dz forms the node's rows of element node - d; the partial sums meet in a
+// fixed xor butterfly), which shortens the dependent chain per pass eightfold.
+constexpr int kBottomLaneNodes = kBottomThreads / 2;
 __device__ void bottom_apply(const BottomLevel &L, const float *sK, const float *in, float *out) {
     const int nn = L.NX * L.NY * L.NZ;
+    if (nn <= kBottomLaneNodes) {
+        const int corner = threadIdx.x & 7;
+        const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
+        const float *K = sK + 3 * corner_index(dx, dy, dz) * 24;
+        for (int base = 0; base < nn; base += kBottomThreads / 8) {
+            const int n = base + (threadIdx.x >> 3);
+            float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+            if (n < nn) {
+                const int i = n % L.NX, j = (n / L.NX) % L.NY, k = n / (L.NX * L.NY);
+                const int ex = i - dx, ey = j - dy, ez = k - dz;
+                if (ex >= 0 && ey >= 0 && ez >= 0 && ex < L.nx && ey < L.ny && ez < L.nz) {
+                    const float e = L.E[ex + L.nx * (ey + L.ny * ez)];
+                    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+                    for (int bc = 0; bc < 8; bc++) {
+                        int bx, by, bz;
+                        corner_bits(bc, bx, by, bz);
+                        const float *u = in + 3 * ((ex + bx) + L.NX * ((ey + by) + L.NY * (ez + bz)));
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            s0 = fmaf(K[3 * bc + c], u[c], s0);
+                            s1 = fmaf(K[24 + 3 * bc + c], u[c], s1);
+                            s2 = fmaf(K[48 + 3 * bc + c], u[c], s2);
+                        }
+                    }
+                    a0 = e * s0;
+                    a1 = e * s1;
+                    a2 = e * s2;
+                }
+            }
+#pragma unroll
+            for (int off = 1; off < 8; off <<= 1) {
+                a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+                a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+                a2 += __shfl_xor_sync(0xffffffffu, a2, off);
+            }
+            if (n < nn && corner < 3) {
+                const float a = corner == 0 ? a0 : (corner == 1 ? a1 : a2);
+                out[3 * n + corner] = L.dinv[3 * n + corner] == 0.0f ? 0.0f : a;
+            }
+        }
+        return;
+    }
     for (int n = threadIdx.x; n < nn; n += kBottomThreads) {
         const int i = n % L.NX, j = (n / L.NX) % L.NY, k = n / (L.NX * L.NY);
         float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
@@ -2481,9 +2540,10 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
         n += enqueue_smooth(b, fac, prec, l, rin, 1, sdeg, cs, 0);
         launch_level_op<2>(b, fac, prec, l, 4, b.mx, rin, b.my, 0);  // my = rin - A mx
         const int clo = b.lvl_prob_lo[l + 1], chi = b.lvl_prob_hi[l + 1];
-        int64_t maxrows = 1;
-        for (int pi = clo; pi < chi; pi++) maxrows = std::max<int64_t>(maxrows, (int64_t)b.h_probs[pi].NY * b.h_probs[pi].NZ);
-        dim3 grid((unsigned)std::min<int64_t>(maxrows, std::max(1, b.vec_grid / (chi - clo))), chi - clo);
+        int64_t maxnodes = 1;
+        for (int pi = clo; pi < chi; pi++)
+            maxnodes = std::max<int64_t>(maxnodes, (int64_t)b.h_probs[pi].NX * b.h_probs[pi].NY * b.h_probs[pi].NZ);
+        dim3 grid(std::max(1u, std::min(blocks_for(maxnodes, 256), 4096u)), chi - clo);
         mg_restrict_kernel<<<grid, 256, 0, b.stream>>>(b.probs, clo, b.states, b.my, b.mb, b.dinv);
         n += 2;
         if (own_coarsest(l)) n += enqueue_smooth(b, fac, prec, l, rin, 1, cdeg, cc, 1);
@@ -2505,11 +2565,11 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
         if (!any_level(l)) continue;
         const float *rin = (l == 0) ? b.r : b.mb;
         const int flo = b.lvl_prob_lo[l], fhi = b.lvl_prob_hi[l];
-        int64_t maxrows = 1;
+        int64_t maxnodes = 1;
         for (int pi = flo; pi < fhi; pi++)
             if (b.h_probs[pi].coarse >= 0)
-                maxrows = std::max<int64_t>(maxrows, (int64_t)b.h_probs[pi].NY * b.h_probs[pi].NZ);
-        dim3 grid((unsigned)std::min<int64_t>(maxrows, std::max(1, b.vec_grid / (fhi - flo))), fhi - flo);
+                maxnodes = std::max<int64_t>(maxnodes, (int64_t)b.h_probs[pi].NX * b.h_probs[pi].NY * b.h_probs[pi].NZ);
+        dim3 grid(std::max(1u, std::min(blocks_for(maxnodes, 256), 4096u)), fhi - flo);
         mg_prolong_kernel<<<grid, 256, 0, b.stream>>>(b.probs, flo, b.states, b.mx, b.dinv);
         launch_level_op<2>(b, fac, prec, l, 4, b.mx, rin, b.my, 0);  // my = rin - A mx
         n += 2 + enqueue_smooth(b, fac, prec, l, b.my, 0, sdeg, cs, 0);
