@@ -551,6 +551,7 @@ def main():
                            "preconditioner": args.preconditioner, "schedule": schedule,
                            "l2": "flushed between steps (512 MB write)",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
+                "step_ms": [round(x, 3) for x in ms],
                 "dof_per_s": value * n,
                 "iterations": reps[-1][0], "refinements": reps[-1][1],
                 "relres_fp64": reps[-1][2], "compliance_rel_err_vs_oracle": comp_err,

@@ -132,6 +132,16 @@ __device__ __forceinline__ void fence_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Programmatic dependent launch: let the next kernel of the stream be scheduled
+// now, then wait until the previous kernel has finished and its writes are
+// visible (a no-op without a programmatic dependency).
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_enter() {
+    pdl_trigger();
+    pdl_wait();
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
@@ -316,6 +326,7 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
     const float *__restrict__ dinv, const float *__restrict__ rhs, float *__restrict__ p0,
     float *__restrict__ p1, float *__restrict__ y, MfState *states, double *__restrict__ col_part,
     int *err) {
+    pdl_enter();
     using PR = Prec<PREC>;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ double red_sh[kColThreads / 32];
@@ -662,6 +673,7 @@ __global__ void __launch_bounds__(kFThreads, 2) mf_fac_kernel(
     const MfProblem *__restrict__ probs, const MfCol *__restrict__ tiles, int t_lo, int t_hi, int sel,
     const FacK2 K, const CUtensorMap *__restrict__ fmaps, const MfState *__restrict__ states, const FacArgs A,
     int *err) {
+    pdl_trigger();
     extern __shared__ __align__(128) float fsm[];
     __shared__ __align__(8) uint64_t bars[kFRing];
     constexpr int NP = fac_planes(MODE);
@@ -673,6 +685,14 @@ __global__ void __launch_bounds__(kFThreads, 2) mf_fac_kernel(
     const uint32_t bar0 = smem_u32(&bars[0]);
     if (tid == 0)
         for (int k = 0; k < kFRing; k++) mbar_init(bar0 + 8 * k, 1);
+    // the tile and problem tables are constant: bring the first tile's into the
+    // caches while the previous kernel drains, then wait for its results
+    if (t_lo + (int)blockIdx.x < t_hi && tid == 0) {
+        const MfCol T0 = tiles[t_lo + blockIdx.x];
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(probs + T0.prob));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(fmaps + (size_t)T0.prob * kFacMaps));
+    }
+    pdl_wait();
     __syncthreads();
     uint32_t phase = 0;   // bit k: parity of slot k's next completion
     uint32_t issued = 0;  // bit k: a load into slot k is outstanding (thread 0)
@@ -867,6 +887,7 @@ __global__ void __launch_bounds__(kThreads) mf_update_kernel(
     float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
     const float *__restrict__ p, const float *__restrict__ q, const float *__restrict__ dinv,
     MfState *states, double *__restrict__ chunk_part, int mg) {
+    pdl_enter();
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
@@ -934,6 +955,7 @@ __global__ void __launch_bounds__(kThreads) mf_dot_rz_kernel(
     const MfChunkDesc *__restrict__ chunks, int n_chunks, const MfProblem *__restrict__ probs,
     const float *__restrict__ r, const float *__restrict__ z, MfState *states,
     double *__restrict__ chunk_part, int init) {
+    pdl_enter();
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
@@ -983,6 +1005,7 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_first_kernel(
     const MfState *states, const float *__restrict__ rin, float *__restrict__ mr,
     float *__restrict__ md, float *__restrict__ mx, const float *__restrict__ dinv,
     float inv_theta, int x0_zero, int sel) {
+    pdl_enter();
     for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
         const MfProblem &Q = probs[C.prob];
@@ -1008,6 +1031,7 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_next_kernel(
     const MfState *states, const float *__restrict__ my, float *__restrict__ mr,
     float *__restrict__ md, float *__restrict__ mx, const float *__restrict__ dinv, float c1,
     float c2, int sel) {
+    pdl_enter();
     for (int ci = lo + blockIdx.x; ci < hi; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
         const MfProblem &Q = probs[C.prob];
@@ -1035,6 +1059,7 @@ __global__ void __launch_bounds__(kThreads) mg_cheb_next_kernel(
 __global__ void __launch_bounds__(256) mg_restrict_kernel(const MfProblem *__restrict__ probs, int plo,
                                                           const MfState *states, const float *__restrict__ my,
                                                           float *__restrict__ mb, const float *__restrict__ dinv) {
+    pdl_enter();
     const MfProblem C = probs[plo + blockIdx.y];
     if (states[C.root].done) return;
     const MfProblem F = probs[C.fine];
@@ -1075,6 +1100,7 @@ __global__ void __launch_bounds__(256) mg_restrict_kernel(const MfProblem *__res
 __global__ void __launch_bounds__(256) mg_prolong_kernel(const MfProblem *__restrict__ probs, int plo,
                                                          const MfState *states, float *__restrict__ mx,
                                                          const float *__restrict__ dinv) {
+    pdl_enter();
     const MfProblem F = probs[plo + blockIdx.y];
     if (F.coarse < 0 || F.bottom || states[F.root].done) return;  // nothing to add here
     const MfProblem C = probs[F.coarse];
@@ -1275,6 +1301,7 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
     const MfProblem *__restrict__ probs, const int *__restrict__ heads, const MfState *states,
     const float *__restrict__ E32, const float *__restrict__ dinv_g, const float *__restrict__ mb,
     float *__restrict__ mx, const double *__restrict__ K0, BottomCheb cc, int sdeg, int cdeg) {
+    pdl_enter();
     extern __shared__ __align__(16) float sbm[];
     const int head = heads[blockIdx.x];
     const MfProblem H = probs[head];
@@ -1393,6 +1420,7 @@ __global__ void __launch_bounds__(kThreads) mf_inner_init_kernel(
     float *__restrict__ z, float *__restrict__ p0, float *__restrict__ p1,
     const float *__restrict__ dinv, MfState *states, double *__restrict__ chunk_part,
     double inner_rtol2, int maxit) {
+    pdl_enter();
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
@@ -1456,6 +1484,7 @@ __device__ __forceinline__ bool inner_finished(const MfState *st) {
 __global__ void mf_refine_kernel(const MfChunkDesc *__restrict__ chunks, int n_chunks,
                                  const float *__restrict__ x, double *__restrict__ u64,
                                  const MfState *states) {
+    pdl_enter();
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
         const MfChunkDesc C = chunks[ci];
         const MfState *st = states + C.prob;
@@ -1469,6 +1498,7 @@ __global__ void mf_refine_kernel(const MfChunkDesc *__restrict__ chunks, int n_c
 // after the refinement update: a stopped inner CG sends its problem back to the
 // FP64 residual, or ends it on a breakdown / NaN (one thread per problem)
 __global__ void mf_phase_kernel(MfState *states, int n_fine) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_fine) return;
     MfState *st = states + i;
@@ -1506,6 +1536,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
     const double *__restrict__ u64, const double *__restrict__ f64, const FacK<double> K,
     double *__restrict__ r64, MfState *states, double *__restrict__ brick_part, double rtol2,
     int max_ref) {
+    pdl_enter();
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
@@ -1821,6 +1852,23 @@ void pack_b_columns(const double *K0, std::vector<uint32_t> &out) {
     }
 }
 
+// Launch with programmatic dependent launch (the kernel starts with pdl_enter):
+// the launch latency of the solver step's kernels overlaps their predecessors.
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 struct ApplyArgs {
     int col_lo, col_hi, in_slot, parity;  // column range
     const float *rhs;
@@ -1833,7 +1881,7 @@ void launch_apply(MfBatch &b, const ApplyArgs &a) {
     const int nc = a.col_hi - a.col_lo;
     if (nc <= 0) return;
     const int grid = std::max(1, std::min(nc, b.col_grid));
-    mf_col_kernel<PREC, MODE><<<grid, kColThreads, kColSmem, b.stream>>>(
+    launch_pdl(mf_col_kernel<PREC, MODE>, grid, kColThreads, kColSmem, b.stream, 
         b.probs, b.cols, a.col_lo, a.col_hi, a.sel, b.tmaps, a.in_slot, a.parity, b.Bop2, b.dinv,
         a.rhs, b.p0, b.p1, a.y, b.states, b.col_part, b.err);
 }
@@ -1866,7 +1914,7 @@ template <int MODE>
 void launch_fac(MfBatch &b, int lo, int hi, int sel, const FacArgs &a) {
     if (hi <= lo || a.in_map < 0) return;
     const int grid = std::max(1, std::min(hi - lo, b.fac_grid));
-    mf_fac_kernel<MODE><<<grid, kFThreads, fac_smem(MODE), b.stream>>>(b.probs, b.fac_tiles, lo, hi, sel, b.fac2,
+    launch_pdl(mf_fac_kernel<MODE>, grid, kFThreads, fac_smem(MODE), b.stream, b.probs, b.fac_tiles, lo, hi, sel, b.fac2,
                                                                       b.fac_maps, b.states, a, b.err);
 }
 
@@ -1973,7 +2021,7 @@ int read_states(MfBatch &b) {
 
 void launch_update(MfBatch &b, float *pnew, bool mg) {
     const int n0 = b.lvl_chunk_hi[0];
-    mf_update_kernel<<<std::max(1, std::min(n0, b.vec_grid)), kThreads, 0, b.stream>>>(
+    launch_pdl(mf_update_kernel, std::max(1, std::min(n0, b.vec_grid)), kThreads, 0, b.stream, 
         b.chunks, n0, b.probs, b.x, b.r, b.z, pnew, b.q, b.dinv, b.states, b.chunk_part, mg ? 1 : 0);
 }
 
@@ -2502,12 +2550,12 @@ long long enqueue_smooth(MfBatch &b, bool fac, int prec, int l, const float *rin
         }
         return n;
     }
-    mg_cheb_first_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, rin,
+    launch_pdl(mg_cheb_first_kernel, grid, kThreads, 0, b.stream, b.chunks, clo, chi, b.probs, b.states, rin,
                                                           b.mr, b.md, b.mx, b.dinv, cc.inv_theta, x0_zero, sel);
     long long n = 1;
     for (int k = 1; k < deg; k++) {
         launch_level_op<3>(b, fac, prec, l, 5, b.md, nullptr, b.my, sel);
-        mg_cheb_next_kernel<<<grid, kThreads, 0, b.stream>>>(b.chunks, clo, chi, b.probs, b.states, b.my,
+        launch_pdl(mg_cheb_next_kernel, grid, kThreads, 0, b.stream, b.chunks, clo, chi, b.probs, b.states, b.my,
                                                              b.mr, b.md, b.mx, b.dinv, cc.c1[k], cc.c2[k], sel);
         n += 2;
     }
@@ -2544,7 +2592,7 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
         for (int pi = clo; pi < chi; pi++)
             maxnodes = std::max<int64_t>(maxnodes, (int64_t)b.h_probs[pi].NX * b.h_probs[pi].NY * b.h_probs[pi].NZ);
         dim3 grid(std::max(1u, std::min(blocks_for(maxnodes, 256), 4096u)), chi - clo);
-        mg_restrict_kernel<<<grid, 256, 0, b.stream>>>(b.probs, clo, b.states, b.my, b.mb, b.dinv);
+        launch_pdl(mg_restrict_kernel, grid, 256, 0, b.stream, b.probs, clo, b.states, b.my, b.mb, b.dinv);
         n += 2;
         if (own_coarsest(l)) n += enqueue_smooth(b, fac, prec, l, rin, 1, cdeg, cc, 1);
     }
@@ -2557,7 +2605,7 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
             bc.c1s[k] = cs.c1[k]; bc.c2s[k] = cs.c2[k];
             bc.c1c[k] = cc.c1[k]; bc.c2c[k] = cc.c2[k];
         }
-        mg_bottom_kernel<<<(unsigned)b.h_heads.size(), kBottomThreads, b.bottom_smem, b.stream>>>(
+        launch_pdl(mg_bottom_kernel, (unsigned)b.h_heads.size(), kBottomThreads, b.bottom_smem, b.stream, 
             b.probs, b.heads, b.states, b.E32, b.dinv, b.mb, b.mx, b.K0, bc, sdeg, cdeg);
         n += 1;
     }
@@ -2570,7 +2618,7 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
             if (b.h_probs[pi].coarse >= 0)
                 maxnodes = std::max<int64_t>(maxnodes, (int64_t)b.h_probs[pi].NX * b.h_probs[pi].NY * b.h_probs[pi].NZ);
         dim3 grid(std::max(1u, std::min(blocks_for(maxnodes, 256), 4096u)), fhi - flo);
-        mg_prolong_kernel<<<grid, 256, 0, b.stream>>>(b.probs, flo, b.states, b.mx, b.dinv);
+        launch_pdl(mg_prolong_kernel, grid, 256, 0, b.stream, b.probs, flo, b.states, b.mx, b.dinv);
         launch_level_op<2>(b, fac, prec, l, 4, b.mx, rin, b.my, 0);  // my = rin - A mx
         n += 2 + enqueue_smooth(b, fac, prec, l, b.my, 0, sdeg, cs, 0);
     }
@@ -2589,10 +2637,10 @@ long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
     const bool use_mg = prm.mg && b.n_levels > 1;
     const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
     const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
-    mf_residual64_kernel<<<std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s>>>(
+    launch_pdl(mf_residual64_kernel, std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s, 
         b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.fac64, b.r64, b.states,
         b.brick_part, prm.rtol * prm.rtol, max_ref);
-    mf_inner_init_kernel<<<vg0, kThreads, 0, s>>>(
+    launch_pdl(mf_inner_init_kernel, vg0, kThreads, 0, s, 
         b.chunks, n0, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.p1, b.dinv, b.states, b.chunk_part,
         prm.inner_rtol * prm.inner_rtol, maxit);
     long long n = 2;
@@ -2601,7 +2649,7 @@ long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
         const int sdeg = prm.smooth_deg > 0 ? prm.smooth_deg : 2;
         const int cdeg = prm.coarse_deg > 0 ? prm.coarse_deg : 8;
         n += enqueue_vcycle(b, prm.mg_operator == 0, mg_precision(prm.precision), sdeg, cdeg);
-        mf_dot_rz_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.probs, b.r, b.mx, b.states,
+        launch_pdl(mf_dot_rz_kernel, vg0, kThreads, 0, s, b.chunks, n0, b.probs, b.r, b.mx, b.states,
                                                  b.chunk_part, 0);
         launch_cg_apply(b, prm.precision, 4, parity);  // p = z + beta p_old, q = A p, alpha
         launch_update(b, pnew, true);                  // x, r, stop test
@@ -2611,8 +2659,8 @@ long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
         launch_update(b, pnew, false);                 // also z = D^-1 r, beta
         n += 2;
     }
-    mf_refine_kernel<<<vg0, kThreads, 0, s>>>(b.chunks, n0, b.x, b.u64, b.states);
-    mf_phase_kernel<<<(b.n_fine + 127) / 128, 128, 0, s>>>(b.states, b.n_fine);
+    launch_pdl(mf_refine_kernel, vg0, kThreads, 0, s, b.chunks, n0, b.x, b.u64, b.states);
+    launch_pdl(mf_phase_kernel, (b.n_fine + 127) / 128, 128, 0, s, b.states, b.n_fine);
     return n + 2;
 }
 
