@@ -2183,11 +2183,13 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
                 for (int i = 0; i < bx; i++)
                     b.h_bricks.push_back(MfBrick{(int)pi, (int16_t)i, (int16_t)j, (int16_t)k, 0});
         nb += P.brick_count;
-        // columns of the tensor-core operator: at most kCZ node planes each, fewer
-        // (at least 4) when that gives a small grid more columns than SM slots
+        // columns of the tensor-core operator: as deep as one wave of resident
+        // columns allows (the level's problems share the 3 x SM slots), 4 to kCZ
+        // node planes; a second, partial wave would double the launch's time
         const int cx = (P.NX + kCX - 1) / kCX, cy = (P.NY + kCY - 1) / kCY;
         const int64_t slots = 3 * (int64_t)sms;
-        P.col_z = (int)std::min<int64_t>(kCZ, std::max<int64_t>(4, (P.NZ * (int64_t)cx * cy + slots - 1) / slots));
+        const int64_t col_per = std::max<int64_t>(1, slots / ((int64_t)cx * cy * level_count[P.level]));
+        P.col_z = (int)std::min<int64_t>(kCZ, std::max<int64_t>(4, (P.NZ + col_per - 1) / col_per));
         const int cz = (P.NZ + P.col_z - 1) / P.col_z;
         P.col_begin = (int)b.h_cols.size();
         P.col_count = cx * cy * cz;

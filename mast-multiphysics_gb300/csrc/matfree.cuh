@@ -21,14 +21,14 @@ constexpr int kBE = kBN + 1;
 constexpr int kBU = kBN + 2;
 constexpr int kNEL = kBE * kBE * kBE;          // 729 elements per brick
 constexpr int kNTILE = (kNEL + 127) / 128;     // 6 MMA tiles of 128 elements
-constexpr int kChunk = 2048;                   // dofs per vector-kernel chunk (two float4 per thread)
+constexpr int kChunk = 4096;                   // dofs per vector-kernel chunk (four float4 per thread)
 constexpr int kMapsPerProblem = 6;             // z, p0, p1, E, mg x, mg d (column operator boxes)
 // Column operator: a column owns kCX x kCY nodes in x, y and up to kCZ node
 // planes in z; it streams through its element planes (8 x 16 elements each,
 // one M = 128 tensor-core tile per plane).
 constexpr int kCX = 7;
 constexpr int kCY = 15;
-constexpr int kCZ = 16;   // most node planes per column
+constexpr int kCZ = 32;   // most node planes per column
 constexpr int kMaxLevels = 8;                  // multigrid levels per design
 
 // Padded vector layout of one problem: node (i,j,k), component c lives at
