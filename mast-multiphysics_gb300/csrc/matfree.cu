@@ -1912,7 +1912,11 @@ int fac_map_of(const MfBatch &b, const float *v) {
 
 template <int MODE>
 void launch_fac(MfBatch &b, int lo, int hi, int sel, const FacArgs &a) {
-    if (hi <= lo || a.in_map < 0) return;
+    if (a.in_map < 0 || ((MODE == 2 || MODE == 4) && a.b_map < 0)) {
+        b.enqueue_error = MG_EINVAL;  // reported by the caller of the enqueue
+        return;
+    }
+    if (hi <= lo) return;
     const int grid = std::max(1, std::min(hi - lo, b.fac_grid));
     launch_pdl(mf_fac_kernel<MODE>, grid, kFThreads, fac_smem(MODE), b.stream, b.probs, b.fac_tiles, lo, hi, sel, b.fac2,
                                                                       b.fac_maps, b.states, a, b.err);
@@ -2464,7 +2468,6 @@ int mf_apply(MfBatch &b, int precision, const double *x_host, double *y_host, in
     MG_CUDA_TRY(cudaMemcpyAsync(b.mx + P.dof_off, pad.data(), P.n_pad * 4, cudaMemcpyHostToDevice, b.stream));
     MG_CUDA_TRY(cudaMemsetAsync(b.states, 0, b.n_probs * sizeof(MfState), b.stream));
     if (precision == MG_OPERATOR_FACTORED_FP32) {
-        const int grid = std::max(1, std::min(P.fac_count, b.fac_grid));
         launch_fac<3>(b, P.fac_begin, P.fac_begin + P.fac_count, -1,
                       FacArgs{kFMapMx, -1, b.my, nullptr, nullptr, 0.0f, 0.0f, 0.0f, 0});
     } else {
@@ -2681,12 +2684,18 @@ int build_step_graph(MfBatch &b, const MfSolveParams &prm, int chunk) {
     }
     long long n = 0;
     cudaGraph_t g = nullptr;
+    b.enqueue_error = 0;
     MG_CUDA_TRY(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < chunk; it++) n += enqueue_step(b, prm, it & 1);
     cudaError_t e = cudaStreamEndCapture(b.stream, &g);
     if (e != cudaSuccess) {
         set_error("graph capture: %s", cudaGetErrorString(e));
         return MG_ECUDA;
+    }
+    if (b.enqueue_error) {
+        cudaGraphDestroy(g);
+        set_error("factored level operator: a vector without a tensor map");
+        return b.enqueue_error;
     }
     e = cudaGraphInstantiate(&b.graph, g, 0);
     cudaGraphDestroy(g);

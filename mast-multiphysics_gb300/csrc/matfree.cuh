@@ -151,6 +151,7 @@ struct MfBatch {
     cudaGraphExec_t graph = nullptr;  // solver steps (see enqueue_step)
     std::vector<double> graph_key;    // parameters the graph was captured with
     long long graph_launches = 0;     // kernel nodes in the graph
+    int enqueue_error = 0;            // an operator asked for a vector without a tensor map
     int apply_grid = 0, vec_grid = 0, col_grid = 0, fac_grid = 0;
     cudaStream_t stream = nullptr;
 };
