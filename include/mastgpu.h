@@ -408,6 +408,30 @@ int mg_filter_apply_device(mg_filter *f, const double *in_dev, double *out_dev, 
                            void *stream);
 void mg_filter_destroy(mg_filter *f);
 
+/* ---- Nastran bulk data (BDF) mesh input ----
+   Replaces MAST::NastranIO::read (src/mesh/nastran_io.cpp:221-339; read_nodes
+   :105-125, read_elements :128-198, read_node_boundaries :201-218), which reads
+   through pyNastran.  Host code, no GPU.  Small-field, large-field (NAME*) and
+   free-field cards with continuation lines; GRID (basic coordinates), CHEXA
+   (8 nodes), CQUAD4, SPC1 (with THRU), SPC (D = 0) and FORCE (basic
+   coordinates).  Nodes in ascending GRID id, elements in ascending element id,
+   element nodes in the card's order (libMesh's local order); constraints and
+   loads of every set id.  The arrays feed mg_mesh_desc / mg_bc_desc. */
+typedef struct mg_bdf_mesh mg_bdf_mesh;
+int mg_bdf_read(const char *path, mg_bdf_mesh **out);
+int mg_bdf_parse(const char *text, int64_t len, mg_bdf_mesh **out);
+int mg_bdf_sizes(const mg_bdf_mesh *m, int64_t *n_nodes, int64_t *n_elems, int32_t *nodes_per_elem);
+/* coords: n_nodes x 3; grid_ids (nullable): the GRID id of each node */
+int mg_bdf_nodes(const mg_bdf_mesh *m, double *coords, int64_t *grid_ids);
+/* conn: n_elems x nodes_per_elem node indices; elem_ids, pids nullable */
+int mg_bdf_elements(const mg_bdf_mesh *m, int32_t *conn, int64_t *elem_ids, int32_t *pids);
+/* homogeneous Dirichlet dofs (dof = dpn*node + component - 1, components
+   1..dpn of the SPC digits); fixed_dofs NULL: only *n */
+int mg_bdf_constraints(const mg_bdf_mesh *m, int32_t dpn, int64_t *fixed_dofs, int64_t *n);
+/* nodal point loads F (components 1..min(dpn, 3)), summed per dof; NULL arrays: only *n */
+int mg_bdf_loads(const mg_bdf_mesh *m, int32_t dpn, int64_t *load_dofs, double *load_values, int64_t *n);
+void mg_bdf_destroy(mg_bdf_mesh *m);
+
 /* parameter kinds for mg_sensitivity_assemble */
 #define MG_PARAM_DENSITY 0      /* rho_e of element param_index (elasticity) */
 #define MG_PARAM_K0 1           /* conductivity k0 (heat) */

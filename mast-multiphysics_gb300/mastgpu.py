@@ -234,6 +234,15 @@ def lib(autobuild=True):
     L.mg_filter_apply_device.argtypes = [_vp, _vp, _vp, _i32, _vp]
     L.mg_filter_destroy.argtypes = [_vp]
     L.mg_filter_destroy.restype = None
+    L.mg_bdf_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(_vp)]
+    L.mg_bdf_parse.argtypes = [ctypes.c_char_p, _i64, ctypes.POINTER(_vp)]
+    L.mg_bdf_sizes.argtypes = [_vp, _vp, _vp, _vp]
+    L.mg_bdf_nodes.argtypes = [_vp, _vp, _vp]
+    L.mg_bdf_elements.argtypes = [_vp, _vp, _vp, _vp]
+    L.mg_bdf_constraints.argtypes = [_vp, _i32, _vp, _vp]
+    L.mg_bdf_loads.argtypes = [_vp, _i32, _vp, _vp, _vp]
+    L.mg_bdf_destroy.argtypes = [_vp]
+    L.mg_bdf_destroy.restype = None
     L.mg_server_clock.restype = ctypes.c_double
     L.mg_server_create.argtypes = [ctypes.POINTER(MaterialDesc), ctypes.POINTER(ServerOpts),
                                    ctypes.POINTER(_vp)]
@@ -708,6 +717,41 @@ def simp_cantilever(nx, ny, nz, load_y0=0, load_y1=None, material=None):
     load_vals = np.full(ys.shape[0], -1.0 / ys.shape[0])
     return Problem(PHYS_HEX8, coords, conn, material or SIMP_MATERIAL, fixed_dofs=fixed,
                    load_dofs=load_dofs, load_values=load_vals, grid=(nx, ny, nz))
+
+
+def read_bdf(path=None, text=None, dpn=3):
+    """Nastran bulk data mesh (mg_bdf_read / mg_bdf_parse): dict with coords
+    (n x 3), conn (n_elems x npe, node indices), grid_ids, elem_ids, pids,
+    fixed_dofs and (load_dofs, load_values) for dpn dofs per node."""
+    L = lib()
+    h = _vp()
+    if text is not None:
+        b = text.encode() if isinstance(text, str) else bytes(text)
+        check(L.mg_bdf_parse(b, len(b), ctypes.byref(h)), "mg_bdf_parse")
+    else:
+        check(L.mg_bdf_read(os.fsencode(path), ctypes.byref(h)), "mg_bdf_read")
+    try:
+        nn, ne, npe = _i64(), _i64(), _i32()
+        check(L.mg_bdf_sizes(h, ctypes.byref(nn), ctypes.byref(ne), ctypes.byref(npe)), "mg_bdf_sizes")
+        coords = np.zeros((nn.value, 3))
+        gids = np.zeros(nn.value, dtype=np.int64)
+        check(L.mg_bdf_nodes(h, _p(coords), _p(gids)), "mg_bdf_nodes")
+        conn = np.zeros((ne.value, npe.value), dtype=np.int32)
+        eids = np.zeros(ne.value, dtype=np.int64)
+        pids = np.zeros(ne.value, dtype=np.int32)
+        check(L.mg_bdf_elements(h, _p(conn), _p(eids), _p(pids)), "mg_bdf_elements")
+        n = _i64()
+        check(L.mg_bdf_constraints(h, dpn, None, ctypes.byref(n)), "mg_bdf_constraints")
+        fixed = np.zeros(n.value, dtype=np.int64)
+        check(L.mg_bdf_constraints(h, dpn, _p(fixed), ctypes.byref(n)), "mg_bdf_constraints")
+        check(L.mg_bdf_loads(h, dpn, None, None, ctypes.byref(n)), "mg_bdf_loads")
+        ld = np.zeros(n.value, dtype=np.int64)
+        lv = np.zeros(n.value)
+        check(L.mg_bdf_loads(h, dpn, _p(ld), _p(lv), ctypes.byref(n)), "mg_bdf_loads")
+    finally:
+        L.mg_bdf_destroy(h)
+    return dict(coords=coords, conn=conn, grid_ids=gids, elem_ids=eids, pids=pids, fixed_dofs=fixed,
+                load_dofs=ld, load_values=lv)
 
 
 BATCH_SIZES = ((16, 8, 8), (32, 16, 16), (48, 24, 24), (64, 32, 32), (96, 48, 48))
