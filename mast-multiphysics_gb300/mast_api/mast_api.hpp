@@ -309,9 +309,10 @@ enum ElemType { HEX8, QUAD4 };
 class Mesh {
 public:
     ElemType type = HEX8;
-    int nx = 0, ny = 0, nz = 0;
+    int nx = 0, ny = 0, nz = 0;  // structured-grid dims (0: an unstructured mesh)
     std::vector<Real> coords;    // n_nodes x dim
     std::vector<int32_t> conn;   // n_elems x npe, libMesh local order
+    std::map<int, std::vector<int64_t>> node_boundary;  // unstructured meshes: nodes per boundary id
     int dim() const { return type == HEX8 ? 3 : 2; }
     int64_t n_nodes() const { return (int64_t)coords.size() / dim(); }
     int64_t n_elem() const { return (int64_t)conn.size() / (type == HEX8 ? 8 : 4); }
@@ -322,6 +323,10 @@ public:
     // nodes on a boundary id
     std::vector<int64_t> boundary_nodes(int bid) const {
         std::vector<int64_t> out;
+        if (nx == 0) {  // unstructured: the boundary node sets read with the mesh
+            auto it = node_boundary.find(bid);
+            return it == node_boundary.end() ? out : it->second;
+        }
         const int NX = nx + 1, NY = ny + 1, NZ = type == HEX8 ? nz + 1 : 1;
         for (int k = 0; k < NZ; k++)
             for (int j = 0; j < NY; j++)
@@ -396,6 +401,50 @@ inline void build_square(Mesh &m, int nx, int ny, Real x0, Real x1, Real y0, Rea
 }
 }  // namespace Generation
 }  // namespace MeshTools
+
+// MAST::NastranIO (src/mesh/nastran_io.h / .cpp): reads a Nastran bulk data
+// deck into the mesh -- GRID nodes (ascending id), CHEXA / CQUAD4 elements
+// (ascending id), every SPC node as boundary id 1 -- through mg_bdf_read
+// instead of pyNastran
+class NastranIO {
+public:
+    explicit NastranIO(Mesh &mesh, bool python_preinitialized = false) : _mesh(mesh) { (void)python_preinitialized; }
+    void read(const std::string &filename) {
+        mg_bdf_mesh *h = nullptr;
+        check(mg_bdf_read(filename.c_str(), &h), "NastranIO::read");
+        int64_t nn = 0, ne = 0, nspc = 0;
+        int32_t npe = 0;
+        mg_bdf_sizes(h, &nn, &ne, &npe);
+        std::vector<double> xyz((size_t)nn * 3);
+        std::vector<int64_t> gids((size_t)nn), eids((size_t)ne);
+        Mesh m;
+        m.type = npe == 8 ? HEX8 : QUAD4;
+        m.conn.resize((size_t)ne * npe);
+        mg_bdf_nodes(h, xyz.data(), gids.data());
+        mg_bdf_elements(h, m.conn.data(), eids.data(), nullptr);
+        mg_bdf_constraints(h, 6, nullptr, &nspc);
+        std::vector<int64_t> spc((size_t)nspc);
+        mg_bdf_constraints(h, 6, spc.data(), &nspc);
+        mg_bdf_destroy(h);
+        for (int64_t n = 0; n < nn; n++)
+            for (int k = 0; k < m.dim(); k++) m.coords.push_back(xyz[3 * n + k]);
+        std::set<int64_t> spc_nodes;
+        for (int64_t d : spc) spc_nodes.insert(d / 6);
+        if (!spc_nodes.empty()) m.node_boundary[1].assign(spc_nodes.begin(), spc_nodes.end());
+        _node_map.clear();
+        _elem_map.clear();
+        for (int64_t n = 0; n < nn; n++) _node_map[(uint64_t)gids[n]] = n;
+        for (int64_t e = 0; e < ne; e++) _elem_map[(uint64_t)eids[e]] = e;
+        _mesh = m;
+    }
+    // Nastran id -> mesh node / element index
+    std::map<uint64_t, int64_t> get_nastran_to_libmesh_node_map() const { return _node_map; }
+    std::map<uint64_t, int64_t> get_nastran_to_libmesh_elem_map() const { return _elem_map; }
+
+private:
+    Mesh &_mesh;
+    std::map<uint64_t, int64_t> _node_map, _elem_map;
+};
 
 // ------------------------------------------------------------------ boundary conditions
 enum BoundaryConditionType { POINT_LOAD, DIRICHLET, CONVECTION_HEAT_FLUX, HEAT_SOURCE };

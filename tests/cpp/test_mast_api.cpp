@@ -92,6 +92,49 @@ TEST_CASE("build_cube_numbering_and_boundary_ids", "[cpu],[mesh]") {
     CHECK(sq.boundary_nodes(3).size() == 5);  // x = 0 edge
 }
 
+// MAST::NastranIO: a 3 x 2 x 2 cube written as GRID / CHEXA / SPC1 cards reads
+// back as build_cube's mesh, the SPC nodes as boundary 1, the Nastran ids mapped
+TEST_CASE("nastran_io_reads_a_cube", "[cpu],[mesh],[nastran]") {
+    MAST::Mesh cube;
+    MAST::MeshTools::Generation::build_cube(cube, 3, 2, 2, 0, 3, 0, 2, 0, 2);
+    std::string deck = "$ cube\nBEGIN BULK\n";
+    char line[128];
+    for (int64_t n = 0; n < cube.n_nodes(); n++) {
+        snprintf(line, sizeof(line), "GRID,%lld,,%g,%g,%g\n", (long long)(501 + n), cube.coords[3 * n],
+                 cube.coords[3 * n + 1], cube.coords[3 * n + 2]);
+        deck += line;
+    }
+    for (int64_t e = 0; e < cube.n_elem(); e++) {
+        const int32_t *c = &cube.conn[8 * e];
+        snprintf(line, sizeof(line), "CHEXA,%lld,7,%d,%d,%d,%d,%d,%d\n,%d,%d\n", (long long)(e + 1), 501 + c[0],
+                 501 + c[1], 501 + c[2], 501 + c[3], 501 + c[4], 501 + c[5], 501 + c[6], 501 + c[7]);
+        deck += line;
+    }
+    const std::vector<int64_t> clamp = cube.boundary_nodes(4);  // x = 0 face
+    for (int64_t n : clamp) {
+        snprintf(line, sizeof(line), "SPC1,1,123,%lld\n", (long long)(501 + n));
+        deck += line;
+    }
+    deck += "ENDDATA\n";
+    const std::string path = "nastran_io_cube.bdf";
+    FILE *fp = fopen(path.c_str(), "w");
+    REQUIRE(fp != nullptr);
+    fputs(deck.c_str(), fp);
+    fclose(fp);
+    MAST::Mesh mesh;
+    MAST::NastranIO io(mesh);
+    io.read(path);
+    REQUIRE(mesh.type == MAST::HEX8);
+    REQUIRE(mesh.coords.size() == cube.coords.size() && mesh.conn.size() == cube.conn.size());
+    for (size_t i = 0; i < cube.coords.size(); i++) CHECK(mesh.coords[i] == Approx(cube.coords[i]));
+    for (size_t i = 0; i < cube.conn.size(); i++) CHECK(mesh.conn[i] == cube.conn[i]);
+    CHECK(mesh.boundary_nodes(1) == clamp);
+    CHECK(io.get_nastran_to_libmesh_node_map().at(501 + 7) == 7);
+    CHECK(io.get_nastran_to_libmesh_elem_map().at(5) == 4);
+    REQUIRE_THROWS(io.read("no_such_deck.bdf"));
+    remove(path.c_str());
+}
+
 TEST_CASE("misuse_is_reported", "[cpu],[errors]") {
     REQUIRE_THROWS(MAST::PointLoadCondition(MAST::DIRICHLET));
     MAST::NonlinearImplicitAssembly assembly;
