@@ -1185,7 +1185,10 @@ __device__ void bottom_apply(const BottomLevel &L, const float *sK, const float 
     if (nn <= kBottomLaneNodes) {
         const int corner = threadIdx.x & 7;
         const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
-        const float *K = sK + 3 * corner_index(dx, dy, dz) * 24;
+        // this corner's 3 x 24 rows of K0 regrouped per neighbour corner bc (9 values in
+        // 12); corner blocks 100 floats apart, so the eight corners of a node read
+        // disjoint banks
+        const float4 *Kt = reinterpret_cast<const float4 *>(sK + 576 + 100 * corner_index(dx, dy, dz));
         for (int base = 0; base < nn; base += kBottomThreads / 8) {
             const int n = base + (threadIdx.x >> 3);
             float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
@@ -1200,12 +1203,11 @@ __device__ void bottom_apply(const BottomLevel &L, const float *sK, const float 
                         int bx, by, bz;
                         corner_bits(bc, bx, by, bz);
                         const float *u = in + 3 * ((ex + bx) + L.NX * ((ey + by) + L.NY * (ez + bz)));
-#pragma unroll
-                        for (int c = 0; c < 3; c++) {
-                            s0 = fmaf(K[3 * bc + c], u[c], s0);
-                            s1 = fmaf(K[24 + 3 * bc + c], u[c], s1);
-                            s2 = fmaf(K[48 + 3 * bc + c], u[c], s2);
-                        }
+                        const float u0 = u[0], u1 = u[1], u2 = u[2];
+                        const float4 k0 = Kt[3 * bc], k1 = Kt[3 * bc + 1], k2 = Kt[3 * bc + 2];
+                        s0 = fmaf(k0.z, u2, fmaf(k0.y, u1, fmaf(k0.x, u0, s0)));
+                        s1 = fmaf(k1.y, u2, fmaf(k1.x, u1, fmaf(k0.w, u0, s1)));
+                        s2 = fmaf(k2.x, u2, fmaf(k1.w, u1, fmaf(k1.z, u0, s2)));
                     }
                     a0 = e * s0;
                     a1 = e * s1;
@@ -1306,13 +1308,17 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
     const int head = heads[blockIdx.x];
     const MfProblem H = probs[head];
     if (states[H.root].done) return;
-    float *sK = sbm;  // 576
+    float *sK = sbm;  // 576, then the regrouped copy for the eight-lane apply (8 x 100)
     for (int i = threadIdx.x; i < 576; i += kBottomThreads) sK[i] = (float)K0[i];
+    for (int i = threadIdx.x; i < 800; i += kBottomThreads) {
+        const int a = i / 100, t = i % 100, bc = t / 12, q = t % 12, r = q / 3, c = q % 3;
+        sbm[576 + i] = (t < 96 && q < 9) ? (float)K0[(3 * a + r) * 24 + 3 * bc + c] : 0.0f;
+    }
     // carve the levels of the chain
     BottomLevel Lv[kBottomMaxLevels];
     int pl[kBottomMaxLevels];
     int m = 0;
-    float *p = sbm + 576;
+    float *p = sbm + 576 + 800;
     for (int q = head; q >= 0 && m < kBottomMaxLevels; q = probs[q].coarse) {
         const MfProblem P = probs[q];
         BottomLevel &L = Lv[m];
@@ -2256,7 +2262,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     b.bottom_smem = 0;
     for (int r = 0; r < b.n_fine; r++) {
         for (int q = b.h_probs[r].coarse; q >= 0; q = b.h_probs[q].coarse) {
-            int64_t floats = 576, depth = 0;
+            int64_t floats = 576 + 800, depth = 0;
             for (int t = q; t >= 0; t = b.h_probs[t].coarse, depth++) {
                 const MfProblem &T = b.h_probs[t];
                 // x, b, r, d, y, D^-1 per dof and E per element
