@@ -228,6 +228,82 @@ int or_hex8_internal(const double X[24], double E, double nu, const double u[24]
     return 0;
 }
 
+/* StructuralElement3D::internal_residual, nonlinear-strain branch
+   (solid_element_3d.cpp:299-409 with initialize_green_lagrange_strain_operator
+   :1309-1463): total Lagrangian, F = grad u at the reference configuration,
+   Green-Lagrange strain E = (F + F^T + F^T F) / 2 in Voigt order with
+   engineering shears, S = C E; f += JxW B_L^T S with B_L = B_lin + the
+   displacement-dependent rows (the reference's mat_x/y/z times Bmat_nl_x/y/z),
+   K += JxW (B_L^T C B_L + the geometric stiffness grad N_a . S . grad N_b per
+   component, the reference's Bmat_nl_u/v/w products with the stress tensor).
+   The incompatible-mode and rotational-dof terms are absent as in the linear
+   branch. */
+int or_hex8_internal_gl(const double X[24], double E, double nu, const double u[24],
+                        double f[24], double K[576]) {
+    double C[36], phi[8], dphi[24], JxW;
+    or_iso_stiffness_3d(E, nu, C);
+    memset(f, 0, 24 * sizeof(double));
+    if (K) memset(K, 0, 576 * sizeof(double));
+    static const int VJ[6] = {0, 1, 2, 0, 1, 0}, VK[6] = {0, 1, 2, 1, 2, 2};
+    for (int qp = 0; qp < 8; qp++) {
+        if (hex8_qp(X, qp, phi, dphi, &JxW) <= 0.) return -1;
+        double F[9] = {0};  /* F[i][j] = d u_i / d X_j */
+        for (int i = 0; i < 3; i++)
+            for (int a = 0; a < 8; a++)
+                for (int j = 0; j < 3; j++) F[i * 3 + j] += u[i * 8 + a] * dphi[a * 3 + j];
+        double eps[6], sig[6] = {0}, BL[144];
+        for (int r = 0; r < 6; r++) {
+            const int j = VJ[r], k = VK[r];
+            double e = 0.5 * (F[j * 3 + k] + F[k * 3 + j]);
+            for (int m = 0; m < 3; m++) e += 0.5 * F[m * 3 + j] * F[m * 3 + k];
+            eps[r] = (r < 3) ? e : 2.0 * e;
+        }
+        for (int r = 0; r < 6; r++)
+            for (int c = 0; c < 6; c++) sig[r] += C[r * 6 + c] * eps[c];
+        /* B_L: the strain variation of dof (component i, node a), dF_mn = delta_im g_n:
+           dE_jk = (delta_ij g_k + delta_ik g_j + g_j F_ik + F_ij g_k) / 2 */
+        for (int i = 0; i < 3; i++)
+            for (int a = 0; a < 8; a++) {
+                const double *g = dphi + a * 3;
+                for (int r = 0; r < 6; r++) {
+                    const int j = VJ[r], k = VK[r];
+                    double de = 0.5 * ((i == j ? g[k] : 0.0) + (i == k ? g[j] : 0.0) + g[j] * F[i * 3 + k] +
+                                       F[i * 3 + j] * g[k]);
+                    BL[r * 24 + i * 8 + a] = (r < 3) ? de : 2.0 * de;
+                }
+            }
+        for (int c = 0; c < 24; c++) {
+            double s = 0;
+            for (int r = 0; r < 6; r++) s += BL[r * 24 + c] * sig[r];
+            f[c] += JxW * s;
+        }
+        if (K) {
+            const double St[9] = {sig[0], sig[3], sig[5], sig[3], sig[1], sig[4], sig[5], sig[4], sig[2]};
+            double CB[144];
+            for (int r = 0; r < 6; r++)
+                for (int c = 0; c < 24; c++) {
+                    double s = 0;
+                    for (int q = 0; q < 6; q++) s += C[r * 6 + q] * BL[q * 24 + c];
+                    CB[r * 24 + c] = s;
+                }
+            for (int i = 0; i < 24; i++)
+                for (int j = 0; j < 24; j++) {
+                    double s = 0;
+                    for (int r = 0; r < 6; r++) s += BL[r * 24 + i] * CB[r * 24 + j];
+                    K[i * 24 + j] += JxW * s;
+                }
+            for (int a = 0; a < 8; a++)
+                for (int b = 0; b < 8; b++) {
+                    double gsg = 0;
+                    for (int m = 0; m < 3; m++)
+                        for (int n = 0; n < 3; n++) gsg += dphi[a * 3 + m] * St[m * 3 + n] * dphi[b * 3 + n];
+                    for (int i = 0; i < 3; i++) K[(i * 8 + a) * 24 + i * 8 + b] += JxW * gsg;
+                }
+        }
+    }
+    return 0;
+}
+
 /* StructuralElement3D::internal_residual_sensitivity, linear branch
    (solid_element_3d.cpp:567-788): C replaced by dC/dp (:640).  With only E
    depending on p (StiffnessMatrix3D::derivative,

@@ -45,6 +45,10 @@ void or_quad4_shape(const double xi[2], double phi[4], double dphi[8]);
 /* element routines (var-blocked order; K may be NULL) */
 int or_hex8_internal(const double X[24], double E, double nu, const double u[24],
                      double f[24], double K[576]);
+/* HEX8 total-Lagrangian Green-Lagrange element (nonlinear-strain branch):
+   f = int B_L^T S, K = int (B_L^T C B_L + geometric stiffness); var-blocked dofs */
+int or_hex8_internal_gl(const double X[24], double E, double nu, const double u[24],
+                        double f[24], double K[576]);
 int or_hex8_internal_sens(const double X[24], double dE, double nu,
                           const double u[24], double df[24]);
 int or_quad4_membrane_internal(const double X[8], double E, double nu, double h,

@@ -70,6 +70,7 @@ def lib():
         L.or_quad4_shape.argtypes = [_f64p, _f64p, _f64p]
         L.or_hex8_internal.argtypes = [_f64p, d, d, _f64p, _f64p, vp]
         L.or_hex8_internal_sens.argtypes = [_f64p, d, d, _f64p, _f64p]
+        L.or_hex8_internal_gl.argtypes = [_f64p, d, d, _f64p, _f64p, ctypes.c_void_p]
         L.or_quad4_membrane_internal.argtypes = [_f64p, d, d, d, _f64p, _f64p, vp]
         L.or_quad4_heat_internal.argtypes = [_f64p, d, d, d, d, _f64p, i32, _f64p, vp]
         L.or_quad4_heat_internal_sens.argtypes = [_f64p, d, d, d, _f64p, _f64p]
@@ -130,6 +131,17 @@ def hex8_internal(X, E, nu, u=None, want_K=True):
     K = np.zeros(576) if want_K else None
     rc = lib().or_hex8_internal(X, E, nu, u, f, _ptr(K))
     if rc:
+        raise ValueError("degenerate HEX8 element")
+    return f, (K.reshape(24, 24) if want_K else None)
+
+
+def hex8_internal_gl(X, E, nu, u, want_K=True):
+    """Green-Lagrange (total Lagrangian) HEX8 residual and tangent, var-blocked dofs."""
+    X = np.ascontiguousarray(X, dtype=np.float64).reshape(24)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    f = np.zeros(24)
+    K = np.zeros(576) if want_K else None
+    if lib().or_hex8_internal_gl(X, E, nu, u, f, _ptr(K)):
         raise ValueError("degenerate HEX8 element")
     return f, (K.reshape(24, 24) if want_K else None)
 
