@@ -33,6 +33,8 @@
  *                              calculate_output_adjoint_sensitivity_multiple_parameters_no_direct
  *                              (src/elasticity/compliance_output.cpp:71-296,
  *                              src/base/assembly_base.cpp:253-333, 594-639)
+ *   mg_adjoint_solve           MAST::NonlinearSystem::adjoint_solve
+ *                              (src/base/nonlinear_system.cpp:798-847)
  *   mg_mean_temperature        an OutputAssemblyElemOperations subclass
  *                              (src/base/output_assembly_elem_operations.h:64-250)
  *                              with NonlinearSystem::adjoint_solve
@@ -69,7 +71,11 @@ typedef enum mg_status {
 typedef enum mg_physics {
     MG_PHYSICS_ELASTICITY_HEX8 = 0, /* StructuralElement3D, 3 translational dofs/node */
     MG_PHYSICS_MEMBRANE_QUAD4 = 1,  /* StructuralElement2D membrane, 2 dofs/node */
-    MG_PHYSICS_HEAT_QUAD4 = 2       /* HeatConductionElementBase, 1 dof/node */
+    MG_PHYSICS_HEAT_QUAD4 = 2,      /* HeatConductionElementBase, 1 dof/node */
+    MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR = 3 /* StructuralElement3D with the section's strain
+                                                type MAST::NONLINEAR_STRAIN (Green-Lagrange,
+                                                total Lagrangian; element_property_card_base.h:
+                                                36-41): Newton on the plain FP64 form */
 } mg_physics;
 
 typedef enum mg_precision {
@@ -190,7 +196,13 @@ const double *mg_solution_device(mg_problem *p);
 /* ---- outputs and sensitivities ---- */
 int mg_sensitivity_assemble(mg_problem *p, const double *X, int32_t param_kind,
                             int64_t param_index, double *dRdp);
+/* compliance C = F.X; dc_drho (nullable) by the adjoint: lambda = -X for the linear
+   form, K_T(X) lambda = F on the GPU for MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR */
 int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc_drho);
+/* J(X)^T lambda = rhs with the consistent Jacobian at X (host vectors; constrained
+   rows give lambda = 0); the Krylov method of opts (BiCGStab for heat) */
+int mg_adjoint_solve(mg_problem *p, const double *X, const double *rhs, const mg_solve_opts *opts,
+                     double *lambda);
 int mg_mean_temperature(mg_problem *p, const double *T, const mg_solve_opts *opts,
                         double *qbar, double *dq_dk0, double *dq_ds);
 

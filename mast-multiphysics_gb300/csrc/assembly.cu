@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "hex8_gl.cuh"
 #include "mg_internal.h"
 
 namespace mg {
@@ -204,6 +205,95 @@ __global__ void __launch_bounds__(256) hex8_kernel(
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc_mode2 += __shfl_xor_sync(full, acc_mode2, o);
             if (lane == 0) out[e] = E_elem[e] * acc_mode2;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Green-Lagrange HEX8 (the NONLINEAR_STRAIN branch, hex8_gl.cuh): one warp per
+// element, four warps per block, the element workspace in shared memory.
+// MODE 0: scatter the tangent (vals != null) and the internal force (R != null)
+// of coloured elements; MODE 1: element tangent (var-blocked) and force;
+// MODE 2: out[e] = E_elem[e] a_e . f1_e(X) with f1 the internal force at unit
+// modulus (f_int is linear in E at fixed displacement: the density term of the
+// adjoint sensitivity, E_elem = dE/drho).
+// ---------------------------------------------------------------------------
+constexpr int kGlWarps = 4;
+
+template <int MODE>
+__global__ void __launch_bounds__(kGlWarps * 32) hex8_gl_kernel(
+    const double *__restrict__ coords, const int32_t *__restrict__ conn,
+    const int32_t *__restrict__ elem_list, int64_t first, int64_t n_items,
+    const double *__restrict__ E_elem, double lam1, double mu1, const double *__restrict__ Xg,
+    const int32_t *__restrict__ rowptr, const uint16_t *__restrict__ emap,
+    double *__restrict__ vals, double *__restrict__ R, double *__restrict__ Ke_out,
+    double *__restrict__ fe_out, const double *__restrict__ va, const uint8_t *__restrict__ fixed,
+    double *__restrict__ out, int *__restrict__ status) {
+    __shared__ gl::Work sh[kGlWarps];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    gl::Work &s = sh[w];
+    for (int64_t item = (int64_t)blockIdx.x * kGlWarps + w; item < n_items;
+         item += (int64_t)gridDim.x * kGlWarps) {
+        const int64_t e = elem_list ? elem_list[item] : first + item;
+        const int32_t *en = conn + e * 8;
+        if (lane < 24) {
+            const int64_t g = (int64_t)en[lane / 3] * 3 + lane % 3;
+            s.X[lane] = coords[g];
+            s.u[lane] = Xg[g];
+        }
+        __syncwarp();
+        if (!gl::phase_jacobian(s, lane)) atomicOr(status, 1);
+        __syncwarp();
+        gl::phase_gradients(s, lane);
+        __syncwarp();
+        const double Ee = (MODE == 2) ? 1.0 : E_elem[e];
+        const double lam = Ee * lam1, mu = Ee * mu1;
+        gl::phase_stress(s, lane, lam, mu);
+        __syncwarp();
+        gl::phase_projections(s, lane);
+        __syncwarp();
+        if (MODE == 2) {
+            double acc = 0.0;
+            if (lane < 24) {
+                const int64_t g = (int64_t)en[lane / 3] * 3 + lane % 3;
+                const double a = (fixed && fixed[g]) ? 0.0 : va[g];
+                acc = a * gl::phase_force(s, lane);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) out[e] = E_elem[e] * acc;
+        } else {
+            if (lane < 24) {
+                const int a = lane / 3, i = lane % 3;
+                const double fl = gl::phase_force(s, lane);
+                if (MODE == 0 && R) R[(int64_t)en[a] * 3 + i] += fl;
+                if (MODE == 1 && fe_out) fe_out[(e - first) * 24 + i * 8 + a] = fl;
+            }
+            if (MODE == 1 || vals) {
+#pragma unroll 1
+                for (int h = 0; h < 2; h++) {
+                    const int p = lane + 32 * h, a = p >> 3, b = p & 7;
+                    double K[9];
+                    gl::phase_tangent(s, a, b, lam, mu, K);
+                    if (MODE == 0) {
+                        const int64_t na = en[a];
+                        const int off = emap[e * 64 + a * 8 + b];
+#pragma unroll
+                        for (int i = 0; i < 3; i++) {
+                            double *dst = vals + rowptr[na * 3 + i] + off;
+#pragma unroll
+                            for (int j = 0; j < 3; j++) dst[j] += K[i * 3 + j];
+                        }
+                    } else {
+                        double *dst = Ke_out + (e - first) * 576;
+#pragma unroll
+                        for (int i = 0; i < 3; i++)
+#pragma unroll
+                            for (int j = 0; j < 3; j++) dst[(i * 8 + a) * 24 + j * 8 + b] = K[i * 3 + j];
+                    }
+                }
+            }
         }
         __syncwarp();
     }
@@ -586,6 +676,39 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
         if (want_jacobian) p->jacobian_valid = true;
         return MG_OK;
     }
+    if (p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
+        // tangent and internal force both depend on X: R = f_int(X) - F
+        double lam1, mu1;
+        lame_3d(p->mat.nu, lam1, mu1);
+        if (want_jacobian)
+            MG_CUDA_TRY(cudaMemsetAsync(p->A.vals, 0, p->A.nnz * sizeof(double), p->stream));
+        if (d_R) MG_CUDA_TRY(cudaMemsetAsync(d_R, 0, p->n_dofs * sizeof(double), p->stream));
+        for (int c = 0; c < p->n_colors; c++) {
+            int64_t cnt = p->color_ptr[c + 1] - p->color_ptr[c];
+            hex8_gl_kernel<0><<<blocks_for(cnt, kGlWarps), kGlWarps * 32, 0, p->stream>>>(
+                p->d_coords, p->d_conn, p->d_color_elems + p->color_ptr[c], 0, cnt, p->d_E, lam1,
+                mu1, d_X, p->A.rowptr, p->d_emap, want_jacobian ? p->A.vals : nullptr, d_R, nullptr,
+                nullptr, nullptr, nullptr, nullptr, st);
+            MG_CUDA_TRY(cudaGetLastError());
+        }
+        count_launches(p->n_colors);
+        if (want_jacobian && (p->n_fix_zero || p->n_fix_diag)) {
+            int64_t m = p->n_fix_zero > p->n_fix_diag ? p->n_fix_zero : p->n_fix_diag;
+            fix_kernel<<<blocks_for(m, 256), 256, 0, p->stream>>>(p->A.vals, p->d_fix_zero,
+                                                                  p->n_fix_zero, p->d_fix_diag,
+                                                                  p->n_fix_diag);
+            MG_CUDA_TRY(cudaGetLastError());
+        }
+        if (d_R) {
+            residual_finish_kernel<<<blocks_for(p->n_dofs, 256), 256, 0, p->stream>>>(
+                d_R, d_X, p->d_F, p->d_fixed, p->n_dofs);
+            MG_CUDA_TRY(cudaGetLastError());
+        }
+        MG_TRY(read_status(p, st));
+        // the CSR holds the tangent at this X only
+        p->jacobian_valid = false;
+        return MG_OK;
+    }
     // linear elasticity / membrane: K depends on the design only
     if (need_K && !p->jacobian_valid) {
         MG_CUDA_TRY(cudaMemsetAsync(p->A.vals, 0, p->A.nnz * sizeof(double), p->stream));
@@ -644,6 +767,12 @@ int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t co
         hex8_kernel<1><<<blocks_for(count, kWarpsPerBlock), 256, 0, p->stream>>>(
             p->d_coords, p->d_conn, nullptr, first, count, p->d_E, lam1, mu1, nullptr, nullptr,
             nullptr, d_Ke, nullptr, nullptr, nullptr, nullptr, st);
+    } else if (p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
+        double lam1, mu1;
+        lame_3d(p->mat.nu, lam1, mu1);
+        hex8_gl_kernel<1><<<blocks_for(count, kGlWarps), kGlWarps * 32, 0, p->stream>>>(
+            p->d_coords, p->d_conn, nullptr, first, count, p->d_E, lam1, mu1, d_X, nullptr,
+            nullptr, nullptr, nullptr, d_Ke, d_fe, nullptr, nullptr, nullptr, st);
     } else if (p->physics == MG_PHYSICS_MEMBRANE_QUAD4) {
         double nu = p->mat.nu;
         membrane_kernel<1><<<blocks_for(count, 128), 128, 0, p->stream>>>(
@@ -656,7 +785,8 @@ int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t co
             nullptr, nullptr, nullptr, d_Ke, d_fe, st);
     }
     MG_CUDA_TRY(cudaGetLastError());
-    if (p->physics != MG_PHYSICS_HEAT_QUAD4 && d_fe) {
+    if (p->physics != MG_PHYSICS_HEAT_QUAD4 && p->physics != MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR &&
+        d_fe) {
         elem_matvec_kernel<<<blocks_for(count * nd, 128), 128, 0, p->stream>>>(
             d_Ke, d_X, p->d_conn, first, count, p->npe, p->dpn, d_fe);
         MG_CUDA_TRY(cudaGetLastError());
@@ -677,6 +807,13 @@ int elem_sensitivity(mg_problem *p, const double *d_X, const double *d_lambda, i
         hex8_kernel<2><<<blocks_for(p->n_elems, kWarpsPerBlock), 256, 0, p->stream>>>(
             p->d_coords, p->d_conn, nullptr, 0, p->n_elems, p->d_dE, lam1, mu1, nullptr,
             nullptr, nullptr, nullptr, d_lambda, d_X, p->d_fixed, d_out_elem, st);
+    } else if (p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR && kind == MG_PARAM_DENSITY) {
+        // out[e] = dE_e lambda_e . f1_e(X)
+        double lam1, mu1;
+        lame_3d(p->mat.nu, lam1, mu1);
+        hex8_gl_kernel<2><<<blocks_for(p->n_elems, kGlWarps), kGlWarps * 32, 0, p->stream>>>(
+            p->d_coords, p->d_conn, nullptr, 0, p->n_elems, p->d_dE, lam1, mu1, d_X, nullptr,
+            nullptr, nullptr, nullptr, nullptr, nullptr, d_lambda, p->d_fixed, d_out_elem, st);
     } else if (p->physics == MG_PHYSICS_HEAT_QUAD4 &&
                (kind == MG_PARAM_K0 || kind == MG_PARAM_ELEM_SCALE)) {
         heat_sens_kernel<<<blocks_for(p->n_elems, 128), 128, 0, p->stream>>>(
@@ -698,18 +835,26 @@ int assemble_param_residual(mg_problem *p, const double *d_X, int kind, int64_t 
     int *st = status_slot(p);
     MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(int), p->stream));
     MG_CUDA_TRY(cudaMemsetAsync(d_dRdp, 0, p->n_dofs * sizeof(double), p->stream));
-    if (p->physics == MG_PHYSICS_ELASTICITY_HEX8 && kind == MG_PARAM_DENSITY) {
+    if ((p->physics == MG_PHYSICS_ELASTICITY_HEX8 ||
+         p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) && kind == MG_PARAM_DENSITY) {
         if (index < 0 || index >= p->n_elems) return MG_EINVAL;
-        // one element: Ke1 * dE, then f = Ke X_e scattered (single element: no races)
-        double *Ke = p->d_tmp2;  // needs 576 doubles
+        // one element: f = dE K1 X_e (linear) or dE f1(X_e) (nonlinear strain: f_int is
+        // linear in E at fixed X), scattered on the host (single element: no races)
+        double *Ke = p->d_tmp2;  // needs 600 doubles
+        double *fe = Ke + 576;
         double lam1, mu1;
         lame_3d(p->mat.nu, lam1, mu1);
-        hex8_kernel<1><<<1, 256, 0, p->stream>>>(p->d_coords, p->d_conn, nullptr, index, 1,
-                                                 p->d_dE, lam1, mu1, nullptr, nullptr, nullptr,
-                                                 Ke, nullptr, nullptr, nullptr, nullptr, st);
-        MG_CUDA_TRY(cudaGetLastError());
-        double *fe = Ke + 576;
-        elem_matvec_kernel<<<1, 32, 0, p->stream>>>(Ke, d_X, p->d_conn, index, 1, 8, 3, fe);
+        if (p->physics == MG_PHYSICS_ELASTICITY_HEX8) {
+            hex8_kernel<1><<<1, 256, 0, p->stream>>>(p->d_coords, p->d_conn, nullptr, index, 1,
+                                                     p->d_dE, lam1, mu1, nullptr, nullptr, nullptr,
+                                                     Ke, nullptr, nullptr, nullptr, nullptr, st);
+            MG_CUDA_TRY(cudaGetLastError());
+            elem_matvec_kernel<<<1, 32, 0, p->stream>>>(Ke, d_X, p->d_conn, index, 1, 8, 3, fe);
+        } else {
+            hex8_gl_kernel<1><<<1, kGlWarps * 32, 0, p->stream>>>(
+                p->d_coords, p->d_conn, nullptr, index, 1, p->d_dE, lam1, mu1, d_X, nullptr,
+                nullptr, nullptr, nullptr, Ke, fe, nullptr, nullptr, nullptr, st);
+        }
         MG_CUDA_TRY(cudaGetLastError());
         std::vector<double> hfe(24);
         std::vector<int32_t> en(8);

@@ -171,7 +171,8 @@ int create_impl(const mg_mesh_desc *mesh, const mg_material_desc *mat, const mg_
                 mg_problem *p) {
     p->physics = mesh->physics;
     switch (mesh->physics) {
-        case MG_PHYSICS_ELASTICITY_HEX8: p->dim = 3; p->npe = 8; p->dpn = 3; break;
+        case MG_PHYSICS_ELASTICITY_HEX8:
+        case MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR: p->dim = 3; p->npe = 8; p->dpn = 3; break;
         case MG_PHYSICS_MEMBRANE_QUAD4: p->dim = 2; p->npe = 4; p->dpn = 2; break;
         case MG_PHYSICS_HEAT_QUAD4: p->dim = 2; p->npe = 4; p->dpn = 1; break;
         default: set_error("unknown physics %d", mesh->physics); return MG_EINVAL;
@@ -196,7 +197,7 @@ int create_impl(const mg_mesh_desc *mesh, const mg_material_desc *mat, const mg_
         set_error("E0 must be positive");
         return MG_EINVAL;
     }
-    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8 && !(mat->thickness > 0)) {
+    if (p->dim == 2 && !(mat->thickness > 0)) {
         set_error("2D section thickness must be positive");
         return MG_EINVAL;
     }
@@ -407,8 +408,9 @@ int create_impl(const mg_mesh_desc *mesh, const mg_material_desc *mat, const mg_
     return MG_OK;
 }
 
-int newton_heat(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
-    // NonlinearSystem::solve under SNES Newton: J dT = -R, T += dT
+int newton_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
+    // NonlinearSystem::solve under SNES Newton: J dX = -R, X += dX (heat conduction and the
+    // nonlinear-strain HEX8 element)
     double r0 = -1.0, rn = 0.0;
     int kry = 0, it_newton = 0, rc = MG_OK;
     const int maxn = o.max_newton > 0 ? o.max_newton : 30;
@@ -651,9 +653,11 @@ int mg_solve(mg_problem *p, const mg_solve_opts *opts, double *X, mg_solve_repor
     }
     int rc;
     if (o.precision == MG_PLAIN_FP64) {
-        rc = (p->physics == MG_PHYSICS_HEAT_QUAD4) ? newton_heat(p, o, &r) : solve_linear(p, o, &r);
+        rc = (p->physics == MG_PHYSICS_HEAT_QUAD4 || p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR)
+                 ? newton_solve(p, o, &r)
+                 : solve_linear(p, o, &r);
     } else {
-        if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) { set_error("mixed precision needs HEX8 SIMP"); return MG_ENOTSUP; }
+        if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) { set_error("mixed precision needs the linear-strain HEX8 SIMP form"); return MG_ENOTSUP; }
         rc = matfree_solve(p, o, &r);
     }
     p->last_solve_mixed = (o.precision != MG_PLAIN_FP64);
@@ -689,13 +693,32 @@ int mg_sensitivity_assemble(mg_problem *p, const double *X, int32_t kind, int64_
 
 int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc) {
     if (!p) return MG_EINVAL;
-    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) return MG_ENOTSUP;
+    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8 && p->physics != MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR)
+        return MG_ENOTSUP;
     const double *dX = p->d_X;
     if (X) {
         MG_TRY(to_device_vec(p, X, p->d_tmp, p->n_dofs));
         dX = p->d_tmp;
     }
     if (compliance) MG_TRY(dot(p, p->d_F, dX, p->n_dofs, compliance));
+    if (dc && p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
+        // C = F.u with f_int(u, rho) = F: dC/drho_e = -lambda . d f_int / d rho_e, where
+        // K_T(u)^T lambda = F (the tangent is symmetric) and d f_int / d rho_e = dE_e f1_e(u)
+        // (AssemblyBase::calculate_output_adjoint_sensitivity, assembly_base.cpp:555-590)
+        mg_solve_opts o;
+        mg_default_solve_opts(&o);
+        o.rtol = 1e-13;
+        MG_TRY(assemble_system(p, dX, nullptr, true, true));
+        double *lam = p->d_R;
+        MG_CUDA_TRY(cudaMemsetAsync(lam, 0, p->n_dofs * 8, p->stream));
+        int its = 0;
+        double rr = 0;
+        MG_TRY(krylov_solve(p, p->A, p->d_F, lam, o, MG_KRYLOV_CG, &its, &rr));
+        MG_TRY(elem_sensitivity(p, dX, lam, MG_PARAM_DENSITY, p->d_elem_out));
+        MG_TRY(to_host_vec(p, p->d_elem_out, dc, p->n_elems));
+        for (int64_t e = 0; e < p->n_elems; e++) dc[e] = -dc[e];
+        return MG_OK;
+    }
     if (dc && p->last_solve_mixed && !X) {
         // structured grid after a mixed solve: shared-K0 FP64 sensitivity kernel
         return matfree_sensitivity(p, dc);
@@ -707,6 +730,38 @@ int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc
         for (int64_t e = 0; e < p->n_elems; e++) dc[e] = -dc[e];
     }
     return MG_OK;
+}
+
+int mg_adjoint_solve(mg_problem *p, const double *X, const double *rhs, const mg_solve_opts *opts,
+                     double *lambda) {
+    // NonlinearSystem::adjoint_solve (nonlinear_system.cpp:798-847): J(X)^T lambda = rhs on the
+    // consistent Jacobian; constrained rows give lambda_d = 0
+    if (!p || !X || !rhs || !lambda) return MG_EINVAL;
+    mg_solve_opts o;
+    if (opts) o = *opts; else mg_default_solve_opts(&o);
+    std::vector<double> b(rhs, rhs + p->n_dofs);
+    for (int64_t i = 0; i < p->n_dofs; i++)
+        if (p->h_fixed[i]) b[i] = 0.0;
+    MG_TRY(to_device_vec(p, X, p->d_tmp, p->n_dofs));
+    MG_TRY(to_device_vec(p, b.data(), p->d_R, p->n_dofs));
+    if (p->physics == MG_PHYSICS_HEAT_QUAD4) p->jacobian_valid = false;
+    MG_TRY(assemble_system(p, p->d_tmp, nullptr, true, true));
+    double *lam = p->d_tmp2;
+    MG_CUDA_TRY(cudaMemsetAsync(lam, 0, p->n_dofs * 8, p->stream));
+    int its = 0;
+    double rr = 0;
+    int rc;
+    if (p->physics == MG_PHYSICS_HEAT_QUAD4) {
+        CsrMatrix At;
+        MG_TRY(transpose_csr(p, p->A, &At));
+        rc = krylov_solve(p, At, p->d_R, lam, o, MG_KRYLOV_BICGSTAB, &its, &rr);
+        free_csr(&At);
+    } else {
+        // elasticity: the (tangent) stiffness is symmetric
+        rc = krylov_solve(p, p->A, p->d_R, lam, o, o.krylov, &its, &rr);
+    }
+    if (rc != MG_OK) return rc;
+    return to_host_vec(p, lam, lambda, p->n_dofs);
 }
 
 int mg_mean_temperature(mg_problem *p, const double *T, const mg_solve_opts *opts, double *qbar,

@@ -277,8 +277,15 @@ private:
     std::vector<std::unique_ptr<MatrixFunction>> _m;
 };
 
+// ElementPropertyCardBase's strain type (element_property_card_base.h:36-41,
+// set_strain / strain_type :183-194): NONLINEAR_STRAIN selects the Green-Lagrange
+// branch of the 3D solid element
+enum StrainType { LINEAR_STRAIN, NONLINEAR_STRAIN };
+
 class ElementPropertyCardBase : public MaterialPropertyCardBase {
 public:
+    void set_strain(StrainType strain) { _strain = strain; }
+    StrainType strain_type() const { return _strain; }
     void set_material(const IsotropicMaterialPropertyCard &m) { _mat = &m; }
     const IsotropicMaterialPropertyCard &get_material() const {
         if (!_mat) throw std::runtime_error("element property card has no material");
@@ -288,6 +295,7 @@ public:
 
 private:
     const IsotropicMaterialPropertyCard *_mat = nullptr;
+    StrainType _strain = LINEAR_STRAIN;
 };
 
 class Solid3DSectionElementPropertyCard : public ElementPropertyCardBase {
@@ -633,6 +641,20 @@ public:
         if (!_p) _create();
         return _p;
     }
+    // mg_physics of the handle (the section's strain type decides the 3D solid branch)
+    int physics() {
+        problem();
+        return _phys;
+    }
+    // the external load vector F (point loads; zero on constrained dofs)
+    Vector load_vector() {
+        const int64_t n = (int64_t)_sys->n_vars() * _sys->mesh().n_nodes();
+        problem();
+        Vector F(n);
+        for (size_t i = 0; i < _ldofs.size(); i++) F(_ldofs[i]) += _lvals[i];
+        for (int64_t d : _fixed) F(d) = 0.0;
+        return F;
+    }
 
     // R = f_int - f_ext at X (R, J nullable); J is the assembled CSR with
     // Dirichlet rows eliminated
@@ -693,7 +715,7 @@ public:
         (void)elem_ops;
         sens.assign(p_vec.size(), 0.0);
         mg_problem *p = problem();
-        if (dynamic_cast<ComplianceOutput *>(&output)) {
+        if (dynamic_cast<ComplianceOutput *>(&output) && physics() != MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
             // the library forms -u^T dK/drho u with its own adjoint (lambda = -u)
             for (size_t i = 0; i < X.size(); i++)
                 if (std::fabs(adj_sol(i) + X(i)) > 1e-12 * (1 + std::fabs(X(i))))
@@ -745,7 +767,10 @@ private:
         const ElementPropertyCardBase &prop = _disc->property();
         const IsotropicMaterialPropertyCard &mat = prop.get_material();
         mg_material_desc md{};
-        const int phys = _ops->physics(m);
+        int phys = _ops->physics(m);
+        if (phys == MG_PHYSICS_ELASTICITY_HEX8 && prop.strain_type() == NONLINEAR_STRAIN)
+            phys = MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR;
+        _phys = phys;
         if (phys == MG_PHYSICS_HEAT_QUAD4) {
             md.k0 = mat.value("k_th");
             md.k_beta = mat.contains("k_beta") ? mat.value("k_beta") : 0.0;
@@ -834,6 +859,7 @@ private:
     std::vector<int64_t> _fixed, _ldofs;
     std::vector<int32_t> _ce, _cs;
     Real _Emin = 1e-9, _penal = 3.0, _res_l2 = 0.0;
+    int _phys = -1;
 };
 
 inline void NonlinearSystem::solve(AssemblyElemOperations &, NonlinearImplicitAssembly &assembly) {
@@ -847,10 +873,19 @@ inline void NonlinearSystem::solve(AssemblyElemOperations &, NonlinearImplicitAs
 
 inline void NonlinearSystem::adjoint_solve(const Vector &X, bool, AssemblyElemOperations &,
                                            OutputAssemblyElemOperations &output,
-                                           NonlinearImplicitAssembly &, Vector &adjoint) {
+                                           NonlinearImplicitAssembly &assembly, Vector &adjoint) {
     if (!dynamic_cast<ComplianceOutput *>(&output))
         throw std::runtime_error("adjoint_solve: the GPU path forms the mean-temperature adjoint inside "
                                  "mg_mean_temperature; use calculate_output_adjoint_sensitivity");
+    if (assembly.physics() == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
+        // C = F.u: K_T(u)^T lambda = -dC/du = -F on the tangent at X
+        Vector rhs = assembly.load_vector();
+        for (size_t i = 0; i < rhs.size(); i++) rhs(i) = -rhs(i);
+        adjoint.resize(X.size());
+        check(mg_adjoint_solve(assembly.problem(), X.data(), rhs.data(), &opts, adjoint.data()),
+              "NonlinearSystem::adjoint_solve");
+        return;
+    }
     // compliance is self-adjoint: K lambda = -f  =>  lambda = -u (example_6.cpp:877-939)
     adjoint.resize(X.size());
     for (size_t i = 0; i < X.size(); i++) adjoint(i) = -X(i);

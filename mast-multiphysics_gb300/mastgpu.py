@@ -82,6 +82,7 @@ def build(force=False, verbose=False):
 MG_OK, MG_EINVAL, MG_ENOMEM, MG_ENOCONV, MG_EBREAKDOWN, MG_ENAN = 0, -1, -2, -3, -4, -5
 MG_ETIMEDOUT, MG_ECUDA, MG_ENOTSUP, MG_EBUSY, MG_EBADELEM = -6, -7, -8, -9, -10
 PHYS_HEX8, PHYS_MEMBRANE, PHYS_HEAT = 0, 1, 2
+PHYS_HEX8_NONLINEAR = 3  # Green-Lagrange strain (MAST::NONLINEAR_STRAIN), Newton
 PLAIN_FP64, MIXED_TF32, MIXED_BF16, MIXED_TF32X3, MIXED_BF16X3 = 0, 1, 2, 3, 4
 KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
 PC_JACOBI, PC_MULTIGRID = 0, 1
@@ -205,6 +206,7 @@ def lib(autobuild=True):
     L.mg_solution_device.restype = _vp
     L.mg_sensitivity_assemble.argtypes = [_vp, _vp, _i32, _i64, _vp]
     L.mg_compliance.argtypes = [_vp, _vp, _vp, _vp]
+    L.mg_adjoint_solve.argtypes = [_vp, _vp, _vp, ctypes.POINTER(SolveOpts), _vp]
     L.mg_mean_temperature.argtypes = [_vp, _vp, ctypes.POINTER(SolveOpts), _vp, _vp, _vp]
     L.mg_debug_matfree_apply.argtypes = [_vp, ctypes.c_int, _vp, _vp]
     L.mg_compliance_resident.argtypes = [_vp, _vp]
@@ -325,7 +327,7 @@ class Problem:
         self.coords = np.ascontiguousarray(coords, dtype=np.float64)
         self.conn = np.ascontiguousarray(conn, dtype=np.int32)
         self.physics = physics
-        self.dpn = {PHYS_HEX8: 3, PHYS_MEMBRANE: 2, PHYS_HEAT: 1}[physics]
+        self.dpn = {PHYS_HEX8: 3, PHYS_HEX8_NONLINEAR: 3, PHYS_MEMBRANE: 2, PHYS_HEAT: 1}[physics]
         self.n_nodes = self.coords.shape[0]
         self.n_elems = self.conn.shape[0]
         self.n_dofs = self.n_nodes * self.dpn
@@ -399,7 +401,7 @@ class Problem:
         return rowptr, cols, vals
 
     def element_matrices(self, first, count, X=None):
-        nd = {PHYS_HEX8: 24, PHYS_MEMBRANE: 8, PHYS_HEAT: 4}[self.physics]
+        nd = {PHYS_HEX8: 24, PHYS_HEX8_NONLINEAR: 24, PHYS_MEMBRANE: 8, PHYS_HEAT: 4}[self.physics]
         Ke = np.zeros((count, nd, nd))
         fe = np.zeros((count, nd))
         Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
@@ -447,6 +449,16 @@ class Problem:
         dc = np.zeros(self.n_elems) if want_sens else None
         check(lib().mg_compliance(self.h, _p(Xa), ctypes.byref(c), _p(dc)), "mg_compliance")
         return c.value, dc
+
+    def adjoint_solve(self, X, rhs, opts=None):
+        """lambda with J(X)^T lambda = rhs (mg_adjoint_solve)"""
+        Xa = np.ascontiguousarray(X, dtype=np.float64)
+        b = np.ascontiguousarray(rhs, dtype=np.float64)
+        lam = np.zeros(self.n_dofs)
+        o = opts if opts is not None else default_opts()
+        check(lib().mg_adjoint_solve(self.h, _p(Xa), _p(b), ctypes.byref(o), _p(lam)),
+              "mg_adjoint_solve")
+        return lam
 
     def mean_temperature(self, T=None, opts=None, want_sens=True):
         Ta = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
@@ -702,9 +714,11 @@ class Server:
 SIMP_MATERIAL = dict(E0=1.0, Emin=1e-9, nu=0.3, penal=3.0, thickness=1.0, k0=0.0, k_beta=0.0)
 
 
-def simp_cantilever(nx, ny, nz, load_y0=0, load_y1=None, material=None):
-    """HEX8 SIMP cantilever: x=0 face clamped, total -z unit load spread over the
-    nodes of the z=0 edge at x=max between node rows load_y0..load_y1."""
+def simp_cantilever(nx, ny, nz, load_y0=0, load_y1=None, material=None, physics=PHYS_HEX8,
+                    load=1.0):
+    """HEX8 SIMP cantilever: x=0 face clamped, total -z load (magnitude `load`) spread
+    over the nodes of the z=0 edge at x=max between node rows load_y0..load_y1.
+    physics PHYS_HEX8_NONLINEAR gives the Green-Lagrange (large-deflection) form."""
     coords, conn = grid_hex8(nx, ny, nz)
     NX, NY, NZ = nx + 1, ny + 1, nz + 1
     k, j = np.meshgrid(np.arange(NZ), np.arange(NY), indexing="ij")
@@ -714,8 +728,8 @@ def simp_cantilever(nx, ny, nz, load_y0=0, load_y1=None, material=None):
     ys = np.arange(load_y0, y1 + 1)
     load_nodes = nx + NX * ys
     load_dofs = load_nodes * 3 + 2
-    load_vals = np.full(ys.shape[0], -1.0 / ys.shape[0])
-    return Problem(PHYS_HEX8, coords, conn, material or SIMP_MATERIAL, fixed_dofs=fixed,
+    load_vals = np.full(ys.shape[0], -float(load) / ys.shape[0])
+    return Problem(physics, coords, conn, material or SIMP_MATERIAL, fixed_dofs=fixed,
                    load_dofs=load_dofs, load_values=load_vals, grid=(nx, ny, nz))
 
 

@@ -778,6 +778,47 @@ int or_assemble_quad4_heat(int64_t n_nodes, int64_t n_elems, const double *coord
     return 0;
 }
 
+/* NonlinearImplicitAssembly::residual_and_jacobian
+   (src/base/nonlinear_implicit_assembly.cpp:111-186) over the Green-Lagrange
+   HEX8 element: R = f_int(u) - F with node-interleaved global dofs (3 node + c),
+   tangent scattered into the CSR; constrained rows R_d = u_d, rows and columns
+   eliminated with a unit diagonal. */
+int or_assemble_hex8_gl(int64_t n_nodes, int64_t n_elems, const double *coords,
+                        const int32_t *conn, const double *E_elem, double nu, const double *u,
+                        const double *F, const int32_t *rowptr, const int32_t *cols,
+                        double *vals, double *R, const uint8_t *fixed) {
+    int64_t n = n_nodes * 3;
+    if (vals) memset(vals, 0, (size_t)rowptr[n] * sizeof(double));
+    if (R) memset(R, 0, (size_t)n * sizeof(double));
+    for (int64_t e = 0; e < n_elems; e++) {
+        const int32_t *en = conn + e * 8;
+        double X[24], ue[24], f[24], K[576];
+        for (int a = 0; a < 8; a++)
+            for (int d = 0; d < 3; d++) {
+                X[a * 3 + d] = coords[(int64_t)en[a] * 3 + d];
+                ue[d * 8 + a] = u[(int64_t)en[a] * 3 + d];
+            }
+        if (or_hex8_internal_gl(X, E_elem[e], nu, ue, f, vals ? K : NULL)) return -1;
+        for (int a = 0; a < 8; a++)
+            for (int i = 0; i < 3; i++) {
+                int64_t row = (int64_t)en[a] * 3 + i;
+                if (R) R[row] += f[i * 8 + a];
+                if (vals)
+                    for (int b = 0; b < 8; b++) {
+                        int64_t p = csr_find(rowptr, cols, row, en[b] * 3);
+                        for (int j = 0; j < 3; j++) vals[p + j] += K[(i * 8 + a) * 24 + j * 8 + b];
+                    }
+            }
+    }
+    if (R)
+        for (int64_t i = 0; i < n; i++) {
+            if (F) R[i] -= F[i];
+            if (fixed && fixed[i]) R[i] = u[i];
+        }
+    if (vals) apply_fixed(n, rowptr, cols, vals, fixed);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Krylov solvers (the role PETSc KSP plays under SNES, ext.)               */
 /* ------------------------------------------------------------------------ */

@@ -95,6 +95,11 @@ int or_assemble_quad4_heat(int64_t n_nodes, int64_t n_elems, const double *coord
                            const double *T, int consistent,
                            const int32_t *rowptr, const int32_t *cols, double *vals,
                            double *R, const uint8_t *fixed);
+/* Green-Lagrange HEX8: R = f_int(u) - F (F nullable), tangent into vals (nullable) */
+int or_assemble_hex8_gl(int64_t n_nodes, int64_t n_elems, const double *coords,
+                        const int32_t *conn, const double *E_elem, double nu, const double *u,
+                        const double *F, const int32_t *rowptr, const int32_t *cols,
+                        double *vals, double *R, const uint8_t *fixed);
 
 /* Krylov (Jacobi preconditioned); return iterations, <0 on breakdown */
 int or_pcg(int64_t n, const int32_t *rowptr, const int32_t *cols, const double *vals,

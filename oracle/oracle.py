@@ -88,6 +88,8 @@ def lib():
                                                  _i32p, _f64p, vp]
         L.or_assemble_quad4_heat.argtypes = [i64, i64, _f64p, _i32p, d, d, vp, d, vp, i64, vp,
                                              vp, d, d, _f64p, i32, _i32p, _i32p, vp, vp, vp]
+        L.or_assemble_hex8_gl.argtypes = [i64, i64, _f64p, _i32p, _f64p, d, _f64p, vp, _i32p,
+                                          _i32p, vp, vp, vp]
         L.or_pcg.argtypes = [i64, _i32p, _i32p, _f64p, _f64p, _f64p, d, i32,
                              ctypes.POINTER(d)]
         L.or_bicgstab.argtypes = L.or_pcg.argtypes
@@ -256,6 +258,56 @@ def assemble_quad4_heat(coords, conn, k0, beta, s_elem, h, q_elem, conv_elem, co
                                  Tinf, np.ascontiguousarray(T, dtype=np.float64),
                                  int(consistent), rowptr, cols, _ptr(vals), _ptr(R), _ptr(fx))
     return vals, R
+
+
+def assemble_hex8_gl(coords, conn, E_elem, nu, u, F, rowptr, cols, fixed, want_K=True):
+    """Green-Lagrange HEX8 system at u: (CSR values of the tangent or None, R = f_int - F)."""
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    n = coords.shape[0] * 3
+    vals = np.zeros(cols.shape[0]) if want_K else None
+    R = np.zeros(n)
+    Fv = None if F is None else np.ascontiguousarray(F, dtype=np.float64)
+    fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+    if lib().or_assemble_hex8_gl(coords.shape[0], conn.shape[0], coords.reshape(-1),
+                                 conn.reshape(-1), np.ascontiguousarray(E_elem, dtype=np.float64),
+                                 nu, np.ascontiguousarray(u, dtype=np.float64), _ptr(Fv), rowptr,
+                                 cols, _ptr(vals), _ptr(R), _ptr(fx)):
+        raise ValueError("degenerate element in assembly")
+    return vals, R
+
+
+def newton_hex8_gl(coords, conn, E_elem, nu, F, fixed, rtol=1e-10, max_newton=30,
+                   krylov_rtol=1e-13):
+    """NonlinearSystem::solve under Newton (src/base/nonlinear_system.cpp:209-235):
+    J du = R, u -= du until ||R|| <= rtol ||R0||.  Returns u and the ||R|| history."""
+    rowptr, cols = csr_pattern(conn, coords.shape[0], 3)
+    u = np.zeros(coords.shape[0] * 3)
+    hist = []
+    for _ in range(max_newton + 1):
+        vals, R = assemble_hex8_gl(coords, conn, E_elem, nu, u, F, rowptr, cols, fixed)
+        hist.append(float(np.linalg.norm(R)))
+        if hist[-1] <= rtol * hist[0] or hist[-1] == 0.0 or len(hist) > max_newton:
+            break
+        du, _, _ = pcg(rowptr, cols, vals, R, krylov_rtol, 100000)
+        u -= du
+    return u, hist
+
+
+def hex8_gl_compliance_sens(coords, conn, dE_elem, nu, u, E_elem, F, fixed):
+    """Adjoint density sensitivity of C = F.u at the equilibrium u of the Green-Lagrange
+    system (AssemblyBase::calculate_output_adjoint_sensitivity, assembly_base.cpp:555-590):
+    K_T(u) lambda = F, dC/drho_e = -dE_e lambda_e . f1_e(u), f1 the unit-modulus force."""
+    rowptr, cols = csr_pattern(conn, coords.shape[0], 3)
+    vals, _ = assemble_hex8_gl(coords, conn, E_elem, nu, u, F, rowptr, cols, fixed)
+    lam, _, _ = pcg(rowptr, cols, vals, np.where(np.asarray(fixed) == 1, 0.0, F), 1e-14, 100000)
+    dc = np.zeros(conn.shape[0])
+    for e in range(conn.shape[0]):
+        ue = u.reshape(-1, 3)[conn[e]].T.reshape(-1)
+        le = lam.reshape(-1, 3)[conn[e]].T.reshape(-1)
+        f1, _ = hex8_internal_gl(coords[conn[e]], 1.0, nu, ue, want_K=False)
+        dc[e] = -dE_elem[e] * float(le @ f1)
+    return dc
 
 
 def spmv(rowptr, cols, vals, x):

@@ -5,6 +5,7 @@
 // here is the FP64 oracle (oracle/mast_oracle.h), itself pinned to the
 // reference's known answers by tests/test_oracle_pins.py.
 #include <cmath>
+#include <memory>
 #include <random>
 #include <vector>
 
@@ -234,6 +235,134 @@ TEST_CASE("hex8_simp_cantilever", "[gpu],[structural],[3D]") {
     Real s = 0;
     for (size_t k = 0; k < dR.size(); k++) s += adjoint(k) * dR(k);
     CHECK(s == Approx(sens[3]).epsilon(1e-9));
+}
+
+TEST_CASE("section_strain_type", "[cpu],[property]") {
+    MAST::Solid3DSectionElementPropertyCard section;
+    REQUIRE(section.strain_type() == MAST::LINEAR_STRAIN);
+    section.set_strain(MAST::NONLINEAR_STRAIN);
+    REQUIRE(section.strain_type() == MAST::NONLINEAR_STRAIN);
+}
+
+// the section's NONLINEAR_STRAIN selects the Green-Lagrange element: a
+// large-deflection cantilever solved by Newton through NonlinearSystem::solve,
+// against a Newton iteration on the oracle's assembly; the compliance
+// sensitivity from adjoint_solve + the general adjoint path against central
+// differences of re-solved compliances
+TEST_CASE("hex8_green_lagrange_cantilever", "[gpu],[structural],[3D],[nonlinear]") {
+    const int nx = 6, ny = 2, nz = 2;
+    const double P = 0.01;
+    MAST::Mesh mesh;
+    MAST::MeshTools::Generation::build_cube(mesh, nx, ny, nz, 0, nx, 0, ny, 0, nz);
+    MAST::Parameter E("E_param", 1.0), nu("nu_param", 0.3);
+    MAST::ConstantFieldFunction E_f("E", E), nu_f("nu", nu);
+    MAST::IsotropicMaterialPropertyCard material;
+    material.add(E_f);
+    material.add(nu_f);
+    MAST::Solid3DSectionElementPropertyCard section;
+    section.set_material(material);
+    section.set_strain(MAST::NONLINEAR_STRAIN);
+    MAST::StructuralDiscipline discipline;
+    discipline.set_property_for_subdomain(0, section);
+    MAST::DirichletBoundaryCondition clamp;
+    clamp.init(4, {0, 1, 2});
+    discipline.add_dirichlet_bc(4, clamp);
+    MAST::PointLoadCondition load(MAST::POINT_LOAD);
+    std::vector<int64_t> tip;
+    for (int64_t n : mesh.boundary_nodes(2))
+        if (mesh.point(n).z == 0.0) tip.push_back(n);
+    for (int64_t n : tip) load.add_node(n);
+    load.set_load({0.0, 0.0, -P / tip.size()});
+    discipline.add_point_load(load);
+    MAST::NonlinearSystem sys;
+    MAST::StructuralSystemInitialization init(sys, mesh);
+    MAST::StructuralNonlinearAssemblyElemOperations ops;
+    MAST::NonlinearImplicitAssembly assembly;
+    assembly.set_discipline_and_system(discipline, init, ops);
+    std::vector<Real> rho(mesh.n_elem());
+    for (int64_t e = 0; e < mesh.n_elem(); e++) rho[e] = 0.7 + 0.3 * e / mesh.n_elem();
+    assembly.set_simp(rho, 1e-9, 3.0);
+    REQUIRE(assembly.physics() == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR);
+    sys.opts.rtol = 1e-12;
+    sys.opts.newton_rtol = 1e-12;
+    sys.solve(ops, assembly);
+    REQUIRE(sys.last_report.status == MG_OK);
+    REQUIRE(sys.last_report.newton_iterations >= 3);
+
+    // oracle Newton on the same system
+    const int64_t nn = mesh.n_nodes(), n = 3 * nn, ne = mesh.n_elem();
+    std::vector<int32_t> rowptr(n + 1);
+    const int64_t nnz = or_csr_pattern(8, 3, nn, ne, mesh.conn.data(), rowptr.data(), nullptr);
+    std::vector<int32_t> cols(nnz);
+    or_csr_pattern(8, 3, nn, ne, mesh.conn.data(), rowptr.data(), cols.data());
+    std::vector<double> Em(ne), dEm(ne), F(n, 0.0), u(n, 0.0), vals(nnz), R(n), du(n);
+    for (int64_t e = 0; e < ne; e++) {
+        const double rmin = 1e-9;
+        Em[e] = rmin + (1 - rmin) * std::pow(rho[e], 3.0);
+        dEm[e] = (1 - rmin) * 3.0 * rho[e] * rho[e];
+    }
+    std::vector<uint8_t> fixed(n, 0);
+    for (int64_t nd : mesh.boundary_nodes(4))
+        for (int c = 0; c < 3; c++) fixed[3 * nd + c] = 1;
+    for (int64_t nd : tip) F[3 * nd + 2] -= P / tip.size();
+    double r0 = -1;
+    for (int it = 0; it < 40; it++) {
+        REQUIRE(or_assemble_hex8_gl(nn, ne, mesh.coords.data(), mesh.conn.data(), Em.data(), 0.3, u.data(),
+                                    F.data(), rowptr.data(), cols.data(), vals.data(), R.data(), fixed.data()) == 0);
+        double rn = 0;
+        for (double v : R) rn += v * v;
+        rn = std::sqrt(rn);
+        if (r0 < 0) r0 = rn;
+        if (rn <= 1e-13 * r0) break;
+        std::fill(du.begin(), du.end(), 0.0);
+        double rr = 0;
+        REQUIRE(or_pcg(n, rowptr.data(), cols.data(), vals.data(), R.data(), du.data(), 1e-14, 100000, &rr) >= 0);
+        for (int64_t i = 0; i < n; i++) u[i] -= du[i];
+    }
+    double err = 0, umax = 0;
+    for (int64_t i = 0; i < n; i++) {
+        err = std::max(err, std::fabs(sys.solution(i) - u[i]));
+        umax = std::max(umax, std::fabs(u[i]));
+    }
+    CHECK(err <= 1e-10 * umax);
+
+    // compliance and its adjoint sensitivity (lambda from adjoint_solve)
+    MAST::ComplianceOutput compliance;
+    assembly.calculate_output(sys.solution, false, compliance);
+    const double c0 = compliance.output_total();
+    MAST::Vector adjoint;
+    sys.adjoint_solve(sys.solution, false, ops, compliance, assembly, adjoint);
+    std::vector<std::unique_ptr<MAST::Parameter>> params;
+    std::vector<const MAST::FunctionBase *> p_vec;
+    const int64_t probe[3] = {0, 11, ne - 1};
+    for (int64_t e : probe) {
+        params.emplace_back(new MAST::Parameter(MAST::NonlinearImplicitAssembly::elem_param_name("rho", e), rho[e]));
+        p_vec.push_back(params.back().get());
+    }
+    std::vector<Real> sens;
+    assembly.calculate_output_adjoint_sensitivity_multiple_parameters_no_direct(sys.solution, false, adjoint, p_vec,
+                                                                              ops, compliance, sens);
+    std::vector<double> dc(ne);
+    double cc = 0;
+    REQUIRE(mg_compliance(assembly.problem(), sys.solution.data(), &cc, dc.data()) == MG_OK);
+    CHECK(cc == Approx(c0).epsilon(1e-14));
+    const double h = 1e-5;
+    for (int k = 0; k < 3; k++) {
+        const int64_t e = probe[k];
+        CHECK(sens[k] == Approx(dc[e]).epsilon(1e-9));
+        double cpm[2];
+        for (int s = 0; s < 2; s++) {
+            std::vector<Real> r2 = rho;
+            r2[e] += s == 0 ? h : -h;
+            assembly.set_simp(r2, 1e-9, 3.0);
+            sys.solve(ops, assembly);
+            REQUIRE(sys.last_report.status == MG_OK);
+            assembly.calculate_output(sys.solution, false, compliance);
+            cpm[s] = compliance.output_total();
+        }
+        CHECK(sens[k] == Approx((cpm[0] - cpm[1]) / (2 * h)).epsilon(1e-6));
+    }
+    assembly.set_simp(rho, 1e-9, 3.0);
 }
 
 // dR/drho_e from sensitivity_assemble against a central difference of the

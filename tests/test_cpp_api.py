@@ -42,10 +42,10 @@ def run(tag):
 
 def test_cpp_mirror_cpu_cases():
     out = run("[cpu]")
-    assert "6 test cases" in out
+    assert "7 test cases" in out
 
 
 @pytest.mark.gpu
 def test_cpp_mirror_gpu_cases():
     out = run("[gpu]")
-    assert "3 test cases" in out
+    assert "4 test cases" in out

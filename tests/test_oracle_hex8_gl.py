@@ -75,3 +75,100 @@ def test_rigid_rotation_is_stress_free():
         # the linear element is not invariant under a finite rotation
         fl, _ = O.hex8_internal(X, 1.0, 0.3, var_blocked(disp))
         assert np.abs(fl).max() > 1e-2
+
+
+# ---------------------------------------------------------------- device source on the host
+def _host_element():
+    import ctypes
+    import os
+    import subprocess
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = os.path.join(repo, "tests", "cpp", "_build")
+    os.makedirs(out, exist_ok=True)
+    so = os.path.join(out, "libgl_element_host.so")
+    src = os.path.join(repo, "tests", "cpp", "gl_element_host.cpp")
+    hdr = os.path.join(repo, "mast-multiphysics_gb300", "csrc", "hex8_gl.cuh")
+    if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        r = subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
+                            "-x", "c++", "-I", os.path.dirname(hdr), src, "-o", so],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    L = ctypes.CDLL(so)
+    p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    L.gl_element_host.argtypes = [p, ctypes.c_double, ctypes.c_double, p, p, p]
+    return L
+
+
+@pytest.mark.parametrize("distort,scale", [(0.0, 0.0), (0.1, 0.05), (0.15, 0.3)])
+def test_device_element_source_matches_the_oracle(distort, scale):
+    """The phases of the CUDA element (hex8_gl.cuh), run lane by lane on the host,
+    against the oracle's 6 x 24 strain-operator form: FP64 round-off only."""
+    L = _host_element()
+    X = element(distort, seed=3)
+    u = np.random.default_rng(4).normal(scale=scale, size=24)
+    f = np.zeros(24)
+    K = np.zeros(576)
+    assert L.gl_element_host(np.ascontiguousarray(X.reshape(24)), 3.0, 0.3, u, f, K) == 0
+    fo, Ko = O.hex8_internal_gl(X, 3.0, 0.3, u)
+    K = K.reshape(24, 24)
+    assert np.abs(K - Ko).max() <= 1e-12 * np.abs(Ko).max()
+    assert np.abs(f - fo).max() <= 1e-12 * max(np.abs(fo).max(), np.abs(Ko).max() * max(scale, 1e-3))
+
+
+# ---------------------------------------------------------------- global system
+def beam(nx=4, ny=1, nz=1, load=0.02):
+    coords, conn = O.grid_hex8(nx, ny, nz)
+    nn = coords.shape[0]
+    fixed = np.zeros(nn * 3, np.uint8)
+    F = np.zeros(nn * 3)
+    tip = np.where(coords[:, 0] == nx)[0]
+    fixed[(np.where(coords[:, 0] == 0)[0][:, None] * 3 + np.arange(3)).reshape(-1)] = 1
+    F[tip * 3 + 2] = -load / tip.shape[0]
+    return coords, conn, fixed, F
+
+
+def test_newton_small_load_gives_the_linear_solution():
+    coords, conn, fixed, F = beam(load=1e-7)
+    E = np.full(conn.shape[0], 1.0)
+    u, hist = O.newton_hex8_gl(coords, conn, E, 0.3, F, fixed)
+    rowptr, cols = O.csr_pattern(conn, coords.shape[0], 3)
+    vals = O.assemble_hex8(coords, conn, E, 0.3, rowptr, cols, fixed)
+    ul, _, _ = O.pcg(rowptr, cols, vals, F, 1e-14, 10000)
+    assert np.abs(u - ul).max() <= 1e-5 * np.abs(ul).max()
+
+
+def test_newton_converges_quadratically_under_a_large_load():
+    coords, conn, fixed, F = beam(load=0.05)
+    u, hist = O.newton_hex8_gl(coords, conn, np.full(conn.shape[0], 1.0), 0.3, F, fixed)
+    assert hist[-1] <= 1e-10 * hist[0]
+    # the last steps square the residual (up to the Krylov tolerance)
+    r = np.array(hist) / hist[0]
+    k = int(np.argmax(r < 1e-3))
+    assert r[k + 1] <= 10 * r[k] ** 1.8 or r[k + 1] <= 1e-10
+    # rotation of the tip: the deflection differs from the linear one
+    rowptr, cols = O.csr_pattern(conn, coords.shape[0], 3)
+    vals = O.assemble_hex8(coords, conn, np.full(conn.shape[0], 1.0), 0.3, rowptr, cols, fixed)
+    ul, _, _ = O.pcg(rowptr, cols, vals, F, 1e-14, 10000)
+    assert abs(np.abs(u).max() - np.abs(ul).max()) > 0.02 * np.abs(ul).max()
+
+
+def test_adjoint_compliance_sensitivity_matches_finite_differences():
+    coords, conn, fixed, F = beam(nx=3, load=0.03)
+    d = O.simp_desc(3, 1, 1)
+    rho = np.array([0.9, 0.6, 0.75])
+
+    def compliance(r):
+        E, _ = O.simp_modulus(d, r)
+        u, _ = O.newton_hex8_gl(coords, conn, E, 0.3, F, fixed, rtol=1e-14)
+        return float(F @ u), u
+
+    c0, u0 = compliance(rho)
+    E, dE = O.simp_modulus(d, rho)
+    dc = O.hex8_gl_compliance_sens(coords, conn, dE, 0.3, u0, E, F, fixed)
+    h = 1e-5
+    for e in range(3):
+        rp, rm = rho.copy(), rho.copy()
+        rp[e] += h
+        rm[e] -= h
+        fd = (compliance(rp)[0] - compliance(rm)[0]) / (2 * h)
+        assert abs(dc[e] - fd) <= 1e-6 * abs(fd)
