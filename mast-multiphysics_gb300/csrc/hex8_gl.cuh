@@ -100,23 +100,27 @@ GL_HD void phase_gradients(Work &s, int lane) {
     }
 }
 
-// phase 3 (lanes 0-7, q = lane): Fd, Green-Lagrange strain, S, Fd Fd^T
+// phase 3 (lanes 0-7, q = lane): Fd, Green-Lagrange strain, S, Fd Fd^T.  The
+// strain is formed from H = grad u as (H + H^T + H^T H) / 2, not as
+// (Fd^T Fd - I) / 2, whose subtraction would cancel the leading digits of small
+// strains (a 1e-8 strain would keep only 8 significant digits).
 GL_HD void phase_stress(Work &s, int lane, double lam, double mu) {
     if (lane >= 8) return;
     const int q = lane;
-    double Fd[9];
+    double H[9], Fd[9];
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
-            double v = (i == j) ? 1.0 : 0.0;
+            double v = 0.0;
             for (int a = 0; a < 8; a++) v += s.u[a * 3 + i] * s.g[q][a][j];
-            Fd[i * 3 + j] = v;
+            H[i * 3 + j] = v;
+            Fd[i * 3 + j] = v + (i == j ? 1.0 : 0.0);
         }
     double E[9];
     for (int j = 0; j < 3; j++)
         for (int k = 0; k < 3; k++) {
             double c = 0.0;
-            for (int m = 0; m < 3; m++) c += Fd[m * 3 + j] * Fd[m * 3 + k];
-            E[j * 3 + k] = 0.5 * (c - (j == k ? 1.0 : 0.0));
+            for (int m = 0; m < 3; m++) c += H[m * 3 + j] * H[m * 3 + k];
+            E[j * 3 + k] = 0.5 * (H[j * 3 + k] + H[k * 3 + j] + c);
         }
     const double tr = E[0] + E[4] + E[8];
     for (int j = 0; j < 3; j++)

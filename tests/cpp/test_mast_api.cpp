@@ -355,6 +355,7 @@ TEST_CASE("hex8_green_lagrange_cantilever", "[gpu],[structural],[3D],[nonlinear]
             std::vector<Real> r2 = rho;
             r2[e] += s == 0 ? h : -h;
             assembly.set_simp(r2, 1e-9, 3.0);
+            sys.solution.zero();  // Newton's stop is relative to the initial residual: start from 0
             sys.solve(ops, assembly);
             REQUIRE(sys.last_report.status == MG_OK);
             assembly.calculate_output(sys.solution, false, compliance);

@@ -115,6 +115,20 @@ def test_device_element_source_matches_the_oracle(distort, scale):
     assert np.abs(f - fo).max() <= 1e-12 * max(np.abs(fo).max(), np.abs(Ko).max() * max(scale, 1e-3))
 
 
+@pytest.mark.parametrize("scale", [1e-6, 1e-9])
+def test_device_element_source_keeps_small_strains(scale):
+    """Tiny displacements: the internal force must keep its relative accuracy (a strain
+    formed as (Fd^T Fd - I)/2 would lose the digits that cancel against the identity)."""
+    L = _host_element()
+    X = element(0.1, seed=5)
+    u = np.random.default_rng(6).normal(scale=scale, size=24)
+    f = np.zeros(24)
+    K = np.zeros(576)
+    assert L.gl_element_host(np.ascontiguousarray(X.reshape(24)), 1.0, 0.3, u, f, K) == 0
+    fo, _ = O.hex8_internal_gl(X, 1.0, 0.3, u)
+    assert np.abs(f - fo).max() <= 1e-12 * np.abs(fo).max()
+
+
 # ---------------------------------------------------------------- global system
 def beam(nx=4, ny=1, nz=1, load=0.02):
     coords, conn = O.grid_hex8(nx, ny, nz)
