@@ -62,7 +62,51 @@ def parse():
                     help="only launch one kernel (tensor-core column operator, FP64 CG SpMV or the "
                          "factored multigrid level operator) --steps times after --warmup "
                          "launches; for profilers")
+    ap.add_argument("--nonlinear-assembly", action="store_true",
+                    help="only time the Green-Lagrange HEX8 residual + tangent assembly "
+                         "(64x32x32 cantilever) and print one JSON line")
     return ap.parse_args()
+
+
+def nonlinear_assembly(args, M):
+    """Time the nonlinear-strain HEX8 assembly (residual and tangent of every colour,
+    scattered into the CSR) on a 64x32x32 cantilever at a random 1e-3-strain state.
+    FP64 operations per element, from the per-pair formulation of the element:
+    tangent blocks 64 pairs x 8 points x 82 = 41,984; Jacobians, gradients, stresses,
+    projections and forces about 10,000: about 52,000 in all.  Bytes per element: the 576-entry tangent scattered as
+    read-modify-write (9,216 B), 24 residual entries (384 B), coordinates, state,
+    connectivity and modulus (424 B)."""
+    import torch
+    nx, ny, nz = 64, 32, 32
+    prob = M.simp_cantilever(nx, ny, nz, physics=M.PHYS_HEX8_NONLINEAR, load=0.01)
+    rng = np.random.default_rng(SEED)
+    prob.set_design(rng.uniform(0.3, 1.0, nx * ny * nz))
+    X = np.ascontiguousarray(rng.normal(scale=1e-3, size=prob.n_dofs))
+    stream = torch.cuda.ExternalStream(prob.stream)
+    L = M.lib()
+    M.check(L.mg_debug_launch_assembly(prob.h, M._p(X), max(3, args.warmup)), "warm")
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = max(1, args.steps)
+    e0.record(stream)
+    M.check(L.mg_debug_launch_assembly(prob.h, None, reps), "assembly")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    n_el = nx * ny * nz
+    flops = 52000.0 * n_el
+    bytes_ = (9216 + 384 + 424) * n_el
+    pk = peaks()
+    print(json.dumps({
+        "metric": "nonlinear_hex8_assembly", "workload": "Green-Lagrange HEX8 residual + tangent, "
+        "cantilever 64x32x32 (%d elements, %d colours)" % (n_el, prob.n_colors),
+        "ms_per_assembly": ms, "elements_per_s": n_el / (ms * 1e-3),
+        "fp64_gflops": flops / (ms * 1e-3) / 1e9, "fp64_peak_nominal_gflops": 1250.0,
+        "fp64_frac_of_nominal": flops / (ms * 1e-3) / 1e9 / 1250.0,
+        "GBps": bytes_ / (ms * 1e-3) / 1e9, "hbm_frac": bytes_ / (ms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6800.0),
+        "reps": reps, "dtype": "f64"}))
+    prob.close()
 
 
 PROFILE = os.path.join(REPO, "profiles", "mf_col_kernel_tf32x3_128x64x64.txt")
@@ -381,6 +425,10 @@ def main():
     if args.kernel_only:
         kernel_only(args, M, prob, prec, rho)
         prob.close()
+        return
+    if args.nonlinear_assembly:
+        prob.close()
+        nonlinear_assembly(args, M)
         return
     def step_resident(o=None):
         prob.set_design_device(d_rho.data_ptr())

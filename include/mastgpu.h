@@ -228,6 +228,10 @@ long long mg_launch_count(void);
    without synchronising (for event timing): the fused CSR SpMV of the CG step
    (MG_PLAIN_FP64) or the tensor-core column operator (MG_MIXED_*). */
 int mg_debug_launch_apply(mg_problem *p, int precision, int reps);
+/* Enqueues `reps` assemblies (residual and tangent, every colour) of the nonlinear-strain
+   HEX8 element at X without synchronising; X (host, nullable) is copied first, NULL reuses
+   the previously copied state.  MG_ENOTSUP for other physics. */
+int mg_debug_launch_assembly(mg_problem *p, const double *X, int reps);
 
 /* ---- allocation-free solve ---- */
 /* No counterpart in the reference (MAST hands its linear systems to PETSc).

@@ -756,6 +756,33 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
     return MG_OK;
 }
 
+// `reps` assemblies of the nonlinear-strain residual and tangent at d_X, enqueued on the
+// handle's stream without synchronising (event timing of the element kernel)
+int launch_assembly(mg_problem *p, const double *d_X, int reps) {
+    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
+        set_error("assembly launch hook: nonlinear-strain HEX8 only");
+        return MG_ENOTSUP;
+    }
+    int *st = status_slot(p);
+    double lam1, mu1;
+    lame_3d(p->mat.nu, lam1, mu1);
+    for (int r = 0; r < reps; r++) {
+        MG_CUDA_TRY(cudaMemsetAsync(p->A.vals, 0, p->A.nnz * sizeof(double), p->stream));
+        MG_CUDA_TRY(cudaMemsetAsync(p->d_R, 0, p->n_dofs * sizeof(double), p->stream));
+        for (int c = 0; c < p->n_colors; c++) {
+            int64_t cnt = p->color_ptr[c + 1] - p->color_ptr[c];
+            hex8_gl_kernel<0><<<blocks_for(cnt, kGlWarps), kGlWarps * 32, 0, p->stream>>>(
+                p->d_coords, p->d_conn, p->d_color_elems + p->color_ptr[c], 0, cnt, p->d_E, lam1,
+                mu1, d_X, p->A.rowptr, p->d_emap, p->A.vals, p->d_R, nullptr, nullptr, nullptr,
+                nullptr, nullptr, st);
+            MG_CUDA_TRY(cudaGetLastError());
+        }
+    }
+    count_launches((long long)reps * p->n_colors);
+    p->jacobian_valid = false;
+    return MG_OK;
+}
+
 int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t count,
                      double *d_Ke, double *d_fe) {
     int *st = status_slot(p);

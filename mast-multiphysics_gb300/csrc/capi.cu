@@ -823,6 +823,12 @@ int mg_compliance_resident(mg_problem *p, double *compliance) {
 
 const double *mg_sensitivities_device(mg_problem *p) { return p ? p->d_elem_out : nullptr; }
 
+int mg_debug_launch_assembly(mg_problem *p, const double *X, int reps) {
+    if (!p || reps <= 0) return MG_EINVAL;
+    if (X) MG_TRY(to_device_vec(p, X, p->d_tmp, p->n_dofs));
+    return launch_assembly(p, p->d_tmp, reps);
+}
+
 int mg_debug_launch_apply(mg_problem *p, int precision, int reps) {
     if (!p || reps <= 0) return MG_EINVAL;
     if (precision == MG_PLAIN_FP64) return krylov_launch_spmv_cg(p, reps);

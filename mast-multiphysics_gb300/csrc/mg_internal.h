@@ -128,6 +128,7 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
                     bool consistent);
 int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t count,
                      double *d_Ke, double *d_fe);
+int launch_assembly(mg_problem *p, const double *d_X, int reps);
 int compute_modulus(mg_problem *p);
 // SIMP E(rho), dE/drho of n elements on stream s; bit 4 of *d_status marks a
 // density outside [0,1] or NaN

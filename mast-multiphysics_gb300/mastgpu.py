@@ -214,6 +214,7 @@ def lib(autobuild=True):
     L.mg_sensitivities_device.restype = _vp
     L.mg_launch_count.restype = ctypes.c_longlong
     L.mg_debug_launch_apply.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
+    L.mg_debug_launch_assembly.argtypes = [_vp, _vp, ctypes.c_int]
     L.mg_debug_fail_alloc_after.argtypes = [ctypes.c_int]
     L.mg_debug_fail_alloc_after.restype = None
     L.mg_batch_create.argtypes = [ctypes.POINTER(BatchProblem), _i32, ctypes.POINTER(MaterialDesc),
