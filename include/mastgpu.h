@@ -33,6 +33,10 @@
  *                              calculate_output_adjoint_sensitivity_multiple_parameters_no_direct
  *                              (src/elasticity/compliance_output.cpp:71-296,
  *                              src/base/assembly_base.cpp:253-333, 594-639)
+ *   mg_ks_stress               MAST::KSStressStrainOutput (src/elasticity/ks_stress_output.cpp)
+ *                              over StructuralElement3D::calculate_stress
+ *                              (src/elasticity/solid_element_3d.cpp:1147-1270), with the
+ *                              adjoint sensitivity of examples/structural/example_6/example_6.cpp:798-874
  *   mg_adjoint_solve           MAST::NonlinearSystem::adjoint_solve
  *                              (src/base/nonlinear_system.cpp:798-847)
  *   mg_mean_temperature        an OutputAssemblyElemOperations subclass
@@ -199,6 +203,16 @@ int mg_sensitivity_assemble(mg_problem *p, const double *X, int32_t param_kind,
 /* compliance C = F.X; dc_drho (nullable) by the adjoint: lambda = -X for the linear
    form, K_T(X) lambda = F on the GPU for MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR */
 int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc_drho);
+/* KS-aggregated von Mises stress over every element (KSStressStrainOutput,
+   ks_stress_output.cpp:41-99) at X (host, nullable: the resident solution):
+   ks = ln(sum_qp exp(p_ks (vm - sigma0)/sigma0) JxW / sum_qp JxW) / p_ks with the stress
+   of E(rho) at the SIMP exponent stress_penalty (<= 0: the material's), max_vm the
+   largest Gauss-point von Mises stress; dks_drho (nullable, n_elems) the total density
+   derivative as example_6.cpp:798-874 forms it: lambda . dR/drho with
+   K(X)^T lambda = -dks/dX (the tangent for the nonlinear strain), plus the direct term
+   through the stress modulus.  HEX8 physics only. */
+int mg_ks_stress(mg_problem *p, const double *X, double p_ks, double sigma0, double stress_penalty,
+                 double *ks, double *max_vm, double *dks_drho);
 /* J(X)^T lambda = rhs with the consistent Jacobian at X (host vectors; constrained
    rows give lambda = 0); the Krylov method of opts (BiCGStab for heat) */
 int mg_adjoint_solve(mg_problem *p, const double *X, const double *rhs, const mg_solve_opts *opts,

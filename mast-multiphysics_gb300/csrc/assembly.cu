@@ -299,6 +299,103 @@ __global__ void __launch_bounds__(kGlWarps * 32) hex8_gl_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------
+// KS stress output (hex8_gl.cuh stress phases): one warp per element, four
+// warps per block.  MODE 0: per-element sums over the Gauss points, written
+// as four planes of n_el: I_e = sum ex JxW, V_e = sum JxW, A_e = sum vm ex
+// JxW, M_e = max vm.  MODE 1 (one colour, atomic-free): g_ia += scale *
+// sum_qp ex JxW d vm / d u_ia.
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kGlWarps * 32) hex8_stress_kernel(
+    const double *__restrict__ coords, const int32_t *__restrict__ conn,
+    const int32_t *__restrict__ elem_list, int64_t n_items, const double *__restrict__ Es,
+    double lam1, double mu1, int nonlinear, double p_ks, double sigma0,
+    const double *__restrict__ Xg, double *__restrict__ sums, int64_t n_el, double scale,
+    double *__restrict__ g, int *__restrict__ status) {
+    __shared__ gl::StressWork sh[kGlWarps];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    gl::StressWork &s = sh[w];
+    for (int64_t item = (int64_t)blockIdx.x * kGlWarps + w; item < n_items;
+         item += (int64_t)gridDim.x * kGlWarps) {
+        const int64_t e = elem_list ? elem_list[item] : item;
+        const int32_t *en = conn + e * 8;
+        if (lane < 24) {
+            const int64_t gi = (int64_t)en[lane / 3] * 3 + lane % 3;
+            s.X[lane] = coords[gi];
+            s.u[lane] = Xg[gi];
+        }
+        __syncwarp();
+        if (!gl::phase_jacobian(s, lane)) atomicOr(status, 1);
+        __syncwarp();
+        gl::phase_gradients(s, lane);
+        __syncwarp();
+        const double Ee = Es[e];
+        gl::phase_von_mises(s, lane, Ee * lam1, Ee * mu1, nonlinear != 0, p_ks, sigma0);
+        __syncwarp();
+        if (MODE == 0) {
+            if (lane == 0) {
+                double I = 0.0, V = 0.0, A = 0.0, M = 0.0;
+                for (int q = 0; q < 8; q++) {
+                    I += s.ex[q] * s.w[q];
+                    V += s.w[q];
+                    A += s.vm[q] * s.ex[q] * s.w[q];
+                    M = fmax(M, s.vm[q]);
+                }
+                sums[e] = I;
+                sums[n_el + e] = V;
+                sums[2 * n_el + e] = A;
+                sums[3 * n_el + e] = M;
+            }
+        } else if (lane < 24) {
+            g[(int64_t)en[lane / 3] * 3 + lane % 3] += scale * gl::phase_vm_gradient(s, lane);
+        }
+        __syncwarp();
+    }
+}
+
+// one block: out = {sum I_e, sum V_e, max M_e} in a fixed order (deterministic)
+constexpr int kKsReduceThreads = 1024;
+__global__ void __launch_bounds__(kKsReduceThreads) ks_reduce_kernel(const double *__restrict__ sums,
+                                                                      int64_t n_el,
+                                                                      double *__restrict__ out) {
+    __shared__ double sI[kKsReduceThreads], sV[kKsReduceThreads], sM[kKsReduceThreads];
+    const int t = threadIdx.x;
+    double I = 0.0, V = 0.0, M = 0.0;
+    for (int64_t i = t; i < n_el; i += kKsReduceThreads) {
+        I += sums[i];
+        V += sums[n_el + i];
+        M = fmax(M, sums[3 * n_el + i]);
+    }
+    sI[t] = I;
+    sV[t] = V;
+    sM[t] = M;
+    __syncthreads();
+    for (int h = kKsReduceThreads / 2; h > 0; h >>= 1) {
+        if (t < h) {
+            sI[t] += sI[t + h];
+            sV[t] += sV[t + h];
+            sM[t] = fmax(sM[t], sM[t + h]);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        out[0] = sI[0];
+        out[1] = sV[0];
+        out[2] = sM[0];
+    }
+}
+
+// out_e = dEs_e / Es_e * A_e * inv_s0I (the direct term through the stress modulus)
+//         + adj_e (lambda . dR/drho_e, nullable)
+__global__ void ks_combine_kernel(const double *__restrict__ sums, int64_t n_el,
+                                  const double *__restrict__ Es, const double *__restrict__ dEs,
+                                  double inv_s0I, const double *adj, double *out) {  // adj may be out
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    out[e] = dEs[e] / Es[e] * sums[2 * n_el + e] * inv_s0I + (adj ? adj[e] : 0.0);
+}
+
 // f_e = K_e u_e for element-matrix requests (var-blocked order)
 __global__ void elem_matvec_kernel(const double *__restrict__ Ke, const double *__restrict__ X,
                                    const int32_t *__restrict__ conn, int64_t first, int64_t count,
@@ -753,6 +850,64 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
             d_R, d_X, p->d_F, p->d_fixed, p->n_dofs);
         MG_CUDA_TRY(cudaGetLastError());
     }
+    return MG_OK;
+}
+
+// KS stress output, value pass: stress modulus Es(rho) at SIMP exponent `penal` into
+// ks[0, n_el), dEs into ks[n_el, 2 n_el), the element sums into ks[2 n_el, 6 n_el) and
+// {I, V, max vm} into ks[6 n_el, 6 n_el + 3); returns the three scalars on the host
+int ks_stress_values(mg_problem *p, const double *d_X, double p_ks, double sigma0, double penal,
+                     double *d_ks, double host_out[3]) {
+    int *st = status_slot(p);
+    MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(int), p->stream));
+    const int64_t n = p->n_elems;
+    mg_material_desc ms = p->mat;
+    ms.penal = penal;
+    MG_TRY(launch_simp_modulus(p->d_rho, n, ms, d_ks, d_ks + n, st, p->stream));
+    double lam1, mu1;
+    lame_3d(p->mat.nu, lam1, mu1);
+    const int nonlinear = p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR;
+    hex8_stress_kernel<0><<<blocks_for(n, kGlWarps), kGlWarps * 32, 0, p->stream>>>(
+        p->d_coords, p->d_conn, nullptr, n, d_ks, lam1, mu1, nonlinear, p_ks, sigma0, d_X,
+        d_ks + 2 * n, n, 0.0, nullptr, st);
+    MG_CUDA_TRY(cudaGetLastError());
+    ks_reduce_kernel<<<1, kKsReduceThreads, 0, p->stream>>>(d_ks + 2 * n, n, d_ks + 6 * n);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(3);
+    MG_CUDA_TRY(cudaMemcpyAsync(host_out, d_ks + 6 * n, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                p->stream));
+    return read_status(p, st);  // synchronises
+}
+
+// KS stress output, gradient pass: d_g = scale * d(sum_qp ex JxW)/du ... scattered per colour
+// (d_g zeroed first); uses the stress modulus left in d_ks by ks_stress_values
+int ks_stress_gradient(mg_problem *p, const double *d_X, double p_ks, double sigma0,
+                       const double *d_ks, double scale, double *d_g) {
+    int *st = status_slot(p);
+    MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(int), p->stream));
+    MG_CUDA_TRY(cudaMemsetAsync(d_g, 0, p->n_dofs * sizeof(double), p->stream));
+    double lam1, mu1;
+    lame_3d(p->mat.nu, lam1, mu1);
+    const int nonlinear = p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR;
+    for (int c = 0; c < p->n_colors; c++) {
+        int64_t cnt = p->color_ptr[c + 1] - p->color_ptr[c];
+        hex8_stress_kernel<1><<<blocks_for(cnt, kGlWarps), kGlWarps * 32, 0, p->stream>>>(
+            p->d_coords, p->d_conn, p->d_color_elems + p->color_ptr[c], cnt, d_ks, lam1, mu1,
+            nonlinear, p_ks, sigma0, d_X, nullptr, p->n_elems, scale, d_g, st);
+        MG_CUDA_TRY(cudaGetLastError());
+    }
+    count_launches(p->n_colors);
+    return read_status(p, st);
+}
+
+// d_out_e = direct term + d_adj_e (nullable)
+int ks_stress_combine(mg_problem *p, const double *d_ks, double inv_s0I, const double *d_adj,
+                      double *d_out) {
+    const int64_t n = p->n_elems;
+    ks_combine_kernel<<<blocks_for(n, 256), 256, 0, p->stream>>>(d_ks + 2 * n, n, d_ks, d_ks + n,
+                                                                  inv_s0I, d_adj, d_out);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
     return MG_OK;
 }
 

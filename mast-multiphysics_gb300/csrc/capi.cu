@@ -143,7 +143,7 @@ int release(mg_problem *p) {
     void *ptrs[] = {p->d_coords, p->d_conn, p->d_color_elems, p->d_fixed, p->d_F, p->d_rho,
                     p->d_E, p->d_dE, p->d_s, p->d_q, p->d_conv_mask, p->A.rowptr, p->A.cols,
                     p->A.vals, p->d_emap, p->d_fix_zero, p->d_fix_diag, p->d_X, p->d_R,
-                    p->d_tmp, p->d_tmp2, p->d_elem_out, p->d_red};
+                    p->d_tmp, p->d_tmp2, p->d_elem_out, p->d_red, p->d_ks};
     for (void *q : ptrs) dev_free(q);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -730,6 +730,55 @@ int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc
         for (int64_t e = 0; e < p->n_elems; e++) dc[e] = -dc[e];
     }
     return MG_OK;
+}
+
+int mg_ks_stress(mg_problem *p, const double *X, double p_ks, double sigma0, double stress_penalty,
+                 double *ks, double *max_vm, double *dks_drho) {
+    // KSStressStrainOutput::functional_for_all_elems (ks_stress_output.cpp:41-99) and, for
+    // dks_drho, the total derivative of example_6.cpp:798-874: the adjoint term lambda .
+    // dR/drho_e (K(X)^T lambda = -dq/dX, the residual at the material's SIMP exponent) plus the
+    // direct term through the stress modulus (functional_sensitivity_for_elem, :117-151)
+    if (!p || !(p_ks > 0) || !(sigma0 > 0)) return MG_EINVAL;
+    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8 && p->physics != MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
+        set_error("the stress output needs HEX8 elasticity");
+        return MG_ENOTSUP;
+    }
+    const double penal = stress_penalty > 0 ? stress_penalty : p->mat.penal;
+    if (!p->d_ks) MG_TRY(dev_alloc_n(&p->d_ks, (size_t)6 * p->n_elems + 8));
+    const double *dX = p->d_X;
+    if (X) {
+        MG_TRY(to_device_vec(p, X, p->d_tmp, p->n_dofs));
+        dX = p->d_tmp;
+    }
+    double red[3] = {0, 0, 0};
+    MG_TRY(ks_stress_values(p, dX, p_ks, sigma0, penal, p->d_ks, red));
+    const double I = red[0], V = red[1];
+    if (!(I > 0) || !std::isfinite(I) || !(V > 0)) {
+        set_error("KS sum %g over volume %g (overflow of exp(p (vm - s0)/s0)?)", I, V);
+        return MG_ENAN;
+    }
+    if (ks) *ks = log(I / V) / p_ks;
+    if (max_vm) *max_vm = red[2];
+    if (!dks_drho) return MG_OK;
+    const double inv_s0I = 1.0 / (sigma0 * I);
+    // rhs = -dq/dX (zero on constrained dofs) in d_R; lambda in d_tmp2
+    MG_TRY(ks_stress_gradient(p, dX, p_ks, sigma0, p->d_ks, inv_s0I, p->d_tmp2));
+    masked_neg_kernel<<<blocks_for(p->n_dofs, 256), 256, 0, p->stream>>>(p->n_dofs, p->d_tmp2, p->d_fixed,
+                                                                        p->d_R);
+    MG_CUDA_TRY(cudaGetLastError());
+    if (p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) p->jacobian_valid = false;
+    MG_TRY(assemble_system(p, dX, nullptr, true, true));
+    mg_solve_opts o;
+    mg_default_solve_opts(&o);
+    o.rtol = 1e-13;
+    double *lam = p->d_tmp2;
+    MG_CUDA_TRY(cudaMemsetAsync(lam, 0, p->n_dofs * 8, p->stream));
+    int its = 0;
+    double rr = 0;
+    MG_TRY(krylov_solve(p, p->A, p->d_R, lam, o, MG_KRYLOV_CG, &its, &rr));
+    MG_TRY(elem_sensitivity(p, dX, lam, MG_PARAM_DENSITY, p->d_elem_out));
+    MG_TRY(ks_stress_combine(p, p->d_ks, inv_s0I, p->d_elem_out, p->d_elem_out));
+    return to_host_vec(p, p->d_elem_out, dks_drho, p->n_elems);
 }
 
 int mg_adjoint_solve(mg_problem *p, const double *X, const double *rhs, const mg_solve_opts *opts,

@@ -22,6 +22,8 @@
 // __syncwarp() and a host loop over the 32 lanes runs the same source.
 #pragma once
 
+#include <math.h>
+
 #ifdef __CUDACC__
 #define GL_HD __host__ __device__ __forceinline__
 #else
@@ -61,8 +63,9 @@ GL_HD void dref(int q, int a, double d[3]) {
 }
 
 // phase 1 (lanes 0-7, q = lane): Jacobian, JxW, inverse.  Returns false for a
-// non-positive determinant.
-GL_HD bool phase_jacobian(Work &s, int lane) {
+// non-positive determinant.  (W: any workspace with X, w, inv.)
+template <class W>
+GL_HD bool phase_jacobian(W &s, int lane) {
     if (lane >= 8) return true;
     const int q = lane;
     double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // J[i][j] = d x_j / d xi_i
@@ -90,7 +93,8 @@ GL_HD bool phase_jacobian(Work &s, int lane) {
 
 // phase 2 (every lane, (q, a) = (p >> 3, p & 7) for p = lane, lane + 32):
 // physical gradients g_j = sum_k (d xi_k / d x_j) d phi / d xi_k
-GL_HD void phase_gradients(Work &s, int lane) {
+template <class W>
+GL_HD void phase_gradients(W &s, int lane) {
     for (int h = 0; h < 2; h++) {
         const int p = lane + 32 * h, q = p >> 3, a = p & 7;
         double d[3];
@@ -173,6 +177,90 @@ GL_HD void phase_tangent(const Work &s, int a, int b, double lam, double mu, dou
                 K[i * 3 + j] += wq * k;
             }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Stress output (StructuralElement3D::calculate_stress, solid_element_3d.cpp:
+// 1147-1270; von Mises and its derivatives, stress_output_base.cpp:183-271;
+// the KS weights of ks_stress_output.cpp:41-99).  Per Gauss point: the strain
+// (linear: B u; nonlinear: the Green-Lagrange strain), sigma = C eps with the
+// stress modulus, sigma_vm, ex = exp(p (sigma_vm - s0) / s0), and the tensor T
+// of t = C (d sigma_vm / d sigma) (T_jj = t_j, off-diagonal = the shear entry),
+// so that d sigma_vm / d u_ia = (Fd T g_a)_i with Fd = I (linear) or I + grad u.
+// ---------------------------------------------------------------------------
+struct StressWork {
+    double X[24], u[24], w[8], inv[8][9], g[8][8][3];
+    double Fd[8][9];
+    double T[8][9];
+    double vm[8];
+    double ex[8];
+};
+
+// lanes 0-7, q = lane
+GL_HD void phase_von_mises(StressWork &s, int lane, double lam, double mu, bool nonlinear,
+                           double p_ks, double sigma0) {
+    if (lane >= 8) return;
+    const int q = lane;
+    double H[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double v = 0.0;
+            for (int a = 0; a < 8; a++) v += s.u[a * 3 + i] * s.g[q][a][j];
+            H[i * 3 + j] = v;
+            s.Fd[q][i * 3 + j] = (nonlinear ? v : 0.0) + (i == j ? 1.0 : 0.0);
+        }
+    // Voigt strain [xx, yy, zz, xy, yz, zx], engineering shears
+    static constexpr int VJ[6] = {0, 1, 2, 0, 1, 0}, VK[6] = {0, 1, 2, 1, 2, 2};
+    double eps[6];
+    for (int r = 0; r < 6; r++) {
+        const int j = VJ[r], k = VK[r];
+        double e = (r < 3) ? H[j * 3 + j] : H[j * 3 + k] + H[k * 3 + j];
+        if (nonlinear) {
+            double c = 0.0;
+            for (int m = 0; m < 3; m++) c += H[m * 3 + j] * H[m * 3 + k];
+            e += (r < 3) ? 0.5 * c : c;
+        }
+        eps[r] = e;
+    }
+    const double tr = eps[0] + eps[1] + eps[2];
+    double sg[6];
+    for (int r = 0; r < 3; r++) sg[r] = lam * tr + 2.0 * mu * eps[r];
+    for (int r = 3; r < 6; r++) sg[r] = mu * eps[r];
+    const double P = 0.5 * ((sg[0] - sg[1]) * (sg[0] - sg[1]) + (sg[1] - sg[2]) * (sg[1] - sg[2]) +
+                            (sg[2] - sg[0]) * (sg[2] - sg[0])) +
+                     3.0 * (sg[3] * sg[3] + sg[4] * sg[4] + sg[5] * sg[5]);
+    const double vm = sqrt(P);
+    double d[6] = {0, 0, 0, 0, 0, 0};  // d sigma_vm / d sigma, zero where sigma_vm = 0
+    if (P > 0.0) {
+        const double c = 0.5 / vm;
+        d[0] = c * (2.0 * sg[0] - sg[1] - sg[2]);
+        d[1] = c * (2.0 * sg[1] - sg[2] - sg[0]);
+        d[2] = c * (2.0 * sg[2] - sg[0] - sg[1]);
+        for (int r = 3; r < 6; r++) d[r] = c * 6.0 * sg[r];
+    }
+    const double trd = d[0] + d[1] + d[2];
+    double *T = s.T[q];
+    T[0] = lam * trd + 2.0 * mu * d[0];
+    T[4] = lam * trd + 2.0 * mu * d[1];
+    T[8] = lam * trd + 2.0 * mu * d[2];
+    T[1] = T[3] = mu * d[3];
+    T[5] = T[7] = mu * d[4];
+    T[2] = T[6] = mu * d[5];
+    s.vm[q] = vm;
+    s.ex[q] = exp(p_ks * (vm - sigma0) / sigma0);
+}
+
+// lanes 0-23, lane = 3 a + i: sum_qp ex JxW d sigma_vm / d u_ia
+GL_HD double phase_vm_gradient(const StressWork &s, int lane) {
+    const int a = lane / 3, i = lane % 3;
+    double acc = 0.0;
+    for (int q = 0; q < 8; q++) {
+        const double *g = s.g[q][a], *T = s.T[q], *F = s.Fd[q] + i * 3;
+        double Tg[3];
+        for (int m = 0; m < 3; m++) Tg[m] = T[m * 3] * g[0] + T[m * 3 + 1] * g[1] + T[m * 3 + 2] * g[2];
+        acc += s.w[q] * s.ex[q] * (F[0] * Tg[0] + F[1] * Tg[1] + F[2] * Tg[2]);
+    }
+    return acc;
 }
 
 }  // namespace gl

@@ -115,6 +115,7 @@ struct mg_problem {
     // state vectors
     double *d_X = nullptr, *d_R = nullptr, *d_tmp = nullptr, *d_tmp2 = nullptr;
     double *d_elem_out = nullptr;     // per-element scalar outputs
+    double *d_ks = nullptr;           // KS stress output scratch (6 n_elems + 8), allocated on use
     double *d_red = nullptr;          // reduction scratch
     int red_blocks = 0;
     mg::KrylovWork kw;
@@ -129,6 +130,13 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
 int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t count,
                      double *d_Ke, double *d_fe);
 int launch_assembly(mg_problem *p, const double *d_X, int reps);
+// KS stress output (d_ks: 6 n_elems + 8 doubles of scratch)
+int ks_stress_values(mg_problem *p, const double *d_X, double p_ks, double sigma0, double penal,
+                     double *d_ks, double host_out[3]);
+int ks_stress_gradient(mg_problem *p, const double *d_X, double p_ks, double sigma0,
+                       const double *d_ks, double scale, double *d_g);
+int ks_stress_combine(mg_problem *p, const double *d_ks, double inv_s0I, const double *d_adj,
+                      double *d_out);
 int compute_modulus(mg_problem *p);
 // SIMP E(rho), dE/drho of n elements on stream s; bit 4 of *d_status marks a
 // density outside [0,1] or NaN

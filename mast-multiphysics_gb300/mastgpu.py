@@ -207,6 +207,7 @@ def lib(autobuild=True):
     L.mg_sensitivity_assemble.argtypes = [_vp, _vp, _i32, _i64, _vp]
     L.mg_compliance.argtypes = [_vp, _vp, _vp, _vp]
     L.mg_adjoint_solve.argtypes = [_vp, _vp, _vp, ctypes.POINTER(SolveOpts), _vp]
+    L.mg_ks_stress.argtypes = [_vp, _vp, _dbl, _dbl, _dbl, _vp, _vp, _vp]
     L.mg_mean_temperature.argtypes = [_vp, _vp, ctypes.POINTER(SolveOpts), _vp, _vp, _vp]
     L.mg_debug_matfree_apply.argtypes = [_vp, ctypes.c_int, _vp, _vp]
     L.mg_compliance_resident.argtypes = [_vp, _vp]
@@ -450,6 +451,16 @@ class Problem:
         dc = np.zeros(self.n_elems) if want_sens else None
         check(lib().mg_compliance(self.h, _p(Xa), ctypes.byref(c), _p(dc)), "mg_compliance")
         return c.value, dc
+
+    def ks_stress(self, p_ks, sigma0, stress_penalty=0.0, X=None, want_sens=True):
+        """KS-aggregated von Mises stress, the largest von Mises stress and (want_sens) the
+        total density derivative of the KS value (mg_ks_stress)"""
+        Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
+        q, vmax = ctypes.c_double(), ctypes.c_double()
+        d = np.zeros(self.n_elems) if want_sens else None
+        check(lib().mg_ks_stress(self.h, _p(Xa), p_ks, sigma0, stress_penalty, ctypes.byref(q),
+                                 ctypes.byref(vmax), _p(d)), "mg_ks_stress")
+        return q.value, vmax.value, d
 
     def adjoint_solve(self, X, rhs, opts=None):
         """lambda with J(X)^T lambda = rhs (mg_adjoint_solve)"""

@@ -308,6 +308,70 @@ int or_hex8_internal_gl(const double X[24], double E, double nu, const double u[
    (solid_element_3d.cpp:567-788): C replaced by dC/dp (:640).  With only E
    depending on p (StiffnessMatrix3D::derivative,
    isotropic_material_property_card.cpp:533-567, dnu/dp = 0) dC/dp = dE C(1,nu). */
+/* StructuralElement3D::calculate_stress (solid_element_3d.cpp:1147-1270): per
+   Gauss point the strain of initialize_green_lagrange_strain_operator (B u for
+   the linear strain, (H + H^T + H^T H)/2 in Voigt form with engineering shears
+   for NONLINEAR_STRAIN), stress C eps, its derivative d sigma / d u = C B (C B_L
+   for the nonlinear strain, nullable) and JxW; von Mises per point by
+   StressStrainOutputBase::Data::von_Mises_stress (stress_output_base.cpp:183-195).
+   sig[qp*6 + r], dsig[(qp*6 + r)*24 + c] with var-blocked dofs c = i 8 + a. */
+int or_hex8_stress(const double X[24], double E, double nu, const double u[24], int nonlinear,
+                   double sig[48], double vm[8], double JxW_out[8], double *dsig) {
+    double C[36], phi[8], dphi[24], JxW;
+    or_iso_stiffness_3d(E, nu, C);
+    static const int VJ[6] = {0, 1, 2, 0, 1, 0}, VK[6] = {0, 1, 2, 1, 2, 2};
+    for (int qp = 0; qp < 8; qp++) {
+        if (hex8_qp(X, qp, phi, dphi, &JxW) <= 0.) return -1;
+        JxW_out[qp] = JxW;
+        double F[9] = {0}, eps[6], B[144];
+        for (int i = 0; i < 3; i++)
+            for (int a = 0; a < 8; a++)
+                for (int j = 0; j < 3; j++) F[i * 3 + j] += u[i * 8 + a] * dphi[a * 3 + j];
+        if (!nonlinear) {
+            hex8_B(dphi, B);
+            for (int r = 0; r < 6; r++) {
+                double e = 0;
+                for (int c = 0; c < 24; c++) e += B[r * 24 + c] * u[c];
+                eps[r] = e;
+            }
+        } else {
+            for (int r = 0; r < 6; r++) {
+                const int j = VJ[r], k = VK[r];
+                double e = 0.5 * (F[j * 3 + k] + F[k * 3 + j]);
+                for (int m = 0; m < 3; m++) e += 0.5 * F[m * 3 + j] * F[m * 3 + k];
+                eps[r] = (r < 3) ? e : 2.0 * e;
+            }
+            for (int i = 0; i < 3; i++)
+                for (int a = 0; a < 8; a++) {
+                    const double *g = dphi + a * 3;
+                    for (int r = 0; r < 6; r++) {
+                        const int j = VJ[r], k = VK[r];
+                        double de = 0.5 * ((i == j ? g[k] : 0.0) + (i == k ? g[j] : 0.0) +
+                                           g[j] * F[i * 3 + k] + F[i * 3 + j] * g[k]);
+                        B[r * 24 + i * 8 + a] = (r < 3) ? de : 2.0 * de;
+                    }
+                }
+        }
+        double *s = sig + qp * 6;
+        for (int r = 0; r < 6; r++) {
+            double v = 0;
+            for (int c = 0; c < 6; c++) v += C[r * 6 + c] * eps[c];
+            s[r] = v;
+        }
+        vm[qp] = sqrt(0.5 * ((s[0] - s[1]) * (s[0] - s[1]) + (s[1] - s[2]) * (s[1] - s[2]) +
+                             (s[2] - s[0]) * (s[2] - s[0])) +
+                      3.0 * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]));
+        if (dsig)
+            for (int r = 0; r < 6; r++)
+                for (int c = 0; c < 24; c++) {
+                    double v = 0;
+                    for (int q = 0; q < 6; q++) v += C[r * 6 + q] * B[q * 24 + c];
+                    dsig[(qp * 6 + r) * 24 + c] = v;
+                }
+    }
+    return 0;
+}
+
 int or_hex8_internal_sens(const double X[24], double dE, double nu,
                           const double u[24], double df[24]) {
     return or_hex8_internal(X, dE, nu, u, df, NULL);

@@ -49,6 +49,9 @@ int or_hex8_internal(const double X[24], double E, double nu, const double u[24]
    f = int B_L^T S, K = int (B_L^T C B_L + geometric stiffness); var-blocked dofs */
 int or_hex8_internal_gl(const double X[24], double E, double nu, const double u[24],
                         double f[24], double K[576]);
+/* Gauss-point stress (Voigt), von Mises, JxW and d sigma / d u (nullable, 8 x 6 x 24) */
+int or_hex8_stress(const double X[24], double E, double nu, const double u[24], int nonlinear,
+                   double sig[48], double vm[8], double JxW_out[8], double *dsig);
 int or_hex8_internal_sens(const double X[24], double dE, double nu,
                           const double u[24], double df[24]);
 int or_quad4_membrane_internal(const double X[8], double E, double nu, double h,

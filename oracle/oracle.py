@@ -71,6 +71,7 @@ def lib():
         L.or_hex8_internal.argtypes = [_f64p, d, d, _f64p, _f64p, vp]
         L.or_hex8_internal_sens.argtypes = [_f64p, d, d, _f64p, _f64p]
         L.or_hex8_internal_gl.argtypes = [_f64p, d, d, _f64p, _f64p, ctypes.c_void_p]
+        L.or_hex8_stress.argtypes = [_f64p, d, d, _f64p, i32, _f64p, _f64p, _f64p, vp]
         L.or_quad4_membrane_internal.argtypes = [_f64p, d, d, d, _f64p, _f64p, vp]
         L.or_quad4_heat_internal.argtypes = [_f64p, d, d, d, d, _f64p, i32, _f64p, vp]
         L.or_quad4_heat_internal_sens.argtypes = [_f64p, d, d, d, _f64p, _f64p]
@@ -308,6 +309,86 @@ def hex8_gl_compliance_sens(coords, conn, dE_elem, nu, u, E_elem, F, fixed):
         f1, _ = hex8_internal_gl(coords[conn[e]], 1.0, nu, ue, want_K=False)
         dc[e] = -dE_elem[e] * float(le @ f1)
     return dc
+
+
+def hex8_stress(X, E, nu, u, nonlinear=False, want_dsig=False):
+    """Gauss-point stress (8, 6), von Mises (8), JxW (8) and d sigma / d u (8, 6, 24)."""
+    sig, vm, jxw = np.zeros(48), np.zeros(8), np.zeros(8)
+    ds = np.zeros(8 * 6 * 24) if want_dsig else None
+    if lib().or_hex8_stress(np.ascontiguousarray(X, dtype=np.float64).reshape(24), E, nu,
+                            np.ascontiguousarray(u, dtype=np.float64), int(nonlinear), sig, vm,
+                            jxw, _ptr(ds)):
+        raise ValueError("degenerate HEX8 element")
+    return sig.reshape(8, 6), vm, jxw, (ds.reshape(8, 6, 24) if want_dsig else None)
+
+
+def _dvm_dsig(s):
+    """d sigma_vm / d sigma (Voigt), zero where sigma_vm = 0
+    (StressStrainOutputBase::Data::dvon_Mises_stress_dX, stress_output_base.cpp:199-233)."""
+    P = 0.5 * ((s[0] - s[1]) ** 2 + (s[1] - s[2]) ** 2 + (s[2] - s[0]) ** 2) + \
+        3.0 * (s[3] ** 2 + s[4] ** 2 + s[5] ** 2)
+    if not P > 0.0:
+        return np.zeros(6)
+    return 0.5 / np.sqrt(P) * np.array([2 * s[0] - s[1] - s[2], 2 * s[1] - s[2] - s[0],
+                                        2 * s[2] - s[0] - s[1], 6 * s[3], 6 * s[4], 6 * s[5]])
+
+
+def ks_stress(coords, conn, Es_elem, dEs_elem, nu, u, p_ks, sigma0, nonlinear=False):
+    """KSStressStrainOutput over every element (ks_stress_output.cpp:41-99, 117-151, 196-246):
+    q = ln(sum_qp exp(p (vm - s0)/s0) JxW / sum_qp JxW) / p with the stress of the modulus
+    Es (the stress penalty of example_6.cpp:579-592).  Returns q, max vm, dq/du (global,
+    node-interleaved) and the direct partial dq/drho_e (through Es at fixed u)."""
+    n_el = conn.shape[0]
+    w_all, jxw_all, vm_all, sig_all, dsig_all = [], [], [], [], []
+    for e in range(n_el):
+        ue = u.reshape(-1, 3)[conn[e]].T.reshape(-1)
+        sig, vm, jxw, ds = hex8_stress(coords[conn[e]], Es_elem[e], nu, ue, nonlinear, True)
+        vm_all.append(vm)
+        jxw_all.append(jxw)
+        sig_all.append(sig)
+        dsig_all.append(ds)
+    vm_all, jxw_all = np.array(vm_all), np.array(jxw_all)
+    w = np.exp(p_ks * (vm_all - sigma0) / sigma0) * jxw_all
+    I, V = w.sum(), jxw_all.sum()
+    q = np.log(I / V) / p_ks
+    dq_du = np.zeros(u.shape[0])
+    for e in range(n_el):
+        ge = np.zeros(24)
+        for qp in range(8):
+            ge += (_dvm_dsig(sig_all[e][qp]) @ dsig_all[e][qp]) * w[e, qp]
+        ge /= sigma0 * I
+        for a in range(8):
+            for i in range(3):
+                dq_du[conn[e][a] * 3 + i] += ge[i * 8 + a]
+    dq_drho = (dEs_elem / Es_elem) * (vm_all * w).sum(axis=1) / (sigma0 * I)
+    return q, vm_all.max(), dq_du, dq_drho
+
+
+def ks_stress_total_sensitivity(coords, conn, E_elem, dE_elem, Es_elem, dEs_elem, nu, u, fixed,
+                                p_ks, sigma0, nonlinear=False):
+    """dq/drho_e = partial + lambda . dR/drho_e with K(u)^T lambda = -dq/du
+    (example_6.cpp:798-874: adjoint_solve, then the adjoint term g1 at the solve's penalty
+    and the direct term g2 at the stress penalty)."""
+    q, vmax, dq_du, dq_drho = ks_stress(coords, conn, Es_elem, dEs_elem, nu, u, p_ks, sigma0,
+                                        nonlinear)
+    rowptr, cols = csr_pattern(conn, coords.shape[0], 3)
+    if nonlinear:
+        vals, _ = assemble_hex8_gl(coords, conn, E_elem, nu, u, None, rowptr, cols, fixed)
+    else:
+        vals = assemble_hex8(coords, conn, E_elem, nu, rowptr, cols, fixed)
+    rhs = np.where(np.asarray(fixed) == 1, 0.0, -dq_du)
+    lam, _, _ = pcg(rowptr, cols, vals, rhs, 1e-14, 100000)
+    total = dq_drho.copy()
+    for e in range(conn.shape[0]):
+        ue = u.reshape(-1, 3)[conn[e]].T.reshape(-1)
+        le = lam.reshape(-1, 3)[conn[e]].T.reshape(-1)
+        if nonlinear:
+            f1, _ = hex8_internal_gl(coords[conn[e]], 1.0, nu, ue, want_K=False)
+        else:
+            _, K1 = hex8_internal(coords[conn[e]], 1.0, nu)
+            f1 = K1 @ ue
+        total[e] += dE_elem[e] * float(le @ f1)
+    return q, vmax, total
 
 
 def spmv(rowptr, cols, vals, x):
