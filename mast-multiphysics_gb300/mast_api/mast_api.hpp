@@ -585,6 +585,26 @@ class ComplianceOutput : public OutputAssemblyElemOperations {};
 // mean temperature (1/|Omega|) int T
 class AverageTemperatureOutput : public OutputAssemblyElemOperations {};
 
+// KS-aggregated von Mises stress over every element (MAST::KSStressStrainOutput,
+// ks_stress_output.cpp:41-99; set_aggregation_coefficients as stress_output_base.h:246-252)
+class KSStressStrainOutput : public OutputAssemblyElemOperations {
+public:
+    void set_aggregation_coefficients(Real p1, Real p2, Real rho, Real sigma0) {
+        _p = p1;
+        _p2 = p2;  // the p-norm weight and rho of the other aggregates: unused by KS
+        _rho = rho;
+        _sigma0 = sigma0;
+    }
+    void set_participating_elements_to_all() {}
+    // SIMP exponent of the modulus the stress is evaluated with: the penalty example_6 sets
+    // on its ElasticityFunction before evaluating the output (example_6.cpp:579-592);
+    // <= 0 uses the solve's exponent
+    void set_stress_penalty(Real penalty) { _penal = penalty; }
+    Real get_maximum_von_mises_stress() const { return _vmax; }
+    Real get_p_stress_val() const { return _p; }
+    Real _p = 0, _p2 = 0, _rho = 0, _sigma0 = 0, _penal = 0, _vmax = 0;
+};
+
 // ------------------------------------------------------------------ assembly + solve
 class NonlinearImplicitAssembly;
 
@@ -699,6 +719,9 @@ public:
             mg_solve_opts o;
             mg_default_solve_opts(&o);
             check(mg_mean_temperature(problem(), X.data(), &o, &q, nullptr, nullptr), "calculate_output");
+        } else if (auto *ks = dynamic_cast<KSStressStrainOutput *>(&output)) {
+            check(mg_ks_stress(problem(), X.data(), ks->_p, ks->_sigma0, ks->_penal, &q, &ks->_vmax, nullptr),
+                  "calculate_output");
         } else
             throw std::runtime_error("calculate_output: unsupported output");
         output._q = q;
@@ -738,6 +761,29 @@ public:
             Real s = 0;
             for (size_t k = 0; k < X.size(); k++) s += adj_sol(k) * d(k);
             sens[i] = s;
+        }
+    }
+
+    // the total design derivative of a KS stress output in one call: what MAST forms as
+    // adjoint_solve + calculate_output_adjoint_sensitivity_multiple_parameters_no_direct (the
+    // adjoint term, at the solve's exponent) + calculate_output_direct_sensitivity (the term
+    // through the stress modulus), example_6.cpp:798-874; density parameters only
+    void calculate_output_total_sensitivity(const Vector &X, KSStressStrainOutput &output,
+                                            const std::vector<const FunctionBase *> &p_vec,
+                                            std::vector<Real> &sens) {
+        std::vector<Real> d(_sys->mesh().n_elem());
+        Real q = 0;
+        check(mg_ks_stress(problem(), X.data(), output._p, output._sigma0, output._penal, &q, &output._vmax,
+                           d.data()),
+              "KS stress sensitivity");
+        output._q = q;
+        sens.assign(p_vec.size(), 0.0);
+        for (size_t i = 0; i < p_vec.size(); i++) {
+            int kind;
+            int64_t index;
+            _param_of(*p_vec[i], kind, index);
+            if (kind != MG_PARAM_DENSITY) throw std::runtime_error("KS stress sensitivity: density parameters only");
+            sens[i] = d[index];
         }
     }
 
@@ -874,6 +920,9 @@ inline void NonlinearSystem::solve(AssemblyElemOperations &, NonlinearImplicitAs
 inline void NonlinearSystem::adjoint_solve(const Vector &X, bool, AssemblyElemOperations &,
                                            OutputAssemblyElemOperations &output,
                                            NonlinearImplicitAssembly &assembly, Vector &adjoint) {
+    if (dynamic_cast<KSStressStrainOutput *>(&output))
+        throw std::runtime_error("adjoint_solve: the GPU path forms the KS stress adjoint inside mg_ks_stress; "
+                                 "use NonlinearImplicitAssembly::calculate_output_total_sensitivity");
     if (!dynamic_cast<ComplianceOutput *>(&output))
         throw std::runtime_error("adjoint_solve: the GPU path forms the mean-temperature adjoint inside "
                                  "mg_mean_temperature; use calculate_output_adjoint_sensitivity");

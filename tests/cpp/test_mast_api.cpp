@@ -237,6 +237,22 @@ TEST_CASE("hex8_simp_cantilever", "[gpu],[structural],[3D]") {
     CHECK(s == Approx(sens[3]).epsilon(1e-9));
 }
 
+TEST_CASE("ks_stress_output_settings", "[cpu],[output]") {
+    MAST::KSStressStrainOutput stress;
+    stress.set_participating_elements_to_all();
+    stress.set_aggregation_coefficients(8.0, 1.0, 0.5, 250.0);
+    stress.set_stress_penalty(0.5);
+    REQUIRE(stress.get_p_stress_val() == 8.0);
+    REQUIRE(stress._sigma0 == 250.0);
+    REQUIRE(stress.get_maximum_von_mises_stress() == 0.0);
+    // the adjoint of the KS output is formed inside the library, not by adjoint_solve
+    MAST::NonlinearSystem sys;
+    MAST::NonlinearImplicitAssembly assembly;
+    MAST::StructuralNonlinearAssemblyElemOperations ops;
+    MAST::Vector X(3), adj;
+    REQUIRE_THROWS(sys.adjoint_solve(X, false, ops, stress, assembly, adj));
+}
+
 TEST_CASE("section_strain_type", "[cpu],[property]") {
     MAST::Solid3DSectionElementPropertyCard section;
     REQUIRE(section.strain_type() == MAST::LINEAR_STRAIN);
