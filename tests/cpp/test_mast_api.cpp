@@ -253,11 +253,17 @@ TEST_CASE("ks_stress_output_settings", "[cpu],[output]") {
     REQUIRE_THROWS(sys.adjoint_solve(X, false, ops, stress, assembly, adj));
 }
 
+// the reference's set_get_strain_type section
+// (tests/property/mast_3d_isotropic_element_property_card.cpp:379-391)
 TEST_CASE("section_strain_type", "[cpu],[property]") {
     MAST::Solid3DSectionElementPropertyCard section;
     REQUIRE(section.strain_type() == MAST::LINEAR_STRAIN);
+    section.set_strain(MAST::LINEAR_STRAIN);
+    REQUIRE(section.strain_type() == MAST::LINEAR_STRAIN);
+    REQUIRE(!(section.strain_type() == MAST::NONLINEAR_STRAIN));
     section.set_strain(MAST::NONLINEAR_STRAIN);
     REQUIRE(section.strain_type() == MAST::NONLINEAR_STRAIN);
+    REQUIRE(!(section.strain_type() == MAST::LINEAR_STRAIN));
 }
 
 // the section's NONLINEAR_STRAIN selects the Green-Lagrange element: a
