@@ -99,3 +99,21 @@ def test_batch_designs_generator_is_seeded_and_in_range():
         assert 1 <= len(x["spans"]) <= 4
         assert all(0 <= j0 <= j1 <= x["ny"] for j0, j1 in x["spans"])
         assert x["rho"].min() >= 0.01 and x["rho"].max() <= 1.0
+
+
+def test_output_entry_points_reject_missing_handles_without_a_gpu():
+    """The adjoint, KS stress and assembly-launch entry points check their arguments on
+    the host first: a missing handle or vector is MG_EINVAL with no CUDA call."""
+    L = M.lib()
+    x = np.zeros(3)
+    q, v = ctypes.c_double(), ctypes.c_double()
+    assert L.mg_ks_stress(None, None, 8.0, 1.0, 0.5, ctypes.byref(q), ctypes.byref(v), None) == M.MG_EINVAL
+    assert L.mg_adjoint_solve(None, M._p(x), M._p(x), None, M._p(x)) == M.MG_EINVAL
+    assert L.mg_debug_launch_assembly(None, None, 1) == M.MG_EINVAL
+    assert L.mg_compliance(None, None, None, None) == M.MG_EINVAL
+
+
+def test_nonlinear_physics_value_is_the_header_enum():
+    txt = open(os.path.join(REPO, "include", "mastgpu.h")).read()
+    m = re.search(r"MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR\s*=\s*(\d+)", txt)
+    assert m and int(m.group(1)) == M.PHYS_HEX8_NONLINEAR
