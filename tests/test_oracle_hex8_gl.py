@@ -186,3 +186,36 @@ def test_adjoint_compliance_sensitivity_matches_finite_differences():
         rm[e] -= h
         fd = (compliance(rp)[0] - compliance(rm)[0]) / (2 * h)
         assert abs(dc[e] - fd) <= 1e-6 * abs(fd)
+
+
+def test_internal_force_is_the_strain_energy_gradient():
+    """St Venant-Kirchhoff is hyperelastic: f_int = dPi/du with Pi = sum_qp JxW E:C:E / 2 over
+    the Green-Lagrange strain (computed here independently, by numpy from the shape data)."""
+    X = element(0.1, seed=9)
+    u = np.random.default_rng(10).normal(scale=0.08, size=24)
+    E, nu = 3.0, 0.25
+    C = O.iso_stiffness_3d(E, nu)
+    g = 1 / np.sqrt(3)
+    signs = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                      [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], dtype=float)
+
+    def energy(uv):
+        disp = uv.reshape(3, 8).T
+        Pi = 0.0
+        for q in range(8):
+            xi = np.array([q & 1, q >> 1 & 1, q >> 2 & 1]) * 2 * g - g
+            dN = np.array([[s[d] / 8 * np.prod([1 + s[k] * xi[k] for k in range(3) if k != d])
+                            for d in range(3)] for s in signs])  # (8, 3) reference gradients
+            J = dN.T @ X
+            gN = dN @ np.linalg.inv(J).T
+            H = disp.T @ gN
+            Eg = 0.5 * (H + H.T + H.T @ H)
+            ev = np.array([Eg[0, 0], Eg[1, 1], Eg[2, 2], 2 * Eg[0, 1], 2 * Eg[1, 2], 2 * Eg[0, 2]])
+            Pi += np.linalg.det(J) * 0.5 * ev @ C @ ev
+        return Pi
+
+    f, _ = O.hex8_internal_gl(X, E, nu, u, want_K=False)
+    h = 1e-6
+    grad = np.array([(energy(u + h * np.eye(24)[c]) - energy(u - h * np.eye(24)[c])) / (2 * h)
+                     for c in range(24)])
+    assert np.abs(f - grad).max() <= 1e-7 * np.abs(f).max()
