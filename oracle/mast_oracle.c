@@ -1,8 +1,8 @@
 /*
  * mast_oracle.c -- FP64 CPU restatement of MAST's HEX8/QUAD4 hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for libmastgpu.so and the timed CPU
- * baseline.  The product never links or calls this file.  Each routine cites
+ * TEST INFRASTRUCTURE ONLY: the FP64 reference the tests compare libmastgpu.so
+ * against, and the timed CPU baseline.  The product never links or calls this file.  Each routine cites
  * the reference source it restates (paths relative to the MAST source tree).
  * Parameters, conventions and pinning status are described in mast_oracle.h.
  */

@@ -2,8 +2,8 @@
  * mast_oracle.h -- FP64 CPU restatement of MAST's HEX8/QUAD4 element,
  * assembly, Krylov and sensitivity arithmetic.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA product
- * (libmastgpu.so) and the timed CPU baseline; nothing in the product links,
+ * TEST INFRASTRUCTURE ONLY.  The tests compare the CUDA product (libmastgpu.so)
+ * against this library, and it is the timed CPU baseline; nothing in the product links,
  * loads or calls it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline arm use it.
  *

@@ -1,8 +1,8 @@
 """ctypes binding of the FP64 CPU oracle (oracle/mast_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker and by bench.py's CPU-baseline arm.  The product library never
-imports this module.
+the reference its results are compared with, and by bench.py's CPU-baseline
+arm.  The product library never imports this module.
 """
 import ctypes
 import os
