@@ -180,6 +180,18 @@ void mg_problem_destroy(mg_problem *p);
 int mg_problem_info(const mg_problem *p, int64_t *n_dofs, int64_t *nnz, int32_t *n_colors);
 void *mg_problem_stream(mg_problem *p); /* the handle's cudaStream_t */
 
+/* ---- side loads ---- */
+/* Side boundary conditions (PhysicsDisciplineBase side loads), replacing earlier ones:
+   HEX8 physics: "pressure" p on element face `side` (libMesh Hex8 side numbering),
+   external load +int phi p n dA with n the outward reference normal
+   (StructuralElement3D::surface_pressure_residual, solid_element_3d.cpp:815-876);
+   heat: "heat_flux" q_n on element edge `side`, residual +int phi q_n th ds
+   (surface_flux_residual, heat_conduction_elem_base.cpp:876-913).  The load is
+   assembled on the GPU into the problem's load vector with the point loads.
+   MG_ENOTSUP for the membrane physics. */
+int mg_set_side_loads(mg_problem *p, int64_t n, const int32_t *elems, const int32_t *sides,
+                      const double *values);
+
 /* ---- design / properties ---- */
 int mg_set_design(mg_problem *p, const double *rho_elem);
 int mg_set_design_device(mg_problem *p, const double *rho_elem_device);

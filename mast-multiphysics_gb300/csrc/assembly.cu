@@ -15,6 +15,7 @@
 #include <math.h>
 
 #include "hex8_gl.cuh"
+#include "side_loads.cuh"
 #include "mg_internal.h"
 
 namespace mg {
@@ -396,6 +397,54 @@ __global__ void ks_combine_kernel(const double *__restrict__ sums, int64_t n_el,
     out[e] = dEs[e] / Es[e] * sums[2 * n_el + e] * inv_s0I + (adj ? adj[e] : 0.0);
 }
 
+// Side loads of the elements of one colour (thread per element; elements of a colour
+// share no node, so the scatter is atomic-free): HEX8 pressure adds +int phi p n to F,
+// QUAD4 heat flux adds -int phi q_n th (the flux enters the residual with +).
+__global__ void side_load_kernel(const double *__restrict__ coords, const int32_t *__restrict__ conn,
+                                 const int32_t *__restrict__ elem_list, int64_t n_items, int hex,
+                                 const double *__restrict__ side_vals, double th, double *__restrict__ F) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_items) return;
+    const int64_t e = elem_list[t];
+    if (hex) {
+        const int32_t *en = conn + e * 8;
+        double X[24], f[24];
+        bool any = false;
+        for (int sd = 0; sd < 6; sd++) {
+            const double v = side_vals[e * 6 + sd];
+            if (v == 0.0) continue;
+            if (!any) {
+                for (int i = 0; i < 24; i++) {
+                    X[i] = coords[(int64_t)en[i / 3] * 3 + i % 3];
+                    f[i] = 0.0;
+                }
+                any = true;
+            }
+            sl::hex8_pressure_load(X, sd, v, f);
+        }
+        if (any)
+            for (int i = 0; i < 24; i++) F[(int64_t)en[i / 3] * 3 + i % 3] += f[i];
+    } else {
+        const int32_t *en = conn + e * 4;
+        double X[8], f[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < 8; i++) X[i] = coords[(int64_t)en[i / 2] * 2 + i % 2];
+        bool any = false;
+        for (int sd = 0; sd < 4; sd++) {
+            const double v = side_vals[e * 4 + sd];
+            if (v == 0.0) continue;
+            any = true;
+            sl::quad4_flux_load(X, sd, v, th, f);
+        }
+        if (any)
+            for (int a = 0; a < 4; a++) F[en[a]] -= f[a];
+    }
+}
+
+__global__ void zero_fixed_kernel(double *__restrict__ v, const uint8_t *__restrict__ fixed, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && fixed[i]) v[i] = 0.0;
+}
+
 // f_e = K_e u_e for element-matrix requests (var-blocked order)
 __global__ void elem_matvec_kernel(const double *__restrict__ Ke, const double *__restrict__ X,
                                    const int32_t *__restrict__ conn, int64_t first, int64_t count,
@@ -766,7 +815,7 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
         }
         if (d_R) {
             residual_finish_kernel<<<blocks_for(p->n_dofs, 256), 256, 0, p->stream>>>(
-                d_R, d_X, nullptr, p->d_fixed, p->n_dofs);
+                d_R, d_X, p->d_F, p->d_fixed, p->n_dofs);
             MG_CUDA_TRY(cudaGetLastError());
         }
         MG_TRY(read_status(p, st));
@@ -850,6 +899,31 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
             d_R, d_X, p->d_F, p->d_fixed, p->n_dofs);
         MG_CUDA_TRY(cudaGetLastError());
     }
+    return MG_OK;
+}
+
+// d_F = the point loads + the side loads of p->d_side (nullable), zero on constrained
+// dofs; h_F receives a copy for the host-side consumers (the mixed form's set-up)
+int assemble_side_loads(mg_problem *p) {
+    MG_CUDA_TRY(cudaMemcpyAsync(p->d_F, p->h_F_point.data(), p->n_dofs * sizeof(double),
+                                cudaMemcpyHostToDevice, p->stream));
+    if (p->d_side) {
+        const int hex = p->dim == 3;
+        for (int c = 0; c < p->n_colors; c++) {
+            int64_t cnt = p->color_ptr[c + 1] - p->color_ptr[c];
+            side_load_kernel<<<blocks_for(cnt, 128), 128, 0, p->stream>>>(
+                p->d_coords, p->d_conn, p->d_color_elems + p->color_ptr[c], cnt, hex, p->d_side,
+                p->mat.thickness, p->d_F);
+            MG_CUDA_TRY(cudaGetLastError());
+        }
+        count_launches(p->n_colors);
+    }
+    zero_fixed_kernel<<<blocks_for(p->n_dofs, 256), 256, 0, p->stream>>>(p->d_F, p->d_fixed, p->n_dofs);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    MG_CUDA_TRY(cudaMemcpyAsync(p->h_F.data(), p->d_F, p->n_dofs * sizeof(double), cudaMemcpyDeviceToHost,
+                                p->stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
     return MG_OK;
 }
 

@@ -143,7 +143,7 @@ int release(mg_problem *p) {
     void *ptrs[] = {p->d_coords, p->d_conn, p->d_color_elems, p->d_fixed, p->d_F, p->d_rho,
                     p->d_E, p->d_dE, p->d_s, p->d_q, p->d_conv_mask, p->A.rowptr, p->A.cols,
                     p->A.vals, p->d_emap, p->d_fix_zero, p->d_fix_diag, p->d_X, p->d_R,
-                    p->d_tmp, p->d_tmp2, p->d_elem_out, p->d_red, p->d_ks};
+                    p->d_tmp, p->d_tmp2, p->d_elem_out, p->d_red, p->d_ks, p->d_side};
     for (void *q : ptrs) dev_free(q);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -253,6 +253,7 @@ int create_impl(const mg_mesh_desc *mesh, const mg_material_desc *mat, const mg_
     }
     for (int64_t d = 0; d < p->n_dofs; d++)
         if (p->h_fixed[d]) p->h_F[d] = 0.0;
+    p->h_F_point = p->h_F;
 
     // ---- colouring (no two elements of a colour share a node) ----
     std::vector<int32_t> color(ne, 0);
@@ -729,6 +730,37 @@ int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc
         MG_TRY(to_host_vec(p, p->d_elem_out, dc, p->n_elems));
         for (int64_t e = 0; e < p->n_elems; e++) dc[e] = -dc[e];
     }
+    return MG_OK;
+}
+
+int mg_set_side_loads(mg_problem *p, int64_t n, const int32_t *elems, const int32_t *sides,
+                      const double *values) {
+    // PhysicsDisciplineBase side boundary conditions: "pressure" on HEX8 faces
+    // (StructuralElement3D::surface_pressure_residual, solid_element_3d.cpp:815-876) and
+    // "heat_flux" on QUAD4 edges (surface_flux_residual, heat_conduction_elem_base.cpp:876-913);
+    // replaces the previous side loads, values of a repeated (element, side) add up
+    if (!p || n < 0 || (n > 0 && (!elems || !sides || !values))) return MG_EINVAL;
+    int ns;
+    if (p->physics == MG_PHYSICS_ELASTICITY_HEX8 || p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) ns = 6;
+    else if (p->physics == MG_PHYSICS_HEAT_QUAD4) ns = 4;
+    else {
+        set_error("side loads: pressure on HEX8 faces or heat flux on QUAD4 edges only");
+        return MG_ENOTSUP;
+    }
+    std::vector<double> h((size_t)p->n_elems * ns, 0.0);
+    for (int64_t i = 0; i < n; i++) {
+        if (elems[i] < 0 || elems[i] >= p->n_elems || sides[i] < 0 || sides[i] >= ns ||
+            !std::isfinite(values[i])) {
+            set_error("side load %lld: element %d side %d value %g", (long long)i, elems[i], sides[i], values[i]);
+            return MG_EINVAL;
+        }
+        h[(size_t)elems[i] * ns + sides[i]] += values[i];
+    }
+    if (!p->d_side) MG_TRY(dev_alloc_n(&p->d_side, h.size()));
+    MG_CUDA_TRY(cudaMemcpyAsync(p->d_side, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                p->stream));
+    MG_TRY(assemble_side_loads(p));
+    matfree_free(p);  // the mixed form copies the load vector when it is set up
     return MG_OK;
 }
 

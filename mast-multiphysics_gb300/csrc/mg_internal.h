@@ -87,7 +87,8 @@ struct mg_problem {
     std::vector<double> h_coords;
     std::vector<int32_t> h_conn;
     std::vector<uint8_t> h_fixed;
-    std::vector<double> h_F;
+    std::vector<double> h_F;         // external load: point loads + side loads
+    std::vector<double> h_F_point;   // the point loads alone
     std::vector<int64_t> color_ptr;  // n_colors + 1 offsets into d_color_elems
     int n_colors = 0;
 
@@ -116,6 +117,7 @@ struct mg_problem {
     double *d_X = nullptr, *d_R = nullptr, *d_tmp = nullptr, *d_tmp2 = nullptr;
     double *d_elem_out = nullptr;     // per-element scalar outputs
     double *d_ks = nullptr;           // KS stress output scratch (6 n_elems + 8), allocated on use
+    double *d_side = nullptr;         // side-load values, n_elems x (6 HEX8 faces | 4 QUAD4 edges)
     double *d_red = nullptr;          // reduction scratch
     int red_blocks = 0;
     mg::KrylovWork kw;
@@ -130,6 +132,7 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
 int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t count,
                      double *d_Ke, double *d_fe);
 int launch_assembly(mg_problem *p, const double *d_X, int reps);
+int assemble_side_loads(mg_problem *p);
 // KS stress output (d_ks: 6 n_elems + 8 doubles of scratch)
 int ks_stress_values(mg_problem *p, const double *d_X, double p_ks, double sigma0, double penal,
                      double *d_ks, double host_out[3]);

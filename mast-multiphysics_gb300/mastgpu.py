@@ -208,6 +208,7 @@ def lib(autobuild=True):
     L.mg_compliance.argtypes = [_vp, _vp, _vp, _vp]
     L.mg_adjoint_solve.argtypes = [_vp, _vp, _vp, ctypes.POINTER(SolveOpts), _vp]
     L.mg_ks_stress.argtypes = [_vp, _vp, _dbl, _dbl, _dbl, _vp, _vp, _vp]
+    L.mg_set_side_loads.argtypes = [_vp, _i64, _vp, _vp, _vp]
     L.mg_mean_temperature.argtypes = [_vp, _vp, ctypes.POINTER(SolveOpts), _vp, _vp, _vp]
     L.mg_debug_matfree_apply.argtypes = [_vp, ctypes.c_int, _vp, _vp]
     L.mg_compliance_resident.argtypes = [_vp, _vp]
@@ -451,6 +452,15 @@ class Problem:
         dc = np.zeros(self.n_elems) if want_sens else None
         check(lib().mg_compliance(self.h, _p(Xa), ctypes.byref(c), _p(dc)), "mg_compliance")
         return c.value, dc
+
+    def set_side_loads(self, elems, sides, values):
+        """pressure on HEX8 faces / heat flux on QUAD4 edges (mg_set_side_loads)"""
+        e = np.ascontiguousarray(elems, dtype=np.int32)
+        s = np.ascontiguousarray(sides, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if not (e.shape == s.shape == v.shape):
+            raise ValueError("elems, sides and values must have one entry per side load")
+        check(lib().mg_set_side_loads(self.h, e.shape[0], _p(e), _p(s), _p(v)), "mg_set_side_loads")
 
     def ks_stress(self, p_ks, sigma0, stress_penalty=0.0, X=None, want_sens=True):
         """KS-aggregated von Mises stress, the largest von Mises stress and (want_sens) the

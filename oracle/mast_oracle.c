@@ -509,6 +509,51 @@ void or_quad4_heat_convection(const double X[8], int side, double hc, double Tin
     }
 }
 
+/* surface_flux_residual (heat_conduction_elem_base.cpp:876-913): the residual
+   gets f += JxW phi q_n th over the edge (2-point rule), q_n the outward flux. */
+void or_quad4_heat_flux(const double X[8], int side, double flux, double th, double f[4]) {
+    int n0 = QUAD4_SIDE[side][0], n1 = QUAD4_SIDE[side][1];
+    double dx = X[n1 * 2] - X[n0 * 2], dy = X[n1 * 2 + 1] - X[n0 * 2 + 1];
+    double L = sqrt(dx * dx + dy * dy);
+    memset(f, 0, 4 * sizeof(double));
+    for (int qp = 0; qp < 2; qp++) {
+        double t = GP[qp], JxW = GW[qp] * 0.5 * L;
+        f[n0] += JxW * 0.5 * (1. - t) * flux * th;
+        f[n1] += JxW * 0.5 * (1. + t) * flux * th;
+    }
+}
+
+/* libMesh Hex8 side -> node map (counter-clockwise seen from outside) */
+static const int HEX8_SIDE[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                                    {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+
+/* StructuralElement3D::surface_pressure_residual (solid_element_3d.cpp:815-876)
+   on the side's own QUAD4 finite element: per 2x2 Gauss point JxW = |x_xi x
+   x_eta|, unit outward normal n = (x_xi x x_eta)/JxW, and the residual gets
+   -JxW phi p n; returned here as the external load f_ext[d*8 + a] (var-blocked)
+   = +sum_qp JxW phi_a p n_d. */
+void or_hex8_pressure(const double X[24], int side, double p, double f[24]) {
+    memset(f, 0, 24 * sizeof(double));
+    for (int qp = 0; qp < 4; qp++) {
+        double xi[2] = {GP[qp & 1], GP[qp >> 1]}, phi[4], dphi[8];
+        or_quad4_shape(xi, phi, dphi);
+        double t1[3] = {0, 0, 0}, t2[3] = {0, 0, 0};
+        for (int i = 0; i < 4; i++) {
+            const double *x = X + 3 * HEX8_SIDE[side][i];
+            for (int d = 0; d < 3; d++) {
+                t1[d] += dphi[i * 2] * x[d];
+                t2[d] += dphi[i * 2 + 1] * x[d];
+            }
+        }
+        double c[3] = {t1[1] * t2[2] - t1[2] * t2[1], t1[2] * t2[0] - t1[0] * t2[2],
+                       t1[0] * t2[1] - t1[1] * t2[0]};
+        const double area = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        const double JxW = GW[qp & 1] * GW[qp >> 1] * area;
+        for (int i = 0; i < 4; i++)
+            for (int d = 0; d < 3; d++) f[d * 8 + HEX8_SIDE[side][i]] += JxW * phi[i] * p * (c[d] / area);
+    }
+}
+
 /* volume_heat_source_residual (heat_conduction_elem_base.cpp:1710-1745):
    f -= JxW phi q th. */
 void or_quad4_heat_source(const double X[8], double q, double th, double f[4]) {

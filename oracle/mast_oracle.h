@@ -50,6 +50,9 @@ int or_hex8_internal(const double X[24], double E, double nu, const double u[24]
 int or_hex8_internal_gl(const double X[24], double E, double nu, const double u[24],
                         double f[24], double K[576]);
 /* Gauss-point stress (Voigt), von Mises, JxW and d sigma / d u (nullable, 8 x 6 x 24) */
+/* side loads: HEX8 pressure as an external load (var-blocked), QUAD4 heat flux residual */
+void or_hex8_pressure(const double X[24], int side, double p, double f[24]);
+void or_quad4_heat_flux(const double X[8], int side, double flux, double th, double f[4]);
 int or_hex8_stress(const double X[24], double E, double nu, const double u[24], int nonlinear,
                    double sig[48], double vm[8], double JxW_out[8], double *dsig);
 int or_hex8_internal_sens(const double X[24], double dE, double nu,

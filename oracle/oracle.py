@@ -72,6 +72,10 @@ def lib():
         L.or_hex8_internal_sens.argtypes = [_f64p, d, d, _f64p, _f64p]
         L.or_hex8_internal_gl.argtypes = [_f64p, d, d, _f64p, _f64p, ctypes.c_void_p]
         L.or_hex8_stress.argtypes = [_f64p, d, d, _f64p, i32, _f64p, _f64p, _f64p, vp]
+        L.or_hex8_pressure.argtypes = [_f64p, i32, d, _f64p]
+        L.or_hex8_pressure.restype = None
+        L.or_quad4_heat_flux.argtypes = [_f64p, i32, d, d, _f64p]
+        L.or_quad4_heat_flux.restype = None
         L.or_quad4_membrane_internal.argtypes = [_f64p, d, d, d, _f64p, _f64p, vp]
         L.or_quad4_heat_internal.argtypes = [_f64p, d, d, d, d, _f64p, i32, _f64p, vp]
         L.or_quad4_heat_internal_sens.argtypes = [_f64p, d, d, d, _f64p, _f64p]
@@ -309,6 +313,20 @@ def hex8_gl_compliance_sens(coords, conn, dE_elem, nu, u, E_elem, F, fixed):
         f1, _ = hex8_internal_gl(coords[conn[e]], 1.0, nu, ue, want_K=False)
         dc[e] = -dE_elem[e] * float(le @ f1)
     return dc
+
+
+def hex8_pressure(X, side, p):
+    """external load (var-blocked) of pressure p on HEX8 side `side`"""
+    f = np.zeros(24)
+    lib().or_hex8_pressure(np.ascontiguousarray(X, dtype=np.float64).reshape(24), side, p, f)
+    return f
+
+
+def quad4_heat_flux(X, side, flux, th):
+    """residual contribution of an outward heat flux on QUAD4 side `side`"""
+    f = np.zeros(4)
+    lib().or_quad4_heat_flux(np.ascontiguousarray(X, dtype=np.float64).reshape(8), side, flux, th, f)
+    return f
 
 
 def hex8_stress(X, E, nu, u, nonlinear=False, want_dsig=False):
