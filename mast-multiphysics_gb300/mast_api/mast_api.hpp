@@ -15,7 +15,8 @@
 //   MAST::Solid2DSectionElementPropertyCard      src/property_cards/solid_*d_section_element_property_card.h
 //   MAST::DirichletBoundaryCondition::init(bid, vars)   src/boundary_condition/dirichlet_boundary_condition.h:67
 //   MAST::PointLoadCondition(POINT_LOAD)::add_node, "load"  src/boundary_condition/point_load_condition.h
-//   MAST::BoundaryConditionBase(CONVECTION_HEAT_FLUX / HEAT_SOURCE)  src/base/boundary_condition_base.h:29-51
+//   MAST::BoundaryConditionBase(CONVECTION_HEAT_FLUX / HEAT_SOURCE / SURFACE_PRESSURE / HEAT_FLUX)
+//                                                src/base/boundary_condition_base.h:29-51
 //   MAST::PhysicsDisciplineBase::add_dirichlet_bc / add_point_load / add_side_load /
 //     add_volume_load / set_property_for_subdomain   src/base/physics_discipline_base.h:94-206
 //   MAST::StructuralSystemInitialization, MAST::HeatConductionSystemInitialization
@@ -351,10 +352,20 @@ public:
                 }
         return out;
     }
-    // element sides on a boundary id (QUAD4: libMesh side numbers 0..3)
+    // element sides on a boundary id of a structured grid (libMesh side numbers: QUAD4
+    // 0..3; HEX8 0..5, where build_cube's boundary id b is side b of the boundary elements)
     std::vector<std::pair<int32_t, int32_t>> boundary_sides(int bid) const {
         std::vector<std::pair<int32_t, int32_t>> out;
-        if (type != QUAD4) return out;
+        if (type == HEX8) {
+            if (nx == 0) return out;
+            for (int k = 0; k < nz; k++)
+                for (int j = 0; j < ny; j++)
+                    for (int i = 0; i < nx; i++) {
+                        const bool on[6] = {k == 0, j == 0, i == nx - 1, j == ny - 1, i == 0, k == nz - 1};
+                        if (bid >= 0 && bid < 6 && on[bid]) out.push_back({i + nx * (j + ny * k), bid});
+                    }
+            return out;
+        }
         for (int j = 0; j < ny; j++)
             for (int i = 0; i < nx; i++) {
                 const int32_t e = i + nx * j;
@@ -455,7 +466,7 @@ private:
 };
 
 // ------------------------------------------------------------------ boundary conditions
-enum BoundaryConditionType { POINT_LOAD, DIRICHLET, CONVECTION_HEAT_FLUX, HEAT_SOURCE };
+enum BoundaryConditionType { POINT_LOAD, DIRICHLET, CONVECTION_HEAT_FLUX, HEAT_SOURCE, SURFACE_PRESSURE, HEAT_FLUX };
 
 class BoundaryConditionBase : public MaterialPropertyCardBase {
 public:
@@ -888,6 +899,21 @@ private:
         mesh.grid_ny = m.ny;
         mesh.grid_nz = m.nz;
         check(mg_problem_create(&mesh, &md, &bc, &_p), "mg_problem_create");
+        // surface pressure (3D solid faces) and heat flux (2D edges) side loads
+        std::vector<int32_t> se, ss;
+        std::vector<Real> sv;
+        for (auto &sl : _disc->_side) {
+            const BoundaryConditionType t = sl.second->type();
+            if (t != SURFACE_PRESSURE && t != HEAT_FLUX) continue;
+            const Real v = sl.second->value(t == SURFACE_PRESSURE ? "pressure" : "heat_flux");
+            for (auto &es : m.boundary_sides(sl.first)) {
+                se.push_back(es.first);
+                ss.push_back(es.second);
+                sv.push_back(v);
+            }
+        }
+        if (!se.empty())
+            check(mg_set_side_loads(_p, (int64_t)se.size(), se.data(), ss.data(), sv.data()), "side loads");
         if (!_rho.empty()) check(mg_set_design(_p, _rho.data()), "set_simp");
         if (!_scale.empty()) check(mg_set_elem_scale(_p, _scale.data()), "set_conductivity_scale");
     }

@@ -255,6 +255,31 @@ TEST_CASE("ks_stress_output_settings", "[cpu],[output]") {
 
 // the reference's set_get_strain_type section
 // (tests/property/mast_3d_isotropic_element_property_card.cpp:379-391)
+// build_cube's boundary id b is libMesh side b of the boundary elements: the
+// side's four nodes lie on that boundary's plane
+TEST_CASE("hex8_boundary_sides", "[cpu],[mesh]") {
+    MAST::Mesh mesh;
+    MAST::MeshTools::Generation::build_cube(mesh, 3, 2, 2, 0, 3, 0, 2, 0, 2);
+    static const int side_nodes[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                                         {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+    const int axis[6] = {2, 1, 0, 1, 0, 2};
+    const double plane[6] = {0, 0, 3, 2, 0, 2};
+    const size_t count[6] = {6, 6, 4, 6, 4, 6};
+    for (int b = 0; b < 6; b++) {
+        auto sides = mesh.boundary_sides(b);
+        REQUIRE(sides.size() == count[b]);
+        for (auto &es : sides) {
+            REQUIRE(es.second == b);
+            for (int i = 0; i < 4; i++) {
+                const int64_t n = mesh.conn[(size_t)es.first * 8 + side_nodes[b][i]];
+                const MAST::Point pt = mesh.point(n);
+                const double c = axis[b] == 0 ? pt.x : axis[b] == 1 ? pt.y : pt.z;
+                REQUIRE(c == plane[b]);
+            }
+        }
+    }
+}
+
 TEST_CASE("section_strain_type", "[cpu],[property]") {
     MAST::Solid3DSectionElementPropertyCard section;
     REQUIRE(section.strain_type() == MAST::LINEAR_STRAIN);

@@ -42,7 +42,7 @@ def run(tag):
 
 def test_cpp_mirror_cpu_cases():
     out = run("[cpu]")
-    assert "8 test cases" in out
+    assert "9 test cases" in out
 
 
 @pytest.mark.gpu
