@@ -268,14 +268,15 @@ int mg_debug_launch_assembly(mg_problem *p, const double *X, int reps);
    cannot call cudaMalloc: code that must not allocate after start-up (a
    request loop running inside a fixed device-memory budget) and host
    applications whose own pool owns all device memory.  The library allocates
-   nothing here: its scratch is one static device array of about 6.3 MB that
+   nothing here: its scratch is one static device array of about 5.3 MB that
    every GPU loading the library holds until exit, which limits n to
-   MG_STATIC_PCG_MAX_N (larger n returns MG_EINVAL).  The first call on a
-   device looks the array's address up (cudaGetSymbolAddress); make that first
-   call before any stream capture.  All calls share the array, so calls that
-   overlap on the GPU race; serialise them.  Returns MG_OK, MG_ENOCONV,
-   MG_EBREAKDOWN or MG_ENAN; *iterations and *relres (nullable) report the
-   iteration count and final relative residual. */
+   MG_STATIC_PCG_MAX_N (larger n returns MG_EINVAL).  Each call looks the
+   array's address up in the current device's context (cudaGetSymbolAddress).
+   The call blocks the calling thread until the solve ends: it synchronises
+   `stream` every 16 iterations to read the convergence state.  All calls share
+   the array, so calls that overlap on the GPU race; serialise them.  Returns
+   MG_OK, MG_ENOCONV, MG_EBREAKDOWN or MG_ENAN; *iterations and *relres
+   (nullable) report the iteration count and final relative residual. */
 #define MG_STATIC_PCG_MAX_N 131072
 int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t *cols, const double *vals,
                       const double *b, double *x, double rtol, int32_t max_iterations,

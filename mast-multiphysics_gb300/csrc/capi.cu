@@ -739,7 +739,10 @@ int mg_set_side_loads(mg_problem *p, int64_t n, const int32_t *elems, const int3
     // (StructuralElement3D::surface_pressure_residual, solid_element_3d.cpp:815-876) and
     // "heat_flux" on QUAD4 edges (surface_flux_residual, heat_conduction_elem_base.cpp:876-913);
     // replaces the previous side loads, values of a repeated (element, side) add up
-    if (!p || n < 0 || (n > 0 && (!elems || !sides || !values))) return MG_EINVAL;
+    if (!p || n < 0 || (n > 0 && (!elems || !sides || !values))) {
+        set_error("mg_set_side_loads: invalid argument");
+        return MG_EINVAL;
+    }
     int ns;
     if (p->physics == MG_PHYSICS_ELASTICITY_HEX8 || p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) ns = 6;
     else if (p->physics == MG_PHYSICS_HEAT_QUAD4) ns = 4;

@@ -17,7 +17,6 @@
 #include <math.h>
 
 #include <algorithm>
-#include <mutex>
 
 #include "mg_internal.h"
 
@@ -632,10 +631,10 @@ int krylov_solve(mg_problem *p, const CsrMatrix &A, const double *d_b, double *d
 // ---------------------------------------------------------------------------
 // Allocation-free Jacobi-PCG on a caller-owned CSR (mg_pcg_csr_static).
 //
-// The solver scratch (r, z, two search directions, A p, the Jacobi inverse,
+// The solver scratch (r, z, the search direction p, A p, the Jacobi inverse,
 // the per-block partial sums and the solver state) lives in the file-scope
 // device array below instead of memory from cudaMalloc.  Every GPU that loads
-// this library holds the array (about 6.3 MB) until the process exits.  All
+// this library holds the array (about 5.3 MB) until the process exits.  All
 // calls on a device share it and it keeps the last call's contents, so each
 // call re-initialises what must start at zero; calls that overlap on the GPU
 // (different streams or threads) race on it.
@@ -644,35 +643,27 @@ namespace mg {
 namespace {
 
 constexpr int64_t kStaticMaxN = MG_STATIC_PCG_MAX_N;
+constexpr int64_t kStaticVectors = 5;           // r, z, p, q = A p, D^-1
 constexpr int64_t kStaticParts = 3 * 152 * 16;  // 3 x the largest grid of the kernels
 constexpr int64_t kStaticStateDoubles = 32;     // >= sizeof(KrylovState) / 8
 static_assert(sizeof(KrylovState) <= kStaticStateDoubles * sizeof(double), "state slot");
 
-static __device__ __align__(256) double g_static_pcg_scratch[6 * kStaticMaxN + kStaticParts +
-                                                            kStaticStateDoubles];
+static __device__ __align__(256) double g_static_pcg_scratch[kStaticVectors * kStaticMaxN +
+                                                            kStaticParts + kStaticStateDoubles];
 
-std::mutex g_static_mutex;
-double *g_static_ptr[128] = {nullptr};
-
-// device address of the static array for the current device (looked up once)
+// Device address of the static array in the current device's context.  It is
+// looked up on every call rather than cached per device ordinal: after a
+// cudaDeviceReset, or under another context of the same device, the module is
+// loaded again at another address.  The lookup costs microseconds against a
+// solve that synchronises its stream every 16 iterations.
 int static_scratch(double **out) {
-    int dev = 0;
-    MG_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 128) {
-        set_error("device ordinal %d out of range", dev);
-        return MG_EINVAL;
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_pcg_scratch);
+    if (e != cudaSuccess || !ptr) {
+        set_error("cudaGetSymbolAddress(static PCG scratch): %s", cudaGetErrorString(e));
+        return MG_ECUDA;
     }
-    std::lock_guard<std::mutex> lock(g_static_mutex);
-    if (!g_static_ptr[dev]) {
-        void *ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_pcg_scratch);
-        if (e != cudaSuccess || !ptr) {
-            set_error("cudaGetSymbolAddress(static PCG scratch): %s", cudaGetErrorString(e));
-            return MG_ECUDA;
-        }
-        g_static_ptr[dev] = static_cast<double *>(ptr);
-    }
-    *out = g_static_ptr[dev];
+    *out = static_cast<double *>(ptr);
     return MG_OK;
 }
 
@@ -697,9 +688,10 @@ extern "C" int mg_pcg_csr_static(int64_t n, const int32_t *rowptr, const int32_t
     MG_TRY(static_scratch(&base));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     double *r = base, *z = base + kStaticMaxN, *p0 = base + 2 * kStaticMaxN,
-           *q = base + 4 * kStaticMaxN,
-           *dinv = base + 5 * kStaticMaxN, *partials = base + 6 * kStaticMaxN;
-    KrylovState *state = reinterpret_cast<KrylovState *>(base + 6 * kStaticMaxN + kStaticParts);
+           *q = base + 3 * kStaticMaxN, *dinv = base + 4 * kStaticMaxN,
+           *partials = base + kStaticVectors * kStaticMaxN;
+    KrylovState *state =
+        reinterpret_cast<KrylovState *>(base + kStaticVectors * kStaticMaxN + kStaticParts);
     CsrMatrix A;
     A.n = n;
     A.nnz = 0;

@@ -1,7 +1,8 @@
 """Extract the known-answer values of MAST's own unit tests into
 reference_pins.json (the fixture tests/test_oracle_pins.py reads).
 
-Reads, as text, from the MAST source tree (default /root/reference):
+Reads, as text, from the MAST source tree whose root is the one required
+argument (python make_reference_pins.py <mast-source-root>):
   tests/material/mast_isotropic_material.cpp        hand-computed C matrices
   tests/element/structural/2D/mast_structural_element_2d.h   default E, nu, h, k
   tests/element/structural/2D/quad4/
@@ -18,7 +19,9 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python make_reference_pins.py <mast-source-root>")
+REF = sys.argv[1]
 
 
 def read(rel):

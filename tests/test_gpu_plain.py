@@ -154,8 +154,8 @@ def test_heat_newton_and_adjoint_match_oracle():
     assert rep.status == 0
     assert rel(T, T_ref) < RTOL_SOL
     assert abs(q - hr.mean_temperature) / abs(hr.mean_temperature) < RTOL_SOL
-    assert abs(dk0 - hr.dq_dk0) / abs(hr.dq_dk0) < 1e-9
-    assert rel(ds, ds_ref) < 1e-9
+    assert abs(dk0 - hr.dq_dk0) / abs(hr.dq_dk0) < RTOL_SOL
+    assert rel(ds, ds_ref) < RTOL_SOL
 
 
 def test_membrane_element_matrices():
