@@ -14,11 +14,13 @@ value  -- solves/s of the mixed-precision form (tcgen05 split-TF32 matrix-free
 e2e    -- the same through the C ABI with host buffers: densities and initial
           guess copied in, solution and sensitivities copied out, every step.
 plain_fp64 -- the FP64 CSR Jacobi-PCG form on the same GPU (the 5x target's base).
-cpu_baseline -- the FP64 CPU restatement (oracle, Jacobi-PCG, all host threads):
-          assembly plus a bounded number of PCG iterations, extrapolated to the
-          oracle's own full-solve iteration count (tests/golden fixture).
+cpu_baseline -- the FP64 CPU restatement (oracle: assembly + Jacobi-PCG to 1e-8, all
+          host threads), one full solve timed; beside it a one-core figure (assembly
+          and a bounded number of PCG iterations on one thread, scaled to the full
+          iteration count, labelled as such).
 
---impl reference runs that CPU implementation alone (the reference arm).
+--impl reference runs that CPU implementation alone (the reference arm): every timed
+step is one full oracle solve of the same workload.
 """
 import argparse
 import ctypes
@@ -41,6 +43,15 @@ METRIC = "solves/s @1e-8 FP64 residual (SIMP cantilever design evaluation)"
 GOLDEN = os.path.join(REPO, "tests", "golden", "simp_128x64x64_seed0.npz")
 
 
+def bench_config(world):
+    """The workload description both arms print under "config" (identical keys and
+    values, so the two lines describe the same job)."""
+    return {"workload": WORKLOAD, "n_dofs": 1635075, "n_elems": 524288, "rtol": 1e-8,
+            "load": "unit -z over the 65 nodes of the x = max, z = 0 edge; x = 0 clamped",
+            "l2": "GPU arm: flushed between timed steps (512 MB write)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -49,7 +60,6 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="tf32x3", choices=["tf32", "bf16", "bf16x3", "tf32x3"])
     ap.add_argument("--preconditioner", default="multigrid", choices=["multigrid", "jacobi"])
-    ap.add_argument("--cpu-iters", type=int, default=40, help="PCG iterations in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -57,7 +67,10 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
     ap.add_argument("--no-autotune", action="store_true",
                     help="solve the headline problem with the default schedule instead of the autotuned one")
-    ap.add_argument("--serve-requests", type=int, default=1000, help="requests per arrival rate")
+    ap.add_argument("--serve-requests", type=int, default=1000,
+                    help="requests per arrival rate of the sweep")
+    ap.add_argument("--serve-full", type=int, default=10000,
+                    help="requests of the full-length stream (at the sweep's highest rate; 0: skip)")
     ap.add_argument("--kernel-only", default=None, choices=["mixed", "plain", "factored"],
                     help="only launch one kernel (tensor-core column operator, FP64 CG SpMV or the "
                          "factored multigrid level operator) --steps times after --warmup "
@@ -226,6 +239,33 @@ def bench_batch(M, n_designs=256, seed=0):
         times.append(time.perf_counter() - t0)
     t = min(times)
     relres = max(r.relres for r in reps)
+    # oracle checks outside the timed solves: the first design of every grid size (its
+    # first load case) and every load case of the first multi-case design of the two
+    # smallest sizes, each against an FP64 oracle solve to 1e-10 with sensitivities
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    picks = {}
+    for d, x in enumerate(designs):
+        key = (x["nx"], x["ny"], x["nz"])
+        if key not in picks:
+            picks[key] = (d, [0])
+    multi = next(d for d, x in enumerate(designs)
+                 if len(x["spans"]) > 1 and (x["nx"], x["ny"], x["nz"]) in M.BATCH_SIZES[:2])
+    checks = list(picks.values()) + [(multi, list(range(len(designs[multi]["spans"]))))]
+    ce, se, checked = 0.0, 0.0, []
+    t_or = time.perf_counter()
+    for d, cases in checks:
+        x = designs[d]
+        comp, dc, _ = b.results(d)
+        for k in cases:
+            j0, j1 = x["spans"][k]
+            _, dc_ref, r = O.simp_solve(O.simp_desc(x["nx"], x["ny"], x["nz"], load_y0=j0, load_y1=j1,
+                                                    rtol=1e-10, maxit=10 ** 6), x["rho"])
+            ce = max(ce, abs(comp[k] - r.compliance) / abs(r.compliance))
+            se = max(se, float(np.abs(dc[k] - dc_ref).max() / np.abs(dc_ref).max()))
+            checked.append("design %d case %d (%dx%dx%d)" % (d, k, x["nx"], x["ny"], x["nz"]))
+    oracle_check = {"checked": checked, "compliance_rel_err_max": ce, "sens_rel_err_max": se,
+                    "oracle": "FP64 Jacobi-PCG to 1e-10, all host threads", "seconds": time.perf_counter() - t_or}
     # plain FP64 estimate: one solve per problem at that problem's size
     sizes = sorted({(d["nx"], d["ny"], d["nz"]) for d in designs})
     tp = plain_time_per_size(M, sizes)
@@ -239,6 +279,7 @@ def bench_batch(M, n_designs=256, seed=0):
                          "coarse_degree": o.coarse_degree, "graph_chunk": o.graph_chunk,
                          "vec_blocks_per_sm": o.vec_blocks_per_sm, "inner_rtol": o.inner_rtol,
                          "tuning_seconds": tune_s},
+           "oracle_check": oracle_check,
            "plain_fp64_est_solves_per_s": b.n_problems / t_plain,
            "plain_fp64_method": "one timed plain solve per grid size x the batch's load cases",
            "speedup_vs_plain_fp64": t_plain / t}
@@ -246,19 +287,37 @@ def bench_batch(M, n_designs=256, seed=0):
     return res
 
 
-def bench_serve(M, rates, n_requests, big=True, seed=0):
-    """Request loop: Poisson streams over 64 design chains (config-4 mix)."""
+def bench_serve(M, rates, n_requests, big=True, seed=0, n_check=6):
+    """Request loop: Poisson streams over 64 design chains (config-4 mix).  After each
+    stream, the first n_check completed requests on grids up to 48x24x24 are checked
+    against the FP64 oracle (every load case: compliance)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
     o = M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0)
     sweep = []
     for rate, n in zip(rates, n_requests):
+        kw = dict(n_chains=64, big_fraction=0.02 if big else 0.0, seed=seed)
         with M.Server(o, hbm_cap_bytes=150 << 30) as s:
-            st, comp = s.run_synthetic(n, rate=rate, n_chains=64, big_fraction=0.02 if big else 0.0,
-                                       seed=seed)
+            st, comp = s.run_synthetic(n, rate=rate, **kw)
+        desc = M.synthetic_desc(n, rate, **kw)
+        err, checked, i = 0.0, 0, 0
+        while checked < n_check and i < n:
+            r = M.synthetic_request(desc, i, want_rho=False)
+            if r["grid"][0] <= 48:
+                r = M.synthetic_request(desc, i)
+                nx, ny, nz = r["grid"]
+                for k, (j0, j1) in enumerate(r["spans"]):
+                    _, _, ref = O.simp_solve(O.simp_desc(nx, ny, nz, load_y0=j0, load_y1=j1, rtol=1e-10,
+                                                         maxit=10 ** 6), r["rho"], want_sens=False)
+                    err = max(err, abs(comp[i, k] - ref.compliance) / abs(ref.compliance))
+                checked += 1
+            i += 1
         sweep.append({"rate_req_per_s": rate, "n_requests": n, "completed": st["completed"],
                       "failed": st["failed"], "p50_ms": st["p50_s"] * 1e3, "p99_ms": st["p99_s"] * 1e3,
                       "mean_ms": st["mean_s"] * 1e3, "requests_per_s": st["solves_per_s"],
                       "dofs_per_s": st["dofs_per_s"], "peak_inflight": st["peak_inflight"],
-                      "rebuilds": st["rebuilds"], "peak_resident_GB": st["peak_resident_bytes"] / 1e9})
+                      "rebuilds": st["rebuilds"], "peak_resident_GB": st["peak_resident_bytes"] / 1e9,
+                      "oracle_checked_requests": checked, "compliance_rel_err_vs_oracle": err})
     return {"workload": "simp_serving_64_chains_poisson", "hbm_cap_GB": 150, "sweep": sweep}
 
 
@@ -344,53 +403,78 @@ def peaks():
         return {}
 
 
-def cpu_sample(iters):
-    """Oracle (FP64 CPU restatement, all host threads): assembly + `iters`
-    Jacobi-PCG iterations of the 128x64x64 problem; solve time extrapolated with
-    the oracle's own full-solve iteration count at 1e-8."""
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O
-    g = np.load(GOLDEN)
-    n_full = int(g["iterations_1e8"])
-    rho = np.random.default_rng(SEED).uniform(0.01, 1.0, NX * NY * NZ)
-    d = O.simp_desc(NX, NY, NZ, rtol=1e-8, maxit=iters)
+def cpu_full_solve(O, rho):
+    """One full oracle solve of the 128x64x64 problem to 1e-8 (FP64 assembly +
+    Jacobi-PCG on all host threads), timed; returns (seconds, report)."""
+    d = O.simp_desc(NX, NY, NZ, rtol=1e-8, maxit=10 ** 6)
     t0 = time.time()
     _, _, rep = O.simp_solve(d, rho, want_sens=False)
-    wall = time.time() - t0
-    t_iter = rep.t_solve / max(rep.iterations, 1)
-    t_solve = rep.t_assemble + n_full * t_iter
-    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": O.max_threads(), "kind": "port",
-            "sample": "assembly + %d Jacobi-PCG iterations of the 128x64x64 problem (%.1f s); "
-                      "solve time = t_assembly %.2f s + %d iterations x %.1f ms (the oracle's own "
-                      "iteration count to 1e-8)" % (rep.iterations, wall, rep.t_assemble, n_full,
-                                                   t_iter * 1e3),
-            "seconds_per_solve": t_solve}
+    return time.time() - t0, rep
+
+
+def cpu_baseline(one_core_iters=20):
+    """The CPU baseline on this host: one full oracle solve on all host threads
+    (measured), and the one-core figure: assembly + `one_core_iters` PCG iterations on
+    one thread, scaled to the full solve's iteration count (an extrapolation, stated)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    rho = np.random.default_rng(SEED).uniform(0.01, 1.0, NX * NY * NZ)
+    cores = O.max_threads()
+    secs, rep = cpu_full_solve(O, rho)
+    O.set_threads(1)
+    try:
+        d1 = O.simp_desc(NX, NY, NZ, rtol=1e-8, maxit=one_core_iters)
+        t0 = time.time()
+        _, _, r1 = O.simp_solve(d1, rho, want_sens=False)
+        wall1 = time.time() - t0
+    finally:
+        O.set_threads(cores)
+    t1 = r1.t_assemble + rep.iterations * r1.t_solve / max(r1.iterations, 1)
+    return {"value": 1.0 / secs, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": "one full solve of the 128x64x64 problem to 1e-8 (FP64 assembly + %d "
+                      "Jacobi-PCG iterations, %.1f s, relres %.2e), measured"
+                      % (rep.iterations, secs, rep.relres),
+            "seconds_per_solve": secs, "iterations": rep.iterations,
+            "one_core": {"solves_per_s": 1.0 / t1, "seconds_per_solve": t1, "cores": 1,
+                         "method": "extrapolated: assembly %.2f s + %d iterations x %.1f ms "
+                                   "(%d iterations timed on one thread, %.1f s)"
+                                   % (r1.t_assemble, rep.iterations,
+                                      1e3 * r1.t_solve / max(r1.iterations, 1), r1.iterations,
+                                      wall1)}}
 
 
 def run_reference(args):
+    """The reference arm: the FP64 CPU restatement on all host threads, each timed step
+    one full solve to 1e-8 of the same workload (warm-up steps: assembly plus a few PCG
+    iterations, which only page the oracle in and start its threads)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    rho = np.random.default_rng(SEED).uniform(0.01, 1.0, NX * NY * NZ)
     for _ in range(args.warmup):
-        cpu_sample(max(5, args.cpu_iters // 4))
-    vals = []
+        O.simp_solve(O.simp_desc(NX, NY, NZ, rtol=1e-8, maxit=5), rho, want_sens=False)
+    secs = []
     t0 = time.time()
     for _ in range(args.steps):
-        vals.append(cpu_sample(args.cpu_iters))
+        t, rep = cpu_full_solve(O, rho)
+        secs.append(t)
     wall = time.time() - t0
-    v = statistics.median([x["value"] for x in vals])
-    cb = dict(vals[-1])
-    cb["value"] = v
+    ms = 1e3 * sum(secs) / len(secs)
+    v = 1e3 / ms
+    cb = {"value": v, "unit": "solves/s", "cores": O.max_threads(), "kind": "port",
+          "sample": "every step one full solve of the 128x64x64 problem to 1e-8 (FP64 assembly "
+                    "+ %d Jacobi-PCG iterations, relres %.2e), measured; warm-up steps: assembly "
+                    "+ 5 iterations" % (rep.iterations, rep.relres)}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U[0.01,1] densities)",
-            "config": {"workload": WORKLOAD, "n_dofs": 1635075, "n_elems": 524288,
-                       "rtol": 1e-8, "solver": "FP64 CSR Jacobi-PCG (CPU restatement)",
-                       "l2": "n/a (CPU)"},
-            "cpu_baseline": cb, "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
-                                        "d2h_bytes_per_step": 0},
-            "wall_s": wall}
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (CPU restatement: CSR assembly + Jacobi-PCG)",
+            "data": "synthetic (seeded U[0.01,1] densities, default_rng(0))",
+            "config": bench_config(world), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "step_s": [round(x, 3) for x in secs], "wall_s": wall}
     print(json.dumps(line), flush=True)
 
 
@@ -542,6 +626,33 @@ def main():
                "host_buffers": "pinned"}
     dc_err = float(np.abs(dch - g["dc"]).max() / np.abs(g["dc"]).max())
 
+    # ---------------- the BF16-input variant on the same workload: split BF16 tensor-core
+    # operator (three BF16 products, FP32 accumulation), the same schedule otherwise;
+    # inputs resident, CUDA events, L2 flushed between solves; errors against the fixture
+    bf16 = None
+    if prec != M.MIXED_BF16X3:
+        ob = M.SolveOpts.from_buffer_copy(opts)
+        ob.precision = M.MIXED_BF16X3
+        step_resident(ob)  # graph capture
+        bt, brep = [], None
+        for _ in range(3):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            b0 = torch.cuda.Event(enable_timing=True)
+            b1 = torch.cuda.Event(enable_timing=True)
+            b0.record(stream)
+            brep, bc = step_resident(ob)
+            b1.record(stream)
+            torch.cuda.synchronize()
+            bt.append(b0.elapsed_time(b1))
+        _, bdc = prob.compliance()
+        bf16 = {"precision": "bf16x3", "solves_per_s": 1e3 * len(bt) / sum(bt),
+                "ms_per_solve": sum(bt) / len(bt), "status": brep.status,
+                "iterations": brep.krylov_iterations, "refinements": brep.refinements,
+                "relres_fp64": brep.relres,
+                "compliance_rel_err_vs_oracle": abs(bc - float(g["compliance"])) / float(g["compliance"]),
+                "sens_rel_err_vs_oracle": float(np.abs(bdc - g["dc"]).max() / np.abs(g["dc"]).max())}
+
     # ---------------- dominant kernel: tensor-core column operator, timed alone
     n = prob.n_dofs
     n_el = NX * NY * NZ
@@ -621,7 +732,11 @@ def main():
     serve = None
     if not args.no_serve:
         rates = [50, 200, 500, 1000, 2000]
-        serve = bench_serve(M, rates, [args.serve_requests] * len(rates))
+        counts = [args.serve_requests] * len(rates)
+        if args.serve_full:
+            rates.append(2000)
+            counts.append(args.serve_full)
+        serve = bench_serve(M, rates, counts)
         plain_sz = plain_time_per_size(M, list(M.BATCH_SIZES) + [(192, 96, 96)])
         # request mix: chain grids uniform over the five sizes, 2 % of chains on
         # 192x96x96, 2.5 load cases on average
@@ -632,7 +747,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_sample(args.cpu_iters)
+        cpu = cpu_baseline()
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
@@ -641,11 +756,9 @@ def main():
                 "dtype": "f32 (TF32 tensor-core operator) / f64 refinement" if args.precision.startswith("tf32")
                 else "f32 (BF16 tensor-core operator) / f64 refinement",
                 "data": "synthetic (seeded U[0.01,1] densities, default_rng(0))",
-                "config": {"workload": WORKLOAD, "n_dofs": n, "n_elems": n_el, "rtol": 1e-8,
-                           "precision": args.precision, "inner_rtol": opts.inner_rtol,
-                           "preconditioner": args.preconditioner, "schedule": schedule,
-                           "l2": "flushed between steps (512 MB write)",
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "config": bench_config(world),
+                "solver": {"precision": args.precision, "inner_rtol": opts.inner_rtol,
+                           "preconditioner": args.preconditioner, "schedule": schedule},
                 "step_ms": [round(x, 3) for x in ms],
                 "dof_per_s": value * n,
                 "iterations": reps[-1][0], "refinements": reps[-1][1],
@@ -654,6 +767,7 @@ def main():
                 "e2e": e2e,
                 "roofline": roof, "roofline_level_operator": roof_fac, "plain_fp64": plain,
                 "speedup_vs_plain_fp64": (value / plain["solves_per_s"]) if plain else None,
+                "bf16x3": bf16,
                 "small_configs": small, "batch": batch, "serving": serve,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "wall_s_timed": t_wall}

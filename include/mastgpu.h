@@ -229,6 +229,37 @@ int mg_ks_stress(mg_problem *p, const double *X, double p_ks, double sigma0, dou
    rows give lambda = 0); the Krylov method of opts (BiCGStab for heat) */
 int mg_adjoint_solve(mg_problem *p, const double *X, const double *rhs, const mg_solve_opts *opts,
                      double *lambda);
+/* J(X) du_dp = -dR/dp for one parameter (kind, index as mg_sensitivity_assemble) with the
+   consistent Jacobian at X: the forward sensitivity of the solution, as
+   MAST::NonlinearSystem::sensitivity_solve (src/base/nonlinear_system.cpp:741-794,
+   declared src/base/nonlinear_system.h:142) forms it for
+   AssemblyBase::calculate_output_direct_sensitivity (src/base/assembly_base.cpp:434-520).
+   Constrained rows give du_dp = 0; the Krylov method of opts (BiCGStab for heat). */
+int mg_sensitivity_solve(mg_problem *p, const double *X, int32_t kind, int64_t index,
+                         const mg_solve_opts *opts, double *du_dp);
+/* dq/dX of an output at X (host, nullable: the resident solution), zero on constrained
+   dofs: MAST::AssemblyBase::calculate_output_derivative (src/base/assembly_base.cpp:336-429).
+   MG_OUTPUT_COMPLIANCE: C = F.X, dC/dX = F (structural physics); MG_OUTPUT_MEAN_TEMPERATURE:
+   the lumped weights of (1/|Omega|) int T (heat). */
+#define MG_OUTPUT_COMPLIANCE 0
+#define MG_OUTPUT_MEAN_TEMPERATURE 1
+int mg_output_derivative(mg_problem *p, int32_t output, const double *X, double *dq_dX);
+/* One element at an element-local solution: the per-element plugin call
+   MAST::NonlinearImplicitAssemblyElemOperations::elem_calculations(if_jac, vec, mat)
+   after init(elem) and set_elem_solution(sol)
+   (src/base/nonlinear_implicit_assembly_elem_operations.h:50-60,
+   src/base/assembly_elem_operation.h:94-139; structural_nonlinear_assembly.cpp:112-139).
+   sol_elem, fe: npe*dpn values, Ke: (npe*dpn)^2 row-major, all var-blocked (component c
+   of local node a at c*npe + a).  fe = f_int - f_ext of the element's own loads (heat
+   convection and source, side loads); point loads are the assembly's.  Ke or fe nullable. */
+int mg_element_calculations(mg_problem *p, int64_t elem, const double *sol_elem, double *Ke,
+                            double *fe);
+/* d fe / dp for one parameter (kind, index as mg_sensitivity_assemble) at the element-local
+   solution: NonlinearImplicitAssemblyElemOperations::elem_sensitivity_calculations
+   (src/base/nonlinear_implicit_assembly_elem_operations.h:75-80,
+   structural_nonlinear_assembly.cpp:170-196).  Zero for another element's parameter. */
+int mg_element_sensitivity(mg_problem *p, int64_t elem, const double *sol_elem, int32_t kind,
+                           int64_t index, double *dfe);
 int mg_mean_temperature(mg_problem *p, const double *T, const mg_solve_opts *opts,
                         double *qbar, double *dq_dk0, double *dq_ds);
 
@@ -428,6 +459,13 @@ typedef struct mg_synthetic_desc {
 } mg_synthetic_desc;
 int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *desc, double *compliance_out,
                             mg_server_stats *stats);
+/* Request `index` of the synthetic stream `desc` describes, regenerated from the same
+   seeded generator (no server needed): info[5] = chain, nx, ny, nz, n_cases; span
+   (nullable) 2*n_cases load spans; rho (nullable) nx*ny*nz densities, bitwise those that
+   mg_server_run_synthetic submitted for that request.  For checking served results
+   against an independent solve. */
+int mg_server_synthetic_request(const mg_synthetic_desc *desc, int64_t index, int32_t *info,
+                                int32_t *span, double *rho);
 
 /* ---- density filter ----
    MAST::FilterBase (src/level_set/filter_base.cpp): x_filtered_i =

@@ -440,6 +440,12 @@ __global__ void side_load_kernel(const double *__restrict__ coords, const int32_
     }
 }
 
+// y += a x over n entries
+__global__ void axpy_kernel(int64_t n, double a, const double *__restrict__ x, double *__restrict__ y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = fma(a, x[i], y[i]);
+}
+
 __global__ void zero_fixed_kernel(double *__restrict__ v, const uint8_t *__restrict__ fixed, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && fixed[i]) v[i] = 0.0;
@@ -1151,6 +1157,119 @@ int assemble_param_residual(mg_problem *p, const double *d_X, int kind, int64_t 
     }
     set_error("parameter kind %d not available for this physics", kind);
     return MG_ENOTSUP;
+}
+
+// ---------------------------------------------------------------------------
+// Per-element plugin calls (NonlinearImplicitAssemblyElemOperations::elem_calculations
+// and elem_sensitivity_calculations, nonlinear_implicit_assembly_elem_operations.h:50-105,
+// after init(elem) and set_elem_solution(sol), assembly_elem_operation.h:94-139).  The
+// element-local solution (var-blocked: component c of local node a at c * npe + a) is
+// scattered into a zeroed global vector; only element e's own dofs are read from it.
+__global__ void elem_scatter_kernel(const double *__restrict__ sol, const int32_t *__restrict__ conn,
+                                    int64_t e, int npe, int dpn, double *__restrict__ X) {
+    const int t = threadIdx.x;
+    if (t >= npe * dpn) return;
+    const int c = t / npe, a = t - c * npe;
+    X[(int64_t)conn[e * npe + a] * dpn + c] = sol[t];
+}
+
+__global__ void elem_gather_kernel(const double *__restrict__ X, const int32_t *__restrict__ conn,
+                                   int64_t e, int npe, int dpn, double *__restrict__ out) {
+    const int t = threadIdx.x;
+    if (t >= npe * dpn) return;
+    const int c = t / npe, a = t - c * npe;
+    out[t] = X[(int64_t)conn[e * npe + a] * dpn + c];
+}
+
+// d_sol: the element-local solution (device); d_Ke, d_fe (nullable) receive the element
+// Jacobian and the element residual f_int - f_ext of the element's own loads (heat:
+// convection and volume source; every physics: its side loads).  Uses d_tmp, d_tmp2.
+int element_calculations(mg_problem *p, int64_t e, const double *d_sol, double *d_Ke,
+                         double *d_fe, int32_t *d_elem_slot) {
+    const int nd = p->npe * p->dpn;
+    MG_CUDA_TRY(cudaMemsetAsync(p->d_tmp, 0, p->n_dofs * sizeof(double), p->stream));
+    elem_scatter_kernel<<<1, 64, 0, p->stream>>>(d_sol, p->d_conn, e, p->npe, p->dpn, p->d_tmp);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    MG_TRY(element_matrices(p, p->d_tmp, e, 1, d_Ke, d_fe));
+    if (d_fe && p->d_side) {
+        // the element's side loads: F_e of side_load_kernel on this one element, then
+        // f_e -= F_e (the residual convention R = f_int - f_ext)
+        const int hex = (p->physics == MG_PHYSICS_ELASTICITY_HEX8 ||
+                         p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) ? 1 : 0;
+        const int32_t e32 = (int32_t)e;
+        MG_CUDA_TRY(cudaMemcpyAsync(d_elem_slot, &e32, sizeof(int32_t), cudaMemcpyHostToDevice, p->stream));
+        MG_CUDA_TRY(cudaMemsetAsync(p->d_tmp2, 0, p->n_dofs * sizeof(double), p->stream));
+        side_load_kernel<<<1, 32, 0, p->stream>>>(p->d_coords, p->d_conn, d_elem_slot, 1, hex, p->d_side,
+                                                  p->mat.thickness, p->d_tmp2);
+        MG_CUDA_TRY(cudaGetLastError());
+        double *d_Fe = p->d_tmp;  // the scattered solution is no longer needed
+        elem_gather_kernel<<<1, 64, 0, p->stream>>>(p->d_tmp2, p->d_conn, e, p->npe, p->dpn, d_Fe);
+        MG_CUDA_TRY(cudaGetLastError());
+        axpy_kernel<<<1, 64, 0, p->stream>>>(nd, -1.0, d_Fe, d_fe);
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(3);
+        MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    }
+    return MG_OK;
+}
+
+// d/dp of element e's residual at the element-local solution d_sol for the parameter
+// (kind, index) of mg_sensitivity_assemble, into d_dfe (device, npe * dpn).  Element
+// parameters of other elements give zero.  Uses d_tmp, d_tmp2.
+int element_sensitivity(mg_problem *p, int64_t e, const double *d_sol, int kind, int64_t index,
+                        double *d_dfe) {
+    const int nd = p->npe * p->dpn;
+    int *st = status_slot(p);
+    MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(int), p->stream));
+    MG_CUDA_TRY(cudaMemsetAsync(d_dfe, 0, nd * sizeof(double), p->stream));
+    const bool elast = p->physics == MG_PHYSICS_ELASTICITY_HEX8 ||
+                       p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR;
+    const bool heat = p->physics == MG_PHYSICS_HEAT_QUAD4;
+    if (!((elast && kind == MG_PARAM_DENSITY) ||
+          (heat && (kind == MG_PARAM_K0 || kind == MG_PARAM_ELEM_SCALE)))) {
+        set_error("parameter kind %d not available for this physics", kind);
+        return MG_ENOTSUP;
+    }
+    if (kind != MG_PARAM_K0 && (index < 0 || index >= p->n_elems)) {
+        set_error("parameter index %lld out of range", (long long)index);
+        return MG_EINVAL;
+    }
+    if (kind != MG_PARAM_K0 && index != e) return read_status(p, st);  // no dependence: zero
+    MG_CUDA_TRY(cudaMemsetAsync(p->d_tmp, 0, p->n_dofs * sizeof(double), p->stream));
+    elem_scatter_kernel<<<1, 64, 0, p->stream>>>(d_sol, p->d_conn, e, p->npe, p->dpn, p->d_tmp);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    if (elast) {
+        // f_int is linear in E at a fixed state: d f_e / d rho_e = dE_e f_e(E = 1)
+        double lam1, mu1;
+        lame_3d(p->mat.nu, lam1, mu1);
+        double *Ke = p->d_tmp2;  // 576 doubles
+        if (p->physics == MG_PHYSICS_ELASTICITY_HEX8) {
+            hex8_kernel<1><<<1, 256, 0, p->stream>>>(p->d_coords, p->d_conn, nullptr, e, 1, p->d_dE,
+                                                     lam1, mu1, nullptr, nullptr, nullptr, Ke, nullptr,
+                                                     nullptr, nullptr, nullptr, st);
+            MG_CUDA_TRY(cudaGetLastError());
+            elem_matvec_kernel<<<1, 32, 0, p->stream>>>(Ke, p->d_tmp, p->d_conn, e, 1, 8, 3, d_dfe);
+        } else {
+            hex8_gl_kernel<1><<<1, kGlWarps * 32, 0, p->stream>>>(
+                p->d_coords, p->d_conn, nullptr, e, 1, p->d_dE, lam1, mu1, p->d_tmp, nullptr, nullptr,
+                nullptr, nullptr, Ke, d_dfe, nullptr, nullptr, nullptr, st);
+        }
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(2);
+    } else {
+        MG_CUDA_TRY(cudaMemsetAsync(p->d_tmp2, 0, p->n_dofs * sizeof(double), p->stream));
+        heat_sens_kernel<<<1, 32, 0, p->stream>>>(p->d_coords, p->d_conn, nullptr, e, 1, p->d_tmp,
+                                                  p->mat.k0, p->mat.k_beta, p->d_s, p->mat.thickness,
+                                                  kind == MG_PARAM_K0 ? 0 : 1, nullptr, nullptr,
+                                                  nullptr, p->d_tmp2);
+        MG_CUDA_TRY(cudaGetLastError());
+        elem_gather_kernel<<<1, 64, 0, p->stream>>>(p->d_tmp2, p->d_conn, e, p->npe, p->dpn, d_dfe);
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(2);
+    }
+    return read_status(p, st);
 }
 
 // m = lumped weights, returned in d_dqdT scaled by 1/area; *qbar = m.T / area

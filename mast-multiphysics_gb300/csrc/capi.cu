@@ -848,6 +848,132 @@ int mg_adjoint_solve(mg_problem *p, const double *X, const double *rhs, const mg
     return to_host_vec(p, lam, lambda, p->n_dofs);
 }
 
+int mg_sensitivity_solve(mg_problem *p, const double *X, int32_t kind, int64_t index,
+                         const mg_solve_opts *opts, double *du_dp) {
+    // NonlinearSystem::sensitivity_solve (nonlinear_system.cpp:741-794): J(X) du/dp = -dR/dp
+    // with the Jacobian at X and dR/dp of sensitivity_assemble; constrained rows give 0
+    // (enforce_constraints_exactly, homogeneous)
+    if (!p || !X || !du_dp) {
+        set_error("mg_sensitivity_solve: invalid argument");
+        return MG_EINVAL;
+    }
+    mg_solve_opts o;
+    if (opts) o = *opts; else mg_default_solve_opts(&o);
+    double *dX = p->d_tmp;  // the resident solution is left as it is
+    MG_TRY(to_device_vec(p, X, dX, p->n_dofs));
+    if (p->physics == MG_PHYSICS_HEAT_QUAD4) p->jacobian_valid = false;
+    MG_TRY(assemble_system(p, dX, nullptr, true, true));
+    MG_TRY(assemble_param_residual(p, dX, kind, index, p->d_R));
+    std::vector<double> b(p->n_dofs);
+    MG_TRY(to_host_vec(p, p->d_R, b.data(), p->n_dofs));
+    for (int64_t i = 0; i < p->n_dofs; i++) b[i] = p->h_fixed[i] ? 0.0 : -b[i];
+    MG_TRY(to_device_vec(p, b.data(), p->d_R, p->n_dofs));
+    double *dsol = p->d_tmp2;
+    MG_CUDA_TRY(cudaMemsetAsync(dsol, 0, p->n_dofs * 8, p->stream));
+    int its = 0;
+    double rr = 0;
+    // the consistent conduction Jacobian is not symmetric: BiCGStab there
+    const int kr = p->physics == MG_PHYSICS_HEAT_QUAD4 ? MG_KRYLOV_BICGSTAB : o.krylov;
+    MG_TRY(krylov_solve(p, p->A, p->d_R, dsol, o, kr, &its, &rr));
+    return to_host_vec(p, dsol, du_dp, p->n_dofs);
+}
+
+int mg_output_derivative(mg_problem *p, int32_t output, const double *X, double *dq_dX) {
+    // AssemblyBase::calculate_output_derivative (assembly_base.cpp:336-429): dq/dX, zero on
+    // constrained dofs
+    if (!p || !dq_dX) {
+        set_error("mg_output_derivative: invalid argument");
+        return MG_EINVAL;
+    }
+    if (output == MG_OUTPUT_COMPLIANCE) {
+        if (p->physics != MG_PHYSICS_ELASTICITY_HEX8 && p->physics != MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR &&
+            p->physics != MG_PHYSICS_MEMBRANE_QUAD4) {
+            set_error("compliance: structural physics only");
+            return MG_ENOTSUP;
+        }
+        // C = F . X with F independent of X: dC/dX = F (the load vector, zero on fixed dofs)
+        for (int64_t i = 0; i < p->n_dofs; i++) dq_dX[i] = p->h_F[i];
+        return MG_OK;
+    }
+    if (output == MG_OUTPUT_MEAN_TEMPERATURE) {
+        if (p->physics != MG_PHYSICS_HEAT_QUAD4) {
+            set_error("mean temperature: heat physics only");
+            return MG_ENOTSUP;
+        }
+        const double *dT = p->d_X;
+        if (X) {
+            MG_TRY(to_device_vec(p, X, p->d_tmp, p->n_dofs));
+            dT = p->d_tmp;
+        }
+        double qbar = 0;
+        MG_TRY(mean_temperature_terms(p, dT, p->d_R, &qbar));
+        MG_TRY(to_host_vec(p, p->d_R, dq_dX, p->n_dofs));
+        for (int64_t i = 0; i < p->n_dofs; i++)
+            if (p->h_fixed[i]) dq_dX[i] = 0.0;
+        return MG_OK;
+    }
+    set_error("mg_output_derivative: unknown output %d", output);
+    return MG_EINVAL;
+}
+
+namespace {
+// device copies of one element's local vector and matrices for the per-element calls
+struct ElemBuffers {
+    double *sol = nullptr, *Ke = nullptr, *fe = nullptr;
+    int32_t *slot = nullptr;
+    ~ElemBuffers() {
+        dev_free(sol);
+        dev_free(Ke);
+        dev_free(fe);
+        dev_free(slot);
+    }
+    int alloc(int nd) {
+        MG_TRY(dev_alloc_n(&sol, (size_t)nd));
+        MG_TRY(dev_alloc_n(&Ke, (size_t)nd * nd));
+        MG_TRY(dev_alloc_n(&fe, (size_t)nd));
+        return dev_alloc(reinterpret_cast<void **>(&slot), 64);
+    }
+};
+}  // namespace
+
+int mg_element_calculations(mg_problem *p, int64_t elem, const double *sol_elem, double *Ke,
+                            double *fe) {
+    if (!p || elem < 0 || elem >= p->n_elems || !sol_elem || (!Ke && !fe)) {
+        set_error("mg_element_calculations: invalid argument");
+        return MG_EINVAL;
+    }
+    const int nd = p->npe * p->dpn;
+    for (int i = 0; i < nd; i++)
+        if (!std::isfinite(sol_elem[i])) {
+            set_error("mg_element_calculations: non-finite element solution");
+            return MG_EINVAL;
+        }
+    ElemBuffers b;
+    MG_TRY(b.alloc(nd));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.sol, sol_elem, nd * 8, cudaMemcpyHostToDevice, p->stream));
+    MG_TRY(element_calculations(p, elem, b.sol, b.Ke, b.fe, b.slot));
+    if (Ke) MG_CUDA_TRY(cudaMemcpyAsync(Ke, b.Ke, (size_t)nd * nd * 8, cudaMemcpyDeviceToHost, p->stream));
+    if (fe) MG_CUDA_TRY(cudaMemcpyAsync(fe, b.fe, (size_t)nd * 8, cudaMemcpyDeviceToHost, p->stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return MG_OK;
+}
+
+int mg_element_sensitivity(mg_problem *p, int64_t elem, const double *sol_elem, int32_t kind,
+                           int64_t index, double *dfe) {
+    if (!p || elem < 0 || elem >= p->n_elems || !sol_elem || !dfe) {
+        set_error("mg_element_sensitivity: invalid argument");
+        return MG_EINVAL;
+    }
+    const int nd = p->npe * p->dpn;
+    ElemBuffers b;
+    MG_TRY(b.alloc(nd));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.sol, sol_elem, nd * 8, cudaMemcpyHostToDevice, p->stream));
+    MG_TRY(element_sensitivity(p, elem, b.sol, kind, index, b.fe));
+    MG_CUDA_TRY(cudaMemcpyAsync(dfe, b.fe, (size_t)nd * 8, cudaMemcpyDeviceToHost, p->stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return MG_OK;
+}
+
 int mg_mean_temperature(mg_problem *p, const double *T, const mg_solve_opts *opts, double *qbar,
                         double *dq_dk0, double *dq_ds) {
     if (!p) return MG_EINVAL;

@@ -151,6 +151,11 @@ int elem_sensitivity(mg_problem *p, const double *d_X, const double *d_lambda, i
 int assemble_param_residual(mg_problem *p, const double *d_X, int kind, int64_t index,
                             double *d_dRdp);
 int mean_temperature_terms(mg_problem *p, const double *d_T, double *d_dqdT, double *qbar);
+// one element at an element-local solution (device pointers; d_elem_slot: one device int32)
+int element_calculations(mg_problem *p, int64_t e, const double *d_sol, double *d_Ke,
+                         double *d_fe, int32_t *d_elem_slot);
+int element_sensitivity(mg_problem *p, int64_t e, const double *d_sol, int kind, int64_t index,
+                        double *d_dfe);
 
 // ---- krylov.cu ----
 int krylov_init(mg_problem *p);

@@ -728,23 +728,34 @@ void mg_server_destroy(mg_server *s) {
     delete s;
 }
 
-int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *d, double *compliance_out,
-                            mg_server_stats *stats) {
-    if (!s || !d || d->n_requests <= 0 || d->rate <= 0 || d->n_chains <= 0 || d->n_sizes <= 0 || !d->sizes ||
-        d->max_cases < 1 || d->max_cases > MG_BATCH_MAX_CASES)
-        return MG_EINVAL;
+}  // extern "C"
+
+namespace {
+// The synthetic stream: chain grids, load cases and spans, arrival times and the chain
+// of every request, all from one seeded generator (cheap); densities come per chain.
+struct SynthChain {
+    int nx, ny, nz, cases;
+    std::vector<int32_t> span;
+};
+
+struct SynthStream {
+    std::vector<SynthChain> ch;
+    std::vector<double> at;
+    std::vector<int> who;
+};
+
+bool synth_valid(const mg_synthetic_desc *d) {
+    return d && d->n_requests > 0 && d->rate > 0 && d->n_chains > 0 && d->n_sizes > 0 && d->sizes &&
+           d->max_cases >= 1 && d->max_cases <= MG_BATCH_MAX_CASES;
+}
+
+void synth_stream(const mg_synthetic_desc *d, SynthStream &st) {
     const int nch = d->n_chains;
     std::mt19937_64 rng(d->seed);
-    // chains: grid, load cases, spans, initial field
-    struct Gen {
-        int nx, ny, nz, cases;
-        std::vector<int32_t> span;
-        std::vector<float> rho;
-    };
-    std::vector<Gen> ch(nch);
+    st.ch.assign(nch, SynthChain{});
     int n_big = d->big_fraction > 0 ? std::max(1, (int)lround(d->big_fraction * nch)) : 0;
     for (int c = 0; c < nch; c++) {
-        Gen &g = ch[c];
+        SynthChain &g = st.ch[c];
         if (c < n_big) {
             g.nx = d->big_nx; g.ny = d->big_ny; g.nz = d->big_nz;
         } else {
@@ -759,16 +770,78 @@ int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *d, double *co
             g.span.push_back(j1);
         }
     }
-    // arrivals and chain of each request
-    std::vector<double> at(d->n_requests);
-    std::vector<int> who(d->n_requests);
+    st.at.assign(d->n_requests, 0.0);
+    st.who.assign(d->n_requests, 0);
     std::exponential_distribution<double> gap(d->rate);
     double t = 0;
     for (int64_t i = 0; i < d->n_requests; i++) {
         t += gap(rng);
-        at[i] = t;
-        who[i] = (int)(rng() % (uint64_t)nch);
+        st.at[i] = t;
+        st.who[i] = (int)(rng() % (uint64_t)nch);
     }
+}
+
+// Walks chain c's density field through the chain's requests in index order
+// (rho_next = clip(rho + N(0, noise), 0.01, 1) per request, from a U[0.01, 1] start);
+// emit(i, field) is called with the field of each request i of the chain.
+template <class F>
+void synth_chain_fields(const mg_synthetic_desc *d, const SynthStream &st, int c,
+                        const std::vector<int64_t> &requests, F emit) {
+    const SynthChain &g = st.ch[c];
+    const int64_t ne = (int64_t)g.nx * g.ny * g.nz;
+    std::mt19937_64 r2(d->seed * 1000003ULL + (uint64_t)c + 1);
+    std::uniform_real_distribution<float> U(0.01f, 1.0f);
+    std::normal_distribution<float> N(0.0f, (float)d->noise);
+    std::vector<float> cur(ne);
+    for (auto &x : cur) x = U(r2);
+    for (int64_t i : requests) {
+        for (auto &x : cur) x = std::min(1.0f, std::max(0.01f, x + N(r2)));
+        if (!emit(i, cur)) return;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int mg_server_synthetic_request(const mg_synthetic_desc *d, int64_t index, int32_t *info,
+                                int32_t *span, double *rho) {
+    if (!synth_valid(d) || index < 0 || index >= d->n_requests || !info) {
+        set_error("mg_server_synthetic_request: invalid argument");
+        return MG_EINVAL;
+    }
+    SynthStream st;
+    synth_stream(d, st);
+    const int c = st.who[index];
+    const SynthChain &g = st.ch[c];
+    info[0] = c;
+    info[1] = g.nx;
+    info[2] = g.ny;
+    info[3] = g.nz;
+    info[4] = g.cases;
+    if (span)
+        for (int k = 0; k < 2 * g.cases; k++) span[k] = g.span[k];
+    if (rho) {
+        std::vector<int64_t> req;
+        for (int64_t i = 0; i <= index; i++)
+            if (st.who[i] == c) req.push_back(i);
+        synth_chain_fields(d, st, c, req, [&](int64_t i, const std::vector<float> &f) {
+            if (i != index) return true;
+            for (size_t k = 0; k < f.size(); k++) rho[k] = (double)f[k];
+            return false;
+        });
+    }
+    return MG_OK;
+}
+
+int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *d, double *compliance_out,
+                            mg_server_stats *stats) {
+    if (!s || !synth_valid(d)) return MG_EINVAL;
+    const int nch = d->n_chains;
+    SynthStream ss;
+    synth_stream(d, ss);
+    const std::vector<SynthChain> &ch = ss.ch;
+    const std::vector<double> &at = ss.at;
+    const std::vector<int> &who = ss.who;
     // densities of every request, chain by chain (threads over chains)
     std::vector<std::vector<float>> fields(d->n_requests);
     {
@@ -778,19 +851,11 @@ int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *d, double *co
         std::vector<std::thread> th;
         for (unsigned w = 0; w < nt; w++)
             th.emplace_back([&, w] {
-                for (int c = (int)w; c < nch; c += (int)nt) {
-                    Gen &g = ch[c];
-                    const int64_t ne = (int64_t)g.nx * g.ny * g.nz;
-                    std::mt19937_64 r2(d->seed * 1000003ULL + (uint64_t)c + 1);
-                    std::uniform_real_distribution<float> U(0.01f, 1.0f);
-                    std::normal_distribution<float> N(0.0f, (float)d->noise);
-                    std::vector<float> cur(ne);
-                    for (auto &x : cur) x = U(r2);
-                    for (int64_t i : per[c]) {
-                        for (auto &x : cur) x = std::min(1.0f, std::max(0.01f, x + N(r2)));
-                        fields[i] = cur;
-                    }
-                }
+                for (int c = (int)w; c < nch; c += (int)nt)
+                    synth_chain_fields(d, ss, c, per[c], [&](int64_t i, const std::vector<float> &f) {
+                        fields[i] = f;
+                        return true;
+                    });
             });
         for (auto &x : th) x.join();
     }
@@ -804,7 +869,7 @@ int mg_server_run_synthetic(mg_server *s, const mg_synthetic_desc *d, double *co
     const double t0 = now_s() + 0.05;
     int rc = MG_OK;
     for (int64_t i = 0; i < d->n_requests && rc == MG_OK; i++) {
-        Gen &g = ch[who[i]];
+        const SynthChain &g = ch[who[i]];
         std::vector<double> rho(fields[i].begin(), fields[i].end());
         std::vector<float>().swap(fields[i]);
         mg_request q{};

@@ -28,8 +28,16 @@
 //     ::calculate_output(X, localize, output)             src/base/assembly_base.h:257-260
 //     ::calculate_output_adjoint_sensitivity_multiple_parameters_no_direct(...)
 //                                               src/base/assembly_base.h:313-321
-//   MAST::NonlinearSystem::solve(elem_ops, assembly), ::adjoint_solve(...)
-//                                               src/base/nonlinear_system.h:133, 155
+//   MAST::NonlinearSystem::solve(elem_ops, assembly), ::adjoint_solve(...),
+//     ::sensitivity_solve(X, localize, elem_ops, assembly, p)  src/base/nonlinear_system.h:133-155
+//   MAST::NonlinearImplicitAssembly::calculate_output_derivative(X, localize, output, dq_dX),
+//     ::calculate_output_direct_sensitivity(X, localize, dXdp, localize_sens, p, output)
+//                                               src/base/assembly_base.h:266-290
+//   MAST::AssemblyElemOperations::set_assembly / init(GeomElem) / set_elem_solution /
+//     clear_elem, MAST::NonlinearImplicitAssemblyElemOperations::elem_calculations(if_jac,
+//     vec, mat) / elem_sensitivity_calculations(f, vec)
+//                                               src/base/assembly_elem_operation.h:40-176,
+//                                               nonlinear_implicit_assembly_elem_operations.h:50-105
 //   MAST::ComplianceOutput                       src/elasticity/compliance_output.h
 //   libMesh::MeshTools::Generation::build_cube / build_square (unit-spaced
 //   HEX8/QUAD4 grids, libMesh node numbering and boundary ids) -> MAST::Mesh
@@ -563,20 +571,87 @@ public:
     HeatConductionSystemInitialization(NonlinearSystem &sys, const Mesh &m) : SystemInitialization(sys, m, 1) {}
 };
 
+class NonlinearImplicitAssembly;
+
+// one element of the mesh (stands in for MAST::GeomElem over a libMesh::Elem)
+class GeomElem {
+public:
+    // the element with index `elem` of the system's mesh (GeomElem::init(elem, system),
+    // geom_elem.cpp:133-160)
+    void init(int64_t elem, const SystemInitialization &) { _id = elem; }
+    int64_t id() const { return _id; }
+
+private:
+    int64_t _id = -1;
+};
+
+// Element operations of an assembly (MAST::AssemblyElemOperations,
+// src/base/assembly_elem_operation.h:40-176).  The per-element calls forward to
+// mg_element_calculations / mg_element_sensitivity on the assembly's problem, one
+// element at a time, as MAST's own assembly loop calls them.
 class AssemblyElemOperations {
 public:
     virtual ~AssemblyElemOperations() {}
+    // mg_physics of the element kernels for this mesh
     virtual int physics(const Mesh &m) const = 0;
+    virtual void set_assembly(NonlinearImplicitAssembly &assembly) { _assembly = &assembly; }
+    virtual NonlinearImplicitAssembly &get_assembly() {
+        if (!_assembly) throw std::runtime_error("element operations: no assembly set");
+        return *_assembly;
+    }
+    virtual void clear_assembly() { _assembly = nullptr; }
+    virtual void set_elem_data(unsigned int, int64_t, GeomElem &) const {}
+    // MAST builds the physics element here (assembly_elem_operation.cpp:195-202)
+    virtual void init(const GeomElem &elem) {
+        if (_elem >= 0) throw std::runtime_error("init: the previous element was not cleared");
+        _elem = elem.id();
+    }
+    virtual void clear_elem() {
+        _elem = -1;
+        _sol.clear();
+    }
+    virtual void set_elem_solution(const RealVectorX &sol) { _sol = sol; }
+
+protected:
+    mg_problem *_problem();
+    int64_t _elem = -1;
+    RealVectorX _sol;
+    NonlinearImplicitAssembly *_assembly = nullptr;
 };
 
-class StructuralNonlinearAssemblyElemOperations : public AssemblyElemOperations {
+// MAST::NonlinearImplicitAssemblyElemOperations
+// (src/base/nonlinear_implicit_assembly_elem_operations.h:50-105)
+class NonlinearImplicitAssemblyElemOperations : public AssemblyElemOperations {
+public:
+    // element residual f_int - f_ext of the element's own loads and, if if_jac, its
+    // Jacobian, at the solution of set_elem_solution (var-blocked element dofs)
+    virtual void elem_calculations(bool if_jac, RealVectorX &vec, RealMatrixX &mat) {
+        const int nd = _ndofs();
+        vec.assign(nd, 0.0);
+        std::vector<Real> K(if_jac ? (size_t)nd * nd : 0);
+        check(mg_element_calculations(_problem(), _elem, _sol.data(), if_jac ? K.data() : nullptr, vec.data()),
+              "elem_calculations");
+        if (if_jac) {
+            mat = RealMatrixX::Zero(nd, nd);
+            for (int i = 0; i < nd; i++)
+                for (int j = 0; j < nd; j++) mat(i, j) = K[(size_t)i * nd + j];
+        }
+    }
+    // d(element residual)/dp for a parameter function ("rho_<e>", "s_<e>", "k0")
+    virtual void elem_sensitivity_calculations(const FunctionBase &f, RealVectorX &vec);
+
+protected:
+    int _ndofs();
+};
+
+class StructuralNonlinearAssemblyElemOperations : public NonlinearImplicitAssemblyElemOperations {
 public:
     int physics(const Mesh &m) const override {
         return m.type == HEX8 ? MG_PHYSICS_ELASTICITY_HEX8 : MG_PHYSICS_MEMBRANE_QUAD4;
     }
 };
 
-class HeatConductionNonlinearAssemblyElemOperations : public AssemblyElemOperations {
+class HeatConductionNonlinearAssemblyElemOperations : public NonlinearImplicitAssemblyElemOperations {
 public:
     int physics(const Mesh &) const override { return MG_PHYSICS_HEAT_QUAD4; }
 };
@@ -586,7 +661,14 @@ class OutputAssemblyElemOperations {
 public:
     virtual ~OutputAssemblyElemOperations() {}
     Real output_total() const { return _q; }
+    // the derivative left by calculate_output_direct_sensitivity for parameter p
+    Real output_sensitivity_total(const FunctionBase &p) const {
+        auto it = _dq_dp.find(p.name());
+        if (it == _dq_dp.end()) throw std::runtime_error("no sensitivity for " + p.name());
+        return it->second;
+    }
     Real _q = 0;
+    std::map<std::string, Real> _dq_dp;
 };
 
 // compliance f.u (the configs' loads are nodal point loads, which MAST's
@@ -617,8 +699,6 @@ public:
 };
 
 // ------------------------------------------------------------------ assembly + solve
-class NonlinearImplicitAssembly;
-
 class NonlinearSystem {
 public:
     NonlinearSystem() { mg_default_solve_opts(&opts); }
@@ -631,6 +711,15 @@ public:
     void adjoint_solve(const Vector &X, bool if_assemble_jacobian, AssemblyElemOperations &elem_ops,
                        OutputAssemblyElemOperations &output, NonlinearImplicitAssembly &assembly,
                        Vector &adjoint);
+    // forward sensitivity J(X) dX/dp = -dR/dp (nonlinear_system.cpp:741-794); the result
+    // is left in get_sensitivity_solution() (add_sensitivity_solution in MAST)
+    void sensitivity_solve(const Vector &X, bool if_localize_sol, AssemblyElemOperations &elem_ops,
+                           NonlinearImplicitAssembly &assembly, const FunctionBase &p,
+                           bool if_assemble_jacobian = true);
+    Vector &get_sensitivity_solution() { return _sens_sol; }
+
+private:
+    Vector _sens_sol;
 };
 
 class NonlinearImplicitAssembly {
@@ -646,8 +735,10 @@ public:
         _disc = &discipline;
         _sys = &system;
         _ops = &elem_ops;
+        elem_ops.set_assembly(*this);
     }
     void clear_discipline_and_system() {
+        if (_ops) _ops->clear_assembly();
         if (_p) mg_problem_destroy(_p);
         _p = nullptr;
         _disc = nullptr;
@@ -714,7 +805,7 @@ public:
         (void)if_localize_sol;
         int kind;
         int64_t index;
-        _param_of(f, kind, index);
+        param_of(f, kind, index);
         rhs.resize(X.size());
         check(mg_sensitivity_assemble(problem(), X.data(), kind, index, rhs.data()), "sensitivity_assemble");
         if (close_vector) rhs.close();
@@ -760,7 +851,7 @@ public:
             for (size_t i = 0; i < p_vec.size(); i++) {
                 int kind;
                 int64_t index;
-                _param_of(*p_vec[i], kind, index);
+                param_of(*p_vec[i], kind, index);
                 sens[i] = dc[index];
             }
             return;
@@ -792,20 +883,49 @@ public:
         for (size_t i = 0; i < p_vec.size(); i++) {
             int kind;
             int64_t index;
-            _param_of(*p_vec[i], kind, index);
+            param_of(*p_vec[i], kind, index);
             if (kind != MG_PARAM_DENSITY) throw std::runtime_error("KS stress sensitivity: density parameters only");
             sens[i] = d[index];
         }
+    }
+
+    // dq/dX of the output at X, zero on constrained dofs (assembly_base.cpp:336-429)
+    void calculate_output_derivative(const Vector &X, bool if_localize_sol, OutputAssemblyElemOperations &output,
+                                     Vector &dq_dX) {
+        (void)if_localize_sol;
+        int kind;
+        if (dynamic_cast<ComplianceOutput *>(&output)) kind = MG_OUTPUT_COMPLIANCE;
+        else if (dynamic_cast<AverageTemperatureOutput *>(&output)) kind = MG_OUTPUT_MEAN_TEMPERATURE;
+        else throw std::runtime_error("calculate_output_derivative: unsupported output");
+        dq_dX.resize(X.size());
+        check(mg_output_derivative(problem(), kind, X.data(), dq_dX.data()), "calculate_output_derivative");
+    }
+
+    // dq/dp = partial dq/dp + dq/dX . dX/dp (assembly_base.cpp:434-520): with dXdp from
+    // NonlinearSystem::sensitivity_solve this is the total (direct) sensitivity, without
+    // it the partial derivative.  The compliance F.X and the mean temperature do not
+    // depend on the density, k0 or the conductivity scale explicitly, so their partial
+    // derivatives are zero.  The value is left in output.output_sensitivity_total(p).
+    void calculate_output_direct_sensitivity(const Vector &X, bool if_localize_sol, const Vector *dXdp,
+                                             bool if_localize_sol_sens, const FunctionBase &p,
+                                             OutputAssemblyElemOperations &output) {
+        (void)if_localize_sol_sens;
+        Real s = 0.0;
+        if (dXdp) {
+            Vector dq;
+            calculate_output_derivative(X, if_localize_sol, output, dq);
+            for (size_t i = 0; i < X.size(); i++) s += dq(i) * (*dXdp)(i);
+        } else if (!dynamic_cast<ComplianceOutput *>(&output) && !dynamic_cast<AverageTemperatureOutput *>(&output))
+            throw std::runtime_error("calculate_output_direct_sensitivity: unsupported output");
+        output._dq_dp[p.name()] = s;
     }
 
     // element-parameter functions: "rho_<e>" / "s_<e>" name element e's density
     // or conductivity scale; "k0" the base conductivity
     static std::string elem_param_name(const char *kind, int64_t e) { return std::string(kind) + "_" + std::to_string(e); }
 
-private:
-    friend class NonlinearSystem;
-
-    void _param_of(const FunctionBase &f, int &kind, int64_t &index) const {
+    // the (mg_sensitivity_assemble kind, index) a parameter function names
+    static void param_of(const FunctionBase &f, int &kind, int64_t &index) {
         const std::string &nm = f.name();
         if (nm == "k0") { kind = MG_PARAM_K0; index = 0; return; }
         const size_t u = nm.find('_');
@@ -933,6 +1053,44 @@ private:
     Real _Emin = 1e-9, _penal = 3.0, _res_l2 = 0.0;
     int _phys = -1;
 };
+
+inline mg_problem *AssemblyElemOperations::_problem() {
+    if (_elem < 0) throw std::runtime_error("element operations: init(elem) was not called");
+    return get_assembly().problem();
+}
+
+inline int NonlinearImplicitAssemblyElemOperations::_ndofs() {
+    mg_problem *p = _problem();
+    int64_t n = 0, nnz = 0;
+    int32_t nc = 0;
+    check(mg_problem_info(p, &n, &nnz, &nc), "mg_problem_info");
+    const int phys = get_assembly().physics();
+    const int nd = (phys == MG_PHYSICS_HEAT_QUAD4) ? 4 : (phys == MG_PHYSICS_MEMBRANE_QUAD4) ? 8 : 24;
+    if ((int)_sol.size() != nd) throw std::runtime_error("set_elem_solution: wrong element vector size");
+    return nd;
+}
+
+inline void NonlinearImplicitAssemblyElemOperations::elem_sensitivity_calculations(const FunctionBase &f,
+                                                                                  RealVectorX &vec) {
+    const int nd = _ndofs();
+    int kind;
+    int64_t index;
+    NonlinearImplicitAssembly::param_of(f, kind, index);
+    vec.assign(nd, 0.0);
+    check(mg_element_sensitivity(_problem(), _elem, _sol.data(), kind, index, vec.data()),
+          "elem_sensitivity_calculations");
+}
+
+inline void NonlinearSystem::sensitivity_solve(const Vector &X, bool, AssemblyElemOperations &,
+                                               NonlinearImplicitAssembly &assembly, const FunctionBase &p,
+                                               bool) {
+    int kind;
+    int64_t index;
+    NonlinearImplicitAssembly::param_of(p, kind, index);
+    _sens_sol.resize(X.size());
+    check(mg_sensitivity_solve(assembly.problem(), X.data(), kind, index, &opts, _sens_sol.data()),
+          "NonlinearSystem::sensitivity_solve");
+}
 
 inline void NonlinearSystem::solve(AssemblyElemOperations &, NonlinearImplicitAssembly &assembly) {
     mg_problem *p = assembly.problem();

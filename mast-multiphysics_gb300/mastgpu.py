@@ -85,6 +85,7 @@ PHYS_HEX8, PHYS_MEMBRANE, PHYS_HEAT = 0, 1, 2
 PHYS_HEX8_NONLINEAR = 3  # Green-Lagrange strain (MAST::NONLINEAR_STRAIN), Newton
 PLAIN_FP64, MIXED_TF32, MIXED_BF16, MIXED_TF32X3, MIXED_BF16X3 = 0, 1, 2, 3, 4
 KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
+OUTPUT_COMPLIANCE, OUTPUT_MEAN_TEMPERATURE = 0, 1
 PC_JACOBI, PC_MULTIGRID = 0, 1
 SMOOTHER_FACTORED, SMOOTHER_TENSOR = 0, 1
 OPERATOR_FACTORED_FP32 = 100  # mg_debug_matfree_apply / mg_debug_launch_apply: factored FP32 operator
@@ -210,6 +211,10 @@ def lib(autobuild=True):
     L.mg_ks_stress.argtypes = [_vp, _vp, _dbl, _dbl, _dbl, _vp, _vp, _vp]
     L.mg_set_side_loads.argtypes = [_vp, _i64, _vp, _vp, _vp]
     L.mg_mean_temperature.argtypes = [_vp, _vp, ctypes.POINTER(SolveOpts), _vp, _vp, _vp]
+    L.mg_sensitivity_solve.argtypes = [_vp, _vp, _i32, _i64, ctypes.POINTER(SolveOpts), _vp]
+    L.mg_output_derivative.argtypes = [_vp, _i32, _vp, _vp]
+    L.mg_element_calculations.argtypes = [_vp, _i64, _vp, _vp, _vp]
+    L.mg_element_sensitivity.argtypes = [_vp, _i64, _vp, _i32, _i64, _vp]
     L.mg_debug_matfree_apply.argtypes = [_vp, ctypes.c_int, _vp, _vp]
     L.mg_compliance_resident.argtypes = [_vp, _vp]
     L.mg_sensitivities_device.argtypes = [_vp]
@@ -259,6 +264,7 @@ def lib(autobuild=True):
     L.mg_server_destroy.restype = None
     L.mg_server_run_synthetic.argtypes = [_vp, ctypes.POINTER(SyntheticDesc), _vp,
                                           ctypes.POINTER(ServerStats)]
+    L.mg_server_synthetic_request.argtypes = [ctypes.POINTER(SyntheticDesc), _i64, _vp, _vp, _vp]
     _lib = L
     return L
 
@@ -492,6 +498,40 @@ class Problem:
               "mg_mean_temperature")
         return q.value, (dk0.value if want_sens else None), ds
 
+    def sensitivity_solve(self, X, kind, index=0, opts=None):
+        """dX/dp with J(X) dX/dp = -dR/dp (mg_sensitivity_solve)"""
+        Xa = np.ascontiguousarray(X, dtype=np.float64)
+        out = np.zeros(self.n_dofs)
+        o = opts if opts is not None else default_opts()
+        check(lib().mg_sensitivity_solve(self.h, _p(Xa), kind, index, ctypes.byref(o), _p(out)),
+              "mg_sensitivity_solve")
+        return out
+
+    def output_derivative(self, output, X=None):
+        """dq/dX of OUTPUT_COMPLIANCE / OUTPUT_MEAN_TEMPERATURE (mg_output_derivative)"""
+        Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
+        out = np.zeros(self.n_dofs)
+        check(lib().mg_output_derivative(self.h, output, _p(Xa), _p(out)), "mg_output_derivative")
+        return out
+
+    def element_calculations(self, elem, sol_elem, want_K=True):
+        """element residual and Jacobian at a var-blocked element-local solution
+        (mg_element_calculations)"""
+        sol = np.ascontiguousarray(sol_elem, dtype=np.float64)
+        nd = sol.shape[0]
+        K = np.zeros((nd, nd)) if want_K else None
+        f = np.zeros(nd)
+        check(lib().mg_element_calculations(self.h, elem, _p(sol), _p(K), _p(f)),
+              "mg_element_calculations")
+        return f, K
+
+    def element_sensitivity(self, elem, sol_elem, kind, index=0):
+        sol = np.ascontiguousarray(sol_elem, dtype=np.float64)
+        out = np.zeros(sol.shape[0])
+        check(lib().mg_element_sensitivity(self.h, elem, _p(sol), kind, index, _p(out)),
+              "mg_element_sensitivity")
+        return out
+
     def sensitivity_assemble(self, kind, index=0, X=None):
         Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
         out = np.zeros(self.n_dofs)
@@ -720,16 +760,40 @@ class Server:
 
     def run_synthetic(self, n_requests, rate, n_chains=64, sizes=None, big=(192, 96, 96),
                       big_fraction=0.02, max_cases=4, noise=0.02, seed=0):
-        sizes = BATCH_SIZES if sizes is None else sizes
-        sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.int32).reshape(-1))
-        d = SyntheticDesc(n_requests=n_requests, rate=rate, n_chains=n_chains, n_sizes=sz.size // 3,
-                          sizes=sz.ctypes.data, big_fraction=big_fraction, big_nx=big[0],
-                          big_ny=big[1], big_nz=big[2], max_cases=max_cases, noise=noise, seed=seed)
+        d = synthetic_desc(n_requests, rate, n_chains, sizes, big, big_fraction, max_cases, noise, seed)
         comp = np.zeros((n_requests, max_cases))
         st = ServerStats()
         check(lib().mg_server_run_synthetic(self.h, ctypes.byref(d), _p(comp), ctypes.byref(st)),
               "mg_server_run_synthetic")
         return st.as_dict(), comp
+
+
+def synthetic_desc(n_requests, rate, n_chains=64, sizes=None, big=(192, 96, 96), big_fraction=0.02,
+                   max_cases=4, noise=0.02, seed=0):
+    """The mg_synthetic_desc of Server.run_synthetic with the same arguments (the sizes
+    array is kept alive on the returned object)."""
+    sizes = BATCH_SIZES if sizes is None else sizes
+    sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.int32).reshape(-1))
+    d = SyntheticDesc(n_requests=n_requests, rate=rate, n_chains=n_chains, n_sizes=sz.size // 3,
+                      sizes=sz.ctypes.data, big_fraction=big_fraction, big_nx=big[0], big_ny=big[1],
+                      big_nz=big[2], max_cases=max_cases, noise=noise, seed=seed)
+    d._sizes = sz
+    return d
+
+
+def synthetic_request(desc, index, want_rho=True):
+    """Request `index` of a synthetic stream (mg_server_synthetic_request): dict with
+    chain, grid, spans and (want_rho) the densities that run_synthetic submitted."""
+    info = np.zeros(5, dtype=np.int32)
+    check(lib().mg_server_synthetic_request(ctypes.byref(desc), index, _p(info), None, None),
+          "mg_server_synthetic_request")
+    span = np.zeros(2 * int(info[4]), dtype=np.int32)
+    rho = np.zeros(int(info[1]) * int(info[2]) * int(info[3])) if want_rho else None
+    check(lib().mg_server_synthetic_request(ctypes.byref(desc), index, _p(info), _p(span), _p(rho)),
+          "mg_server_synthetic_request")
+    return {"chain": int(info[0]), "grid": (int(info[1]), int(info[2]), int(info[3])),
+            "spans": [(int(span[2 * k]), int(span[2 * k + 1])) for k in range(int(info[4]))],
+            "rho": rho}
 
 
 # ------------------------------------------------------------------ benchmark problems

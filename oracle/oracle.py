@@ -246,6 +246,22 @@ def assemble_hex8(coords, conn, E_elem, nu, rowptr, cols, fixed=None):
     return vals
 
 
+def assemble_quad4_membrane(coords, conn, E_elem, nu, h, rowptr, cols, fixed=None):
+    """Linear QUAD4 membrane stiffness (2 dofs per node, node-interleaved) into the CSR
+    pattern of csr_pattern(conn, n_nodes, 2); Dirichlet rows and columns eliminated."""
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    vals = np.zeros(cols.shape[0])
+    fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+    rc = lib().or_assemble_quad4_membrane(coords.shape[0], conn.shape[0], coords.reshape(-1),
+                                          conn.reshape(-1),
+                                          np.ascontiguousarray(E_elem, dtype=np.float64), nu, h,
+                                          rowptr, cols, vals, _ptr(fx))
+    if rc:
+        raise ValueError("degenerate element in assembly")
+    return vals
+
+
 def assemble_quad4_heat(coords, conn, k0, beta, s_elem, h, q_elem, conv_elem, conv_side, hc,
                         Tinf, T, consistent, rowptr, cols, fixed):
     coords = np.ascontiguousarray(coords, dtype=np.float64)

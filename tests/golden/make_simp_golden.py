@@ -3,7 +3,8 @@
 Densities: numpy.random.default_rng(0).uniform(0.01, 1.0, 524288), element
 order x-fastest.  Runs the oracle (Jacobi-PCG, FP64) twice: to 1e-8 (the
 iteration count the CPU baseline extrapolates with) and to 1e-11 (reference
-compliance and sensitivities for the mixed-precision error checks).
+compliance and sensitivities, stored in FP64, for the mixed-precision
+error checks).
 Writes simp_128x64x64_seed0.npz next to this script.
 """
 import os
@@ -31,7 +32,7 @@ def main():
                         iterations_1e8=r8.iterations, relres_1e8=r8.relres,
                         compliance_1e8=r8.compliance, iterations_1e11=r11.iterations,
                         relres_1e11=r11.relres, compliance=r11.compliance,
-                        dc=dc.astype(np.float32), u_tip=u[(NX + (NX + 1) * 0) * 3 + 2],
+                        dc=dc, u_tip=u[(NX + (NX + 1) * 0) * 3 + 2],
                         threads=O.max_threads(), seconds_1e8=t8, seconds_1e11=t11,
                         t_assemble=r8.t_assemble, t_solve_1e8=r8.t_solve)
     print("1e-8: %d it, C=%.15g (%.1fs); 1e-11: %d it, C=%.15g (%.1fs)"

@@ -102,7 +102,8 @@ def test_batch_designs_generator_is_seeded_and_in_range():
 
 
 def test_output_entry_points_reject_missing_handles_without_a_gpu():
-    """The adjoint, KS stress and assembly-launch entry points check their arguments on
+    """The adjoint, KS stress, sensitivity-solve, element and assembly-launch entry points
+    check their arguments on
     the host first: a missing handle or vector is MG_EINVAL with no CUDA call."""
     L = M.lib()
     x = np.zeros(3)
@@ -111,9 +112,41 @@ def test_output_entry_points_reject_missing_handles_without_a_gpu():
     assert L.mg_adjoint_solve(None, M._p(x), M._p(x), None, M._p(x)) == M.MG_EINVAL
     assert L.mg_debug_launch_assembly(None, None, 1) == M.MG_EINVAL
     assert L.mg_compliance(None, None, None, None) == M.MG_EINVAL
+    assert L.mg_sensitivity_solve(None, M._p(x), 0, 0, None, M._p(x)) == M.MG_EINVAL
+    assert L.mg_output_derivative(None, 0, None, M._p(x)) == M.MG_EINVAL
+    assert L.mg_element_calculations(None, 0, M._p(x), None, M._p(x)) == M.MG_EINVAL
+    assert L.mg_element_sensitivity(None, 0, M._p(x), 0, 0, M._p(x)) == M.MG_EINVAL
+    assert b"invalid argument" in L.mg_last_error()
 
 
 def test_nonlinear_physics_value_is_the_header_enum():
     txt = open(os.path.join(REPO, "include", "mastgpu.h")).read()
     m = re.search(r"MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR\s*=\s*(\d+)", txt)
     assert m and int(m.group(1)) == M.PHYS_HEX8_NONLINEAR
+
+
+def test_synthetic_request_regeneration_is_deterministic():
+    """mg_server_synthetic_request is host code: it regenerates a request of the seeded
+    synthetic stream (chain, grid, spans, densities) without a GPU."""
+    d = M.synthetic_desc(50, 300.0, n_chains=5, sizes=((8, 4, 4), (16, 8, 8)), big_fraction=0.0,
+                         max_cases=3, seed=9)
+    by_chain = {}
+    for i in range(50):
+        a = M.synthetic_request(d, i)
+        b = M.synthetic_request(d, i)
+        assert a["chain"] == b["chain"] and a["spans"] == b["spans"]
+        assert np.array_equal(a["rho"], b["rho"])
+        nx, ny, nz = a["grid"]
+        assert (nx, ny, nz) in ((8, 4, 4), (16, 8, 8)) and 1 <= len(a["spans"]) <= 3
+        assert all(0 <= j0 <= j1 <= ny for j0, j1 in a["spans"])
+        assert a["rho"].shape == (nx * ny * nz,)
+        assert a["rho"].min() >= 0.01 - 1e-7 and a["rho"].max() <= 1.0
+        by_chain.setdefault(a["chain"], []).append(a["rho"])
+    # consecutive requests of a chain differ by the N(0, 0.02) step, clipped
+    for seq in by_chain.values():
+        for x, y in zip(seq, seq[1:]):
+            dlt = np.abs(x - y)
+            assert 0.0 < dlt.max() < 0.2 and 0.005 < dlt.mean() < 0.03
+    bad = M.synthetic_desc(50, 300.0, n_chains=5)
+    info = np.zeros(5, dtype=np.int32)
+    assert M.lib().mg_server_synthetic_request(ctypes.byref(bad), 50, M._p(info), None, None) == M.MG_EINVAL

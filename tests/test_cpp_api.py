@@ -48,4 +48,4 @@ def test_cpp_mirror_cpu_cases():
 @pytest.mark.gpu
 def test_cpp_mirror_gpu_cases():
     out = run("[gpu]")
-    assert "4 test cases" in out
+    assert "6 test cases" in out

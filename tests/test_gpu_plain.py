@@ -168,6 +168,159 @@ def test_membrane_element_matrices():
     assert rel(Ke[0], K_ref) < RTOL_ELEM
 
 
+MEMBRANE_MAT = dict(E0=72e9, Emin=72e9 * 1e-9, nu=0.33, penal=3.0, thickness=0.06, k0=0.0,
+                    k_beta=0.0)
+
+
+def distorted_quad4(nx, ny, lx, ly, seed):
+    """A QUAD4 grid with every interior node moved by up to 20 % of a cell."""
+    coords, conn = M.grid_quad4(nx, ny, lx, ly)
+    rng = np.random.default_rng(seed)
+    hx, hy = lx / nx, ly / ny
+    i = np.arange(coords.shape[0]) % (nx + 1)
+    j = np.arange(coords.shape[0]) // (nx + 1)
+    inner = (i > 0) & (i < nx) & (j > 0) & (j < ny)
+    coords[inner, 0] += rng.uniform(-0.2, 0.2, inner.sum()) * hx
+    coords[inner, 1] += rng.uniform(-0.2, 0.2, inner.sum()) * hy
+    return coords, conn
+
+
+def membrane_modulus(rho):
+    m = MEMBRANE_MAT
+    rmin = m["Emin"] / m["E0"]
+    return m["E0"] * (rmin + (1.0 - rmin) * rho ** m["penal"])
+
+
+def test_membrane_distorted_elements_at_a_displacement():
+    """Distorted QUAD4 membranes with per-element moduli, K_e and f_e = K_e u_e at a
+    random displacement (StructuralElement2D::internal_residual, membrane part)."""
+    coords, conn = distorted_quad4(4, 3, 2.0, 1.0, seed=5)
+    rng = np.random.default_rng(6)
+    rho = rng.uniform(0.1, 1.0, conn.shape[0])
+    X = rng.standard_normal(coords.shape[0] * 2) * 1e-3
+    with M.Problem(M.PHYS_MEMBRANE, coords, conn, MEMBRANE_MAT) as p:
+        p.set_design(rho)
+        Ke, fe = p.element_matrices(0, conn.shape[0], X)
+    E = membrane_modulus(rho)
+    for e in range(conn.shape[0]):
+        ue = np.concatenate([X[conn[e] * 2], X[conn[e] * 2 + 1]])  # var-blocked (u | v)
+        f_ref, K_ref = O.quad4_membrane_internal(coords[conn[e]], E[e], 0.33, 0.06, ue)
+        assert rel(Ke[e], K_ref) < RTOL_ELEM
+        assert rel(fe[e], f_ref) < RTOL_ELEM
+
+
+def membrane_cantilever(nx, ny, seed):
+    """Plane-stress cantilever: x = 0 edge clamped, a unit -y load spread over the
+    x = lx edge; distorted interior nodes, random densities."""
+    lx, ly = 4.0, 1.0
+    coords, conn = distorted_quad4(nx, ny, lx, ly, seed)
+    nodes = np.arange(coords.shape[0])
+    left = nodes[nodes % (nx + 1) == 0]
+    right = nodes[nodes % (nx + 1) == nx]
+    fixed_dofs = np.sort(np.concatenate([2 * left, 2 * left + 1]))
+    load_dofs = 2 * right + 1
+    load_values = np.full(right.shape[0], -1.0 / right.shape[0])
+    rho = np.random.default_rng(seed + 1).uniform(0.05, 1.0, conn.shape[0])
+    return coords, conn, fixed_dofs, load_dofs, load_values, rho
+
+
+def test_membrane_csr_and_residual_match_oracle():
+    coords, conn, fixed_dofs, load_dofs, load_values, rho = membrane_cantilever(9, 4, seed=8)
+    n = coords.shape[0] * 2
+    rng = np.random.default_rng(9)
+    X = rng.standard_normal(n)
+    X[fixed_dofs] = 0.0
+    with M.Problem(M.PHYS_MEMBRANE, coords, conn, MEMBRANE_MAT, fixed_dofs=fixed_dofs,
+                   load_dofs=load_dofs, load_values=load_values) as p:
+        p.set_design(rho)
+        R = p.residual_and_jacobian(X)
+        rowptr, cols, vals = p.get_csr()
+    rp_ref, cols_ref = O.csr_pattern(conn, coords.shape[0], 2)
+    assert np.array_equal(rowptr, rp_ref) and np.array_equal(cols, cols_ref)
+    fixed = np.zeros(n, dtype=np.uint8)
+    fixed[fixed_dofs] = 1
+    vals_ref = O.assemble_quad4_membrane(coords, conn, membrane_modulus(rho), 0.33, 0.06,
+                                         rp_ref, cols_ref, fixed)
+    assert rel(vals, vals_ref) < RTOL_ELEM
+    F = np.zeros(n)
+    F[load_dofs] = load_values
+    R_ref = O.spmv(rp_ref, cols_ref, vals_ref, X) - F
+    R_ref[fixed_dofs] = X[fixed_dofs]
+    assert rel(R, R_ref) < RTOL_ELEM
+
+
+def test_membrane_cantilever_solve_matches_oracle():
+    """Assembled QUAD4 membrane solve (plain FP64 CG) against the oracle's own
+    assembly and Jacobi-PCG: solution and compliance to 1e-10."""
+    coords, conn, fixed_dofs, load_dofs, load_values, rho = membrane_cantilever(40, 10, seed=11)
+    n = coords.shape[0] * 2
+    with M.Problem(M.PHYS_MEMBRANE, coords, conn, MEMBRANE_MAT, fixed_dofs=fixed_dofs,
+                   load_dofs=load_dofs, load_values=load_values) as p:
+        p.set_design(rho)
+        u, rep = p.solve(M.default_opts(rtol=1e-13, krylov=M.KRYLOV_CG, max_iterations=200000))
+    assert rep.status == 0
+    fixed = np.zeros(n, dtype=np.uint8)
+    fixed[fixed_dofs] = 1
+    rp, cols = O.csr_pattern(conn, coords.shape[0], 2)
+    vals = O.assemble_quad4_membrane(coords, conn, membrane_modulus(rho), 0.33, 0.06, rp, cols,
+                                     fixed)
+    F = np.zeros(n)
+    F[load_dofs] = load_values
+    u_ref, it, rr = O.pcg(rp, cols, vals, F, 1e-14, 10 ** 6)
+    assert rr < 1e-13
+    assert rel(u, u_ref) < RTOL_SOL
+    assert abs(F @ u - F @ u_ref) / abs(F @ u_ref) < RTOL_SOL
+
+
+def test_sensitivity_solve_matches_fd_and_the_adjoint():
+    """J du/drho_e = -dR/drho_e (NonlinearSystem::sensitivity_solve): the direct compliance
+    sensitivity F . du/drho_e equals the adjoint dC/drho_e, and du/drho_e matches central
+    differences of re-solved displacements."""
+    nx, ny, nz = 6, 3, 3
+    rho = np.random.default_rng(21).uniform(0.1, 1.0, nx * ny * nz)
+    opts = M.default_opts(rtol=1e-13, max_iterations=100000)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        u, _ = p.solve(opts)
+        _, dc = p.compliance()
+        F = p.output_derivative(M.OUTPUT_COMPLIANCE, u)
+        for e in (0, 17, 53):
+            du = p.sensitivity_solve(u, M.PARAM_DENSITY, e, opts)
+            assert abs(F @ du - dc[e]) <= 1e-9 * abs(dc[e])
+        h = 1e-5
+        e = 17
+        du = p.sensitivity_solve(u, M.PARAM_DENSITY, e, opts)
+        r2 = rho.copy()
+        r2[e] += h
+        p.set_design(r2)
+        up, _ = p.solve(opts)
+        r2[e] -= 2 * h
+        p.set_design(r2)
+        um, _ = p.solve(opts)
+    assert rel((up - um) / (2 * h), du) < 1e-6
+
+
+def test_element_calculations_at_a_local_solution():
+    """The per-element plugin call (elem_calculations after set_elem_solution) on the
+    element-local solution against the oracle element, and its density sensitivity."""
+    coords, conn = distorted_hex8()
+    rng = np.random.default_rng(4)
+    rho = rng.uniform(0.1, 1.0, conn.shape[0])
+    with M.Problem(M.PHYS_HEX8, coords, conn, M.SIMP_MATERIAL) as p:
+        p.set_design(rho)
+        d = O.simp_desc(1, 1, 1)
+        E, dE = O.simp_modulus(d, rho)
+        for e in range(conn.shape[0]):
+            ue = rng.standard_normal(24)
+            f, K = p.element_calculations(e, ue)
+            f_ref, K_ref = O.hex8_internal(coords[conn[e]], E[e], 0.3, ue)
+            assert rel(K, K_ref) < RTOL_ELEM and rel(f, f_ref) < RTOL_ELEM
+            df = p.element_sensitivity(e, ue, M.PARAM_DENSITY, e)
+            assert rel(df, O.hex8_internal_sens(coords[conn[e]], dE[e], 0.3, ue)) < RTOL_ELEM
+            other = p.element_sensitivity(e, ue, M.PARAM_DENSITY, (e + 1) % conn.shape[0])
+            assert np.all(other == 0.0)
+
+
 def test_bad_inputs_return_status():
     nx, ny, nz = 3, 2, 2
     with M.simp_cantilever(nx, ny, nz) as p:

@@ -144,3 +144,23 @@ def test_synthetic_stream_reports_latency_percentiles():
     assert 0 < st["p50_s"] <= st["p99_s"] <= st["max_s"]
     assert st["solves_per_s"] > 0 and st["peak_inflight"] >= 2
     assert np.all(comp[:, 0] > 0)
+
+
+def test_synthetic_stream_results_match_the_oracle():
+    """Served completions of the synthetic Poisson stream, checked one by one: each sampled
+    request's densities and load spans are regenerated from the stream's seed
+    (mg_server_synthetic_request) and solved by the FP64 oracle; compliance within 1e-6."""
+    sizes = ((8, 4, 4), (16, 8, 8), (12, 6, 6))
+    kw = dict(n_chains=6, sizes=sizes, big_fraction=0.0, max_cases=3, seed=5)
+    with M.Server(opts()) as s:
+        st, comp = s.run_synthetic(40, rate=400.0, **kw)
+    assert st["completed"] == 40 and st["failed"] == 0
+    desc = M.synthetic_desc(40, 400.0, **kw)
+    for i in (0, 7, 19, 33, 39):
+        r = M.synthetic_request(desc, i)
+        nx, ny, nz = r["grid"]
+        for k, (j0, j1) in enumerate(r["spans"]):
+            _, _, ref = O.simp_solve(O.simp_desc(nx, ny, nz, load_y0=j0, load_y1=j1, rtol=1e-12,
+                                                 maxit=10 ** 6), r["rho"], want_sens=False)
+            assert abs(comp[i, k] - ref.compliance) <= 1e-6 * abs(ref.compliance), (i, k)
+        assert np.all(comp[i, len(r["spans"]):] == 0.0)
