@@ -288,37 +288,106 @@ __device__ __forceinline__ bool is_bad(double x) { return !isfinite(x); }
 // pair (dx = 0, 1 at fixed dy, dz) uses K chunks 16 bytes apart (the node and
 // its x-neighbour), so the element operator is 4 MMAs per product (3 products
 // in the split forms) against four B tiles cut from K0.
+//
+// Warp roles (no CTA-wide barrier inside the plane stream; every hand-off is an
+// mbarrier with a bounded wait):
+//   warp 0      one thread issues the TMA loads of each node plane (z and, in the
+//               CG step, p_old; the moduli of the element plane) into a 4-slot ring;
+//   warp 1      one thread issues the MMAs of element plane s once node planes s
+//               and s+1 are converted, into one of four TMEM accumulators;
+//   warps 2-3   convert a node plane into the operand records (hi and lo parts)
+//               and an FP32 copy u (with p = z + beta p_old fused), plus the
+//               plane's moduli, into 4-slot rings;
+//   warps 4-7   drain: thread = element (TMEM lane), reads its 24 results, scales
+//               by E_e, sums the corner results into nodes (x: warp shuffle, y:
+//               shuffle and, at the warp's first row, the previous warp's last row
+//               through shared memory; z: the top corners of plane s-1 carried in
+//               registers) and writes node plane s of y (and p_new) -- every node
+//               sum in a fixed order, deterministic and atomic-free.
+// The column sequence is chosen by the TMA thread alone and travels with the data
+// (a record per ring slot), ending with a sentinel plane.
 constexpr int kColThreads = 256;
 constexpr int kCPX = kCX + 2;                 // 9 nodes per plane row
 constexpr int kCPY = kCY + 2;                 // 17 node rows per plane
 constexpr int kCPN = kCPX * kCPY;             // 153 nodes per plane
 constexpr int kCPB = kCPN * 16;               // 2448 bytes per converted plane (one part)
-constexpr int kCRaw = 3;                      // TMA ring: plane being converted + 2 in flight
-constexpr int kCConv = 3;                     // operand records: planes s+1, s+2 of MMA(s+1) + the next
-constexpr int kCU = 4;                        // FP32 u and E of the planes (read after the next conversion)
 constexpr int kCRawX = 32;                    // TMA node box: 32 floats x 17 rows x 1 plane
 constexpr int kCRawNode = kCRawX * kCPY * 4;  // 2176
 constexpr int kCRawE = 12 * 16 * 4;           // E box: 12 elements x 16 rows x 1 plane = 768
 constexpr int kCRawSlot = 2 * kCRawNode + kCRawE;  // 5120 (z, p_old, E)
-constexpr int kCResStride = 25;
-// issuer of the MMAs and waiter on them (warp 7 has one drain task)
-constexpr int kColIssuer = 224;
+constexpr int kCNR = 4;                       // TMA ring slots
+constexpr int kCNC = 4;                       // operand-record ring slots (hi | lo)
+constexpr int kCNU = 4;                       // u / E ring slots (the drain's inputs)
+constexpr int kCNT = 4;                       // TMEM accumulators (32 columns each)
+constexpr int kCUSlot = kCPN * 16 + 128 * 4;  // u as (x, y, z, -) records + 128 moduli = 2960
+constexpr int kCConvFloats = kCPN * 3;        // 459 values per node plane
+constexpr int kCConvThreads = 64;             // warps 2-3
+constexpr int kCConvRounds = (kCConvFloats + kCConvThreads - 1) / kCConvThreads;  // 8
+constexpr int kCXch = 4 * 8 * 8;              // exchange slot: 4 warps x 8 lanes x (6 + 2 pad) floats
 
-constexpr int kC_OffB = 0;                                      // 4 B tiles x 1 KB, hi | lo
-constexpr int kC_OffConv = 8192;                                // kCConv x (hi, lo) converted planes
-constexpr int kC_OffU = kC_OffConv + kCConv * 2 * kCPB;         // 22880: FP32 u of the planes
-constexpr int kC_OffE = kC_OffU + kCU * kCPN * 3 * 4;           // 30224: E of the element planes
-constexpr int kC_OffRaw = (kC_OffE + kCU * 128 * 4 + 127) / 128 * 128;  // 32256: TMA ring
-constexpr int kC_OffR = kC_OffRaw + kCRaw * kCRawSlot;          // 47616: drained plane results
-constexpr int kC_OffBar = (kC_OffR + 2 * 128 * kCResStride * 4 + 127) / 128 * 128;  // 73216
-constexpr int kColSmem = kC_OffBar + 64;                        // three CTAs per SM
+constexpr int kC_OffB = 0;                                          // 4 B tiles x 1 KB, hi | lo
+constexpr int kC_OffConv = 8192;                                    // kCNC x (hi, lo) records
+constexpr int kC_OffRaw = kC_OffConv + kCNC * 2 * kCPB;             // 27776: TMA ring
+constexpr int kC_OffU = kC_OffRaw + kCNR * kCRawSlot;               // 48256: u / E ring
+constexpr int kC_OffX = kC_OffU + kCNU * kCUSlot;                   // 60096: y-exchange, 2 slots
+constexpr int kC_OffMeta = kC_OffX + 2 * kCXch * 4;                 // 62144: plane records (int4)
+constexpr int kC_OffRed = kC_OffMeta + (kCNR + kCNC + kCNU) * 16;   // 62336: column partials [2][4]
+constexpr int kC_OffBar = kC_OffRed + 64;                           // 62400: mbarriers
+// barriers: raw full/empty, conv full/empty, u full/empty, tmem full/empty, xch[2], red[2], fin
+constexpr int kCBarRawFull = 0, kCBarRawEmpty = kCBarRawFull + kCNR, kCBarConvFull = kCBarRawEmpty + kCNR,
+              kCBarConvEmpty = kCBarConvFull + kCNC, kCBarUFull = kCBarConvEmpty + kCNC,
+              kCBarUEmpty = kCBarUFull + kCNU, kCBarTFull = kCBarUEmpty + kCNU, kCBarTEmpty = kCBarTFull + kCNT,
+              kCBarXch = kCBarTEmpty + kCNT, kCBarRed = kCBarXch + 2, kCBarFin = kCBarRed + 2,
+              kCBarCount = kCBarFin + 1;
+constexpr int kC_OffFlags = kC_OffBar + kCBarCount * 8;             // tmem slot, abort flag
+constexpr int kColSmem = kC_OffFlags + 16;                          // three CTAs per SM
 static_assert(kC_OffRaw % 128 == 0 && kCRawSlot % 128 == 0 && kCRawNode % 128 == 0, "TMA destinations");
-static_assert(kC_OffConv % 16 == 0 && kCPB % 16 == 0, "operand alignment");
+static_assert(kC_OffConv % 16 == 0 && kCPB % 16 == 0 && kC_OffU % 16 == 0 && kCUSlot % 16 == 0, "alignment");
+static_assert(kC_OffMeta % 16 == 0 && kC_OffBar % 8 == 0, "alignment");
+static_assert(3 * (kColSmem + 1024) <= 228 * 1024, "three CTAs per SM");
+static_assert(kCNT * 32 * 3 <= 512, "TMEM columns of three CTAs");
+
+// bounded mbarrier wait that also gives up when another role has set the CTA's
+// abort flag; a wait that runs out of polls sets the flag
+__device__ __forceinline__ bool col_wait(uint32_t mbar, uint32_t phase, volatile int *abort_flag) {
+    for (int i = 0; i < (1 << 22); i++) {
+        if (mbar_try_wait(mbar, phase)) return true;
+        if ((i & 63) == 63 && *abort_flag) return false;
+    }
+    *abort_flag = 1;
+    return false;
+}
+
+// columns [taddr, taddr + 24) of the warp's 32 TMEM lanes, one wait for both loads
+__device__ __forceinline__ void tmem_ld24(uint32_t taddr, float (&v)[24]) {
+    uint32_t r[24];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+          "=r"(r[23])
+        : "r"(taddr + 16));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 24; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
 
 // Columns col_lo .. col_hi-1; the input vector is tensor map `in_slot`.
 // MODE 1: CG step, gathered u = z + beta p_old (z = in_slot, p_old = map 1 +
 //         parity), p_new (owned) = u, q = A u, per-problem alpha = rz / (p.q).
 // MODE 2: y = rhs - A x.   MODE 3: y = A x.   (Both 0 on Dirichlet dofs.)
+// A wait that times out sets bit 1 (tensor-core hand-offs) or bit 2 (data
+// hand-offs) of *err and ends the block after its copies and MMAs have landed.
 template <int PREC, int MODE>
 __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
     const MfProblem *__restrict__ probs, const MfCol *__restrict__ cols, int col_lo, int col_hi, int sel,
@@ -329,289 +398,392 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
     pdl_enter();
     using PR = Prec<PREC>;
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ double red_sh[kColThreads / 32];
-    __shared__ double tree[kColThreads];
-    __shared__ int sh_last;
-    uint32_t *convHi = reinterpret_cast<uint32_t *>(smem + kC_OffConv);  // slot s: + s * 2 * kCPB
-    float *sU = reinterpret_cast<float *>(smem + kC_OffU);
-    float *sE = reinterpret_cast<float *>(smem + kC_OffE);
-    float *sR = reinterpret_cast<float *>(smem + kC_OffR);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kC_OffBar);  // tma[3], mma[2]
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kC_OffBar + 56);
-    const uint32_t tma_bar0 = smem_u32(&bars[0]);
-    const uint32_t mma_bar0 = smem_u32(&bars[3]);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int4 *meta_raw = reinterpret_cast<int4 *>(smem + kC_OffMeta);
+    int4 *meta_conv = meta_raw + kCNR;
+    int4 *meta_u = meta_conv + kCNC;
+    double *red = reinterpret_cast<double *>(smem + kC_OffRed);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kC_OffFlags);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kC_OffFlags + 4);
+    const uint32_t bar0 = smem_u32(smem + kC_OffBar);
+    auto bar = [&](int i) -> uint32_t { return bar0 + 8u * (uint32_t)i; };
     float *p_new = (MODE == 1) ? (parity ? p0 : p1) : nullptr;
 
-    auto usable = [&](int ci) {
-        const MfProblem &Q = probs[cols[ci].prob];
-        return !states[Q.root].done && !Q.bottom && (sel < 0 || sel == (Q.coarse < 0 ? 1 : 0));
-    };
-    int ci = col_lo + blockIdx.x;
-    while (ci < col_hi && !usable(ci)) ci += gridDim.x;
-    if (ci >= col_hi) return;  // uniform: no work for this block
-
     if (tid == 0) {
-        for (int k = 0; k < kCRaw; k++) mbar_init(tma_bar0 + 8 * k, 1);
-        for (int k = 0; k < 2; k++) mbar_init(mma_bar0 + 8 * k, 1);
+        for (int k = 0; k < kCNR; k++) {
+            mbar_init(bar(kCBarRawFull + k), 1);
+            mbar_init(bar(kCBarRawEmpty + k), 2);   // the two converter warps
+        }
+        for (int k = 0; k < kCNC; k++) {
+            mbar_init(bar(kCBarConvFull + k), 2);
+            mbar_init(bar(kCBarConvEmpty + k), 1);  // an MMA commit
+        }
+        for (int k = 0; k < kCNU; k++) {
+            mbar_init(bar(kCBarUFull + k), 2);
+            mbar_init(bar(kCBarUEmpty + k), 4);     // the four drain warps
+        }
+        for (int k = 0; k < kCNT; k++) {
+            mbar_init(bar(kCBarTFull + k), 1);
+            mbar_init(bar(kCBarTEmpty + k), 4);
+        }
+        for (int k = 0; k < 2; k++) {
+            mbar_init(bar(kCBarXch + k), 4);
+            mbar_init(bar(kCBarRed + k), 4);
+        }
+        mbar_init(bar(kCBarFin), 1);
+        *abort_flag = 0;
     }
-    if (warp == 0) tmem_alloc(smem_u32(tslot), 64);  // 2 accumulator slots x 32 columns
+    if (warp == 1) tmem_alloc(smem_u32(tslot), kCNT * 32);
     {
         // B tiles: [tf32 hi 1024 | tf32 lo 1024 | bf16 hi 1024 | bf16 lo 1024] words
         const uint32_t *src = Bop2 + (PR::kTf32 ? 0 : 2048);
         uint32_t *dst = reinterpret_cast<uint32_t *>(smem + kC_OffB);
         for (int i = tid; i < 2048; i += kColThreads) dst[i] = src[i];
         // node records: the unused lanes stay 0 (B has zero rows there; 0 x NaN is NaN)
-        for (int i = tid; i < kCConv * 2 * kCPB / 4; i += kColThreads) convHi[i] = 0u;
+        uint32_t *conv = reinterpret_cast<uint32_t *>(smem + kC_OffConv);
+        for (int i = tid; i < kCNC * 2 * kCPB / 4; i += kColThreads) conv[i] = 0u;
     }
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t b_base = smem_u32(smem + kC_OffB), conv_base = smem_u32(smem + kC_OffConv);
 
-    uint32_t tma_phase[kCRaw] = {0, 0, 0}, mma_phase[2] = {0, 0};
-    uint32_t tma_issued = 0;  // bit k: a TMA into raw slot k is outstanding
-    bool failed = false;
-    int run = 0;  // columns of the current problem since the last counter update (MODE 1)
-    for (; ci < col_hi && !failed;) {
-        int nci = ci + gridDim.x;
-        while (nci < col_hi && !usable(nci)) nci += gridDim.x;
-        const MfCol cl = cols[ci];
-        const MfProblem P = probs[cl.prob];
-        MfState *st = states + cl.prob;
-        const float beta = (MODE == 1) ? (float)st->beta : 0.0f;
-        const int x0 = cl.cx * kCX, y0 = cl.cy * kCY, z0 = cl.cz * P.col_z;
-        const int z1 = min(z0 + P.col_z, P.NZ);
-        const int S = z1 - z0 + 1;                     // element planes z0-1 .. z1-1
-        const int xs = (3 * (x0 - 1)) & ~3, ox = 3 * (x0 - 1) - xs;  // 16-byte aligned box starts
-        const int xe = (x0 - 1) & ~3, oe = (x0 - 1) - xe;
-        const CUtensorMap *maps = tmaps + (size_t)cl.prob * kMapsPerProblem;
-        // TMA of node plane p (nz = z0 - 1 + p) and, for p < S, element plane p
-        auto issue = [&](int p) {
-            const int slot = p % kCRaw;
-            uint8_t *raw = smem + kC_OffRaw + slot * kCRawSlot;
-            const uint32_t bar = tma_bar0 + 8 * slot;
-            const uint32_t bytes = (MODE == 1 ? 2 : 1) * kCRawNode + (p < S ? kCRawE : 0);
-            mbar_expect_tx(bar, bytes);
-            tma_load_3d(smem_u32(raw), maps + in_slot, xs, y0 - 1, z0 - 1 + p, bar);
-            if (MODE == 1) tma_load_3d(smem_u32(raw + kCRawNode), maps + 1 + parity, xs, y0 - 1, z0 - 1 + p, bar);
-            if (p < S) tma_load_3d(smem_u32(raw + 2 * kCRawNode), maps + 3, xe, y0 - 1, z0 - 1 + p, bar);
-        };
-        // wait for plane p (every thread polls the barrier) and convert it into the
-        // operand records, u and E; returns this thread's wait status
-        auto convert = [&](int p) -> bool {
-            const int slot = p % kCRaw, cs = p % kCConv, us = p % kCU;
-            const bool ok = mbar_wait_bounded(tma_bar0 + 8 * slot, tma_phase[slot]);
-            tma_phase[slot] ^= 1u;
-            tma_issued &= ~(1u << slot);
-            const float *rz = reinterpret_cast<const float *>(smem + kC_OffRaw + slot * kCRawSlot);
-            const float *rp = rz + kCRawNode / 4;
-            const float *re = rz + 2 * kCRawNode / 4;
-            uint32_t *hi = convHi + cs * (2 * kCPB / 4);
-            uint32_t *lo = hi + kCPB / 4;
-            float *u = sU + us * kCPN * 3;
-            for (int i = tid; i < kCPN * 3; i += kColThreads) {
-                const int n = i / 3, c = i - 3 * n;
-                const int nx = n % kCPX, ny = n / kCPX;
-                const int bo = ny * kCRawX + ox + 3 * nx + c;
-                const float v = (MODE == 1) ? fmaf(beta, rp[bo], rz[bo]) : rz[bo];
-                u[i] = v;
-                if (PR::kTf32) {
-                    const uint32_t h = to_tf32(v);
-                    hi[n * 4 + c] = h;
-                    if (PR::kSplit) lo[n * 4 + c] = __float_as_uint(v - __uint_as_float(h));
-                } else {
-                    const __nv_bfloat16 h = __float2bfloat16_rn(v);
-                    reinterpret_cast<__nv_bfloat16 *>(hi)[n * 8 + c] = h;
-                    if (PR::kSplit)
-                        reinterpret_cast<__nv_bfloat16 *>(lo)[n * 8 + c] = __float2bfloat16_rn(v - __bfloat162float(h));
-                }
-            }
-            if (p < S)
-                for (int e = tid; e < 128; e += kColThreads) sE[us * 128 + e] = re[(e >> 3) * 12 + oe + (e & 7)];
-            fence_async_smem();  // the records are read by the tensor core (async proxy)
-            return ok;
-        };
-        // MMA of element plane s into accumulator slot s % 2
-        auto mma = [&](int s) {
-            const uint32_t d = tmem + (s & 1) * 32;
-            uint32_t acc = 0u;
-            const int nprod = PR::kSplit ? 3 : 1;
-            for (int prod = 0; prod < nprod; prod++) {
-                const uint32_t apart = (prod == 2) ? kCPB : 0u;         // lo records
-                const uint32_t bpart = (prod == 1) ? 4096u : 0u;        // lo B
-#pragma unroll
-                for (int st4 = 0; st4 < 4; st4++) {
-                    const int dy = st4 & 1, dz = st4 >> 1;
-                    const uint32_t a = conv_base + ((s + dz) % kCConv) * 2 * kCPB + apart + dy * kCPX * 16;
-                    umma<PR::kTf32>(d, umma_desc(a, 16, kCPX * 16), umma_desc(b_base + bpart + st4 * 1024, 128, 256),
-                                    acc);
-                    acc = 1u;
-                }
-            }
-            umma_commit(mma_bar0 + 8 * (s & 1));
-        };
-
-        // ---- prologue: planes 0, 1 converted, 2 and 3 in flight, MMA(0) issued
-        if (tid == 0) {
-            fence_async_smem();
-            for (int p = 0; p <= min(2, S); p++) issue(p);
-        }
-        for (int p = 0; p <= min(2, S); p++) tma_issued |= 1u << (p % kCRaw);
-        {
-            bool ok = convert(0);
-            ok = convert(1) && ok;
-            fence_before();
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                if (tid == 0) atomicOr(err, 2);
-                break;
-            }
-            fence_after();
-        }
-        if (S >= 3) {
-            if (tid == 0) {
-                fence_async_smem();
-                issue(3);  // into the slot of plane 0
-            }
-            tma_issued |= 1u << (3 % kCRaw);
-        }
-        if (tid == kColIssuer) mma(0);
-        float part = 0.0f;
-        // ---- one element plane per step, two CTA barriers per step:
-        //      (a) convert plane s+2 | barrier | TMA(s+4), MMA(s+1)
-        //      (c) wait MMA(s), drain plane s | barrier | (d) node sums of node plane s
-        for (int s = 0; s < S && !failed; s++) {
+    if (warp == 0) {
+        // ------------------------------------------------------------ TMA producer
+        if (lane == 0) {
+            uint32_t k = 0;
+            int last_issue[kCNR] = {-1, -1, -1, -1};
+            auto usable = [&](int ci) {
+                const MfProblem &Q = probs[cols[ci].prob];
+                return !states[Q.root].done && !Q.bottom && (sel < 0 || sel == (Q.coarse < 0 ? 1 : 0));
+            };
             bool ok = true;
-            if (s + 2 <= S) ok = convert(s + 2);
-            fence_before();
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                if (tid == 0) atomicOr(err, 2);
-                break;
-            }
-            fence_after();
-            if (s + 4 <= S) {
-                if (tid == 0) {
-                    fence_async_smem();
-                    issue(s + 4);  // into the slot of plane s + 1, converted a step ago
-                }
-                tma_issued |= 1u << ((s + 4) % kCRaw);
-            }
-            if (tid == kColIssuer && s + 1 < S) mma(s + 1);
-            // (c) every thread waits for MMA(s), then drains its TMEM quarter
-            const bool mok = mbar_wait_bounded(mma_bar0 + 8 * (s & 1), mma_phase[s & 1]);
-            mma_phase[s & 1] ^= 1u;
-            fence_after();
-            {
-                const float *Es = sE + (s % kCU) * 128;
-                float *R = sR + (s & 1) * 128 * kCResStride;
-                for (int task = warp; task < 12; task += kColThreads / 32) {
-                    const int lg = task & 3, cg = task >> 2;
-                    const int r = lg * 32 + lane;
-                    float v[8];
-                    tmem_ld8(tmem + (s & 1) * 32 + cg * 8 + ((uint32_t)(lg * 32) << 16), v);
-                    const float e = Es[r];
-#pragma unroll
-                    for (int n = 0; n < 8; n++) R[r * kCResStride + cg * 8 + n] = e * v[n];
-                }
-            }
-            fence_before();
-            if (__syncthreads_or(!mok)) {
-                failed = true;
-                if (tid == kColIssuer) atomicOr(err, 1);
-                break;
-            }
-            // (d) node sums of node plane nz = z0 - 1 + s (owned planes z0 .. z1-1)
-            const int nz = z0 - 1 + s;
-            if (s >= 1 && nz < z1) {
-                const float *R0 = sR + (s & 1) * 128 * kCResStride;         // element plane nz (dz = 0)
-                const float *R1 = sR + ((s - 1) & 1) * 128 * kCResStride;   // element plane nz - 1 (dz = 1)
-                const float *u = sU + (s % kCU) * kCPN * 3;
-                for (int i = tid; i < kCX * kCY * 3; i += kColThreads) {
-                    const int n = i / 3, c = i - 3 * n;
-                    const int oxn = n % kCX, oyn = n / kCX;
-                    const int gx = x0 + oxn, gy = y0 + oyn;
-                    if (gx >= P.NX || gy >= P.NY) continue;
-                    float acc = 0.0f;
-#pragma unroll
-                    for (int a = 0; a < 8; a++) {
-                        int dx, dy, dz;
-                        corner_bits(a, dx, dy, dz);
-                        const int r = (oyn + 1 - dy) * 8 + (oxn + 1 - dx);
-                        acc += (dz ? R1 : R0)[r * kCResStride + 3 * a + c];
+            int ci = col_lo + blockIdx.x;
+            while (ci < col_hi && !usable(ci)) ci += gridDim.x;
+            for (; ci < col_hi && ok;) {
+                const MfCol cl = cols[ci];
+                const MfProblem &P = probs[cl.prob];
+                const int x0 = cl.cx * kCX, y0 = cl.cy * kCY, z0 = cl.cz * P.col_z;
+                const int z1 = min(z0 + P.col_z, P.NZ);
+                const int S = z1 - z0 + 1;                      // element planes z0-1 .. z1-1
+                const int xs = (3 * (x0 - 1)) & ~3, xe = (x0 - 1) & ~3;  // 16-byte aligned box starts
+                const CUtensorMap *maps = tmaps + (size_t)cl.prob * kMapsPerProblem;
+                for (int p = 0; p <= S; p++, k++) {
+                    const int slot = (int)(k % kCNR);
+                    if (!col_wait(bar(kCBarRawEmpty + slot), ((k / kCNR) & 1u) ^ 1u, abort_flag)) {
+                        ok = false;
+                        break;
                     }
-                    const int64_t gd = dof_index(P, gx, gy, nz, c);
-                    if (MODE == 1) {
-                        const float pv = u[((oyn + 1) * kCPX + oxn + 1) * 3 + c];
-                        y[gd] = acc;
-                        p_new[gd] = pv;
-                        part = fmaf(pv, acc, part);
-                    } else if (MODE == 2) {
-                        y[gd] = (dinv[gd] == 0.0f) ? 0.0f : rhs[gd] - acc;
+                    meta_raw[slot] = make_int4(ci, p, S, 0);
+                    uint8_t *raw = smem + kC_OffRaw + slot * kCRawSlot;
+                    const uint32_t bytes = (MODE == 1 ? 2 : 1) * kCRawNode + (p < S ? kCRawE : 0);
+                    mbar_expect_tx(bar(kCBarRawFull + slot), bytes);
+                    tma_load_3d(smem_u32(raw), maps + in_slot, xs, y0 - 1, z0 - 1 + p, bar(kCBarRawFull + slot));
+                    if (MODE == 1)
+                        tma_load_3d(smem_u32(raw + kCRawNode), maps + 1 + parity, xs, y0 - 1, z0 - 1 + p,
+                                    bar(kCBarRawFull + slot));
+                    if (p < S)
+                        tma_load_3d(smem_u32(raw + 2 * kCRawNode), maps + 3, xe, y0 - 1, z0 - 1 + p,
+                                    bar(kCBarRawFull + slot));
+                    last_issue[slot] = (int)k;
+                }
+                ci += gridDim.x;
+                while (ci < col_hi && !usable(ci)) ci += gridDim.x;
+            }
+            if (ok) {
+                // sentinel: no data, the stream ends
+                const int slot = (int)(k % kCNR);
+                if (col_wait(bar(kCBarRawEmpty + slot), ((k / kCNR) & 1u) ^ 1u, abort_flag)) {
+                    meta_raw[slot] = make_int4(-1, 0, 0, 0);
+                    mbar_arrive(bar(kCBarRawFull + slot));
+                }
+            }
+            if (*abort_flag) {
+                atomicOr(err, 2);
+                // let the copies in flight land before the block exits
+                for (int s = 0; s < kCNR; s++)
+                    if (last_issue[s] >= 0) {
+                        const uint32_t ph = ((uint32_t)last_issue[s] / kCNR) & 1u;
+                        for (int i = 0; i < (1 << 22) && !mbar_try_wait(bar(kCBarRawFull + s), ph); i++) {
+                        }
+                    }
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            const uint32_t b_base = smem_u32(smem + kC_OffB), conv_base = smem_u32(smem + kC_OffConv);
+            uint32_t es = 0;
+            for (uint32_t k = 0;; k++) {
+                const int cs = (int)(k % kCNC);
+                if (!col_wait(bar(kCBarConvFull + cs), (k / kCNC) & 1u, abort_flag)) break;
+                const int4 m = meta_conv[cs];
+                if (m.x < 0) break;
+                if (m.y >= 1) {
+                    // element plane m.y - 1 from node planes k - 1 (dz = 0) and k (dz = 1)
+                    const int ts = (int)(es % kCNT);
+                    if (!col_wait(bar(kCBarTEmpty + ts), ((es / kCNT) & 1u) ^ 1u, abort_flag)) break;
+                    fence_after();
+                    const uint32_t d = tmem + (uint32_t)ts * 32;
+                    const int cprev = (int)((k - 1) % kCNC);
+                    uint32_t acc = 0u;
+                    const int nprod = PR::kSplit ? 3 : 1;
+                    for (int prod = 0; prod < nprod; prod++) {
+                        const uint32_t apart = (prod == 2) ? kCPB : 0u;  // lo records
+                        const uint32_t bpart = (prod == 1) ? 4096u : 0u; // lo B
+#pragma unroll
+                        for (int st4 = 0; st4 < 4; st4++) {
+                            const int dy = st4 & 1, dz = st4 >> 1;
+                            const uint32_t a = conv_base + (dz ? cs : cprev) * 2 * kCPB + apart + dy * kCPX * 16;
+                            umma<PR::kTf32>(d, umma_desc(a, 16, kCPX * 16),
+                                            umma_desc(b_base + bpart + st4 * 1024, 128, 256), acc);
+                            acc = 1u;
+                        }
+                    }
+                    umma_commit(bar(kCBarTFull + ts));
+                    umma_commit(bar(kCBarConvEmpty + cprev));             // node plane k - 1 is done
+                    if (m.y == m.z) umma_commit(bar(kCBarConvEmpty + cs)); // the column's last node plane
+                    es++;
+                }
+            }
+            // every MMA issued has completed before the accumulators are freed
+            umma_commit(bar(kCBarFin));
+            for (int i = 0; i < (1 << 22) && !mbar_try_wait(bar(kCBarFin), 0u); i++) {
+            }
+            if (*abort_flag) atomicOr(err, 1);
+        }
+    } else if (warp < 4) {
+        // ------------------------------------------------------------ converters
+        const int ct = tid - 64;
+        int src[kCConvRounds], dst[kCConvRounds];  // raw-box float index (ox added), record word
+#pragma unroll
+        for (int j = 0; j < kCConvRounds; j++) {
+            const int i = ct + kCConvThreads * j;
+            const int row = i / 27, kk = i - 27 * row;
+            src[j] = (i < kCConvFloats) ? row * kCRawX + kk : -1;
+            dst[j] = (row * kCPX + kk / 3) * 4 + kk % 3;  // node n, component c: word 4 n + c
+        }
+        float beta = 0.0f;
+        int ox = 0, oe = 0;
+        for (uint32_t k = 0;; k++) {
+            const int rs = (int)(k % kCNR), cs = (int)(k % kCNC), us = (int)(k % kCNU);
+            bool ok = col_wait(bar(kCBarRawFull + rs), (k / kCNR) & 1u, abort_flag);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            const int4 m = meta_raw[rs];
+            ok = col_wait(bar(kCBarConvEmpty + cs), ((k / kCNC) & 1u) ^ 1u, abort_flag) &&
+                 col_wait(bar(kCBarUEmpty + us), ((k / kCNU) & 1u) ^ 1u, abort_flag);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            if (m.x >= 0) {
+                if (m.y == 0) {
+                    const MfCol cl = cols[m.x];
+                    const int x0 = cl.cx * kCX;
+                    ox = 3 * (x0 - 1) - ((3 * (x0 - 1)) & ~3);
+                    oe = (x0 - 1) - ((x0 - 1) & ~3);
+                    beta = (MODE == 1) ? (float)states[cl.prob].beta : 0.0f;
+                }
+                const float *rz = reinterpret_cast<const float *>(smem + kC_OffRaw + rs * kCRawSlot);
+                const float *rp = rz + kCRawNode / 4;
+                const float *re = rz + 2 * kCRawNode / 4;
+                uint32_t *hi = reinterpret_cast<uint32_t *>(smem + kC_OffConv + cs * 2 * kCPB);
+                uint32_t *lo = hi + kCPB / 4;
+                float *u = reinterpret_cast<float *>(smem + kC_OffU + us * kCUSlot);
+#pragma unroll
+                for (int j = 0; j < kCConvRounds; j++) {
+                    if (src[j] < 0) continue;
+                    const int bo = src[j] + ox;
+                    const float v = (MODE == 1) ? fmaf(beta, rp[bo], rz[bo]) : rz[bo];
+                    u[dst[j]] = v;
+                    if (PR::kTf32) {
+                        const uint32_t h = to_tf32(v);
+                        hi[dst[j]] = h;
+                        if (PR::kSplit) lo[dst[j]] = __float_as_uint(v - __uint_as_float(h));
                     } else {
-                        y[gd] = (dinv[gd] == 0.0f) ? 0.0f : acc;
+                        // BF16 record: halves x, y, z at 8 n + c
+                        const int hw = (dst[j] >> 2) * 8 + (dst[j] & 3);
+                        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                        reinterpret_cast<__nv_bfloat16 *>(hi)[hw] = h;
+                        if (PR::kSplit)
+                            reinterpret_cast<__nv_bfloat16 *>(lo)[hw] = __float2bfloat16_rn(v - __bfloat162float(h));
                     }
                 }
+                if (m.y < m.z) {
+                    float *Eu = u + kCPN * 4;
+                    for (int e = ct; e < 128; e += kCConvThreads) Eu[e] = re[(e >> 3) * 12 + oe + (e & 7)];
+                }
+                fence_async_smem();  // the records are read by the tensor core (async proxy)
             }
+            __syncwarp();
+            if (lane == 0) {
+                if (warp == 2) {
+                    meta_conv[cs] = m;
+                    meta_u[us] = m;
+                }
+                mbar_arrive(bar(kCBarRawEmpty + rs));
+                mbar_arrive(bar(kCBarConvFull + cs));
+                mbar_arrive(bar(kCBarUFull + us));
+            }
+            if (m.x < 0) break;
         }
-        if (failed) break;
-        if (MODE == 1) {
-            // column partial: FP32 within a warp, FP64 across warps
+    } else {
+        // ------------------------------------------------------------ drain
+        const int dw = warp - 4;                   // TMEM lane quarter
+        const int r = dw * 32 + lane, ex = lane & 7, ey = r >> 3;
+        float *xch = reinterpret_cast<float *>(smem + kC_OffX);
+        uint32_t es = 0, xk = 0, rk = 0;
+        float top[3] = {0.0f, 0.0f, 0.0f}, part = 0.0f;
+        MfProblem P{};
+        int x0 = 0, y0 = 0, z0 = 0, prob = 0;
+        bool own = false;
+        for (uint32_t k = 0;; k++) {
+            const int us = (int)(k % kCNU);
+            bool ok = col_wait(bar(kCBarUFull + us), (k / kCNU) & 1u, abort_flag);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            const int4 m = meta_u[us];
+            if (m.x < 0) break;
+            const float *u = reinterpret_cast<const float *>(smem + kC_OffU + us * kCUSlot);
+            if (m.y == 0) {
+                const MfCol cl = cols[m.x];
+                prob = cl.prob;
+                P = probs[prob];
+                x0 = cl.cx * kCX;
+                y0 = cl.cy * kCY;
+                z0 = cl.cz * P.col_z;
+                own = ex >= 1 && ey >= 1 && x0 + ex - 1 < P.NX && y0 + ey - 1 < P.NY;
+                part = 0.0f;
+                top[0] = top[1] = top[2] = 0.0f;
+            }
+            if (m.y < m.z) {
+                // element plane s = m.y: its accumulator, scaled by E_e
+                const int ts = (int)(es % kCNT);
+                ok = col_wait(bar(kCBarTFull + ts), (es / kCNT) & 1u, abort_flag);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                fence_after();
+                float v[24];
+                tmem_ld24(tmem + ((uint32_t)(dw * 32) << 16) + (uint32_t)ts * 32, v);
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(kCBarTEmpty + ts));
+                es++;
+                const float e = u[kCPN * 4 + r];
+                // in-plane sums: A = row-ey corners of node (ex, ey), B = row-ey corners of
+                // node (ex, ey + 1); [0] bottom corners (dz = 0), [1] top corners (dz = 1)
+                float A[2][3], B[2][3];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-            if (lane == 0) red_sh[warp] = (double)part;
+                for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float a00 = e * v[3 * corner_index(0, 0, dz) + c];
+                        const float a10 = e * v[3 * corner_index(1, 0, dz) + c];
+                        const float a01 = e * v[3 * corner_index(0, 1, dz) + c];
+                        const float a11 = e * v[3 * corner_index(1, 1, dz) + c];
+                        A[dz][c] = a00 + __shfl_up_sync(0xffffffffu, a10, 1);
+                        B[dz][c] = a01 + __shfl_up_sync(0xffffffffu, a11, 1);
+                    }
+                // B of the row below: within the warp by a shuffle, across warps through
+                // shared memory (the previous warp's last row)
+                float Bp[2][3];
+#pragma unroll
+                for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) Bp[dz][c] = __shfl_up_sync(0xffffffffu, B[dz][c], 8);
+                const int xs2 = (int)(xk & 1u);
+                float *xw = xch + xs2 * kCXch;
+                if (lane >= 24) {
+#pragma unroll
+                    for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+                        for (int c = 0; c < 3; c++) xw[(dw * 8 + ex) * 8 + dz * 3 + c] = B[dz][c];
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(kCBarXch + xs2));
+                ok = col_wait(bar(kCBarXch + xs2), (xk >> 1) & 1u, abort_flag);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                xk++;
+                if (lane < 8 && dw > 0) {
+#pragma unroll
+                    for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+                        for (int c = 0; c < 3; c++) Bp[dz][c] = xw[((dw - 1) * 8 + ex) * 8 + dz * 3 + c];
+                }
+                // node plane m.y = bottom corners of element plane m.y + top corners of m.y - 1
+                if (m.y >= 1 && own) {
+                    const int gx = x0 + ex - 1, gy = y0 + ey - 1, gz = z0 - 1 + m.y;
+                    const int64_t gd = dof_index(P, gx, gy, gz, 0);
+                    const float4 uv = *reinterpret_cast<const float4 *>(u + (ey * kCPX + ex) * 4);
+                    const float un[3] = {uv.x, uv.y, uv.z};
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float acc = (A[0][c] + Bp[0][c]) + top[c];
+                        if (MODE == 1) {
+                            y[gd + c] = acc;
+                            p_new[gd + c] = un[c];
+                            part = fmaf(un[c], acc, part);
+                        } else if (MODE == 2) {
+                            y[gd + c] = (dinv[gd + c] == 0.0f) ? 0.0f : rhs[gd + c] - acc;
+                        } else {
+                            y[gd + c] = (dinv[gd + c] == 0.0f) ? 0.0f : acc;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++) top[c] = A[1][c] + Bp[1][c];
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(kCBarUEmpty + us));
+            if (MODE == 1 && m.y == m.z) {
+                // column partial of p.q: FP32 within a warp, FP64 across the four warps
+                float w = part;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+                const int rb = (int)(rk & 1u);
+                if (lane == 0) {
+                    red[rb * 4 + dw] = (double)w;
+                    mbar_arrive(bar(kCBarRed + rb));
+                }
+                if (dw == 0) {
+                    ok = col_wait(bar(kCBarRed + rb), (rk >> 1) & 1u, abort_flag);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (!ok) break;
+                    MfState *st = states + prob;
+                    int last = 0;
+                    if (lane == 0) {
+                        const double sum = ((red[rb * 4] + red[rb * 4 + 1]) + red[rb * 4 + 2]) + red[rb * 4 + 3];
+                        col_part[m.x] = sum;
+                        __threadfence();
+                        const unsigned tk = atomicAdd(&st->cnt_apply, 1u);
+                        last = (tk + 1u == (unsigned)P.col_count);
+                    }
+                    last = __shfl_sync(0xffffffffu, last, 0);
+                    if (last) {
+                        __threadfence();
+                        double s = 0.0;
+                        for (int c = lane; c < P.col_count; c += 32) s += __ldcg(col_part + P.col_begin + c);
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                        if (lane == 0) {
+                            st->cnt_apply = 0;
+                            st->pq = s;
+                            if (is_bad(s)) { st->status = MG_ENAN; st->done = 1; }
+                            else if (!(s > 0.0)) { st->status = MG_EBREAKDOWN; st->done = 1; }
+                            else st->alpha = st->rz / s;
+                        }
+                    }
+                }
+                rk++;
+            }
         }
-        __syncthreads();  // all of this column's shared data may be reused
-        if (MODE == 1) {
-            if (tid == 0) {
-                double sum = 0.0;
-                for (int w = 0; w < kColThreads / 32; w++) sum += red_sh[w];
-                col_part[ci] = sum;
-            }
-            run++;
-            const bool flush = nci >= col_hi || cols[nci].prob != cl.prob;
-            if (flush) {
-                if (tid == 0) {
-                    __threadfence();
-                    const unsigned tk = atomicAdd(&st->cnt_apply, (unsigned)run);
-                    sh_last = (tk + (unsigned)run == (unsigned)P.col_count);
-                }
-                run = 0;
-                __syncthreads();
-            }
-            if (flush && sh_last) {
-                double sum = 0.0;
-                for (int k = tid; k < P.col_count; k += kColThreads) sum += __ldcg(col_part + P.col_begin + k);
-                tree[tid] = sum;
-                __syncthreads();
-                for (int w = kColThreads / 2; w > 0; w >>= 1) {
-                    if (tid < w) tree[tid] += tree[tid + w];
-                    __syncthreads();
-                }
-                if (tid == 0) {
-                    const double pq = tree[0];
-                    st->cnt_apply = 0;
-                    st->pq = pq;
-                    if (is_bad(pq)) { st->status = MG_ENAN; st->done = 1; }
-                    else if (!(pq > 0.0)) { st->status = MG_EBREAKDOWN; st->done = 1; }
-                    else st->alpha = st->rz / pq;
-                }
-                __syncthreads();
-            }
-        }
-        ci = nci;
+        if (*abort_flag && lane == 0) atomicOr(err, 2);
     }
-    // after a failed wait, give the outstanding halo loads a bounded chance to land
-    if (failed)
-        for (int k = 0; k < kCRaw; k++)
-            if (tma_issued & (1u << k)) (void)mbar_wait_bounded(tma_bar0 + 8 * k, tma_phase[k]);
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 64);
+    if (warp == 1) tmem_dealloc(tmem, kCNT * 32);
 }
 
 // ------------------------------------------------- factored CUDA-core operator
