@@ -91,29 +91,29 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
     return d;  // base offset 0, LBO mode 0, layout type 0 (SWIZZLE_NONE)
 }
 
-// instruction descriptor: D F32, A/B K-major, N = 32, M = 128
-template <bool TF32>
+// instruction descriptor: D F32, A/B K-major, N columns, M = 128
+template <bool TF32, int N>
 __host__ __device__ constexpr uint32_t umma_idesc() {
     return (1u << 4) |                   // D format F32
            ((TF32 ? 2u : 1u) << 7) |     // A: TF32 (kind::tf32) / BF16 (kind::f16)
            ((TF32 ? 2u : 1u) << 10) |    // B
-           ((32u >> 3) << 17) |          // N >> 3
+           (((uint32_t)N >> 3) << 17) |  // N >> 3
            ((128u >> 4) << 24);          // M >> 4
 }
 
-template <bool TF32>
+template <bool TF32, int N>
 __device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                      uint32_t accumulate) {
     if (TF32) {
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<TF32>()), "r"(accumulate));
+            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<TF32, N>()), "r"(accumulate));
     } else {
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<TF32>()), "r"(accumulate));
+            ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(umma_idesc<TF32, N>()), "r"(accumulate));
     }
 }
 
@@ -289,16 +289,23 @@ __device__ __forceinline__ bool is_bad(double x) { return !isfinite(x); }
 // its x-neighbour), so the element operator is 4 MMAs per product (3 products
 // in the split forms) against four B tiles cut from K0.
 //
+// The cost of one tcgen05.mma (M = 128, K = 8 TF32) grows little with N up to
+// 64 (46, 48, 64, 128 cycles for N = 32, 64, 128, 256, measured on the GB300), so
+// the split forms issue the hi records against [K0_hi | K0_lo] as one N = 64 MMA
+// and the lo records against K0_hi as an N = 32 MMA: 8 MMAs per element plane
+// instead of 12.  The accumulator holds hi.K_hi + lo.K_hi in columns 0-31 and
+// hi.K_lo in columns 32-63; the drain adds the two.
+//
 // Warp roles (no CTA-wide barrier inside the plane stream; every hand-off is an
-// mbarrier with a bounded wait):
+// mbarrier with a bounded wait), two CTAs of 12 warps per SM:
 //   warp 0      one thread issues the TMA loads of each node plane (z and, in the
-//               CG step, p_old; the moduli of the element plane) into a 4-slot ring;
+//               CG step, p_old; the moduli of the element plane) into a ring;
 //   warp 1      one thread issues the MMAs of element plane s once node planes s
 //               and s+1 are converted, into one of four TMEM accumulators;
-//   warps 2-3   convert a node plane into the operand records (hi and lo parts)
-//               and an FP32 copy u (with p = z + beta p_old fused), plus the
-//               plane's moduli, into 4-slot rings;
-//   warps 4-7   drain: thread = element (TMEM lane), reads its 24 results, scales
+//   warps 2-7   convert a node plane into the operand records (hi and lo parts)
+//               and an FP32 copy u of the owned nodes (with p = z + beta p_old
+//               fused), plus the plane's moduli, into rings;
+//   warps 8-11  drain: thread = element (TMEM lane), reads its 24 results, scales
 //               by E_e, sums the corner results into nodes (x: warp shuffle, y:
 //               shuffle and, at the warp's first row, the previous warp's last row
 //               through shared memory; z: the top corners of plane s-1 carried in
@@ -306,7 +313,10 @@ __device__ __forceinline__ bool is_bad(double x) { return !isfinite(x); }
 //               sum in a fixed order, deterministic and atomic-free.
 // The column sequence is chosen by the TMA thread alone and travels with the data
 // (a record per ring slot), ending with a sentinel plane.
-constexpr int kColThreads = 256;
+constexpr int kColThreads = 384;
+constexpr int kColCtas = 2;                   // CTAs per SM
+constexpr int kCConvWarps = 6;                // warps 2-7
+constexpr int kCDrain0 = 2 + kCConvWarps;     // first drain warp (8: TMEM lane quarter = warp % 4)
 constexpr int kCPX = kCX + 2;                 // 9 nodes per plane row
 constexpr int kCPY = kCY + 2;                 // 17 node rows per plane
 constexpr int kCPN = kCPX * kCPY;             // 153 nodes per plane
@@ -316,23 +326,25 @@ constexpr int kCRawNode = kCRawX * kCPY * 4;  // 2176
 constexpr int kCRawE = 12 * 16 * 4;           // E box: 12 elements x 16 rows x 1 plane = 768
 constexpr int kCRawSlot = 2 * kCRawNode + kCRawE;  // 5120 (z, p_old, E)
 constexpr int kCNR = 4;                       // TMA ring slots
-constexpr int kCNC = 4;                       // operand-record ring slots (hi | lo)
-constexpr int kCNU = 4;                       // u / E ring slots (the drain's inputs)
-constexpr int kCNT = 4;                       // TMEM accumulators (32 columns each)
-constexpr int kCUSlot = kCPN * 16 + 128 * 4;  // u as (x, y, z, -) records + 128 moduli = 2960
+constexpr int kCNC = 6;                       // operand-record ring slots (hi | lo)
+constexpr int kCNU = 8;                       // u / E ring slots (the drain's inputs)
+constexpr int kCNT = 4;                       // TMEM accumulators (64 columns each)
+constexpr int kCTCols = 64;                   // TMEM columns per accumulator
+constexpr int kCOwn = kCX * kCY;              // 105 owned nodes per plane
+constexpr int kCUSlot = kCOwn * 16 + 128 * 4; // u of the owned nodes as (x, y, z, -) + 128 moduli = 2192
 constexpr int kCConvFloats = kCPN * 3;        // 459 values per node plane
-constexpr int kCConvThreads = 64;             // warps 2-3
-constexpr int kCConvRounds = (kCConvFloats + kCConvThreads - 1) / kCConvThreads;  // 8
+constexpr int kCConvThreads = 32 * kCConvWarps;
+constexpr int kCConvRounds = (kCConvFloats + kCConvThreads - 1) / kCConvThreads;  // 3
 constexpr int kCXch = 4 * 8 * 8;              // exchange slot: 4 warps x 8 lanes x (6 + 2 pad) floats
 
-constexpr int kC_OffB = 0;                                          // 4 B tiles x 1 KB, hi | lo
+constexpr int kC_OffB = 0;                                          // 4 B tiles x 2 KB: [K_hi | K_lo]
 constexpr int kC_OffConv = 8192;                                    // kCNC x (hi, lo) records
-constexpr int kC_OffRaw = kC_OffConv + kCNC * 2 * kCPB;             // 27776: TMA ring
-constexpr int kC_OffU = kC_OffRaw + kCNR * kCRawSlot;               // 48256: u / E ring
-constexpr int kC_OffX = kC_OffU + kCNU * kCUSlot;                   // 60096: y-exchange, 2 slots
-constexpr int kC_OffMeta = kC_OffX + 2 * kCXch * 4;                 // 62144: plane records (int4)
-constexpr int kC_OffRed = kC_OffMeta + (kCNR + kCNC + kCNU) * 16;   // 62336: column partials [2][4]
-constexpr int kC_OffBar = kC_OffRed + 64;                           // 62400: mbarriers
+constexpr int kC_OffRaw = (kC_OffConv + kCNC * 2 * kCPB + 127) / 128 * 128;  // TMA ring
+constexpr int kC_OffU = kC_OffRaw + kCNR * kCRawSlot;               // u / E ring
+constexpr int kC_OffX = kC_OffU + kCNU * kCUSlot;                   // y-exchange, 2 slots
+constexpr int kC_OffMeta = kC_OffX + 2 * kCXch * 4;                 // plane records (int4)
+constexpr int kC_OffRed = kC_OffMeta + (kCNR + kCNC + kCNU) * 16;   // column partials [2][4]
+constexpr int kC_OffBar = kC_OffRed + 64;                           // mbarriers
 // barriers: raw full/empty, conv full/empty, u full/empty, tmem full/empty, xch[2], red[2], fin
 constexpr int kCBarRawFull = 0, kCBarRawEmpty = kCBarRawFull + kCNR, kCBarConvFull = kCBarRawEmpty + kCNR,
               kCBarConvEmpty = kCBarConvFull + kCNC, kCBarUFull = kCBarConvEmpty + kCNC,
@@ -340,12 +352,13 @@ constexpr int kCBarRawFull = 0, kCBarRawEmpty = kCBarRawFull + kCNR, kCBarConvFu
               kCBarXch = kCBarTEmpty + kCNT, kCBarRed = kCBarXch + 2, kCBarFin = kCBarRed + 2,
               kCBarCount = kCBarFin + 1;
 constexpr int kC_OffFlags = kC_OffBar + kCBarCount * 8;             // tmem slot, abort flag
-constexpr int kColSmem = kC_OffFlags + 16;                          // three CTAs per SM
+constexpr int kColSmem = kC_OffFlags + 16;
 static_assert(kC_OffRaw % 128 == 0 && kCRawSlot % 128 == 0 && kCRawNode % 128 == 0, "TMA destinations");
 static_assert(kC_OffConv % 16 == 0 && kCPB % 16 == 0 && kC_OffU % 16 == 0 && kCUSlot % 16 == 0, "alignment");
 static_assert(kC_OffMeta % 16 == 0 && kC_OffBar % 8 == 0, "alignment");
-static_assert(3 * (kColSmem + 1024) <= 228 * 1024, "three CTAs per SM");
-static_assert(kCNT * 32 * 3 <= 512, "TMEM columns of three CTAs");
+static_assert(kColCtas * (kColSmem + 1024) <= 228 * 1024, "CTAs per SM");
+static_assert(kCNT * kCTCols * kColCtas <= 512, "TMEM columns of the CTAs on an SM");
+static_assert(kColThreads == 32 * (kCDrain0 + 4), "warp roles");
 
 // bounded mbarrier wait that also gives up when another role has set the CTA's
 // abort flag; a wait that runs out of polls sets the flag
@@ -389,7 +402,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
 // A wait that times out sets bit 1 (tensor-core hand-offs) or bit 2 (data
 // hand-offs) of *err and ends the block after its copies and MMAs have landed.
 template <int PREC, int MODE>
-__global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
+__global__ void __launch_bounds__(kColThreads, kColCtas) mf_col_kernel(
     const MfProblem *__restrict__ probs, const MfCol *__restrict__ cols, int col_lo, int col_hi, int sel,
     const CUtensorMap *__restrict__ tmaps, int in_slot, int parity, const uint32_t *__restrict__ Bop2,
     const float *__restrict__ dinv, const float *__restrict__ rhs, float *__restrict__ p0,
@@ -412,14 +425,14 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
     if (tid == 0) {
         for (int k = 0; k < kCNR; k++) {
             mbar_init(bar(kCBarRawFull + k), 1);
-            mbar_init(bar(kCBarRawEmpty + k), 2);   // the two converter warps
+            mbar_init(bar(kCBarRawEmpty + k), kCConvWarps);
         }
         for (int k = 0; k < kCNC; k++) {
-            mbar_init(bar(kCBarConvFull + k), 2);
+            mbar_init(bar(kCBarConvFull + k), kCConvWarps);
             mbar_init(bar(kCBarConvEmpty + k), 1);  // an MMA commit
         }
         for (int k = 0; k < kCNU; k++) {
-            mbar_init(bar(kCBarUFull + k), 2);
+            mbar_init(bar(kCBarUFull + k), kCConvWarps);
             mbar_init(bar(kCBarUEmpty + k), 4);     // the four drain warps
         }
         for (int k = 0; k < kCNT; k++) {
@@ -433,12 +446,17 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
         mbar_init(bar(kCBarFin), 1);
         *abort_flag = 0;
     }
-    if (warp == 1) tmem_alloc(smem_u32(tslot), kCNT * 32);
+    if (warp == 1) tmem_alloc(smem_u32(tslot), kCNT * kCTCols);
     {
-        // B tiles: [tf32 hi 1024 | tf32 lo 1024 | bf16 hi 1024 | bf16 lo 1024] words
+        // B tiles in global memory: [tf32 hi 1024 | tf32 lo 1024 | bf16 hi 1024 | bf16 lo 1024]
+        // words, tile t at 256 t in each part; in shared memory tile t at 512 t words as
+        // [hi 256 | lo 256]: N = 64 rows, the lo rows one SBO step after the hi rows
         const uint32_t *src = Bop2 + (PR::kTf32 ? 0 : 2048);
         uint32_t *dst = reinterpret_cast<uint32_t *>(smem + kC_OffB);
-        for (int i = tid; i < 2048; i += kColThreads) dst[i] = src[i];
+        for (int i = tid; i < 2048; i += kColThreads) {
+            const int part = i >> 10, t = (i >> 8) & 3, w = i & 255;
+            dst[t * 512 + part * 256 + w] = src[i];
+        }
         // node records: the unused lanes stay 0 (B has zero rows there; 0 x NaN is NaN)
         uint32_t *conv = reinterpret_cast<uint32_t *>(smem + kC_OffConv);
         for (int i = tid; i < kCNC * 2 * kCPB / 4; i += kColThreads) conv[i] = 0u;
@@ -525,20 +543,20 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
                     const int ts = (int)(es % kCNT);
                     if (!col_wait(bar(kCBarTEmpty + ts), ((es / kCNT) & 1u) ^ 1u, abort_flag)) break;
                     fence_after();
-                    const uint32_t d = tmem + (uint32_t)ts * 32;
+                    const uint32_t d = tmem + (uint32_t)ts * kCTCols;
                     const int cprev = (int)((k - 1) % kCNC);
-                    uint32_t acc = 0u;
-                    const int nprod = PR::kSplit ? 3 : 1;
-                    for (int prod = 0; prod < nprod; prod++) {
-                        const uint32_t apart = (prod == 2) ? kCPB : 0u;  // lo records
-                        const uint32_t bpart = (prod == 1) ? 4096u : 0u; // lo B
 #pragma unroll
-                        for (int st4 = 0; st4 < 4; st4++) {
-                            const int dy = st4 & 1, dz = st4 >> 1;
-                            const uint32_t a = conv_base + (dz ? cs : cprev) * 2 * kCPB + apart + dy * kCPX * 16;
-                            umma<PR::kTf32>(d, umma_desc(a, 16, kCPX * 16),
-                                            umma_desc(b_base + bpart + st4 * 1024, 128, 256), acc);
-                            acc = 1u;
+                    for (int st4 = 0; st4 < 4; st4++) {
+                        const int dy = st4 & 1, dz = st4 >> 1;
+                        const uint32_t a = conv_base + (dz ? cs : cprev) * 2 * kCPB + dy * kCPX * 16;
+                        const uint64_t bd = umma_desc(b_base + st4 * 2048, 128, 256);
+                        if (PR::kSplit) {
+                            // hi records against [K_hi | K_lo] (columns 0-63), lo records
+                            // against K_hi (columns 0-31)
+                            umma<PR::kTf32, 64>(d, umma_desc(a, 16, kCPX * 16), bd, st4 ? 1u : 0u);
+                            umma<PR::kTf32, 32>(d, umma_desc(a + kCPB, 16, kCPX * 16), bd, 1u);
+                        } else {
+                            umma<PR::kTf32, 32>(d, umma_desc(a, 16, kCPX * 16), bd, st4 ? 1u : 0u);
                         }
                     }
                     umma_commit(bar(kCBarTFull + ts));
@@ -553,16 +571,19 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
             }
             if (*abort_flag) atomicOr(err, 1);
         }
-    } else if (warp < 4) {
+    } else if (warp < kCDrain0) {
         // ------------------------------------------------------------ converters
         const int ct = tid - 64;
-        int src[kCConvRounds], dst[kCConvRounds];  // raw-box float index (ox added), record word
+        // per round: raw-box float index (ox added), record word, word of u (owned nodes)
+        int src[kCConvRounds], dst[kCConvRounds], udst[kCConvRounds];
 #pragma unroll
         for (int j = 0; j < kCConvRounds; j++) {
             const int i = ct + kCConvThreads * j;
-            const int row = i / 27, kk = i - 27 * row;
+            const int row = i / 27, kk = i - 27 * row, nx = kk / 3;
             src[j] = (i < kCConvFloats) ? row * kCRawX + kk : -1;
-            dst[j] = (row * kCPX + kk / 3) * 4 + kk % 3;  // node n, component c: word 4 n + c
+            dst[j] = (row * kCPX + nx) * 4 + kk % 3;  // node n, component c: word 4 n + c
+            const bool owned = nx >= 1 && nx <= kCX && row >= 1 && row <= kCY;
+            udst[j] = owned ? ((row - 1) * kCX + nx - 1) * 4 + kk % 3 : -1;
         }
         float beta = 0.0f;
         int ox = 0, oe = 0;
@@ -590,12 +611,20 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
                 uint32_t *hi = reinterpret_cast<uint32_t *>(smem + kC_OffConv + cs * 2 * kCPB);
                 uint32_t *lo = hi + kCPB / 4;
                 float *u = reinterpret_cast<float *>(smem + kC_OffU + us * kCUSlot);
+                // all loads first: the stores below cannot alias them, but the compiler
+                // cannot tell, and would otherwise order each round after the last
+                float vz[kCConvRounds], vp[kCConvRounds];
+#pragma unroll
+                for (int j = 0; j < kCConvRounds; j++) {
+                    const int bo = (src[j] < 0 ? 0 : src[j]) + ox;
+                    vz[j] = rz[bo];
+                    vp[j] = (MODE == 1) ? rp[bo] : 0.0f;
+                }
 #pragma unroll
                 for (int j = 0; j < kCConvRounds; j++) {
                     if (src[j] < 0) continue;
-                    const int bo = src[j] + ox;
-                    const float v = (MODE == 1) ? fmaf(beta, rp[bo], rz[bo]) : rz[bo];
-                    u[dst[j]] = v;
+                    const float v = (MODE == 1) ? fmaf(beta, vp[j], vz[j]) : vz[j];
+                    if (MODE == 1 && udst[j] >= 0) u[udst[j]] = v;
                     if (PR::kTf32) {
                         const uint32_t h = to_tf32(v);
                         hi[dst[j]] = h;
@@ -610,7 +639,7 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
                     }
                 }
                 if (m.y < m.z) {
-                    float *Eu = u + kCPN * 4;
+                    float *Eu = u + kCOwn * 4;
                     for (int e = ct; e < 128; e += kCConvThreads) Eu[e] = re[(e >> 3) * 12 + oe + (e & 7)];
                 }
                 fence_async_smem();  // the records are read by the tensor core (async proxy)
@@ -629,7 +658,7 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
         }
     } else {
         // ------------------------------------------------------------ drain
-        const int dw = warp - 4;                   // TMEM lane quarter
+        const int dw = warp & 3;                   // TMEM lane quarter (warps 8-11)
         const int r = dw * 32 + lane, ex = lane & 7, ey = r >> 3;
         float *xch = reinterpret_cast<float *>(smem + kC_OffX);
         uint32_t es = 0, xk = 0, rk = 0;
@@ -664,12 +693,21 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
                 if (!ok) break;
                 fence_after();
                 float v[24];
-                tmem_ld24(tmem + ((uint32_t)(dw * 32) << 16) + (uint32_t)ts * 32, v);
+                {
+                    const uint32_t ta = tmem + ((uint32_t)(dw * 32) << 16) + (uint32_t)ts * kCTCols;
+                    tmem_ld24(ta, v);
+                    if (PR::kSplit) {
+                        float w[24];
+                        tmem_ld24(ta + 32, w);
+#pragma unroll
+                        for (int i = 0; i < 24; i++) v[i] += w[i];
+                    }
+                }
                 fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar(kCBarTEmpty + ts));
                 es++;
-                const float e = u[kCPN * 4 + r];
+                const float e = u[kCOwn * 4 + r];
                 // in-plane sums: A = row-ey corners of node (ex, ey), B = row-ey corners of
                 // node (ex, ey + 1); [0] bottom corners (dz = 0), [1] top corners (dz = 1)
                 float A[2][3], B[2][3];
@@ -715,7 +753,8 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
                 if (m.y >= 1 && own) {
                     const int gx = x0 + ex - 1, gy = y0 + ey - 1, gz = z0 - 1 + m.y;
                     const int64_t gd = dof_index(P, gx, gy, gz, 0);
-                    const float4 uv = *reinterpret_cast<const float4 *>(u + (ey * kCPX + ex) * 4);
+                    float4 uv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (MODE == 1) uv = *reinterpret_cast<const float4 *>(u + ((ey - 1) * kCX + ex - 1) * 4);
                     const float un[3] = {uv.x, uv.y, uv.z};
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
@@ -783,7 +822,7 @@ __global__ void __launch_bounds__(kColThreads, 3) mf_col_kernel(
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 1) tmem_dealloc(tmem, kCNT * 32);
+    if (warp == 1) tmem_dealloc(tmem, kCNT * kCTCols);
 }
 
 // ------------------------------------------------- factored CUDA-core operator
@@ -2369,7 +2408,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         // columns allows (the level's problems share the 3 x SM slots), 4 to kCZ
         // node planes; a second, partial wave would double the launch's time
         const int cx = (P.NX + kCX - 1) / kCX, cy = (P.NY + kCY - 1) / kCY;
-        const int64_t slots = 3 * (int64_t)sms;
+        const int64_t slots = kColCtas * (int64_t)sms;
         const int64_t col_per = std::max<int64_t>(1, slots / ((int64_t)cx * cy * level_count[P.level]));
         P.col_z = (int)std::min<int64_t>(kCZ, std::max<int64_t>(4, (P.NZ + col_per - 1) / col_per));
         const int cz = (P.NZ + P.col_z - 1) / P.col_z;
@@ -2452,7 +2491,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         }
     }
     b.apply_grid = std::max(1, std::min(nb, 2 * sms));  // FP64 residual: two CTAs per SM
-    b.col_grid = std::max(1, std::min(b.n_cols, 3 * sms));  // three column CTAs per SM
+    b.col_grid = std::max(1, std::min(b.n_cols, kColCtas * sms));  // column CTAs per SM
     b.fac_grid = 2 * sms;                                     // two factored-operator CTAs per SM
     b.vec_grid = std::max(1, std::min(nc, 8 * sms));
     MG_TRY(dev_alloc_n(&b.probs, b.h_probs.size()));
