@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-design batch section")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
+    ap.add_argument("--no-small", action="store_true", help="skip the 24x12x12 and heat-conduction lines")
+    ap.add_argument("--no-bf16", action="store_true", help="skip the split-BF16 line")
     ap.add_argument("--no-autotune", action="store_true",
                     help="solve the headline problem with the default schedule instead of the autotuned one")
     ap.add_argument("--serve-requests", type=int, default=1000,
@@ -630,7 +632,7 @@ def main():
     # operator (three BF16 products, FP32 accumulation), the same schedule otherwise;
     # inputs resident, CUDA events, L2 flushed between solves; errors against the fixture
     bf16 = None
-    if prec != M.MIXED_BF16X3:
+    if prec != M.MIXED_BF16X3 and not args.no_bf16:
         ob = M.SolveOpts.from_buffer_copy(opts)
         ob.precision = M.MIXED_BF16X3
         step_resident(ob)  # graph capture
@@ -727,7 +729,7 @@ def main():
                  "spmv_us": sp_ms * 1e3, "spmv_GBps": sp_bytes / (sp_ms * 1e-3) / 1e9,
                  "spmv_frac": sp_bytes / (sp_ms * 1e-3) / 1e9 / peak}
 
-    small = bench_small_configs(M, with_cpu=not args.no_cpu)
+    small = None if args.no_small else bench_small_configs(M, with_cpu=not args.no_cpu)
     batch = None if args.no_batch else bench_batch(M)
     serve = None
     if not args.no_serve:

@@ -1505,6 +1505,16 @@ __device__ void bottom_residual(const BottomLevel &L, const float *sK) {
     __syncthreads();
 }
 
+// Direct coarse solve: the coarsest grid of a bottom chain, when it has at most
+// kCoarseDirectMax dofs, is solved exactly with the inverse of its assembled
+// operator (FP64 Gauss-Jordan on the host, stored in FP32) instead of a Chebyshev smoother
+// of degree cdeg: one matrix-vector product instead of cdeg - 1 operator
+// applications, each a CTA-wide barrier round.  The operator is assembled from
+// the level's moduli and K0 like the level operators (Dirichlet dofs: identity
+// rows and zero columns), so the inverse is symmetric and the V-cycle stays a
+// fixed symmetric preconditioner.
+constexpr int kCoarseDirectMax = 144;
+
 struct BottomCheb {
     float inv_theta_s, inv_theta_c;
     float c1s[32], c2s[32], c1c[32], c2c[32];
@@ -1513,7 +1523,8 @@ struct BottomCheb {
 __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
     const MfProblem *__restrict__ probs, const int *__restrict__ heads, const MfState *states,
     const float *__restrict__ E32, const float *__restrict__ dinv_g, const float *__restrict__ mb,
-    float *__restrict__ mx, const double *__restrict__ K0, BottomCheb cc, int sdeg, int cdeg) {
+    float *__restrict__ mx, const double *__restrict__ K0, BottomCheb cc, int sdeg, int cdeg,
+    const int64_t *__restrict__ coarse_off, const float *__restrict__ coarse_inv) {
     pdl_enter();
     extern __shared__ __align__(16) float sbm[];
     const int head = heads[blockIdx.x];
@@ -1593,8 +1604,23 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
         }
         __syncthreads();
     }
-    // coarsest grid of the chain
-    bottom_smooth(Lv[m - 1], sK, Lv[m - 1].b, true, cdeg, cc.inv_theta_c, cc.c1c, cc.c2c);
+    // coarsest grid of the chain: exact solve with the stored inverse, or smoothing
+    {
+        const int64_t off = coarse_off[blockIdx.x];
+        const BottomLevel &L = Lv[m - 1];
+        if (off >= 0) {
+            const int nd = 3 * L.NX * L.NY * L.NZ;
+            const float *Ai = coarse_inv + off;
+            for (int q = threadIdx.x; q < nd; q += kBottomThreads) {
+                float s = 0.0f;
+                for (int r = 0; r < nd; r++) s = fmaf(Ai[q * nd + r], L.b[r], s);
+                L.x[q] = L.dinv[q] == 0.0f ? 0.0f : s;
+            }
+            __syncthreads();
+        } else {
+            bottom_smooth(Lv[m - 1], sK, Lv[m - 1].b, true, cdeg, cc.inv_theta_c, cc.c1c, cc.c2c);
+        }
+    }
     // up: prolong, residual, post-smooth
     for (int l = m - 2; l >= 0; l--) {
         const BottomLevel &F = Lv[l], &C = Lv[l + 1];
@@ -2246,6 +2272,96 @@ void launch_update(MfBatch &b, float *pnew, bool mg) {
         b.chunks, n0, b.probs, b.x, b.r, b.z, pnew, b.q, b.dinv, b.states, b.chunk_part, mg ? 1 : 0);
 }
 
+// coarse inverses of the chains of the listed level-0 problems (all when null):
+// the coarsest level's moduli and Dirichlet mask come back to the host, which
+// assembles the level operator in FP64 (each row over the node's elements in a
+// fixed order, Dirichlet rows and columns eliminated), inverts it by Gauss-Jordan
+// (symmetric positive definite: no pivoting), symmetrises and uploads it in FP32
+int coarse_factor(MfBatch &b, const std::vector<int> *level0) {
+    struct Job {
+        int h, c;
+        std::vector<float> E, D;
+    };
+    std::vector<Job> jobs;
+    for (size_t h = 0; h < b.h_heads.size(); h++) {
+        if (b.h_coarse_off[h] < 0) continue;
+        if (level0 && std::find(level0->begin(), level0->end(), b.h_head_root[h]) == level0->end()) continue;
+        int c = b.h_heads[h];
+        while (b.h_probs[c].coarse >= 0) c = b.h_probs[c].coarse;
+        const MfProblem &C = b.h_probs[c];
+        Job j{(int)h, c, std::vector<float>((size_t)C.pitch_e * C.ny * C.nz), std::vector<float>((size_t)C.n_pad)};
+        jobs.push_back(std::move(j));
+    }
+    if (jobs.empty()) return MG_OK;
+    for (Job &j : jobs) {
+        const MfProblem &C = b.h_probs[j.c];
+        MG_CUDA_TRY(cudaMemcpyAsync(j.E.data(), b.E32 + C.elem_off, j.E.size() * 4, cudaMemcpyDeviceToHost, b.stream));
+        MG_CUDA_TRY(cudaMemcpyAsync(j.D.data(), b.dinv + C.dof_off, j.D.size() * 4, cudaMemcpyDeviceToHost, b.stream));
+    }
+    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
+    std::vector<std::vector<float>> outs(jobs.size());
+    for (size_t t = 0; t < jobs.size(); t++) {
+        const Job &j = jobs[t];
+        const MfProblem &C = b.h_probs[j.c];
+        const int nn = C.NX * C.NY * C.NZ, nd = 3 * nn;
+        std::vector<double> A((size_t)nd * nd, 0.0);
+        std::vector<char> fixed(nd);
+        for (int q = 0; q < nd; q++) {
+            const int n = q / 3, cq = q - 3 * n;
+            const int i = n % C.NX, jj = (n / C.NX) % C.NY, k = n / (C.NX * C.NY);
+            fixed[q] = j.D[((size_t)k * C.NY + jj) * C.pitch + 3 * i + cq] == 0.0f;
+        }
+        for (int q = 0; q < nd; q++) {
+            const int n = q / 3, cq = q - 3 * n;
+            const int i = n % C.NX, jj = (n / C.NX) % C.NY, k = n / (C.NX * C.NY);
+            for (int a = 0; a < 8; a++) {
+                int dx, dy, dz;
+                corner_bits(a, dx, dy, dz);
+                const int ex = i - dx, ey = jj - dy, ez = k - dz;
+                if (ex < 0 || ey < 0 || ez < 0 || ex >= C.nx || ey >= C.ny || ez >= C.nz) continue;
+                const double e = (double)j.E[((size_t)ez * C.ny + ey) * C.pitch_e + ex];
+                for (int bc = 0; bc < 8; bc++) {
+                    int bx, by, bz;
+                    corner_bits(bc, bx, by, bz);
+                    const int m = (ex + bx) + C.NX * ((ey + by) + C.NY * (ez + bz));
+                    for (int cb = 0; cb < 3; cb++)
+                        A[(size_t)q * nd + 3 * m + cb] += e * b.h_K0[(3 * a + cq) * 24 + 3 * bc + cb];
+                }
+            }
+        }
+        for (int q = 0; q < nd; q++)
+            for (int r = 0; r < nd; r++)
+                if (fixed[q] || fixed[r]) A[(size_t)q * nd + r] = (q == r) ? 1.0 : 0.0;
+        for (int k = 0; k < nd; k++) {
+            const double piv = A[(size_t)k * nd + k];
+            if (!(piv > 0.0) || !std::isfinite(piv)) {
+                set_error("coarse-grid operator is not positive definite (pivot %d: %g)", k, piv);
+                return MG_EBREAKDOWN;
+            }
+            const double p = 1.0 / piv;
+            for (int r = 0; r < nd; r++)
+                if (r != k) A[(size_t)k * nd + r] *= p;
+            for (int q = 0; q < nd; q++) {
+                if (q == k) continue;
+                const double f = A[(size_t)q * nd + k];
+                if (f == 0.0) continue;
+                for (int r = 0; r < nd; r++)
+                    if (r != k) A[(size_t)q * nd + r] -= f * A[(size_t)k * nd + r];
+            }
+            for (int q = 0; q < nd; q++) A[(size_t)q * nd + k] = (q == k) ? p : -A[(size_t)q * nd + k] * p;
+        }
+        std::vector<float> &o = outs[t];
+        o.resize((size_t)nd * nd);
+        for (int q = 0; q < nd; q++)
+            for (int r = 0; r < nd; r++)
+                o[(size_t)q * nd + r] = (float)(0.5 * (A[(size_t)q * nd + r] + A[(size_t)r * nd + q]));
+        MG_CUDA_TRY(cudaMemcpyAsync(b.coarse_inv + b.h_coarse_off[j.h], o.data(), o.size() * 4,
+                                    cudaMemcpyHostToDevice, b.stream));
+    }
+    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));  // the host buffers are temporaries
+    return MG_OK;
+}
+
 int compute_diag(MfBatch &b) {
     int64_t maxpad = 1;
     for (const MfProblem &P : b.h_probs) maxpad = std::max(maxpad, P.n_pad);
@@ -2253,7 +2369,7 @@ int compute_diag(MfBatch &b) {
     mf_diag_kernel<<<grid, 256, 0, b.stream>>>(b.probs, nullptr, b.E32, b.node_fix, b.K0, b.dinv);
     MG_CUDA_TRY(cudaGetLastError());
     count_launches(1);
-    return MG_OK;
+    return MG_OK;  // the operator-only paths need no coarse inverse; activation forms it
 }
 
 // Jacobi inverse of the listed level-0 problems and all their coarse levels
@@ -2274,7 +2390,7 @@ int compute_diag_list(MfBatch &b, const std::vector<int> &level0) {
     count_launches(1);
     // the list is a host temporary: finish the copy before it goes away
     MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
-    return MG_OK;
+    return coarse_factor(b, &level0);
 }
 
 }  // namespace
@@ -2470,6 +2586,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     // the bottom kernel's shared memory; larger levels run level by level on the
     // whole GPU (the one-CTA kernel is bound by one SM's shared-memory pipe there)
     b.h_heads.clear();
+    b.h_head_root.clear();
     b.bottom_smem = 0;
     for (int r = 0; r < b.n_fine; r++) {
         for (int q = b.h_probs[r].coarse; q >= 0; q = b.h_probs[q].coarse) {
@@ -2484,11 +2601,29 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
             if (depth <= kBottomMaxLevels && bytes <= kBottomSmemMax &&
                 (int64_t)Hd.NX * Hd.NY * Hd.NZ <= kBottomMaxHeadNodes) {
                 b.h_heads.push_back(q);
+                b.h_head_root.push_back(r);
                 b.bottom_smem = std::max(b.bottom_smem, (int)bytes);
                 for (int t = q; t >= 0; t = b.h_probs[t].coarse) b.h_probs[t].bottom = 1;
                 break;
             }
         }
+    }
+    // direct coarse solves: the chains whose coarsest grid is small enough
+    {
+        int64_t inv_floats = 0;
+        b.h_coarse_off.assign(b.h_heads.size(), -1);
+        for (size_t h = 0; h < b.h_heads.size(); h++) {
+            int c = b.h_heads[h];
+            while (b.h_probs[c].coarse >= 0) c = b.h_probs[c].coarse;
+            const MfProblem &C = b.h_probs[c];
+            const int64_t nd = 3LL * C.NX * C.NY * C.NZ;
+            if (nd <= kCoarseDirectMax) {
+                b.h_coarse_off[h] = inv_floats;
+                inv_floats += nd * nd;
+            }
+        }
+        MG_TRY(dev_alloc_n(&b.coarse_off, std::max<size_t>(1, b.h_coarse_off.size())));
+        MG_TRY(dev_alloc_n(&b.coarse_inv, (size_t)std::max<int64_t>(1, inv_floats)));
     }
     b.apply_grid = std::max(1, std::min(nb, 2 * sms));  // FP64 residual: two CTAs per SM
     b.col_grid = std::max(1, std::min(b.n_cols, kColCtas * sms));  // column CTAs per SM
@@ -2575,6 +2710,10 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     }
     MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
+    b.h_K0.assign(K0, K0 + 576);
+    if (!b.h_coarse_off.empty())
+        MG_CUDA_TRY(cudaMemcpyAsync(b.coarse_off, b.h_coarse_off.data(), b.h_coarse_off.size() * sizeof(int64_t),
+                                    cudaMemcpyHostToDevice, s));
     if (!b.h_heads.empty())
         MG_CUDA_TRY(cudaMemcpyAsync(b.heads, b.h_heads.data(), b.h_heads.size() * sizeof(int),
                                     cudaMemcpyHostToDevice, s));
@@ -2599,7 +2738,8 @@ void mf_batch_free(MfBatch &b) {
     void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.K0, b.mb, b.mx, b.md,
-                    b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles, b.fac_maps};
+                    b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles, b.fac_maps,
+                    b.coarse_off, b.coarse_inv};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
     b = MfBatch();
@@ -2828,7 +2968,8 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
             bc.c1c[k] = cc.c1[k]; bc.c2c[k] = cc.c2[k];
         }
         launch_pdl(mg_bottom_kernel, (unsigned)b.h_heads.size(), kBottomThreads, b.bottom_smem, b.stream, 
-            b.probs, b.heads, b.states, b.E32, b.dinv, b.mb, b.mx, b.K0, bc, sdeg, cdeg);
+            b.probs, b.heads, b.states, b.E32, b.dinv, b.mb, b.mx, b.K0, bc, sdeg, cdeg, b.coarse_off,
+            b.coarse_inv);
         n += 1;
     }
     for (int l = L - 2; l >= 0; l--) {

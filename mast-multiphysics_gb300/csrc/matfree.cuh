@@ -139,6 +139,14 @@ struct MfBatch {
     // bottom V-cycle: the head (first bottom level) of every chain that has one
     std::vector<int> h_heads;
     int *heads = nullptr;
+    // direct solve on a chain's coarsest grid (when it has at most kCoarseDirectMax
+    // dofs): the FP32 inverse of its assembled operator per chain, at coarse_off[head]
+    // (-1: Chebyshev smoothing instead); refreshed whenever the moduli change
+    std::vector<int64_t> h_coarse_off;
+    std::vector<int> h_head_root;   // level-0 problem of each chain
+    int64_t *coarse_off = nullptr;
+    float *coarse_inv = nullptr;
+    std::vector<double> h_K0;       // K0 on the host (576, element dof 3 a + c)
     int bottom_smem = 0;        // dynamic shared memory of the bottom kernel
     // FP64 refinement vectors (padded layout)
     double *u64 = nullptr, *r64 = nullptr, *f64 = nullptr;
