@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
     ap.add_argument("--no-small", action="store_true", help="skip the 24x12x12 and heat-conduction lines")
     ap.add_argument("--no-bf16", action="store_true", help="skip the split-BF16 line")
+    ap.add_argument("--opt", action="append", default=[],
+                    help="mg_solve_opts field=value for the solve (with --no-autotune: a fixed schedule)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="solve the headline problem with the default schedule instead of the autotuned one")
     ap.add_argument("--serve-requests", type=int, default=1000,
@@ -523,6 +525,9 @@ def main():
     pc = M.PC_MULTIGRID if args.preconditioner == "multigrid" else M.PC_JACOBI
     opts = M.default_opts(precision=prec, rtol=1e-8, inner_rtol=1e-3, timeout_s=600.0,
                           preconditioner=pc)
+    for kv in args.opt:
+        k, v = kv.split("=")
+        setattr(opts, k, type(getattr(opts, k))(float(v)) if isinstance(getattr(opts, k), float) else int(v))
     if args.kernel_only:
         kernel_only(args, M, prob, prec, rho)
         prob.close()

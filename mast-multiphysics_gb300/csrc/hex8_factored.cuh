@@ -83,9 +83,72 @@ inline bool hex8_factored_build(const double *K0, FacK<double> &k64, FacK<float>
     return true;
 }
 
+// Double-float number: the unevaluated sum hi + lo of two FP32 values with
+// |lo| <= ulp(hi) / 2, a 48-bit significand carried on the FP32 pipes (GB300's
+// FP64 pipe issues two DFMA per cycle per SM, its FP32 pipes 128 FFMA).  The
+// operations are the classical error-free transformations: Knuth's two-sum for
+// additions and the FMA form of Dekker's two-product for products, each followed
+// by a renormalising fast two-sum.  Explicitly rounded intrinsics keep the
+// compiler from contracting or reassociating them.
+struct dfloat {
+    float hi, lo;
+};
+
+inline dfloat dfloat_of(double x) {
+    dfloat r;
+    r.hi = (float)x;
+    r.lo = (float)(x - (double)r.hi);
+    return r;
+}
+
 #ifdef __CUDACC__
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+
+__device__ __forceinline__ dfloat df_renorm(float s, float e) {
+    dfloat r;
+    r.hi = __fadd_rn(s, e);
+    r.lo = __fsub_rn(e, __fsub_rn(r.hi, s));
+    return r;
+}
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    return df_renorm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) {
+    dfloat nb;
+    nb.hi = -b.hi;
+    nb.lo = -b.lo;
+    return a + nb;
+}
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return df_renorm(p, e);
+}
+__device__ __forceinline__ dfloat &operator+=(dfloat &a, dfloat b) { return a = a + b; }
+__device__ __forceinline__ dfloat &operator*=(dfloat &a, dfloat b) { return a = a * b; }
+__device__ __forceinline__ dfloat fma_t(dfloat a, dfloat b, dfloat c) { return a * b + c; }
+__device__ __forceinline__ dfloat df_from(double x) {
+    dfloat r;
+    r.hi = __double2float_rn(x);
+    r.lo = __double2float_rn(x - (double)r.hi);
+    return r;
+}
+__device__ __forceinline__ double df_to(dfloat a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ dfloat df_zero() {
+    dfloat r;
+    r.hi = 0.0f;
+    r.lo = 0.0f;
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ T zero_t() { return T(0); }
+template <>
+__device__ __forceinline__ dfloat zero_t<dfloat>() { return df_zero(); }
 
 // v[c][b]: component c at lexicographic corner b; on return e * (K0 u_e) in the
 // same layout.  Fixed operation order (deterministic).
@@ -151,7 +214,7 @@ __device__ __forceinline__ void hex8_factored_apply(const FacK<T> &K, T e, T (&v
     // back to the corners: the transpose butterflies, mode 0 is zero
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        yh[c][0] = T(0);
+        yh[c][0] = zero_t<T>();
 #pragma unroll
         for (int m = 1; m < 8; m++) yh[c][m] *= e;
 #pragma unroll

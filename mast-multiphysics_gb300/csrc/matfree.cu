@@ -1776,16 +1776,16 @@ static_assert(kBE % 3 == 0 && kRGroupEl <= kThreads, "one element per thread and
 __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
     const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int n_bricks,
     const double *__restrict__ E64, const uint8_t *__restrict__ node_fix,
-    const double *__restrict__ u64, const double *__restrict__ f64, const FacK<double> K,
+    const double *__restrict__ u64, const double *__restrict__ f64, const FacK<dfloat> K,
     double *__restrict__ r64, MfState *states, double *__restrict__ brick_part, double rtol2,
     int max_ref) {
     pdl_enter();
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ double red_sh[kThreads / 32];
     __shared__ int sh_last;
-    double *su = reinterpret_cast<double *>(smem + kOffU64);
-    double *sE = reinterpret_cast<double *>(smem + kOffE64);
-    double(*sY)[kRGroupEl] = reinterpret_cast<double(*)[kRGroupEl]>(smem + kOffY64);  // [b * 3 + c][element]
+    dfloat *su = reinterpret_cast<dfloat *>(smem + kOffU64);
+    dfloat *sE = reinterpret_cast<dfloat *>(smem + kOffE64);
+    dfloat(*sY)[kRGroupEl] = reinterpret_cast<dfloat(*)[kRGroupEl]>(smem + kOffY64);  // [b * 3 + c][element]
     for (int bi = blockIdx.x; bi < n_bricks; bi += gridDim.x) {
         const MfBrick br = bricks[bi];
         const MfProblem P = probs[br.prob];
@@ -1804,7 +1804,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
                 const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
                 if (!((node_fix[P.node_off + gn] >> c) & 1)) v = u64[dof_index(P, gx, gy, gz, c)];
             }
-            su[i] = v;
+            su[i] = df_from(v);
         }
         for (int l = threadIdx.x; l < (u_zero ? 0 : kNEL); l += kThreads) {
             const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
@@ -1812,28 +1812,28 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
             double e = 0.0;
             if (gx >= 0 && gx < P.nx && gy >= 0 && gy < P.ny && gz >= 0 && gz < P.nz)
                 e = E64[P.elem_off + ((int64_t)gz * P.ny + gy) * P.pitch_e + gx];
-            sE[l] = e;
+            sE[l] = df_from(e);
         }
-        double acc[kRNodesPerThread][3];
+        dfloat acc[kRNodesPerThread][3];
 #pragma unroll
-        for (int k = 0; k < kRNodesPerThread; k++) acc[k][0] = acc[k][1] = acc[k][2] = 0.0;
+        for (int k = 0; k < kRNodesPerThread; k++) acc[k][0] = acc[k][1] = acc[k][2] = df_zero();
         for (int g = 0; g < (u_zero ? 0 : 3); g++) {
             __syncthreads();  // su / sE loaded; the previous group's readers of sY are done
             const int l = threadIdx.x;
             if (l < kRGroupEl) {
                 const int ex = l % kBE, ey = (l / kBE) % kBE, ez = g * kRGroupLayers + l / (kBE * kBE);
-                const double e = sE[ex + kBE * (ey + kBE * ez)];
-                double v[3][8];
+                const dfloat e = sE[ex + kBE * (ey + kBE * ez)];
+                dfloat v[3][8];
 #pragma unroll
                 for (int b = 0; b < 8; b++) {
-                    const double *ub = su + (((ez + (b >> 2)) * kBU + ey + ((b >> 1) & 1)) * kBU + ex + (b & 1)) * 3;
+                    const dfloat *ub = su + (((ez + (b >> 2)) * kBU + ey + ((b >> 1) & 1)) * kBU + ex + (b & 1)) * 3;
                     v[0][b] = ub[0]; v[1][b] = ub[1]; v[2][b] = ub[2];
                 }
-                if (e != 0.0) {
+                if (e.hi != 0.0f) {
                     hex8_factored_apply(K, e, v);
                 } else {
 #pragma unroll
-                    for (int b = 0; b < 8; b++) v[0][b] = v[1][b] = v[2][b] = 0.0;
+                    for (int b = 0; b < 8; b++) v[0][b] = v[1][b] = v[2][b] = df_zero();
                 }
 #pragma unroll
                 for (int b = 0; b < 8; b++) {
@@ -1874,7 +1874,7 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
             for (int c = 0; c < 3; c++) {
                 const int64_t gd = dof_index(P, gx, gy, gz, c);
                 const double fv = f64[gd];
-                double rv = fv - acc[k][c];
+                double rv = fv - df_to(acc[k][c]);
                 if ((fix >> c) & 1) rv = 0.0;
                 r64[gd] = rv;
                 part = fma(rv, rv, part);
@@ -2659,6 +2659,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     double K0[576];
     hex8_box_stiffness(hx, hy, hz, nu, K0);
     if (!hex8_factored_build(K0, b.fac64, b.fac32)) return MG_EINVAL;
+    for (int k = 0; k < kFacN; k++) b.facdf.v[k] = dfloat_of(b.fac64.v[k]);
     for (int k = 0; k < kFacN; k++) b.fac2.v[k] = make_float2(b.fac32.v[k], b.fac32.v[k]);
     // Gershgorin bound of D^-1 A: every assembled row is a positive combination
     // of K0 rows, so max_i sum_j |K0_ij| / K0_ii bounds it on every level
@@ -3001,7 +3002,7 @@ long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
     const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
     const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
     launch_pdl(mf_residual64_kernel, std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s, 
-        b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.fac64, b.r64, b.states,
+        b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.facdf, b.r64, b.states,
         b.brick_part, prm.rtol * prm.rtol, max_ref);
     launch_pdl(mf_inner_init_kernel, vg0, kThreads, 0, s, 
         b.chunks, n0, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.p1, b.dinv, b.states, b.chunk_part,

@@ -117,6 +117,7 @@ struct MfBatch {
     std::vector<int> lvl_fac_lo, lvl_fac_hi;
     FacK<float> fac32{};          // K0 in the per-axis sum/difference basis
     FacK<double> fac64{};
+    FacK<dfloat> facdf{};         // fac64 as double-float pairs (the outer residual)
     FacK2 fac2{};                 // fac32 as (k, k) pairs for the packed FP32x2 kernels
     MfChunkDesc *chunks = nullptr;
     MfState *states = nullptr;
