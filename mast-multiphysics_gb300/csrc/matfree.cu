@@ -2743,6 +2743,7 @@ void mf_batch_free(MfBatch &b) {
                     b.coarse_off, b.coarse_inv};
     for (void *q : ptrs) dev_free(q);
     if (b.states_host) cudaFreeHost(b.states_host);
+    if (b.err_host) cudaFreeHost(b.err_host);
     b = MfBatch();
 }
 
@@ -3136,6 +3137,29 @@ int mf_batch_step(MfBatch &b) {
     MG_CUDA_TRY(cudaGraphLaunch(b.graph, b.stream));
     count_launches(b.graph_launches);
     return read_states(b);  // synchronises
+}
+
+int mf_batch_step_begin(MfBatch &b) {
+    if (!b.graph) {
+        set_error("mf_batch_step before mf_batch_prepare");
+        return MG_EINVAL;
+    }
+    if (!b.err_host) MG_CUDA_TRY(cudaMallocHost(&b.err_host, sizeof(int)));
+    MG_CUDA_TRY(cudaGraphLaunch(b.graph, b.stream));
+    count_launches(b.graph_launches);
+    MG_CUDA_TRY(cudaMemcpyAsync(b.states_host, b.states, b.n_probs * sizeof(MfState), cudaMemcpyDeviceToHost,
+                                b.stream));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.err_host, b.err, sizeof(int), cudaMemcpyDeviceToHost, b.stream));
+    return MG_OK;
+}
+
+int mf_batch_step_end(MfBatch &b) {
+    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
+    if (*b.err_host) {
+        set_error("tensor-core pipeline wait exceeded its bound (error flag %d)", *b.err_host);
+        return MG_ETIMEDOUT;
+    }
+    return MG_OK;
 }
 
 int mf_batch_finish(MfBatch &b, int i) {

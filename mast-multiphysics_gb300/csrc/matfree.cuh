@@ -122,6 +122,7 @@ struct MfBatch {
     MfChunkDesc *chunks = nullptr;
     MfState *states = nullptr;
     MfState *states_host = nullptr;  // pinned
+    int *err_host = nullptr;         // pinned copy of *err (step_begin / step_end)
     CUtensorMap *tmaps = nullptr;    // kMapsPerProblem per problem
     // element / node tables
     float *E32 = nullptr;
@@ -205,6 +206,10 @@ int mf_batch_prepare(MfBatch &b, const MfSolveParams &prm);
 int mf_batch_reset_states(MfBatch &b);
 int mf_batch_activate(MfBatch &b, const std::vector<int> &level0, bool warm_start);
 int mf_batch_step(MfBatch &b);
+// the same in two halves, so that several batches can run on the GPU at once:
+// begin launches the step graph and the state copy, end waits for them
+int mf_batch_step_begin(MfBatch &b);
+int mf_batch_step_end(MfBatch &b);
 int mf_batch_finish(MfBatch &b, int i);
 // active (nullable, per level-0 problem): 0 = leave that problem's dc untouched
 int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded_dev,

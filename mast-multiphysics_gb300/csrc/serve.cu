@@ -1,20 +1,23 @@
 // serve.cu -- the request loop (mg_server_*): continuous batching of SIMP design
 // evaluations on one GPU.
 //
-// A worker thread owns the resident batch (one mg_batch holding every resident
-// chain's tables, solutions and multigrid hierarchy) and drives the
-// multi-problem solver one graph launch (a few solver steps) at a time.
+// A worker thread owns the resident chains, held in a few shards (each one
+// mg_batch with its chains' tables, solutions and multigrid hierarchy, on its
+// own stream), and drives the multi-problem solver one graph launch (a few
+// solver steps) at a time, the shards' launches running on the GPU together.
 // Between launches it
 //   * admits the requests that arrived: a request of a resident, idle chain gets
 //     its densities and loads written and its load cases activated at the FP64
 //     residual, warm-started from the chain's last solution, so it joins the
 //     problems already in flight;
+//   * admits new chains without stopping the others: when they fit under the
+//     device-memory cap they get a shard of their own, or join a shard none of
+//     whose chains is on the GPU when the shard count is at its limit;
 //   * posts the requests whose load cases have all finished (compliance and
 //     dC/drho written into the caller's buffers);
-//   * when a request names a chain that is not resident, stops admitting, lets
-//     the in-flight work finish and rebuilds the resident batch with the new
-//     chains (keeping every retained chain's solutions), evicting least
-//     recently used idle chains when the device-memory cap requires it.
+//   * only when the cap requires evictions (least recently used idle chains
+//     first) does it let the in-flight work finish and rebuild one shard over
+//     the retained and the new chains (keeping every retained chain's solutions).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -66,7 +69,8 @@ struct Request {
 struct Chain {
     int id = 0;
     int nx = 0, ny = 0, nz = 0, n_cases = 0;
-    int design = -1;                 // design index in the resident batch (-1: not resident)
+    int shard = -1;                  // resident shard (-1: not resident)
+    int design = -1;                 // design index in that shard's batch
     bool rejected = false;           // does not fit the cap even alone
     bool has_solution = false;       // warm start available in the resident batch
     std::vector<int32_t> span;       // loads currently written into the batch
@@ -117,8 +121,7 @@ struct mg_server {
     std::string worker_error;
     // worker-only state
     std::map<int, Chain> chains;
-    mg_batch *batch = nullptr;
-    std::vector<int> design_chain;       // resident design -> chain id
+    std::vector<mg_batch *> shards;      // resident batches; the chains record theirs
 };
 
 namespace mg {
@@ -144,17 +147,31 @@ void post(mg_server *s, const Request &q, int status, int its, int refs, double 
     s->cv_out.notify_all();
 }
 
-// rebuild the resident batch over `keep` (resident chains that stay) plus
-// `add` (new chains); retained chains keep their solutions
-int rebuild(mg_server *s, const std::vector<int> &keep, const std::vector<int> &add) {
-    TRACE("rebuild: keep %zu add %zu", keep.size(), add.size());
-    mg_batch *old = s->batch;
+constexpr int kMaxShards = 6;
+
+void update_residency(mg_server *s) {
+    int64_t bytes = 0;
+    int n = 0;
+    for (mg_batch *b : s->shards) bytes += b->device_bytes;
+    for (auto &kv : s->chains) n += kv.second.shard >= 0 ? 1 : 0;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->resident_bytes = bytes;
+    s->peak_resident = std::max(s->peak_resident, bytes);
+    s->resident_chains = n;
+}
+
+// A new batch over the chains `order` (retained chains keep their solutions, copied
+// from their current shards); the chains are pointed at it as shard `slot`, and the
+// shards they came from are left to the caller.
+int build_shard(mg_server *s, const std::vector<int> &order, int slot, mg_batch **out) {
+    *out = nullptr;
     // stash the retained solutions (u of every load case) in one device buffer
     std::vector<std::pair<int, int64_t>> stash;  // (chain, offset)
     int64_t total = 0;
-    for (int id : keep) {
+    for (int id : order) {
         Chain &c = s->chains[id];
-        if (!c.has_solution) continue;
+        if (!c.has_solution || c.shard < 0) continue;
+        mg_batch *old = s->shards[c.shard];
         stash.push_back({id, total});
         for (int k = 0; k < c.n_cases; k++) total += old->mf.h_probs[old->first[c.design] + k].n_pad;
     }
@@ -163,6 +180,7 @@ int rebuild(mg_server *s, const std::vector<int> &keep, const std::vector<int> &
         MG_TRY(dev_alloc_n(&d_stash, (size_t)total));
         for (auto &st : stash) {
             Chain &c = s->chains[st.first];
+            mg_batch *old = s->shards[c.shard];
             int64_t o = st.second;
             for (int k = 0; k < c.n_cases; k++) {
                 const MfProblem &P = old->mf.h_probs[old->first[c.design] + k];
@@ -170,19 +188,10 @@ int rebuild(mg_server *s, const std::vector<int> &keep, const std::vector<int> &
                                 old->stream);
                 o += P.n_pad;
             }
+            cudaStreamSynchronize(old->stream);
         }
-        cudaStreamSynchronize(old->stream);
     }
-    if (old) {
-        mg_batch_destroy(old);
-        s->batch = nullptr;
-    }
-    for (auto &kv : s->chains) kv.second.design = -1;
-    // new batch: retained chains first, then the new ones
-    std::vector<int> order = keep;
-    order.insert(order.end(), add.begin(), add.end());
     std::vector<mg_batch_problem> des(order.size());
-    std::vector<std::vector<double>> rhos(order.size());
     for (size_t i = 0; i < order.size(); i++) {
         Chain &c = s->chains[order[i]];
         // a new chain's first request provides its densities and loads
@@ -196,38 +205,113 @@ int rebuild(mg_server *s, const std::vector<int> &keep, const std::vector<int> &
         des[i].rho = c.rho.data();
         des[i].span = c.span.data();
     }
-    int rc = MG_OK;
     mg_batch *nb = nullptr;
-    if (!order.empty()) rc = mg_batch_create(des.data(), (int32_t)des.size(), &s->mat, &nb);
+    int rc = mg_batch_create(des.data(), (int32_t)des.size(), &s->mat, &nb);
     if (rc != MG_OK) {
         dev_free(d_stash);
         return rc;
     }
-    s->batch = nb;
-    s->design_chain = order;
-    for (size_t i = 0; i < order.size(); i++) s->chains[order[i]].design = (int)i;
     for (auto &st : stash) {
         Chain &c = s->chains[st.first];
+        const int d = (int)(std::find(order.begin(), order.end(), st.first) - order.begin());
         int64_t o = st.second;
         for (int k = 0; k < c.n_cases; k++) {
-            const MfProblem &P = nb->mf.h_probs[nb->first[c.design] + k];
+            const MfProblem &P = nb->mf.h_probs[nb->first[d] + k];
             cudaMemcpyAsync(nb->mf.u64 + P.dof_off, d_stash + o, P.n_pad * 8, cudaMemcpyDeviceToDevice,
                             nb->stream);
             o += P.n_pad;
         }
     }
-    if (nb) cudaStreamSynchronize(nb->stream);
+    cudaStreamSynchronize(nb->stream);
     dev_free(d_stash);
-    if (nb) MG_TRY(mf_batch_reset_states(nb->mf));
-    if (nb) MG_TRY(mf_batch_prepare(nb->mf, params_from(s->opts.solve)));
-    int64_t bytes = 0;
-    for (int id : order) bytes += s->chains[id].bytes;
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->rebuilds++;
-    s->resident_bytes = nb ? nb->device_bytes : 0;
-    s->peak_resident = std::max(s->peak_resident, s->resident_bytes);
-    s->resident_chains = (int)order.size();
-    (void)bytes;
+    rc = mf_batch_reset_states(nb->mf);
+    if (rc == MG_OK) rc = mf_batch_prepare(nb->mf, params_from(s->opts.solve));
+    if (rc != MG_OK) {
+        mg_batch_destroy(nb);
+        return rc;
+    }
+    for (size_t i = 0; i < order.size(); i++) {
+        Chain &c = s->chains[order[i]];
+        c.shard = slot;
+        c.design = (int)i;
+    }
+    *out = nb;
+    return MG_OK;
+}
+
+// every resident chain in `keep` plus the new chains `add` in one shard (the
+// in-flight work has finished); the others are evicted
+int rebuild_all(mg_server *s, const std::vector<int> &keep, const std::vector<int> &add) {
+    TRACE("rebuild all: keep %zu add %zu", keep.size(), add.size());
+    std::vector<int> order = keep;
+    order.insert(order.end(), add.begin(), add.end());
+    mg_batch *nb = nullptr;
+    if (!order.empty()) MG_TRY(build_shard(s, order, 0, &nb));
+    for (mg_batch *b : s->shards) mg_batch_destroy(b);
+    s->shards.clear();
+    for (auto &kv : s->chains)
+        if (std::find(order.begin(), order.end(), kv.first) == order.end()) {
+            kv.second.shard = -1;
+            kv.second.design = -1;
+        }
+    if (nb) s->shards.push_back(nb);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->rebuilds++;  // every shard stopped for it
+    }
+    update_residency(s);
+    return MG_OK;
+}
+
+// new chains that fit under the cap, without stopping the shards at work: a shard
+// of their own, or, at the shard limit, a rebuild of a shard none of whose chains
+// is on the GPU together with them; false when they have to wait
+int admit_new(mg_server *s, const std::vector<int> &add, bool *admitted) {
+    *admitted = false;
+    if ((int)s->shards.size() < kMaxShards) {
+        mg_batch *nb = nullptr;
+        MG_TRY(build_shard(s, add, (int)s->shards.size(), &nb));
+        s->shards.push_back(nb);
+        TRACE("new shard %zu: %zu chains", s->shards.size() - 1, add.size());
+        *admitted = true;
+        update_residency(s);
+        return MG_OK;
+    }
+    // the idle shard with the fewest chains
+    int best = -1;
+    size_t best_n = 0;
+    for (int i = 0; i < (int)s->shards.size(); i++) {
+        bool idle = true;
+        size_t n = 0;
+        for (auto &kv : s->chains)
+            if (kv.second.shard == i) {
+                n++;
+                idle &= !kv.second.inflight;
+            }
+        if (idle && (best < 0 || n < best_n)) {
+            best = i;
+            best_n = n;
+        }
+    }
+    if (best < 0) return MG_OK;  // every shard has work on the GPU: wait
+    std::vector<int> order;
+    for (auto &kv : s->chains)
+        if (kv.second.shard == best) order.push_back(kv.first);
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        return s->chains[a].design < s->chains[b].design;
+    });
+    order.insert(order.end(), add.begin(), add.end());
+    mg_batch *nb = nullptr;
+    MG_TRY(build_shard(s, order, best, &nb));
+    mg_batch_destroy(s->shards[best]);
+    s->shards[best] = nb;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->rebuilds++;  // one idle shard rebuilt; the others kept working
+    }
+    TRACE("shard %d rebuilt with %zu new chains", best, add.size());
+    *admitted = true;
+    update_residency(s);
     return MG_OK;
 }
 
@@ -247,7 +331,7 @@ AdmissionPlan plan_admission(mg_server *s) {
     AdmissionPlan pl;
     int64_t used = 0;
     for (auto &kv : s->chains)
-        if (kv.second.design >= 0) {
+        if (kv.second.shard >= 0) {
             pl.keep.push_back(kv.first);
             used += kv.second.bytes;
         }
@@ -255,7 +339,7 @@ AdmissionPlan plan_admission(mg_server *s) {
     std::vector<std::pair<double, int>> want;
     for (auto &kv : s->chains) {
         const Chain &c = kv.second;
-        if (c.design < 0 && !c.rejected && !c.queue.empty()) want.push_back({oldest(c), kv.first});
+        if (c.shard < 0 && !c.rejected && !c.queue.empty()) want.push_back({oldest(c), kv.first});
     }
     std::sort(want.begin(), want.end());
     for (auto &w : want) {
@@ -300,7 +384,7 @@ void reject_oversized(mg_server *s) {
     const int64_t cap = s->opts.hbm_cap_bytes > 0 ? s->opts.hbm_cap_bytes : (int64_t)150 << 30;
     for (auto &kv : s->chains) {
         Chain &c = kv.second;
-        if (c.design < 0 && c.bytes > cap) c.rejected = true;
+        if (c.shard < 0 && c.bytes > cap) c.rejected = true;
         while (c.rejected && !c.queue.empty()) {
             post(s, *c.queue.front(), MG_ENOMEM, 0, 0, 0.0, 0);
             c.queue.pop_front();
@@ -316,12 +400,12 @@ int apply_admission(mg_server *s, const AdmissionPlan &pl) {
         std::lock_guard<std::mutex> lk(s->mu);
         s->evictions++;
     }
-    return rebuild(s, pl.keep, pl.add);
+    return rebuild_all(s, pl.keep, pl.add);
 }
 
 // start the head request of an idle resident chain
 int start_request(mg_server *s, Chain &c) {
-    mg_batch *b = s->batch;
+    mg_batch *b = s->shards[c.shard];
     std::unique_ptr<Request> q = std::move(c.queue.front());
     c.queue.pop_front();
     q->admit = now_s();
@@ -351,9 +435,8 @@ int start_request(mg_server *s, Chain &c) {
     return MG_OK;
 }
 
-// post the finished requests
-int finish_requests(mg_server *s, const std::vector<int> &done_chains) {
-    mg_batch *b = s->batch;
+// post the finished requests (chains of shard b)
+int finish_requests(mg_server *s, mg_batch *b, const std::vector<int> &done_chains) {
     std::vector<uint8_t> active(b->n_probs, 0);
     for (int id : done_chains) {
         Chain &c = s->chains[id];
@@ -440,24 +523,33 @@ void worker_main(mg_server *s) {
         }
         int rc = MG_OK;
         reject_oversized(s);
-        // a rebuild is due when some waiting chain can be admitted; admissions of
-        // resident chains' requests pause until the in-flight work has finished
+        // new chains: admitted at once when they fit under the cap (a shard of their
+        // own); when the cap requires evictions, admissions of resident chains pause
+        // until the in-flight work has finished and one shard is rebuilt
         bool waiting = false;
         for (auto &kv : s->chains)
-            waiting |= (kv.second.design < 0 && !kv.second.rejected && !kv.second.queue.empty());
+            waiting |= (kv.second.shard < 0 && !kv.second.rejected && !kv.second.queue.empty());
         AdmissionPlan plan;
         if (waiting) plan = plan_admission(s);
-        const bool need_rebuild = !plan.add.empty();
         int inflight = 0;
         for (auto &kv : s->chains) inflight += kv.second.inflight ? 1 : 0;
-        if (need_rebuild && inflight == 0) rc = apply_admission(s, plan);
+        bool need_rebuild = false;
+        if (!plan.add.empty()) {
+            if (plan.evict.empty()) {
+                bool admitted = false;
+                rc = admit_new(s, plan.add, &admitted);
+            } else {
+                need_rebuild = true;
+                if (inflight == 0) rc = apply_admission(s, plan);
+            }
+        }
         // admit requests of resident idle chains unless a rebuild is waiting
-        if (rc == MG_OK && !need_rebuild && s->batch) {
+        if (rc == MG_OK && !need_rebuild && !s->shards.empty()) {
             const int cap = s->opts.max_inflight > 0 ? s->opts.max_inflight : 1 << 30;
             std::vector<std::pair<double, int>> ready;
             for (auto &kv : s->chains) {
                 Chain &c = kv.second;
-                if (c.design >= 0 && !c.inflight && !c.queue.empty()) ready.push_back({c.queue.front()->arrival, kv.first});
+                if (c.shard >= 0 && !c.inflight && !c.queue.empty()) ready.push_back({c.queue.front()->arrival, kv.first});
             }
             std::sort(ready.begin(), ready.end());
             for (auto &r : ready) {
@@ -475,7 +567,7 @@ void worker_main(mg_server *s) {
             for (auto &kv : s->chains) {
                 Chain &c = kv.second;
                 if (!c.inflight || now - c.inflight->admit <= limit) continue;
-                mg_batch *b = s->batch;
+                mg_batch *b = s->shards[c.shard];
                 for (int k = 0; k < c.n_cases; k++) {
                     const int i = b->first[c.design] + k;
                     MfState &h = b->mf.states_host[i];
@@ -493,29 +585,31 @@ void worker_main(mg_server *s) {
             }
         }
         if (rc == MG_OK && inflight > 0) {
-            rc = mf_batch_step(s->batch->mf);
-            if (trace_on()) {
-                static long long n_steps = 0;
-                if (++n_steps % 50 == 0)
-                    for (auto &kv : s->chains)
-                        if (kv.second.inflight) {
-                            const MfState &h = s->batch->mf.states_host[s->batch->first[kv.second.design]];
-                            TRACE("step %lld chain %d phase %d done %d iter %d refine %d rr %.3e rr64 %.3e", n_steps,
-                                  kv.first, h.phase, h.done, h.iter, h.refine, h.rr, h.rr64);
-                        }
-            }
-            std::vector<int> done;
-            if (rc == MG_OK)
+            // one graph launch on every shard with work, all on the GPU at once
+            std::vector<int> busy(s->shards.size(), 0);
+            for (auto &kv : s->chains)
+                if (kv.second.inflight) busy[kv.second.shard] = 1;
+            for (size_t i = 0; i < s->shards.size() && rc == MG_OK; i++)
+                if (busy[i]) rc = mf_batch_step_begin(s->shards[i]->mf);
+            for (size_t i = 0; i < s->shards.size(); i++)
+                if (busy[i]) {
+                    const int r2 = mf_batch_step_end(s->shards[i]->mf);
+                    if (rc == MG_OK) rc = r2;
+                }
+            for (size_t i = 0; i < s->shards.size() && rc == MG_OK; i++) {
+                if (!busy[i]) continue;
+                mg_batch *b = s->shards[i];
+                std::vector<int> done;
                 for (auto &kv : s->chains) {
                     Chain &c = kv.second;
-                    if (!c.inflight) continue;
+                    if (!c.inflight || c.shard != (int)i) continue;
                     bool fin = true;
-                    for (int k = 0; k < c.n_cases; k++)
-                        fin &= s->batch->mf.states_host[s->batch->first[c.design] + k].phase == kPhaseFin;
+                    for (int k = 0; k < c.n_cases; k++) fin &= b->mf.states_host[b->first[c.design] + k].phase == kPhaseFin;
                     if (fin) done.push_back(kv.first);
                 }
-            if (rc == MG_OK && !done.empty()) rc = finish_requests(s, done);
-            inflight -= (int)done.size();
+                if (!done.empty()) rc = finish_requests(s, b, done);
+                inflight -= (int)done.size();
+            }
         }
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -526,11 +620,10 @@ void worker_main(mg_server *s) {
             TRACE("error %d: %s", rc, mg_last_error());
             // answer everything with the error and start again from no resident chain
             fail_all(rc);
-            if (s->batch) {
-                mg_batch_destroy(s->batch);
-                s->batch = nullptr;
-            }
+            for (mg_batch *b : s->shards) mg_batch_destroy(b);
+            s->shards.clear();
             for (auto &kv : s->chains) {
+                kv.second.shard = -1;
                 kv.second.design = -1;
                 kv.second.has_solution = false;
                 kv.second.span.clear();
@@ -552,10 +645,8 @@ void worker_main(mg_server *s) {
             if (s->inbox.empty() && !s->stop) s->cv_in.wait_for(lk, std::chrono::milliseconds(1));
         }
     }
-    if (s->batch) {
-        mg_batch_destroy(s->batch);
-        s->batch = nullptr;
-    }
+    for (mg_batch *b : s->shards) mg_batch_destroy(b);
+    s->shards.clear();
 }
 
 double percentile(std::vector<double> v, double p) {
