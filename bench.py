@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop section")
     ap.add_argument("--no-small", action="store_true", help="skip the 24x12x12 and heat-conduction lines")
     ap.add_argument("--no-bf16", action="store_true", help="skip the split-BF16 line")
+    ap.add_argument("--ks-stress", action="store_true",
+                    help="only time the KS-aggregated von Mises stress output (value; value and "
+                         "adjoint density sensitivity) on a 64x32x32 cantilever and print one JSON line")
     ap.add_argument("--opt", action="append", default=[],
                     help="mg_solve_opts field=value for the solve (with --no-autotune: a fixed schedule)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -123,6 +126,38 @@ def nonlinear_assembly(args, M):
         "fp64_frac_of_nominal": flops / (ms * 1e-3) / 1e9 / 1250.0,
         "GBps": bytes_ / (ms * 1e-3) / 1e9, "hbm_frac": bytes_ / (ms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6800.0),
         "reps": reps, "dtype": "f64"}))
+    prob.close()
+
+
+def ks_stress_timing(args, M):
+    """Time mg_ks_stress on a 64x32x32 cantilever (65,536 elements) at its solved state:
+    the value pass (Gauss-point stresses of every element, the KS and max reductions) and
+    the value with the total density sensitivity (value pass, gradient scatter, adjoint
+    CG solve of the plain FP64 form, element sensitivities).  Wall-clock per call through
+    the ABI (each call synchronises)."""
+    nx, ny, nz = 64, 32, 32
+    prob = M.simp_cantilever(nx, ny, nz)
+    rho = np.random.default_rng(SEED).uniform(0.3, 1.0, nx * ny * nz)
+    prob.set_design(rho)
+    u, rep = prob.solve(M.default_opts(rtol=1e-10))
+    for _ in range(max(1, args.warmup)):
+        prob.ks_stress(8.0, 1.0, 3.0, want_sens=True)
+    reps = max(1, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        q, vmax, _ = prob.ks_stress(8.0, 1.0, 3.0, want_sens=False)
+    t_val = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        prob.ks_stress(8.0, 1.0, 3.0, want_sens=True)
+    t_sens = (time.perf_counter() - t0) / reps
+    n_el = nx * ny * nz
+    print(json.dumps({
+        "metric": "ks_stress_output", "workload": "KS-aggregated von Mises stress, p = 8, SIMP "
+        "cantilever 64x32x32 (%d elements), FP64" % n_el,
+        "ms_per_value": t_val * 1e3, "ms_per_value_and_sensitivity": t_sens * 1e3,
+        "elements_per_s_value": n_el / t_val, "adjoint_cg_iterations_of_the_solve": rep.krylov_iterations,
+        "ks": q, "max_von_mises": vmax, "reps": reps, "dtype": "f64"}))
     prob.close()
 
 
@@ -535,6 +570,10 @@ def main():
     if args.nonlinear_assembly:
         prob.close()
         nonlinear_assembly(args, M)
+        return
+    if args.ks_stress:
+        prob.close()
+        ks_stress_timing(args, M)
         return
     def step_resident(o=None):
         prob.set_design_device(d_rho.data_ptr())

@@ -375,16 +375,19 @@ int mg_batch_autotune(mg_batch *b, mg_solve_opts *opts, int32_t max_trials, doub
 
 /* ---- request loop (continuous batching of design evaluations) ----
    No counterpart in the reference (its design loop calls `evaluate` serially,
-   examples/structural/example_6/example_6.cpp:450-655).  A server owns one GPU
-   stream and a worker thread.  Requests belong to design chains: a chain has one
+   examples/structural/example_6/example_6.cpp:450-655).  A server owns a worker
+   thread and the resident chains, held in a few shards (batches with a stream
+   each, stepped on the GPU together).  Requests belong to design chains: a chain has one
    grid and one number of load cases; its mesh tables and last solutions stay
    resident in device memory and every request of the chain warm-starts from the
    chain's previous solution.  Requests that arrive while others are on the GPU
    join the running multi-problem solve at the next step boundary (a few CG
    iterations), so work of different requests overlaps in the same kernels.  New
-   chains are admitted against the device-memory cap (least recently used idle
-   chains are evicted when needed); a chain that cannot fit alone is rejected
-   (MG_ENOMEM in its completions). */
+   chains are admitted against the device-memory cap without stopping the
+   resident ones (a shard of their own, or an idle shard rebuilt with them); only
+   when the cap requires evictions (least recently used idle chains first) does
+   the worker let the in-flight work finish and rebuild; a chain that cannot fit
+   alone is rejected (MG_ENOMEM in its completions). */
 typedef struct mg_server mg_server;
 
 typedef struct mg_request {
