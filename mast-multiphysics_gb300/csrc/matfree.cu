@@ -1557,6 +1557,14 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
         pl[m] = q;
         m++;
     }
+    // the coarsest grid's inverse (direct solve), fetched with the level tables
+    const int64_t inv_off = coarse_off[blockIdx.x];
+    float *sInv = p;
+    if (inv_off >= 0) {
+        const BottomLevel &Lc = Lv[m - 1];
+        const int ndc = 3 * Lc.NX * Lc.NY * Lc.NZ;
+        for (int i = threadIdx.x; i < ndc * ndc; i += kBottomThreads) sInv[i] = coarse_inv[inv_off + i];
+    }
     // load E, D^-1 (and the rhs of the head) from the padded global layout
     for (int l = 0; l < m; l++) {
         const MfProblem P = probs[pl[l]];
@@ -1606,15 +1614,18 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
     }
     // coarsest grid of the chain: exact solve with the stored inverse, or smoothing
     {
-        const int64_t off = coarse_off[blockIdx.x];
         const BottomLevel &L = Lv[m - 1];
-        if (off >= 0) {
-            const int nd = 3 * L.NX * L.NY * L.NZ;
-            const float *Ai = coarse_inv + off;
-            for (int q = threadIdx.x; q < nd; q += kBottomThreads) {
-                float s = 0.0f;
-                for (int r = 0; r < nd; r++) s = fmaf(Ai[q * nd + r], L.b[r], s);
-                L.x[q] = L.dinv[q] == 0.0f ? 0.0f : s;
+        if (inv_off >= 0) {
+            // four lanes per row, partial sums met by two shuffles (fixed order)
+            const int nd = 3 * L.NX * L.NY * L.NZ, part = threadIdx.x & 3;
+            for (int q0 = 0; q0 < nd; q0 += kBottomThreads / 4) {
+                const int q = q0 + (threadIdx.x >> 2);
+                float sacc = 0.0f;
+                if (q < nd)
+                    for (int r = part; r < nd; r += 4) sacc = fmaf(sInv[q * nd + r], L.b[r], sacc);
+                sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
+                sacc += __shfl_xor_sync(0xffffffffu, sacc, 2);
+                if (q < nd && part == 0) L.x[q] = L.dinv[q] == 0.0f ? 0.0f : sacc;
             }
             __syncthreads();
         } else {
@@ -2608,18 +2619,25 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
             }
         }
     }
-    // direct coarse solves: the chains whose coarsest grid is small enough
+    // direct coarse solves: the chains whose coarsest grid is small enough and
+    // whose inverse fits the bottom kernel's shared memory beside the levels
     {
         int64_t inv_floats = 0;
         b.h_coarse_off.assign(b.h_heads.size(), -1);
         for (size_t h = 0; h < b.h_heads.size(); h++) {
+            int64_t floats = 576 + 800;
             int c = b.h_heads[h];
-            while (b.h_probs[c].coarse >= 0) c = b.h_probs[c].coarse;
+            for (int t = c; t >= 0; t = b.h_probs[t].coarse) {
+                const MfProblem &T = b.h_probs[t];
+                floats += 18LL * T.NX * T.NY * T.NZ + (int64_t)T.nx * T.ny * T.nz;
+                c = t;
+            }
             const MfProblem &C = b.h_probs[c];
             const int64_t nd = 3LL * C.NX * C.NY * C.NZ;
-            if (nd <= kCoarseDirectMax) {
+            if (nd <= kCoarseDirectMax && (floats + nd * nd) * 4 <= kBottomSmemMax) {
                 b.h_coarse_off[h] = inv_floats;
                 inv_floats += nd * nd;
+                b.bottom_smem = std::max(b.bottom_smem, (int)((floats + nd * nd) * 4));
             }
         }
         MG_TRY(dev_alloc_n(&b.coarse_off, std::max<size_t>(1, b.h_coarse_off.size())));
