@@ -1507,9 +1507,9 @@ __device__ void bottom_residual(const BottomLevel &L, const float *sK) {
 
 // Direct coarse solve: the coarsest grid of a bottom chain, when it has at most
 // kCoarseDirectMax dofs, is solved exactly with the inverse of its assembled
-// operator (FP64 Gauss-Jordan on the host, stored in FP32) instead of a Chebyshev smoother
-// of degree cdeg: one matrix-vector product instead of cdeg - 1 operator
-// applications, each a CTA-wide barrier round.  The operator is assembled from
+// operator (FP32, formed on the device by mg_coarse_inverse_kernel) instead of a
+// Chebyshev smoother of degree cdeg: one matrix-vector product instead of cdeg - 1
+// operator applications, each a CTA-wide barrier round.  The operator is assembled from
 // the level's moduli and K0 like the level operators (Dirichlet dofs: identity
 // rows and zero columns), so the inverse is symmetric and the V-cycle stays a
 // fixed symmetric preconditioner.
@@ -1524,7 +1524,8 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
     const MfProblem *__restrict__ probs, const int *__restrict__ heads, const MfState *states,
     const float *__restrict__ E32, const float *__restrict__ dinv_g, const float *__restrict__ mb,
     float *__restrict__ mx, const double *__restrict__ K0, BottomCheb cc, int sdeg, int cdeg,
-    const int64_t *__restrict__ coarse_off, const float *__restrict__ coarse_inv) {
+    const int64_t *__restrict__ coarse_off, const float *__restrict__ coarse_inv,
+    const int *__restrict__ coarse_ok) {
     pdl_enter();
     extern __shared__ __align__(16) float sbm[];
     const int head = heads[blockIdx.x];
@@ -1558,7 +1559,7 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
         m++;
     }
     // the coarsest grid's inverse (direct solve), fetched with the level tables
-    const int64_t inv_off = coarse_off[blockIdx.x];
+    const int64_t inv_off = coarse_ok[blockIdx.x] ? coarse_off[blockIdx.x] : -1;
     float *sInv = p;
     if (inv_off >= 0) {
         const BottomLevel &Lc = Lv[m - 1];
@@ -1664,6 +1665,151 @@ __global__ void __launch_bounds__(kBottomThreads, 1) mg_bottom_kernel(
             mx[dof_index(P, i, j, k, c)] = Lv[0].x[q];
         }
     }
+}
+
+// FP32 inverse of a chain's coarsest-grid operator (the direct coarse solve), one
+// CTA per chain, formed whenever the chain's moduli change.  The operator is
+// assembled from K0 and the level's moduli (one thread per row, the node's
+// elements in a fixed order; Dirichlet rows and columns replaced by the identity;
+// the upper triangle taken for both halves), padded to kCoarseDirectMax with the
+// identity and inverted in place by the symmetric sweep operator (Goodnight,
+// "A tutorial on the SWEEP operator", 1979): sweeping pivot k maps
+// a_ij -> a_ij - a_ik a_kj / a_kk (i, j != k), a_ik -> a_ik / a_kk and
+// a_kk -> -1 / a_kk; sweeping every pivot leaves -A^-1.  Each thread keeps a 6 x 6
+// tile in registers and forms a_ik a_kj as one product, so the tiles stay bitwise
+// symmetric and the stored inverse is exactly symmetric (the V-cycle stays a
+// fixed symmetric preconditioner).  No pivoting: the pivots of a symmetric
+// positive definite matrix are positive.  A pivot that is not (a singular or
+// indefinite coarse operator) clears coarse_ok and the bottom kernel smooths that
+// chain's coarsest grid instead.
+constexpr int kCoarseTile = 6;
+constexpr int kCoarseTiles = kCoarseDirectMax / kCoarseTile;
+constexpr int kCoarseInvThreads = kCoarseTiles * kCoarseTiles;
+constexpr int kCoarseMaxElems = 64;  // nodes <= kCoarseDirectMax / 3 = 48, so elements < 48
+constexpr int kCoarseInvSmem =
+    (kCoarseDirectMax * kCoarseDirectMax + 576 + kCoarseMaxElems + 3 * kCoarseDirectMax) * 4;
+static_assert(kCoarseDirectMax % kCoarseTile == 0, "the sweep tiles cover the padded operator");
+
+__global__ void __launch_bounds__(kCoarseInvThreads, 1) mg_coarse_inverse_kernel(
+    const MfProblem *__restrict__ probs, const int *__restrict__ heads, const int *__restrict__ list,
+    const float *__restrict__ E32, const float *__restrict__ dinv, const double *__restrict__ K0,
+    const int64_t *__restrict__ coarse_off, float *__restrict__ coarse_inv, int *__restrict__ coarse_ok) {
+    constexpr int NP = kCoarseDirectMax, T = kCoarseTile;
+    extern __shared__ __align__(16) float sci[];
+    float *sA = sci;              // NP x NP assembled operator
+    float *sK = sA + NP * NP;     // K0 (576)
+    float *sE = sK + 576;         // the level's moduli
+    float *sv = sE + kCoarseMaxElems;  // pivot rows, double-buffered (2 x NP)
+    int *sfix = reinterpret_cast<int *>(sv + 2 * NP);
+    const int h = list[blockIdx.x];
+    const int64_t off = coarse_off[h];
+    if (off < 0) return;
+    int c = heads[h];
+    while (probs[c].coarse >= 0) c = probs[c].coarse;
+    const MfProblem C = probs[c];
+    const int nd = 3 * C.NX * C.NY * C.NZ, ne = C.nx * C.ny * C.nz;
+    if (nd > NP || ne > kCoarseMaxElems) {  // not a direct chain (the host never lists one)
+        if (threadIdx.x == 0) coarse_ok[h] = 0;
+        return;
+    }
+    const int tid = threadIdx.x;
+    for (int i = tid; i < 576; i += kCoarseInvThreads) sK[i] = (float)K0[i];
+    for (int e = tid; e < ne; e += kCoarseInvThreads) {
+        const int ex = e % C.nx, ey = (e / C.nx) % C.ny, ez = e / (C.nx * C.ny);
+        sE[e] = E32[C.elem_off + ((int64_t)ez * C.ny + ey) * C.pitch_e + ex];
+    }
+    for (int q = tid; q < nd; q += kCoarseInvThreads) {
+        const int n = q / 3, cq = q - 3 * n;
+        const int i = n % C.NX, j = (n / C.NX) % C.NY, k = n / (C.NX * C.NY);
+        sfix[q] = dinv[dof_index(C, i, j, k, cq)] == 0.0f;
+    }
+    __syncthreads();
+    for (int q = tid; q < nd; q += kCoarseInvThreads) {
+        float *row = sA + q * NP;
+        for (int r = 0; r < NP; r++) row[r] = 0.0f;
+        const int n = q / 3, cq = q - 3 * n;
+        const int i = n % C.NX, jj = (n / C.NX) % C.NY, k = n / (C.NX * C.NY);
+        for (int a = 0; a < 8; a++) {
+            int dx, dy, dz;
+            corner_bits(a, dx, dy, dz);
+            const int ex = i - dx, ey = jj - dy, ez = k - dz;
+            if (ex < 0 || ey < 0 || ez < 0 || ex >= C.nx || ey >= C.ny || ez >= C.nz) continue;
+            const float e = sE[ex + C.nx * (ey + C.ny * ez)];
+            for (int bc = 0; bc < 8; bc++) {
+                int bx, by, bz;
+                corner_bits(bc, bx, by, bz);
+                const int m = (ex + bx) + C.NX * ((ey + by) + C.NY * (ez + bz));
+                for (int cb = 0; cb < 3; cb++)
+                    row[3 * m + cb] = fmaf(e, sK[(3 * a + cq) * 24 + 3 * bc + cb], row[3 * m + cb]);
+            }
+        }
+    }
+    __syncthreads();
+    const int ti = tid / kCoarseTiles, tj = tid - ti * kCoarseTiles;
+    const int i0 = ti * T, j0 = tj * T;
+    float a[T][T];
+#pragma unroll
+    for (int r = 0; r < T; r++)
+#pragma unroll
+        for (int cc = 0; cc < T; cc++) {
+            const int i = i0 + r, j = j0 + cc;
+            float v = i == j ? 1.0f : 0.0f;
+            if (i < nd && j < nd && !sfix[i] && !sfix[j]) v = i <= j ? sA[i * NP + j] : sA[j * NP + i];
+            a[r][cc] = v;
+        }
+    if (ti == 0)
+#pragma unroll
+        for (int cc = 0; cc < T; cc++) sv[j0 + cc] = a[0][cc];
+    __syncthreads();
+    int ok = 1, cur = 0;
+    for (int k = 0; k < nd; k++) {
+        const float *v = sv + cur * NP;
+        const float d = v[k];  // the same value in every thread: the exit below is uniform
+        if (!(d > 0.0f) || !isfinite(d)) {
+            ok = 0;
+            break;
+        }
+        const float p = 1.0f / d;
+        float vi[T], vj[T];
+#pragma unroll
+        for (int r = 0; r < T; r++) {
+            vi[r] = v[i0 + r];
+            vj[r] = v[j0 + r];
+        }
+#pragma unroll
+        for (int r = 0; r < T; r++)
+#pragma unroll
+            for (int cc = 0; cc < T; cc++) a[r][cc] = fmaf(-(vi[r] * vj[cc]), p, a[r][cc]);
+        const int kr = k - i0, kc = k - j0;
+        if ((unsigned)kr < (unsigned)T || (unsigned)kc < (unsigned)T) {
+#pragma unroll
+            for (int r = 0; r < T; r++)
+#pragma unroll
+                for (int cc = 0; cc < T; cc++)
+                    if (r == kr || cc == kc) a[r][cc] = (r == kr && cc == kc) ? -p : (r == kr ? vj[cc] : vi[r]) * p;
+        }
+        const int nr = k + 1 - i0;  // the next pivot row
+        if ((unsigned)nr < (unsigned)T) {
+            float *vn = sv + (cur ^ 1) * NP;
+#pragma unroll
+            for (int r = 0; r < T; r++)
+                if (r == nr)
+#pragma unroll
+                    for (int cc = 0; cc < T; cc++) vn[j0 + cc] = a[r][cc];
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    if (tid == 0) coarse_ok[h] = ok;
+    if (!ok) return;
+    float *out = coarse_inv + off;
+#pragma unroll
+    for (int r = 0; r < T; r++)
+#pragma unroll
+        for (int cc = 0; cc < T; cc++) {
+            const int i = i0 + r, j = j0 + cc;
+            if (i < nd && j < nd) out[i * nd + j] = -a[r][cc];
+        }
 }
 
 // inner CG start (problems in INIT): b = scale r64 (unit norm), x = 0, r = b,
@@ -2222,6 +2368,8 @@ int configure_kernels() {
     MG_CUDA_TRY(cudaFuncSetAttribute(mf_fac_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, fac_smem(5)));
     MG_CUDA_TRY(cudaFuncSetAttribute(mg_bottom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kBottomSmemMax));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mg_coarse_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kCoarseInvSmem));
     done = true;
     return MG_OK;
 }
@@ -2283,96 +2431,6 @@ void launch_update(MfBatch &b, float *pnew, bool mg) {
         b.chunks, n0, b.probs, b.x, b.r, b.z, pnew, b.q, b.dinv, b.states, b.chunk_part, mg ? 1 : 0);
 }
 
-// coarse inverses of the chains of the listed level-0 problems (all when null):
-// the coarsest level's moduli and Dirichlet mask come back to the host, which
-// assembles the level operator in FP64 (each row over the node's elements in a
-// fixed order, Dirichlet rows and columns eliminated), inverts it by Gauss-Jordan
-// (symmetric positive definite: no pivoting), symmetrises and uploads it in FP32
-int coarse_factor(MfBatch &b, const std::vector<int> *level0) {
-    struct Job {
-        int h, c;
-        std::vector<float> E, D;
-    };
-    std::vector<Job> jobs;
-    for (size_t h = 0; h < b.h_heads.size(); h++) {
-        if (b.h_coarse_off[h] < 0) continue;
-        if (level0 && std::find(level0->begin(), level0->end(), b.h_head_root[h]) == level0->end()) continue;
-        int c = b.h_heads[h];
-        while (b.h_probs[c].coarse >= 0) c = b.h_probs[c].coarse;
-        const MfProblem &C = b.h_probs[c];
-        Job j{(int)h, c, std::vector<float>((size_t)C.pitch_e * C.ny * C.nz), std::vector<float>((size_t)C.n_pad)};
-        jobs.push_back(std::move(j));
-    }
-    if (jobs.empty()) return MG_OK;
-    for (Job &j : jobs) {
-        const MfProblem &C = b.h_probs[j.c];
-        MG_CUDA_TRY(cudaMemcpyAsync(j.E.data(), b.E32 + C.elem_off, j.E.size() * 4, cudaMemcpyDeviceToHost, b.stream));
-        MG_CUDA_TRY(cudaMemcpyAsync(j.D.data(), b.dinv + C.dof_off, j.D.size() * 4, cudaMemcpyDeviceToHost, b.stream));
-    }
-    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
-    std::vector<std::vector<float>> outs(jobs.size());
-    for (size_t t = 0; t < jobs.size(); t++) {
-        const Job &j = jobs[t];
-        const MfProblem &C = b.h_probs[j.c];
-        const int nn = C.NX * C.NY * C.NZ, nd = 3 * nn;
-        std::vector<double> A((size_t)nd * nd, 0.0);
-        std::vector<char> fixed(nd);
-        for (int q = 0; q < nd; q++) {
-            const int n = q / 3, cq = q - 3 * n;
-            const int i = n % C.NX, jj = (n / C.NX) % C.NY, k = n / (C.NX * C.NY);
-            fixed[q] = j.D[((size_t)k * C.NY + jj) * C.pitch + 3 * i + cq] == 0.0f;
-        }
-        for (int q = 0; q < nd; q++) {
-            const int n = q / 3, cq = q - 3 * n;
-            const int i = n % C.NX, jj = (n / C.NX) % C.NY, k = n / (C.NX * C.NY);
-            for (int a = 0; a < 8; a++) {
-                int dx, dy, dz;
-                corner_bits(a, dx, dy, dz);
-                const int ex = i - dx, ey = jj - dy, ez = k - dz;
-                if (ex < 0 || ey < 0 || ez < 0 || ex >= C.nx || ey >= C.ny || ez >= C.nz) continue;
-                const double e = (double)j.E[((size_t)ez * C.ny + ey) * C.pitch_e + ex];
-                for (int bc = 0; bc < 8; bc++) {
-                    int bx, by, bz;
-                    corner_bits(bc, bx, by, bz);
-                    const int m = (ex + bx) + C.NX * ((ey + by) + C.NY * (ez + bz));
-                    for (int cb = 0; cb < 3; cb++)
-                        A[(size_t)q * nd + 3 * m + cb] += e * b.h_K0[(3 * a + cq) * 24 + 3 * bc + cb];
-                }
-            }
-        }
-        for (int q = 0; q < nd; q++)
-            for (int r = 0; r < nd; r++)
-                if (fixed[q] || fixed[r]) A[(size_t)q * nd + r] = (q == r) ? 1.0 : 0.0;
-        for (int k = 0; k < nd; k++) {
-            const double piv = A[(size_t)k * nd + k];
-            if (!(piv > 0.0) || !std::isfinite(piv)) {
-                set_error("coarse-grid operator is not positive definite (pivot %d: %g)", k, piv);
-                return MG_EBREAKDOWN;
-            }
-            const double p = 1.0 / piv;
-            for (int r = 0; r < nd; r++)
-                if (r != k) A[(size_t)k * nd + r] *= p;
-            for (int q = 0; q < nd; q++) {
-                if (q == k) continue;
-                const double f = A[(size_t)q * nd + k];
-                if (f == 0.0) continue;
-                for (int r = 0; r < nd; r++)
-                    if (r != k) A[(size_t)q * nd + r] -= f * A[(size_t)k * nd + r];
-            }
-            for (int q = 0; q < nd; q++) A[(size_t)q * nd + k] = (q == k) ? p : -A[(size_t)q * nd + k] * p;
-        }
-        std::vector<float> &o = outs[t];
-        o.resize((size_t)nd * nd);
-        for (int q = 0; q < nd; q++)
-            for (int r = 0; r < nd; r++)
-                o[(size_t)q * nd + r] = (float)(0.5 * (A[(size_t)q * nd + r] + A[(size_t)r * nd + q]));
-        MG_CUDA_TRY(cudaMemcpyAsync(b.coarse_inv + b.h_coarse_off[j.h], o.data(), o.size() * 4,
-                                    cudaMemcpyHostToDevice, b.stream));
-    }
-    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));  // the host buffers are temporaries
-    return MG_OK;
-}
-
 int compute_diag(MfBatch &b) {
     int64_t maxpad = 1;
     for (const MfProblem &P : b.h_probs) maxpad = std::max(maxpad, P.n_pad);
@@ -2383,9 +2441,10 @@ int compute_diag(MfBatch &b) {
     return MG_OK;  // the operator-only paths need no coarse inverse; activation forms it
 }
 
-// Jacobi inverse of the listed level-0 problems and all their coarse levels
+// Jacobi inverse of the listed level-0 problems and all their coarse levels, and
+// the inverse of the coarsest grid of their direct chains; nothing waits on the host
 int compute_diag_list(MfBatch &b, const std::vector<int> &level0) {
-    std::vector<int> list;
+    std::vector<int> list, inv;
     int64_t maxpad = 1;
     for (int i : level0)
         for (int q = i; q >= 0; q = b.h_probs[q].coarse) {
@@ -2393,15 +2452,29 @@ int compute_diag_list(MfBatch &b, const std::vector<int> &level0) {
             maxpad = std::max(maxpad, b.h_probs[q].n_pad);
         }
     if (list.empty()) return MG_OK;
-    MG_CUDA_TRY(cudaMemcpyAsync(b.diag_list, list.data(), list.size() * sizeof(int),
+    for (size_t h = 0; h < b.h_heads.size(); h++)
+        if (b.h_coarse_off[h] >= 0 && std::find(level0.begin(), level0.end(), b.h_head_root[h]) != level0.end())
+            inv.push_back((int)h);
+    // the pinned staging buffer: the previous call's copy must have read it
+    if (b.stage_pending) MG_CUDA_TRY(cudaEventSynchronize(b.stage_ev));
+    memcpy(b.stage_host, list.data(), list.size() * sizeof(int));
+    memcpy(b.stage_host + list.size(), inv.data(), inv.size() * sizeof(int));
+    MG_CUDA_TRY(cudaMemcpyAsync(b.diag_list, b.stage_host, (list.size() + inv.size()) * sizeof(int),
                                 cudaMemcpyHostToDevice, b.stream));
+    MG_CUDA_TRY(cudaEventRecord(b.stage_ev, b.stream));
+    b.stage_pending = true;
     dim3 grid(std::max(1u, std::min(blocks_for(maxpad, 256), 4096u)), (unsigned)list.size());
     mf_diag_kernel<<<grid, 256, 0, b.stream>>>(b.probs, b.diag_list, b.E32, b.node_fix, b.K0, b.dinv);
     MG_CUDA_TRY(cudaGetLastError());
     count_launches(1);
-    // the list is a host temporary: finish the copy before it goes away
-    MG_CUDA_TRY(cudaStreamSynchronize(b.stream));
-    return coarse_factor(b, &level0);
+    if (!inv.empty()) {
+        mg_coarse_inverse_kernel<<<(unsigned)inv.size(), kCoarseInvThreads, kCoarseInvSmem, b.stream>>>(
+            b.probs, b.heads, b.diag_list + list.size(), b.E32, b.dinv, b.K0, b.coarse_off, b.coarse_inv,
+            b.coarse_ok);
+        MG_CUDA_TRY(cudaGetLastError());
+        count_launches(1);
+    }
+    return MG_OK;
 }
 
 }  // namespace
@@ -2642,6 +2715,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         }
         MG_TRY(dev_alloc_n(&b.coarse_off, std::max<size_t>(1, b.h_coarse_off.size())));
         MG_TRY(dev_alloc_n(&b.coarse_inv, (size_t)std::max<int64_t>(1, inv_floats)));
+        MG_TRY(dev_alloc_n(&b.coarse_ok, std::max<size_t>(1, b.h_coarse_off.size())));
     }
     b.apply_grid = std::max(1, std::min(nb, 2 * sms));  // FP64 residual: two CTAs per SM
     b.col_grid = std::max(1, std::min(b.n_cols, kColCtas * sms));  // column CTAs per SM
@@ -2671,7 +2745,9 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.brick_part, (size_t)2 * nb));  // operator partials | ||f||^2 partials
     MG_TRY(dev_alloc_n(&b.chunk_part, (size_t)2 * nc));
     MG_TRY(dev_alloc_n(&b.err, 1));
-    MG_TRY(dev_alloc_n(&b.diag_list, (size_t)b.n_probs));
+    MG_TRY(dev_alloc_n(&b.diag_list, (size_t)b.n_probs + b.h_heads.size()));
+    MG_CUDA_TRY(cudaMallocHost(&b.stage_host, ((size_t)b.n_probs + b.h_heads.size()) * sizeof(int)));
+    MG_CUDA_TRY(cudaEventCreateWithFlags(&b.stage_ev, cudaEventDisableTiming));
     MG_TRY(dev_alloc_n(&b.heads, std::max<size_t>(1, b.h_heads.size())));
     MG_TRY(dev_alloc_n(&b.K0, 576));
     double K0[576];
@@ -2729,10 +2805,11 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     }
     MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
-    b.h_K0.assign(K0, K0 + 576);
-    if (!b.h_coarse_off.empty())
+    if (!b.h_coarse_off.empty()) {
         MG_CUDA_TRY(cudaMemcpyAsync(b.coarse_off, b.h_coarse_off.data(), b.h_coarse_off.size() * sizeof(int64_t),
                                     cudaMemcpyHostToDevice, s));
+        MG_CUDA_TRY(cudaMemsetAsync(b.coarse_ok, 0, b.h_coarse_off.size() * sizeof(int), s));
+    }
     if (!b.h_heads.empty())
         MG_CUDA_TRY(cudaMemcpyAsync(b.heads, b.h_heads.data(), b.h_heads.size() * sizeof(int),
                                     cudaMemcpyHostToDevice, s));
@@ -2758,8 +2835,10 @@ void mf_batch_free(MfBatch &b) {
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.K0, b.mb, b.mx, b.md,
                     b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles, b.fac_maps,
-                    b.coarse_off, b.coarse_inv};
+                    b.coarse_off, b.coarse_inv, b.coarse_ok};
     for (void *q : ptrs) dev_free(q);
+    if (b.stage_host) cudaFreeHost(b.stage_host);
+    if (b.stage_ev) cudaEventDestroy(b.stage_ev);
     if (b.states_host) cudaFreeHost(b.states_host);
     if (b.err_host) cudaFreeHost(b.err_host);
     b = MfBatch();
@@ -2989,7 +3068,7 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
         }
         launch_pdl(mg_bottom_kernel, (unsigned)b.h_heads.size(), kBottomThreads, b.bottom_smem, b.stream, 
             b.probs, b.heads, b.states, b.E32, b.dinv, b.mb, b.mx, b.K0, bc, sdeg, cdeg, b.coarse_off,
-            b.coarse_inv);
+            b.coarse_inv, b.coarse_ok);
         n += 1;
     }
     for (int l = L - 2; l >= 0; l--) {

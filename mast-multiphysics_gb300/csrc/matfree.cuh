@@ -143,18 +143,22 @@ struct MfBatch {
     int *heads = nullptr;
     // direct solve on a chain's coarsest grid (when it has at most kCoarseDirectMax
     // dofs): the FP32 inverse of its assembled operator per chain, at coarse_off[head]
-    // (-1: Chebyshev smoothing instead); refreshed whenever the moduli change
+    // (-1: Chebyshev smoothing instead); formed on the device whenever the moduli
+    // change, coarse_ok[head] = 0 where that met a non-positive pivot (smoothing then)
     std::vector<int64_t> h_coarse_off;
     std::vector<int> h_head_root;   // level-0 problem of each chain
     int64_t *coarse_off = nullptr;
     float *coarse_inv = nullptr;
-    std::vector<double> h_K0;       // K0 on the host (576, element dof 3 a + c)
+    int *coarse_ok = nullptr;
     int bottom_smem = 0;        // dynamic shared memory of the bottom kernel
     // FP64 refinement vectors (padded layout)
     double *u64 = nullptr, *r64 = nullptr, *f64 = nullptr;
     double *brick_part = nullptr, *chunk_part = nullptr;
     int *err = nullptr;
-    int *diag_list = nullptr;  // problem list of a partial Jacobi update
+    int *diag_list = nullptr;  // problem list of a partial Jacobi update, then its direct chains
+    int *stage_host = nullptr;  // pinned staging of diag_list
+    cudaEvent_t stage_ev = nullptr;  // its last copy
+    bool stage_pending = false;
     // operator data
     double *K0 = nullptr;     // 24x24 FP64, node-interleaved element order
     double hx = 1, hy = 1, hz = 1, nu = 0.3;
