@@ -1376,7 +1376,6 @@ __global__ void mg_coarsen_kernel(const MfProblem *__restrict__ probs, int plo,
 // one launch per level operation.  Per level the shared memory holds x, b, r,
 // d, y, D^-1 (per dof, compact node-interleaved order) and E (per element).
 constexpr int kBottomThreads = 512;
-constexpr int kBottomMaxLevels = 6;
 constexpr int kBottomSmemMax = 200 * 1024;  // per chain: 576 + sum over levels (18 NN + ne) floats
 constexpr int kBottomMaxHeadNodes = 2 * kBottomThreads;
 
@@ -1810,6 +1809,363 @@ __global__ void __launch_bounds__(kCoarseInvThreads, 1) mg_coarse_inverse_kernel
             const int i = i0 + r, j = j0 + cc;
             if (i < nd && j < nd) out[i * nd + j] = -a[r][cc];
         }
+}
+
+// ------------------------------------------------- bottom V-cycle on a cluster
+// The same bottom V-cycle as mg_bottom_kernel, spread over a thread-block
+// cluster of up to 16 CTAs (one cluster per chain) so that a single design's
+// chain can start at a larger level.  CTA r owns the nodes [r chunk, (r + 1) chunk)
+// of every level of the chain and keeps their x, b, r, d, y in its shared memory
+// (with D^-1 and the moduli of whole levels); a phase reads other CTAs' nodes
+// through distributed shared memory (mapa + ld.shared::cluster) and a cluster
+// barrier (release / acquire) separates the phases.  Global memory is touched only
+// at the start (rhs, tables) and at the end (the head's correction).  Every dof is
+// computed by one thread in a fixed order whatever the cluster size, so the result
+// does not depend on it.
+constexpr int kClusterThreads = 512;
+constexpr int kClusterMaxHeadNodes = 4096;
+constexpr int kClusterMax = 16;
+constexpr int kClusterK0 = 576 + 800;  // K0 and its regrouped copy (floats)
+
+__device__ __forceinline__ unsigned cluster_ctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_nctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+// component c of node n of a vector whose slabs sit at `slab` in every CTA
+__device__ __forceinline__ float cl_get(const float *slab, int chunk, int n, int c, int rank) {
+    const int owner = n / chunk;
+    const float *p = slab + (n - owner * chunk) * 3 + c;
+    if (owner == rank) return *p;
+    uint32_t ra;
+    float v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(p)), "r"(owner));
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(ra) : "memory");
+    return v;
+}
+
+enum { kClX = 0, kClB, kClR, kClD, kClY };
+__device__ __forceinline__ float *cl_slab(float *sm, const ClusterLevel &L, int v) {
+    return sm + L.s_vec + v * 3 * L.chunk;
+}
+
+// One phase of the cluster V-cycle on level L: y = A in with eight lanes per node
+// (as bottom_apply), the elementwise update that follows it done by the lanes that
+// hold each dof's sum, so that the phase needs no second barrier:
+//   STEP 0, residual:             in = x;   r = b - y
+//   STEP 1, first smoothing step: in = D^-1 rin theta (formed while staging rin);
+//           r0 = rin, d0 = D^-1 r0 theta, x0 = d0 or x + d0, then the step-1 update
+//   STEP 2, later smoothing step: in = d;   r -= y, d' = c1 d + c2 D^-1 r, x += d'
+// (0 on Dirichlet dofs throughout).  The operand over the CTA's nodes and their
+// one-layer halo (nodes n0 - H .. n1 - 1 + H, H = NX NY + NX + 1) is first staged
+// in shared memory; no phase writes a slab that another CTA reads in it (the
+// callers rotate r, d and y).
+struct ClusterStep {
+    const float *in, *b, *r_src, *d_src;  // slabs (this CTA's shared memory)
+    float *r_dst, *d_dst, *x;
+    bool x0_zero;
+    float inv_theta, c1, c2;
+};
+
+template <int STEP>
+__device__ void cl_step(const ClusterLevel &L, float *sm, const float *sK, float *stage, const ClusterStep &S,
+                        int rank) {
+    const int nn = L.NX * L.NY * L.NZ;
+    const int n0 = rank * L.chunk, n1 = min(nn, n0 + L.chunk);
+    const int H = L.NX * L.NY + L.NX + 1;
+    const float *dinvL = sm + L.s_dinv, *EL = sm + L.s_E;
+    const int nlo = max(0, n0 - H);
+    if (n0 < n1) {
+        const int cnt = 3 * (min(nn - 1, n1 - 1 + H) - nlo + 1);
+        for (int t = threadIdx.x; t < cnt; t += kClusterThreads) {
+            const int n = nlo + t / 3, c = t - 3 * (t / 3);
+            const float v = cl_get(S.in, L.chunk, n, c, rank);
+            stage[t] = STEP == 1 ? dinvL[3 * n + c] * v * S.inv_theta : v;
+        }
+    }
+    __syncthreads();
+    const int corner = threadIdx.x & 7;
+    const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
+    const float4 *Kt = reinterpret_cast<const float4 *>(sK + 576 + 100 * corner_index(dx, dy, dz));
+    for (int base = n0; base < n1; base += kClusterThreads / 8) {
+        const int n = base + (threadIdx.x >> 3);
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        if (n < n1) {
+            const int i = n % L.NX, j = (n / L.NX) % L.NY, k = n / (L.NX * L.NY);
+            const int ex = i - dx, ey = j - dy, ez = k - dz;
+            if (ex >= 0 && ey >= 0 && ez >= 0 && ex < L.nx && ey < L.ny && ez < L.nz) {
+                const float e = EL[ex + L.nx * (ey + L.ny * ez)];
+                const float *u0p = stage + 3 * (ex + L.NX * (ey + L.NY * ez) - nlo);
+                float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+                for (int bc = 0; bc < 8; bc++) {
+                    int bx, by, bz;
+                    corner_bits(bc, bx, by, bz);
+                    const float *u = u0p + 3 * (bx + L.NX * (by + L.NY * bz));
+                    const float4 k0 = Kt[3 * bc], k1 = Kt[3 * bc + 1], k2 = Kt[3 * bc + 2];
+                    s0 = fmaf(k0.z, u[2], fmaf(k0.y, u[1], fmaf(k0.x, u[0], s0)));
+                    s1 = fmaf(k1.y, u[2], fmaf(k1.x, u[1], fmaf(k0.w, u[0], s1)));
+                    s2 = fmaf(k2.x, u[2], fmaf(k1.w, u[1], fmaf(k1.z, u[0], s2)));
+                }
+                a0 = e * s0;
+                a1 = e * s1;
+                a2 = e * s2;
+            }
+        }
+#pragma unroll
+        for (int off = 1; off < 8; off <<= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, off);
+        }
+        if (n < n1 && corner < 3) {
+            const int lo = 3 * (n - n0) + corner;
+            const float dn = dinvL[3 * n + corner];
+            const float y = dn == 0.0f ? 0.0f : (corner == 0 ? a0 : (corner == 1 ? a1 : a2));
+            if (STEP == 0) {
+                S.r_dst[lo] = dn == 0.0f ? 0.0f : S.b[lo] - y;
+            } else {
+                const float rv0 = S.r_src[lo];
+                float d0, x0;
+                if (STEP == 1) {
+                    d0 = dn * rv0 * S.inv_theta;
+                    x0 = S.x0_zero ? d0 : S.x[lo] + d0;
+                } else {
+                    d0 = S.d_src[lo];
+                    x0 = S.x[lo];
+                }
+                const float rv = rv0 - y;
+                const float dv = fmaf(S.c1, d0, S.c2 * dn * rv);
+                S.r_dst[lo] = rv;
+                S.d_dst[lo] = dv;
+                S.x[lo] = x0 + dv;
+            }
+        }
+    }
+}
+
+// x (+)= Chebyshev-Jacobi smoothing of degree deg for rhs rin (as bottom_smooth):
+// deg - 1 phases (one for deg = 1); r, d and y are rotated so that no phase
+// writes what other CTAs read in it
+__device__ void cl_smooth(const ClusterLevel &L, float *sm, const float *sK, float *stage, const float *rin,
+                          bool x0_zero, int deg, float inv_theta, const float *c1, const float *c2, int rank) {
+    float *x = cl_slab(sm, L, kClX), *r = cl_slab(sm, L, kClR), *d = cl_slab(sm, L, kClD),
+          *sp = cl_slab(sm, L, kClY);
+    if (deg <= 1) {
+        const int nn = L.NX * L.NY * L.NZ;
+        const int n0 = rank * L.chunk, nown = max(0, min(nn, n0 + L.chunk) - n0);
+        const float *dinvL = sm + L.s_dinv + 3 * n0;
+        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
+            const float rv = rin[q], dv = dinvL[q] * rv * inv_theta;
+            r[q] = rv;
+            d[q] = dv;
+            x[q] = x0_zero ? dv : x[q] + dv;
+        }
+        cluster_barrier();
+        return;
+    }
+    ClusterStep S{};
+    S.x = x;
+    S.inv_theta = inv_theta;
+    S.x0_zero = x0_zero;
+    // step 1 reads rin at the neighbours: its residual goes to the spare slab when rin is r
+    S.in = rin;
+    S.r_src = rin;
+    S.r_dst = rin == r ? sp : r;
+    S.d_dst = d;
+    S.c1 = c1[1];
+    S.c2 = c2[1];
+    cl_step<1>(L, sm, sK, stage, S, rank);
+    cluster_barrier();
+    if (rin == r) {
+        float *t = r; r = sp; sp = t;
+    }
+    for (int k = 2; k < deg; k++) {
+        // reads d at the neighbours: the new direction goes to the spare slab
+        S.in = d;
+        S.r_src = r;
+        S.r_dst = r;
+        S.d_src = d;
+        S.d_dst = sp;
+        S.c1 = c1[k];
+        S.c2 = c2[k];
+        cl_step<2>(L, sm, sK, stage, S, rank);
+        cluster_barrier();
+        float *t = d; d = sp; sp = t;
+    }
+}
+
+// r = b - A x (0 on Dirichlet dofs), one phase
+__device__ void cl_residual(const ClusterLevel &L, float *sm, const float *sK, float *stage, int rank) {
+    ClusterStep S{};
+    S.in = cl_slab(sm, L, kClX);
+    S.b = cl_slab(sm, L, kClB);
+    S.r_dst = cl_slab(sm, L, kClR);
+    cl_step<0>(L, sm, sK, stage, S, rank);
+    cluster_barrier();
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
+    const ClusterChain *__restrict__ chains, const MfState *states, const float *__restrict__ E32,
+    const float *__restrict__ dinv, const float *__restrict__ mb, float *__restrict__ mx,
+    const float *__restrict__ k0f, BottomCheb cc, int sdeg, int cdeg, const int64_t *__restrict__ coarse_off,
+    const float *__restrict__ coarse_inv, const int *__restrict__ coarse_ok) {
+    pdl_enter();
+    extern __shared__ __align__(16) float sm[];  // K0 tables, stage, per level: D^-1, E, slabs
+    __shared__ ClusterChain sc;
+    const int csize = (int)cluster_nctarank(), rank = (int)cluster_ctarank();
+    const int chain = blockIdx.x / csize;
+    {
+        const int *src = reinterpret_cast<const int *>(chains + chain);
+        int *dst = reinterpret_cast<int *>(&sc);
+        for (int i = threadIdx.x; i < (int)(sizeof(ClusterChain) / 4); i += kClusterThreads) dst[i] = src[i];
+    }
+    for (int i = threadIdx.x; i < kClusterK0; i += kClusterThreads) sm[i] = k0f[i];
+    __syncthreads();
+    // the same state in every CTA of the cluster: all return, or none
+    if (states[sc.root].done) return;
+    const int m = sc.m;
+    const float *sK = sm;
+    float *stage = sm + sc.s_stage;
+    // D^-1 and E of every level (compact order), the head's rhs over this CTA's nodes
+    for (int l = 0; l < m; l++) {
+        const ClusterLevel &L = sc.L[l];
+        const int nn = L.NX * L.NY * L.NZ, ne = L.nx * L.ny * L.nz;
+        for (int q = threadIdx.x; q < 3 * nn; q += kClusterThreads) {
+            const int n = q / 3, c = q - 3 * n;
+            const int i = n % L.NX, j = (n / L.NX) % L.NY, k = n / (L.NX * L.NY);
+            sm[L.s_dinv + q] = dinv[L.dof_off + ((int64_t)k * L.NY + j) * L.pitch + 3 * i + c];
+        }
+        for (int e = threadIdx.x; e < ne; e += kClusterThreads) {
+            const int ex = e % L.nx, ey = (e / L.nx) % L.ny, ez = e / (L.nx * L.ny);
+            sm[L.s_E + e] = E32[L.elem_off + ((int64_t)ez * L.ny + ey) * L.pitch_e + ex];
+        }
+    }
+    const ClusterLevel &L0 = sc.L[0];
+    {
+        const int nn = L0.NX * L0.NY * L0.NZ, n0 = rank * L0.chunk, nown = max(0, min(nn, n0 + L0.chunk) - n0);
+        float *b0 = cl_slab(sm, L0, kClB);
+        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
+            const int n = n0 + q / 3, c = q - 3 * (q / 3);
+            const int i = n % L0.NX, j = (n / L0.NX) % L0.NY, k = n / (L0.NX * L0.NY);
+            b0[q] = mb[L0.dof_off + ((int64_t)k * L0.NY + j) * L0.pitch + 3 * i + c];
+        }
+    }
+    // the direct solve's rows of this CTA (one warp per row), loaded now
+    const ClusterLevel &Lc = sc.L[m - 1];
+    const int64_t inv_off = coarse_ok[chain] ? coarse_off[chain] : -1;
+    const int nnc = Lc.NX * Lc.NY * Lc.NZ, ndc = 3 * nnc;
+    const int c0 = rank * Lc.chunk, crows = 3 * max(0, min(nnc, c0 + Lc.chunk) - c0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int kInvPer = (kCoarseDirectMax + 31) / 32;
+    float inv[kInvPer];
+#pragma unroll
+    for (int t = 0; t < kInvPer; t++) {
+        const int r = lane + 32 * t;
+        inv[t] = (inv_off >= 0 && warp < crows && r < ndc)
+                     ? __ldg(coarse_inv + inv_off + (int64_t)(3 * c0 + warp) * ndc + r)
+                     : 0.0f;
+    }
+    cluster_barrier();  // every CTA's tables and rhs are in place
+    // down: smooth, residual, restrict
+    for (int l = 0; l < m - 1; l++) {
+        const ClusterLevel &F = sc.L[l], &C = sc.L[l + 1];
+        cl_smooth(F, sm, sK, stage, cl_slab(sm, F, kClB), true, sdeg, cc.inv_theta_s, cc.c1s, cc.c2s, rank);
+        cl_residual(F, sm, sK, stage, rank);
+        const int nnC = C.NX * C.NY * C.NZ, n0 = rank * C.chunk, nown = max(0, min(nnC, n0 + C.chunk) - n0);
+        const float *rF = cl_slab(sm, F, kClR);
+        float *bC = cl_slab(sm, C, kClB);
+        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
+            const int n = n0 + q / 3, c = q - 3 * (q / 3);
+            const int I = n % C.NX, J = (n / C.NX) % C.NY, K = n / (C.NX * C.NY);
+            float out = 0.0f;
+            if (sm[C.s_dinv + 3 * n + c] != 0.0f)
+                for (int dz = -1; dz <= 1; dz++) {
+                    const int kk = 2 * K + dz;
+                    if (kk < 0 || kk >= F.NZ) continue;
+                    for (int dy = -1; dy <= 1; dy++) {
+                        const int jj = 2 * J + dy;
+                        if (jj < 0 || jj >= F.NY) continue;
+                        for (int dx = -1; dx <= 1; dx++) {
+                            const int ii = 2 * I + dx;
+                            if (ii < 0 || ii >= F.NX) continue;
+                            const float w = (dx ? 0.5f : 1.0f) * (dy ? 0.5f : 1.0f) * (dz ? 0.5f : 1.0f);
+                            out = fmaf(w, cl_get(rF, F.chunk, ii + F.NX * (jj + F.NY * kk), c, rank), out);
+                        }
+                    }
+                }
+            bC[q] = out;
+        }
+        cluster_barrier();
+    }
+    // coarsest grid of the chain: exact solve with the stored inverse, or smoothing
+    if (inv_off >= 0) {
+        // one warp per own row, partial sums met by a fixed xor butterfly; the
+        // first pass uses the rows loaded at the start
+        const float *bc = cl_slab(sm, Lc, kClB);
+        float *xc = cl_slab(sm, Lc, kClX);
+        for (int w0 = 0; w0 < crows; w0 += kClusterThreads / 32) {
+            const int w = w0 + warp;
+            if (w >= crows) break;  // whole warps leave together
+            float sacc = 0.0f;
+#pragma unroll
+            for (int t = 0; t < kInvPer; t++) {
+                const int r = lane + 32 * t;
+                if (r < ndc) {
+                    const float a = w0 == 0 ? inv[t] : __ldg(coarse_inv + inv_off + (int64_t)(3 * c0 + w) * ndc + r);
+                    sacc = fmaf(a, cl_get(bc, Lc.chunk, r / 3, r - 3 * (r / 3), rank), sacc);
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, off);
+            if (lane == 0) xc[w] = sm[Lc.s_dinv + 3 * c0 + w] == 0.0f ? 0.0f : sacc;
+        }
+        cluster_barrier();
+    } else {
+        cl_smooth(Lc, sm, sK, stage, cl_slab(sm, Lc, kClB), true, cdeg, cc.inv_theta_c, cc.c1c, cc.c2c, rank);
+    }
+    // up: prolong, residual, post-smooth
+    for (int l = m - 2; l >= 0; l--) {
+        const ClusterLevel &F = sc.L[l], &C = sc.L[l + 1];
+        const int nnF = F.NX * F.NY * F.NZ, n0 = rank * F.chunk, nown = max(0, min(nnF, n0 + F.chunk) - n0);
+        const float *xC = cl_slab(sm, C, kClX);
+        float *xF = cl_slab(sm, F, kClX);
+        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
+            const int n = n0 + q / 3, c = q - 3 * (q / 3);
+            if (sm[F.s_dinv + 3 * n + c] == 0.0f) continue;
+            const int ii = n % F.NX, jj = (n / F.NX) % F.NY, kk = n / (F.NX * F.NY);
+            const int Is[2] = {ii >> 1, (ii + 1) >> 1}, Js[2] = {jj >> 1, (jj + 1) >> 1}, Ks[2] = {kk >> 1, (kk + 1) >> 1};
+            const float w = ((ii & 1) ? 0.5f : 1.0f) * ((jj & 1) ? 0.5f : 1.0f) * ((kk & 1) ? 0.5f : 1.0f);
+            float acc = 0.0f;
+            for (int a = 0; a < ((kk & 1) ? 2 : 1); a++)
+                for (int bb = 0; bb < ((jj & 1) ? 2 : 1); bb++)
+                    for (int cc2 = 0; cc2 < ((ii & 1) ? 2 : 1); cc2++)
+                        acc = fmaf(w, cl_get(xC, C.chunk, Is[cc2] + C.NX * (Js[bb] + C.NY * Ks[a]), c, rank), acc);
+            xF[q] += acc;
+        }
+        cluster_barrier();
+        cl_residual(F, sm, sK, stage, rank);
+        // post-smoothing on the residual: x += S(r) (the smoother starts from r in place)
+        cl_smooth(F, sm, sK, stage, cl_slab(sm, F, kClR), false, sdeg, cc.inv_theta_s, cc.c1s, cc.c2s, rank);
+    }
+    // the head's correction over this CTA's nodes back to the padded global layout
+    {
+        const int nn = L0.NX * L0.NY * L0.NZ, n0 = rank * L0.chunk, nown = max(0, min(nn, n0 + L0.chunk) - n0);
+        const float *x0 = cl_slab(sm, L0, kClX);
+        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
+            const int n = n0 + q / 3, c = q - 3 * (q / 3);
+            const int i = n % L0.NX, j = (n / L0.NX) % L0.NY, k = n / (L0.NX * L0.NY);
+            mx[L0.dof_off + ((int64_t)k * L0.NY + j) * L0.pitch + 3 * i + c] = x0[q];
+        }
+    }
 }
 
 // inner CG start (problems in INIT): b = scale r64 (unit norm), x = 0, r = b,
@@ -2269,6 +2625,27 @@ void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cu
     cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
+// launch_pdl with a thread-block cluster of csize CTAs along x
+template <typename... KArgs, typename... Args>
+void launch_cluster_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, int csize, cudaStream_t s,
+                        Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    attr[1].id = cudaLaunchAttributeClusterDimension;
+    attr[1].val.clusterDim.x = (unsigned)csize;
+    attr[1].val.clusterDim.y = 1;
+    attr[1].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 struct ApplyArgs {
     int col_lo, col_hi, in_slot, parity;  // column range
     const float *rhs;
@@ -2370,6 +2747,9 @@ int configure_kernels() {
                                      kBottomSmemMax));
     MG_CUDA_TRY(cudaFuncSetAttribute(mg_coarse_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      kCoarseInvSmem));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mg_bottom_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    MG_CUDA_TRY(cudaFuncSetAttribute(mg_bottom_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kBottomSmemMax));
     done = true;
     return MG_OK;
 }
@@ -2514,8 +2894,52 @@ void hex8_box_stiffness(double hx, double hy, double hz, double nu, double K[576
         }
 }
 
+// shared-memory layout of the cluster bottom kernel for clusters of cs CTAs: per
+// chain its level table (nodes per CTA, offsets of D^-1, E and the CTA's slabs);
+// returns the dynamic shared memory (bytes) of the largest chain
+int64_t cluster_layout(const MfBatch &b, int cs, std::vector<ClusterChain> &chains) {
+    chains.assign(b.h_heads.size(), ClusterChain{});
+    int64_t most = 0;
+    for (size_t h = 0; h < b.h_heads.size(); h++) {
+        ClusterChain &ch = chains[h];
+        ch.root = b.h_head_root[h];
+        int m = 0;
+        int64_t stage = 0;
+        for (int t = b.h_heads[h]; t >= 0 && m < kBottomMaxLevels; t = b.h_probs[t].coarse, m++) {
+            const MfProblem &T = b.h_probs[t];
+            ClusterLevel &L = ch.L[m];
+            L.NX = T.NX; L.NY = T.NY; L.NZ = T.NZ;
+            L.nx = T.nx; L.ny = T.ny; L.nz = T.nz;
+            L.pitch = T.pitch; L.pitch_e = T.pitch_e;
+            L.dof_off = T.dof_off; L.elem_off = T.elem_off;
+            const int nn = T.NX * T.NY * T.NZ, H = T.NX * T.NY + T.NX + 1;
+            L.chunk = (nn + cs - 1) / cs;
+            for (int r = 0; r < cs; r++) {
+                const int n0 = r * L.chunk, n1 = std::min(nn, n0 + L.chunk);
+                if (n0 < n1) stage = std::max<int64_t>(stage, 3LL * (std::min(nn - 1, n1 - 1 + H) - std::max(0, n0 - H) + 1));
+            }
+        }
+        ch.m = m;
+        int64_t off = kClusterK0;
+        ch.s_stage = (int)off;
+        off += (stage + 3) / 4 * 4;
+        for (int l = 0; l < m; l++) {
+            ClusterLevel &L = ch.L[l];
+            const int64_t nn = (int64_t)L.NX * L.NY * L.NZ, ne = (int64_t)L.nx * L.ny * L.nz;
+            L.s_dinv = (int)off;
+            off += (3 * nn + 3) / 4 * 4;
+            L.s_E = (int)off;
+            off += (ne + 3) / 4 * 4;
+            L.s_vec = (int)off;
+            off += 15LL * L.chunk;
+        }
+        most = std::max(most, off * 4);
+    }
+    return most;
+}
+
 int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, double hy,
-                  double hz, double nu, cudaStream_t stream, int max_levels) {
+                  double hz, double nu, cudaStream_t stream, int max_levels, bool bottom_cluster) {
     MG_TRY(configure_kernels());
     EncodeTiledFn enc = nullptr;
     MG_TRY(encode_fn(&enc));
@@ -2668,10 +3092,13 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     // bottom chains: for every design, the first level below the finest with at
     // most kBottomMaxHeadNodes nodes whose chain (it and all coarser levels) fits
     // the bottom kernel's shared memory; larger levels run level by level on the
-    // whole GPU (the one-CTA kernel is bound by one SM's shared-memory pipe there)
+    // whole GPU (the one-CTA kernel is bound by one SM's shared-memory pipe there).
+    // With a cluster per chain (bottom_cluster: single-design solves), the first
+    // level with at most kClusterMaxHeadNodes nodes.
     b.h_heads.clear();
     b.h_head_root.clear();
     b.bottom_smem = 0;
+    b.bottom_cluster = 0;
     for (int r = 0; r < b.n_fine; r++) {
         for (int q = b.h_probs[r].coarse; q >= 0; q = b.h_probs[q].coarse) {
             int64_t floats = 576 + 800, depth = 0;
@@ -2682,11 +3109,13 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
             }
             const int64_t bytes = floats * 4;
             const MfProblem &Hd = b.h_probs[q];
-            if (depth <= kBottomMaxLevels && bytes <= kBottomSmemMax &&
-                (int64_t)Hd.NX * Hd.NY * Hd.NZ <= kBottomMaxHeadNodes) {
+            const int64_t head_nodes = (int64_t)Hd.NX * Hd.NY * Hd.NZ;
+            const bool fits = bottom_cluster ? head_nodes <= kClusterMaxHeadNodes
+                                             : bytes <= kBottomSmemMax && head_nodes <= kBottomMaxHeadNodes;
+            if (depth <= kBottomMaxLevels && fits) {
                 b.h_heads.push_back(q);
                 b.h_head_root.push_back(r);
-                b.bottom_smem = std::max(b.bottom_smem, (int)bytes);
+                b.bottom_smem = bottom_cluster ? (576 + 800) * 4 : std::max(b.bottom_smem, (int)bytes);
                 for (int t = q; t >= 0; t = b.h_probs[t].coarse) b.h_probs[t].bottom = 1;
                 break;
             }
@@ -2707,15 +3136,46 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
             }
             const MfProblem &C = b.h_probs[c];
             const int64_t nd = 3LL * C.NX * C.NY * C.NZ;
-            if (nd <= kCoarseDirectMax && (floats + nd * nd) * 4 <= kBottomSmemMax) {
+            if (nd <= kCoarseDirectMax && (bottom_cluster || (floats + nd * nd) * 4 <= kBottomSmemMax)) {
                 b.h_coarse_off[h] = inv_floats;
                 inv_floats += nd * nd;
-                b.bottom_smem = std::max(b.bottom_smem, (int)((floats + nd * nd) * 4));
+                if (!bottom_cluster) b.bottom_smem = std::max(b.bottom_smem, (int)((floats + nd * nd) * 4));
             }
         }
         MG_TRY(dev_alloc_n(&b.coarse_off, std::max<size_t>(1, b.h_coarse_off.size())));
         MG_TRY(dev_alloc_n(&b.coarse_inv, (size_t)std::max<int64_t>(1, inv_floats)));
         MG_TRY(dev_alloc_n(&b.coarse_ok, std::max<size_t>(1, b.h_coarse_off.size())));
+    }
+    if (bottom_cluster && !b.h_heads.empty()) {
+        // the largest cluster (16 CTAs: non-portable size) the device can place
+        for (int cs = kClusterMax; cs >= 1 && !b.bottom_cluster; cs /= 2) {
+            std::vector<ClusterChain> chains;
+            const int64_t smem = cluster_layout(b, cs, chains);
+            if (smem > kBottomSmemMax) continue;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(cs);
+            cfg.blockDim = dim3(kClusterThreads);
+            cfg.dynamicSmemBytes = smem;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)cs;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int n = 0;
+            if (cudaOccupancyMaxActiveClusters(&n, mg_bottom_cluster_kernel, &cfg) == cudaSuccess && n >= 1) {
+                b.bottom_cluster = cs;
+                b.bottom_smem = (int)smem;
+                b.h_cl_chains.swap(chains);
+            }
+            else
+                cudaGetLastError();  // clear the failed query
+        }
+        if (!b.bottom_cluster) {
+            set_error("no thread-block cluster of the bottom kernel fits the device");
+            return MG_ECUDA;
+        }
     }
     b.apply_grid = std::max(1, std::min(nb, 2 * sms));  // FP64 residual: two CTAs per SM
     b.col_grid = std::max(1, std::min(b.n_cols, kColCtas * sms));  // column CTAs per SM
@@ -2805,6 +3265,21 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     }
     MG_CUDA_TRY(cudaMemcpyAsync(b.chunks, b.h_chunks.data(), b.h_chunks.size() * sizeof(MfChunkDesc), cudaMemcpyHostToDevice, s));
     MG_CUDA_TRY(cudaMemcpyAsync(b.K0, K0, 576 * 8, cudaMemcpyHostToDevice, s));
+    if (b.bottom_cluster) {
+        // K0 and its regrouped copy in FP32 (as mg_bottom_kernel forms them), the chains' level tables
+        std::vector<float> k0f(kClusterK0);
+        for (int i = 0; i < 576; i++) k0f[i] = (float)K0[i];
+        for (int i = 0; i < 800; i++) {
+            const int a = i / 100, t = i % 100, bc = t / 12, q = t % 12, r = q / 3, c = q % 3;
+            k0f[576 + i] = (t < 96 && q < 9) ? (float)K0[(3 * a + r) * 24 + 3 * bc + c] : 0.0f;
+        }
+        MG_TRY(dev_alloc_n(&b.cl_k0, (size_t)kClusterK0));
+        MG_TRY(dev_alloc_n(&b.cl_chains, b.h_cl_chains.size()));
+        MG_CUDA_TRY(cudaMemcpyAsync(b.cl_k0, k0f.data(), k0f.size() * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA_TRY(cudaMemcpyAsync(b.cl_chains, b.h_cl_chains.data(), b.h_cl_chains.size() * sizeof(ClusterChain),
+                                    cudaMemcpyHostToDevice, s));
+        MG_CUDA_TRY(cudaStreamSynchronize(s));  // k0f is a host temporary
+    }
     if (!b.h_coarse_off.empty()) {
         MG_CUDA_TRY(cudaMemcpyAsync(b.coarse_off, b.h_coarse_off.data(), b.h_coarse_off.size() * sizeof(int64_t),
                                     cudaMemcpyHostToDevice, s));
@@ -2835,7 +3310,7 @@ void mf_batch_free(MfBatch &b) {
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.K0, b.mb, b.mx, b.md,
                     b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles, b.fac_maps,
-                    b.coarse_off, b.coarse_inv, b.coarse_ok};
+                    b.coarse_off, b.coarse_inv, b.coarse_ok, b.cl_chains, b.cl_k0};
     for (void *q : ptrs) dev_free(q);
     if (b.stage_host) cudaFreeHost(b.stage_host);
     if (b.stage_ev) cudaEventDestroy(b.stage_ev);
@@ -3066,9 +3541,15 @@ long long enqueue_vcycle(MfBatch &b, bool fac, int prec, int sdeg, int cdeg) {
             bc.c1s[k] = cs.c1[k]; bc.c2s[k] = cs.c2[k];
             bc.c1c[k] = cc.c1[k]; bc.c2c[k] = cc.c2[k];
         }
-        launch_pdl(mg_bottom_kernel, (unsigned)b.h_heads.size(), kBottomThreads, b.bottom_smem, b.stream, 
-            b.probs, b.heads, b.states, b.E32, b.dinv, b.mb, b.mx, b.K0, bc, sdeg, cdeg, b.coarse_off,
-            b.coarse_inv, b.coarse_ok);
+        if (b.bottom_cluster)
+            launch_cluster_pdl(mg_bottom_cluster_kernel, (unsigned)(b.h_heads.size() * b.bottom_cluster),
+                               kClusterThreads, b.bottom_smem, b.bottom_cluster, b.stream, b.cl_chains, b.states,
+                               b.E32, b.dinv, b.mb, b.mx, b.cl_k0, bc, sdeg, cdeg, b.coarse_off, b.coarse_inv,
+                               b.coarse_ok);
+        else
+            launch_pdl(mg_bottom_kernel, (unsigned)b.h_heads.size(), kBottomThreads, b.bottom_smem, b.stream,
+                b.probs, b.heads, b.states, b.E32, b.dinv, b.mb, b.mx, b.K0, bc, sdeg, cdeg, b.coarse_off,
+                b.coarse_inv, b.coarse_ok);
         n += 1;
     }
     for (int l = L - 2; l >= 0; l--) {
@@ -3377,7 +3858,7 @@ int matfree_setup(mg_problem *p) {
     MfProblem P{};
     P.nx = nx; P.ny = ny; P.nz = nz;
     P.share_elems = -1;
-    int rc = mf_batch_init(w->batch, {P}, hx, hy, hz, p->mat.nu, p->stream);
+    int rc = mf_batch_init(w->batch, {P}, hx, hy, hz, p->mat.nu, p->stream, kMaxLevels, true);
     if (rc == MG_OK) {
         std::vector<uint8_t> nf(p->n_nodes, 0);
         for (int64_t n = 0; n < p->n_nodes; n++)

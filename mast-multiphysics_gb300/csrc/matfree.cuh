@@ -30,6 +30,20 @@ constexpr int kCX = 7;
 constexpr int kCY = 15;
 constexpr int kCZ = 32;   // most node planes per column
 constexpr int kMaxLevels = 8;                  // multigrid levels per design
+constexpr int kBottomMaxLevels = 6;            // levels of a bottom chain (one-CTA or cluster kernel)
+
+// level table of the cluster bottom kernel (one chain, one cluster)
+struct ClusterLevel {
+    int NX, NY, NZ, nx, ny, nz;
+    int pitch, pitch_e;
+    int64_t dof_off, elem_off;
+    int chunk;                // nodes per CTA (CTA r owns nodes [r chunk, (r + 1) chunk))
+    int s_dinv, s_E, s_vec;   // shared-memory offsets (floats): D^-1 and E of the level, the CTA's slabs
+};
+struct ClusterChain {
+    int m, root, s_stage, pad;
+    ClusterLevel L[kBottomMaxLevels];
+};
 
 // Padded vector layout of one problem: node (i,j,k), component c lives at
 //   dof_off + (k NY + j) pitch + 3 i + c,   pitch = roundup(3 NX, 4)
@@ -151,6 +165,10 @@ struct MfBatch {
     float *coarse_inv = nullptr;
     int *coarse_ok = nullptr;
     int bottom_smem = 0;        // dynamic shared memory of the bottom kernel
+    int bottom_cluster = 0;     // CTAs per chain of the cluster bottom kernel (0: one-CTA kernel)
+    std::vector<ClusterChain> h_cl_chains;  // its per-chain level tables
+    ClusterChain *cl_chains = nullptr;
+    float *cl_k0 = nullptr;     // K0 and its regrouped copy in FP32
     // FP64 refinement vectors (padded layout)
     double *u64 = nullptr, *r64 = nullptr, *f64 = nullptr;
     double *brick_part = nullptr, *chunk_part = nullptr;
@@ -191,9 +209,13 @@ struct MfSolveParams {
 void hex8_box_stiffness(double hx, double hy, double hz, double nu, double K[576]);
 
 // shapes: the designs' own grids (level 0); max_levels > 1 adds the coarse
-// multigrid levels of every design (coarsening while all dims stay even)
+// multigrid levels of every design (coarsening while all dims stay even);
+// bottom_cluster: each chain's bottom V-cycle on a thread-block cluster from a
+// larger level on (single-design solves; batches keep the one-CTA form, so a
+// design's preconditioner is the same in every batch)
 int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, double hy,
-                  double hz, double nu, cudaStream_t stream, int max_levels = kMaxLevels);
+                  double hz, double nu, cudaStream_t stream, int max_levels = kMaxLevels,
+                  bool bottom_cluster = false);
 void mf_batch_free(MfBatch &b);
 // per-problem Dirichlet mask (per node, bit c = component c fixed) and load (unpadded host)
 int mf_batch_set_bc(MfBatch &b, int i, const uint8_t *node_fix_host, const double *f_host);
