@@ -1840,16 +1840,29 @@ __device__ __forceinline__ unsigned cluster_nctarank() {
 __device__ __forceinline__ void cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
-// component c of node n of a vector whose slabs sit at `slab` in every CTA
-__device__ __forceinline__ float cl_get(const float *slab, int chunk, int n, int c, int rank) {
-    const int owner = n / chunk;
-    const float *p = slab + (n - owner * chunk) * 3 + c;
-    if (owner == rank) return *p;
-    uint32_t ra;
-    float v;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(p)), "r"(owner));
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(ra) : "memory");
-    return v;
+// generic address of p (this CTA's shared memory) in CTA `rank` of the cluster
+__device__ __forceinline__ const float *cl_map(const float *p, int rank) {
+    uint64_t r;
+    asm("mapa.u64 %0, %1, %2;" : "=l"(r) : "l"(reinterpret_cast<uint64_t>(p)), "r"(rank));
+    return reinterpret_cast<const float *>(r);
+}
+// n / d for the level's small divisors by one rounded product (exact for every n
+// of the level: the host checks each reciprocal against integer division)
+__device__ __forceinline__ int cl_div(int n, float r) {
+    return __float2int_rz(__fmul_rn(__fadd_rn(__int2float_rn(n), 0.5f), r));
+}
+__device__ __forceinline__ void cl_ijk(const ClusterLevel &L, int n, int &i, int &j, int &k) {
+    k = cl_div(n, L.rNXY);
+    const int rem = n - k * L.NXY;
+    j = cl_div(rem, L.rNX);
+    i = rem - j * L.NX;
+}
+// component c of node n of a vector whose slabs sit at `slab` in every CTA: a
+// plain load through the generic window, so that independent loads overlap
+__device__ __forceinline__ float cl_get(const float *slab, const ClusterLevel &L, int n, int c, int rank) {
+    const int owner = cl_div(n, L.rchunk);
+    const float *p = slab + (n - owner * L.chunk) * 3 + c;
+    return owner == rank ? *p : *cl_map(p, owner);
 }
 
 enum { kClX = 0, kClB, kClR, kClD, kClY };
@@ -1887,7 +1900,7 @@ __device__ void cl_step(const ClusterLevel &L, float *sm, const float *sK, float
         const int cnt = 3 * (min(nn - 1, n1 - 1 + H) - nlo + 1);
         for (int t = threadIdx.x; t < cnt; t += kClusterThreads) {
             const int n = nlo + t / 3, c = t - 3 * (t / 3);
-            const float v = cl_get(S.in, L.chunk, n, c, rank);
+            const float v = cl_get(S.in, L, n, c, rank);
             stage[t] = STEP == 1 ? dinvL[3 * n + c] * v * S.inv_theta : v;
         }
     }
@@ -1899,7 +1912,8 @@ __device__ void cl_step(const ClusterLevel &L, float *sm, const float *sK, float
         const int n = base + (threadIdx.x >> 3);
         float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
         if (n < n1) {
-            const int i = n % L.NX, j = (n / L.NX) % L.NY, k = n / (L.NX * L.NY);
+            int i, j, k;
+            cl_ijk(L, n, i, j, k);
             const int ex = i - dx, ey = j - dy, ez = k - dz;
             if (ex >= 0 && ey >= 0 && ez >= 0 && ex < L.nx && ey < L.ny && ez < L.nz) {
                 const float e = EL[ex + L.nx * (ey + L.ny * ez)];
@@ -2018,7 +2032,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
     const float *__restrict__ dinv, const float *__restrict__ mb, float *__restrict__ mx,
     const float *__restrict__ k0f, BottomCheb cc, int sdeg, int cdeg, const int64_t *__restrict__ coarse_off,
     const float *__restrict__ coarse_inv, const int *__restrict__ coarse_ok) {
-    pdl_enter();
+    // D^-1, the moduli and the coarse inverse were formed before this graph ran
+    // (activation); they are loaded while the preceding kernel finishes, the
+    // head's rhs and the solver state only after it
+    pdl_trigger();
     extern __shared__ __align__(16) float sm[];  // K0 tables, stage, per level: D^-1, E, slabs
     __shared__ ClusterChain sc;
     const int csize = (int)cluster_nctarank(), rank = (int)cluster_ctarank();
@@ -2030,8 +2047,6 @@ __global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
     }
     for (int i = threadIdx.x; i < kClusterK0; i += kClusterThreads) sm[i] = k0f[i];
     __syncthreads();
-    // the same state in every CTA of the cluster: all return, or none
-    if (states[sc.root].done) return;
     const int m = sc.m;
     const float *sK = sm;
     float *stage = sm + sc.s_stage;
@@ -2049,16 +2064,6 @@ __global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
             sm[L.s_E + e] = E32[L.elem_off + ((int64_t)ez * L.ny + ey) * L.pitch_e + ex];
         }
     }
-    const ClusterLevel &L0 = sc.L[0];
-    {
-        const int nn = L0.NX * L0.NY * L0.NZ, n0 = rank * L0.chunk, nown = max(0, min(nn, n0 + L0.chunk) - n0);
-        float *b0 = cl_slab(sm, L0, kClB);
-        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
-            const int n = n0 + q / 3, c = q - 3 * (q / 3);
-            const int i = n % L0.NX, j = (n / L0.NX) % L0.NY, k = n / (L0.NX * L0.NY);
-            b0[q] = mb[L0.dof_off + ((int64_t)k * L0.NY + j) * L0.pitch + 3 * i + c];
-        }
-    }
     // the direct solve's rows of this CTA (one warp per row), loaded now
     const ClusterLevel &Lc = sc.L[m - 1];
     const int64_t inv_off = coarse_ok[chain] ? coarse_off[chain] : -1;
@@ -2074,35 +2079,55 @@ __global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
                      ? __ldg(coarse_inv + inv_off + (int64_t)(3 * c0 + warp) * ndc + r)
                      : 0.0f;
     }
+    const ClusterLevel &L0 = sc.L[0];
+    pdl_wait();
+    // the same state in every CTA of the cluster: all return, or none
+    if (states[sc.root].done) return;
+    {
+        const int nn = L0.NX * L0.NY * L0.NZ, n0 = rank * L0.chunk, nown = max(0, min(nn, n0 + L0.chunk) - n0);
+        float *b0 = cl_slab(sm, L0, kClB);
+        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
+            const int n = n0 + q / 3, c = q - 3 * (q / 3);
+            int i, j, k;
+            cl_ijk(L0, n, i, j, k);
+            b0[q] = __ldcg(mb + L0.dof_off + ((int64_t)k * L0.NY + j) * L0.pitch + 3 * i + c);
+        }
+    }
     cluster_barrier();  // every CTA's tables and rhs are in place
     // down: smooth, residual, restrict
     for (int l = 0; l < m - 1; l++) {
         const ClusterLevel &F = sc.L[l], &C = sc.L[l + 1];
         cl_smooth(F, sm, sK, stage, cl_slab(sm, F, kClB), true, sdeg, cc.inv_theta_s, cc.c1s, cc.c2s, rank);
         cl_residual(F, sm, sK, stage, rank);
-        const int nnC = C.NX * C.NY * C.NZ, n0 = rank * C.chunk, nown = max(0, min(nnC, n0 + C.chunk) - n0);
+        // one warp per coarse node: lane t < 27 takes fine neighbour t (all three
+        // components), the weighted values meet in a fixed xor butterfly
+        const int nnC = C.NX * C.NY * C.NZ, n0 = rank * C.chunk, n1 = min(nnC, n0 + C.chunk);
         const float *rF = cl_slab(sm, F, kClR);
         float *bC = cl_slab(sm, C, kClB);
-        for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
-            const int n = n0 + q / 3, c = q - 3 * (q / 3);
-            const int I = n % C.NX, J = (n / C.NX) % C.NY, K = n / (C.NX * C.NY);
-            float out = 0.0f;
-            if (sm[C.s_dinv + 3 * n + c] != 0.0f)
-                for (int dz = -1; dz <= 1; dz++) {
-                    const int kk = 2 * K + dz;
-                    if (kk < 0 || kk >= F.NZ) continue;
-                    for (int dy = -1; dy <= 1; dy++) {
-                        const int jj = 2 * J + dy;
-                        if (jj < 0 || jj >= F.NY) continue;
-                        for (int dx = -1; dx <= 1; dx++) {
-                            const int ii = 2 * I + dx;
-                            if (ii < 0 || ii >= F.NX) continue;
-                            const float w = (dx ? 0.5f : 1.0f) * (dy ? 0.5f : 1.0f) * (dz ? 0.5f : 1.0f);
-                            out = fmaf(w, cl_get(rF, F.chunk, ii + F.NX * (jj + F.NY * kk), c, rank), out);
-                        }
-                    }
-                }
-            bC[q] = out;
+        const int warp_r = threadIdx.x >> 5, lane_r = threadIdx.x & 31;
+        for (int n = n0 + warp_r; n < n1; n += kClusterThreads / 32) {
+            int I, J, K;
+            cl_ijk(C, n, I, J, K);
+            const int dx = lane_r % 3 - 1, dy = (lane_r / 3) % 3 - 1, dz = lane_r / 9 - 1;
+            const int ii = 2 * I + dx, jj = 2 * J + dy, kk = 2 * K + dz;
+            float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+            if (lane_r < 27 && ii >= 0 && ii < F.NX && jj >= 0 && jj < F.NY && kk >= 0 && kk < F.NZ) {
+                const int nf = ii + F.NX * (jj + F.NY * kk);
+                const float w = (dz ? 0.5f : 1.0f) * (dy ? 0.5f : 1.0f) * (dx ? 0.5f : 1.0f);
+                v0 = w * cl_get(rF, F, nf, 0, rank);
+                v1 = w * cl_get(rF, F, nf, 1, rank);
+                v2 = w * cl_get(rF, F, nf, 2, rank);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                v0 += __shfl_xor_sync(0xffffffffu, v0, off);
+                v1 += __shfl_xor_sync(0xffffffffu, v1, off);
+                v2 += __shfl_xor_sync(0xffffffffu, v2, off);
+            }
+            if (lane_r < 3) {
+                const float v = lane_r == 0 ? v0 : (lane_r == 1 ? v1 : v2);
+                bC[3 * (n - n0) + lane_r] = sm[C.s_dinv + 3 * n + lane_r] != 0.0f ? v : 0.0f;
+            }
         }
         cluster_barrier();
     }
@@ -2121,7 +2146,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
                 const int r = lane + 32 * t;
                 if (r < ndc) {
                     const float a = w0 == 0 ? inv[t] : __ldg(coarse_inv + inv_off + (int64_t)(3 * c0 + w) * ndc + r);
-                    sacc = fmaf(a, cl_get(bc, Lc.chunk, r / 3, r - 3 * (r / 3), rank), sacc);
+                    sacc = fmaf(a, cl_get(bc, Lc, r / 3, r - 3 * (r / 3), rank), sacc);
                 }
             }
 #pragma unroll
@@ -2141,14 +2166,24 @@ __global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
         for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
             const int n = n0 + q / 3, c = q - 3 * (q / 3);
             if (sm[F.s_dinv + 3 * n + c] == 0.0f) continue;
-            const int ii = n % F.NX, jj = (n / F.NX) % F.NY, kk = n / (F.NX * F.NY);
-            const int Is[2] = {ii >> 1, (ii + 1) >> 1}, Js[2] = {jj >> 1, (jj + 1) >> 1}, Ks[2] = {kk >> 1, (kk + 1) >> 1};
+            int ii, jj, kk;
+            cl_ijk(F, n, ii, jj, kk);
             const float w = ((ii & 1) ? 0.5f : 1.0f) * ((jj & 1) ? 0.5f : 1.0f) * ((kk & 1) ? 0.5f : 1.0f);
+            // the 1, 2, 4 or 8 parents' loads first, then the sums in a fixed order
+            float v[8];
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int a = t >> 2, bb = (t >> 1) & 1, cc2 = t & 1;
+                const bool use = (a == 0 || (kk & 1)) && (bb == 0 || (jj & 1)) && (cc2 == 0 || (ii & 1));
+                v[t] = use ? cl_get(xC, C, ((ii + cc2) >> 1) + C.NX * (((jj + bb) >> 1) + C.NY * ((kk + a) >> 1)), c, rank)
+                           : 0.0f;
+            }
             float acc = 0.0f;
-            for (int a = 0; a < ((kk & 1) ? 2 : 1); a++)
-                for (int bb = 0; bb < ((jj & 1) ? 2 : 1); bb++)
-                    for (int cc2 = 0; cc2 < ((ii & 1) ? 2 : 1); cc2++)
-                        acc = fmaf(w, cl_get(xC, C.chunk, Is[cc2] + C.NX * (Js[bb] + C.NY * Ks[a]), c, rank), acc);
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int a = t >> 2, bb = (t >> 1) & 1, cc2 = t & 1;
+                if ((a == 0 || (kk & 1)) && (bb == 0 || (jj & 1)) && (cc2 == 0 || (ii & 1))) acc = fmaf(w, v[t], acc);
+            }
             xF[q] += acc;
         }
         cluster_barrier();
@@ -2162,7 +2197,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) mg_bottom_cluster_kernel(
         const float *x0 = cl_slab(sm, L0, kClX);
         for (int q = threadIdx.x; q < 3 * nown; q += kClusterThreads) {
             const int n = n0 + q / 3, c = q - 3 * (q / 3);
-            const int i = n % L0.NX, j = (n / L0.NX) % L0.NY, k = n / (L0.NX * L0.NY);
+            int i, j, k;
+            cl_ijk(L0, n, i, j, k);
             mx[L0.dof_off + ((int64_t)k * L0.NY + j) * L0.pitch + 3 * i + c] = x0[q];
         }
     }
@@ -2914,6 +2950,16 @@ int64_t cluster_layout(const MfBatch &b, int cs, std::vector<ClusterChain> &chai
             L.dof_off = T.dof_off; L.elem_off = T.elem_off;
             const int nn = T.NX * T.NY * T.NZ, H = T.NX * T.NY + T.NX + 1;
             L.chunk = (nn + cs - 1) / cs;
+            L.NXY = T.NX * T.NY;
+            L.rNX = 1.0f / (float)T.NX;
+            L.rNXY = 1.0f / (float)L.NXY;
+            L.rchunk = 1.0f / (float)L.chunk;
+            // the device divides by one rounded product: check it for every node
+            auto fdiv = [](int n, float r) { return (int)(((float)n + 0.5f) * r); };
+            for (int n = 0; n < nn; n++)
+                if (fdiv(n, L.rNXY) != n / L.NXY || fdiv(n, L.rchunk) != n / L.chunk ||
+                    (n < L.NXY && fdiv(n, L.rNX) != n / T.NX))
+                    return -1;
             for (int r = 0; r < cs; r++) {
                 const int n0 = r * L.chunk, n1 = std::min(nn, n0 + L.chunk);
                 if (n0 < n1) stage = std::max<int64_t>(stage, 3LL * (std::min(nn - 1, n1 - 1 + H) - std::max(0, n0 - H) + 1));
@@ -3151,7 +3197,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
         for (int cs = kClusterMax; cs >= 1 && !b.bottom_cluster; cs /= 2) {
             std::vector<ClusterChain> chains;
             const int64_t smem = cluster_layout(b, cs, chains);
-            if (smem > kBottomSmemMax) continue;
+            if (smem < 0 || smem > kBottomSmemMax) continue;
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(cs);
             cfg.blockDim = dim3(kClusterThreads);

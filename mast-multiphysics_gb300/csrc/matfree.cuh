@@ -39,6 +39,8 @@ struct ClusterLevel {
     int64_t dof_off, elem_off;
     int chunk;                // nodes per CTA (CTA r owns nodes [r chunk, (r + 1) chunk))
     int s_dinv, s_E, s_vec;   // shared-memory offsets (floats): D^-1 and E of the level, the CTA's slabs
+    int NXY;                  // NX NY
+    float rNX, rNXY, rchunk;  // 1 / NX, 1 / NXY, 1 / chunk: n / d = trunc((n + 1/2) (1 / d)) (checked on the host)
 };
 struct ClusterChain {
     int m, root, s_stage, pad;
