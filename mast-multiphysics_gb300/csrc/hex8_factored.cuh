@@ -150,10 +150,10 @@ __device__ __forceinline__ T zero_t() { return T(0); }
 template <>
 __device__ __forceinline__ dfloat zero_t<dfloat>() { return df_zero(); }
 
-// v[c][b]: component c at lexicographic corner b; on return e * (K0 u_e) in the
-// same layout.  Fixed operation order (deterministic).
+// v[c][b]: component c at lexicographic corner b; on return its sum/difference
+// modes u~ = H^T u (per component, the 8-point Walsh-Hadamard butterfly)
 template <typename T>
-__device__ __forceinline__ void hex8_factored_apply(const FacK<T> &K, T e, T (&v)[3][8]) {
+__device__ __forceinline__ void hex8_factored_forward(T (&v)[3][8]) {
 #pragma unroll
     for (int c = 0; c < 3; c++)
 #pragma unroll
@@ -165,7 +165,13 @@ __device__ __forceinline__ void hex8_factored_apply(const FacK<T> &K, T e, T (&v
                     v[c][b] = lo + hi;
                     v[c][b | t] = hi - lo;
                 }
-    T yh[3][8];
+}
+
+// yh[c][m] = (Khat / 64 u~)[c][m] for the modes m = 1..7 (mode 0, the rigid
+// translation, is in the kernel: yh[c][0] is not set).  u_e^T K0 u_e equals the
+// sum over c, m of u~[c][m] yh[c][m].
+template <typename T>
+__device__ __forceinline__ void hex8_factored_khat(const FacK<T> &K, const T (&v)[3][8], T (&yh)[3][8]) {
     yh[0][1] = K.v[0] * v[0][1];
     yh[0][1] = fma_t(K.v[1], v[1][2], yh[0][1]);
     yh[0][1] = fma_t(K.v[2], v[2][4], yh[0][1]);
@@ -211,6 +217,15 @@ __device__ __forceinline__ void hex8_factored_apply(const FacK<T> &K, T e, T (&v
     yh[2][6] = K.v[42] * v[0][3];
     yh[2][6] = fma_t(K.v[43], v[2][6], yh[2][6]);
     yh[2][7] = K.v[44] * v[2][7];
+}
+
+// v[c][b]: component c at lexicographic corner b; on return e * (K0 u_e) in the
+// same layout.  Fixed operation order (deterministic).
+template <typename T>
+__device__ __forceinline__ void hex8_factored_apply(const FacK<T> &K, T e, T (&v)[3][8]) {
+    hex8_factored_forward(v);
+    T yh[3][8];
+    hex8_factored_khat(K, v, yh);
     // back to the corners: the transpose butterflies, mode 0 is zero
 #pragma unroll
     for (int c = 0; c < 3; c++) {

@@ -177,6 +177,7 @@ struct MfBatch {
     int *err = nullptr;
     int *diag_list = nullptr;  // problem list of a partial Jacobi update, then its direct chains
     int *stage_host = nullptr;  // pinned staging of diag_list
+    int64_t *sens_offs = nullptr, *sens_offs_host = nullptr;  // dC/drho output offsets (device, pinned)
     cudaEvent_t stage_ev = nullptr;  // its last copy
     bool stage_pending = false;
     // operator data
