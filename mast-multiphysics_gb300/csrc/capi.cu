@@ -659,7 +659,7 @@ int mg_solve(mg_problem *p, const mg_solve_opts *opts, double *X, mg_solve_repor
                  : solve_linear(p, o, &r);
     } else {
         if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) { set_error("mixed precision needs the linear-strain HEX8 SIMP form"); return MG_ENOTSUP; }
-        rc = matfree_solve(p, o, &r);
+        rc = matfree_solve(p, o, &r, !o.warm_start && !X);
     }
     p->last_solve_mixed = (o.precision != MG_PLAIN_FP64);
     if (X && (rc == MG_OK || rc == MG_ENOCONV)) {

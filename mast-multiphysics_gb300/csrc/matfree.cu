@@ -3928,12 +3928,14 @@ int matfree_setup(mg_problem *p) {
 
 }  // namespace
 
-int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
+int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep, bool x_zero) {
     MG_TRY(matfree_setup(p));
     MfBatch &b = p->mf->batch;
     MG_TRY(mf_batch_set_moduli(b, 0, p->d_E, p->d_dE));
-    MG_TRY(mf_batch_set_u(b, 0, p->d_X));
-    count_launches(1);
+    if (!x_zero) {
+        MG_TRY(mf_batch_set_u(b, 0, p->d_X));
+        count_launches(1);
+    }
     MfSolveParams prm;
     prm.precision = o.precision;
     prm.rtol = o.rtol;
@@ -3947,7 +3949,8 @@ int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep) {
     prm.coarse_deg = o.coarse_degree;
     prm.vec_blocks_per_sm = o.vec_blocks_per_sm;
     prm.mg_operator = o.smoother_operator == MG_SMOOTHER_TENSOR ? 1 : 0;
-    int rc = mf_batch_solve(b, prm, true);
+    // from 0 (activation clears u): the first residual is f without an operator pass
+    int rc = mf_batch_solve(b, prm, !x_zero);
     MG_TRY(mf_batch_get_u(b, 0, p->d_X));
     count_launches(1);
     MG_CUDA_TRY(cudaStreamSynchronize(p->stream));

@@ -168,7 +168,8 @@ int transpose_csr(mg_problem *p, const CsrMatrix &A, CsrMatrix *At);
 void free_csr(CsrMatrix *A);
 
 // ---- matfree.cu ----
-int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep);
+// x_zero: the initial guess is 0 (the first refinement residual is f, no operator pass)
+int matfree_solve(mg_problem *p, const mg_solve_opts &o, mg_solve_report *rep, bool x_zero);
 int matfree_apply_debug(mg_problem *p, int precision, const double *x_host, double *y_host);
 int matfree_sensitivity(mg_problem *p, double *dc_host);
 int matfree_compliance_resident(mg_problem *p, double *compliance);
