@@ -1700,6 +1700,7 @@ __global__ void __launch_bounds__(kCoarseInvThreads, 1) mg_coarse_inverse_kernel
     float *sE = sK + 576;         // the level's moduli
     float *sv = sE + kCoarseMaxElems;  // pivot rows, double-buffered (2 x NP)
     int *sfix = reinterpret_cast<int *>(sv + 2 * NP);
+    __shared__ float s_rcp[2];         // 1 / pivot of each buffered row, formed once by its writer
     const int h = list[blockIdx.x];
     const int64_t off = coarse_off[h];
     if (off < 0) return;
@@ -1759,6 +1760,7 @@ __global__ void __launch_bounds__(kCoarseInvThreads, 1) mg_coarse_inverse_kernel
     if (ti == 0)
 #pragma unroll
         for (int cc = 0; cc < T; cc++) sv[j0 + cc] = a[0][cc];
+    if (tid == 0) s_rcp[0] = 1.0f / a[0][0];
     __syncthreads();
     int ok = 1, cur = 0;
     for (int k = 0; k < nd; k++) {
@@ -1768,7 +1770,7 @@ __global__ void __launch_bounds__(kCoarseInvThreads, 1) mg_coarse_inverse_kernel
             ok = 0;
             break;
         }
-        const float p = 1.0f / d;
+        const float p = s_rcp[cur];
         float vi[T], vj[T];
 #pragma unroll
         for (int r = 0; r < T; r++) {
@@ -1780,21 +1782,34 @@ __global__ void __launch_bounds__(kCoarseInvThreads, 1) mg_coarse_inverse_kernel
 #pragma unroll
             for (int cc = 0; cc < T; cc++) a[r][cc] = fmaf(-(vi[r] * vj[cc]), p, a[r][cc]);
         const int kr = k - i0, kc = k - j0;
-        if ((unsigned)kr < (unsigned)T || (unsigned)kc < (unsigned)T) {
+        // row and column k: a_kj = v_j / d, a_ik = v_i / d, a_kk = -1 / d
+        if ((unsigned)kr < (unsigned)T) {
 #pragma unroll
             for (int r = 0; r < T; r++)
+                if (r == kr)
 #pragma unroll
-                for (int cc = 0; cc < T; cc++)
-                    if (r == kr || cc == kc) a[r][cc] = (r == kr && cc == kc) ? -p : (r == kr ? vj[cc] : vi[r]) * p;
+                    for (int cc = 0; cc < T; cc++) a[r][cc] = cc == kc ? -p : vj[cc] * p;
         }
-        const int nr = k + 1 - i0;  // the next pivot row
+        if ((unsigned)kc < (unsigned)T) {
+#pragma unroll
+            for (int cc = 0; cc < T; cc++)
+                if (cc == kc)
+#pragma unroll
+                    for (int r = 0; r < T; r++)
+                        if (r != kr) a[r][cc] = vi[r] * p;
+        }
+        const int nr = k + 1 - i0;  // the next pivot row (and its reciprocal pivot)
         if ((unsigned)nr < (unsigned)T) {
             float *vn = sv + (cur ^ 1) * NP;
+            const int nc = k + 1 - j0;
 #pragma unroll
             for (int r = 0; r < T; r++)
                 if (r == nr)
 #pragma unroll
-                    for (int cc = 0; cc < T; cc++) vn[j0 + cc] = a[r][cc];
+                    for (int cc = 0; cc < T; cc++) {
+                        vn[j0 + cc] = a[r][cc];
+                        if (cc == nc) s_rcp[cur ^ 1] = 1.0f / a[r][cc];
+                    }
         }
         __syncthreads();
         cur ^= 1;

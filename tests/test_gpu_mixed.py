@@ -178,3 +178,33 @@ def test_outer_residual_matches_the_fp64_csr_residual():
     true_relres = np.linalg.norm(R) / np.linalg.norm(F)
     assert rep.status == 0 and rep.relres <= 1e-8
     assert abs(rep.relres - true_relres) <= 1e-11, (rep.relres, true_relres)
+
+
+@pytest.mark.parametrize("shape", [(32, 16, 16), (20, 10, 10)])
+def test_cluster_bottom_vcycle_matches_the_one_cta_form(shape):
+    """A single-design solve runs the small multigrid levels on a thread-block
+    cluster (from the first level below the design with at most 4,096 nodes: the
+    whole chain 16x8x8 .. 4x2x2 of the 32x16x16 design); a batch runs them in one
+    CTA from the first level with at most 1,024 nodes and the rest level by level.
+    Both are the same V-cycle up to FP32 rounding: the same iteration count within
+    one, and results that match each other and the FP64 oracle.  (20x10x10 has a
+    single coarse level, 10x5x5, smoothed rather than solved directly.)"""
+    nx, ny, nz = shape
+    rho = np.random.default_rng(11).uniform(0.01, 1.0, nx * ny * nz)
+    o = M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8, inner_rtol=1e-3, timeout_s=300.0)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design(rho)
+        _, rep = p.solve(o)
+        c, dc = p.compliance()
+    with M.Batch([dict(nx=nx, ny=ny, nz=nz, rho=rho, spans=[(0, ny)])]) as b:
+        rc, reps = b.solve(o)
+        cb, dcb, _ = b.results(0)
+    assert rep.status == 0 and rep.relres <= 1e-8
+    assert rc == 0 and reps[0].status == 0 and reps[0].relres <= 1e-8
+    assert abs(rep.krylov_iterations - reps[0].krylov_iterations) <= 1, \
+        (rep.krylov_iterations, reps[0].krylov_iterations)
+    assert abs(c - cb[0]) / abs(cb[0]) < 1e-8
+    assert np.abs(dc - dcb[0]).max() / np.abs(dcb[0]).max() < 1e-7
+    _, dc_ref, r = O.simp_solve(O.simp_desc(nx, ny, nz, rtol=1e-12, maxit=10 ** 6), rho)
+    assert abs(c - r.compliance) / r.compliance < 1e-6
+    assert np.abs(dc - dc_ref).max() / np.abs(dc_ref).max() < 1e-6
