@@ -139,6 +139,36 @@ __device__ __forceinline__ dfloat df_from(double x) {
     return r;
 }
 __device__ __forceinline__ double df_to(dfloat a) { return (double)a.hi + (double)a.lo; }
+// df_from by integer operations on the bits of x (the FP64 pipe stays free):
+// hi = x rounded to nearest even at 24 bits, lo = x - hi (exact) rounded to
+// nearest, the same pair as df_from.  Zeros give (0, 0); magnitudes outside
+// [2^-74, 2^100) (where lo would not be a normal float) take df_from.
+__device__ __forceinline__ dfloat df_split(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    dfloat r;
+    if ((b << 1) == 0ull) {
+        r.hi = 0.0f;
+        r.lo = 0.0f;
+        return r;
+    }
+    const int e = (int)((b >> 52) & 0x7FFull);
+    if (e < 949 || e > 1122) return df_from(x);
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);  // x = m 2^(e - 1075)
+    unsigned long long q = m >> 29;
+    const unsigned long long rem = m & ((1ull << 29) - 1ull);
+    if (rem > (1ull << 28) || (rem == (1ull << 28) && (q & 1ull))) q++;
+    const int d = (int)((long long)m - (long long)(q << 29));  // (x - hi) / 2^(e - 1075), |d| <= 2^28
+    unsigned eh = (unsigned)(e - 1023 + 127), qh = (unsigned)q;
+    if (qh == (1u << 24)) {
+        qh >>= 1;
+        eh += 1;
+    }
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    r.hi = __uint_as_float(sign | (eh << 23) | (qh & 0x7FFFFFu));
+    // 2^(e - 1075) is a normal float for e >= 949; d to float rounds once, the scaling is exact
+    r.lo = __fmul_rn(__int2float_rn(sign ? -d : d), __uint_as_float((unsigned)(e - 1075 + 127) << 23));
+    return r;
+}
 __device__ __forceinline__ dfloat df_zero() {
     dfloat r;
     r.hi = 0.0f;

@@ -2339,7 +2339,7 @@ static_assert(kBE % 3 == 0 && kRGroupEl <= kThreads, "one element per thread and
 
 __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
     const MfProblem *__restrict__ probs, const MfBrick *__restrict__ bricks, int n_bricks,
-    const double *__restrict__ E64, const uint8_t *__restrict__ node_fix,
+    const dfloat *__restrict__ Edf, const uint8_t *__restrict__ node_fix,
     const double *__restrict__ u64, const double *__restrict__ f64, const FacK<dfloat> K,
     double *__restrict__ r64, MfState *states, double *__restrict__ brick_part, double rtol2,
     int max_ref) {
@@ -2368,15 +2368,15 @@ __global__ void __launch_bounds__(kThreads) mf_residual64_kernel(
                 const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
                 if (!((node_fix[P.node_off + gn] >> c) & 1)) v = u64[dof_index(P, gx, gy, gz, c)];
             }
-            su[i] = df_from(v);
+            su[i] = df_split(v);
         }
         for (int l = threadIdx.x; l < (u_zero ? 0 : kNEL); l += kThreads) {
             const int ex = l % kBE, ey = (l / kBE) % kBE, ez = l / (kBE * kBE);
             const int gx = gx0 - 1 + ex, gy = gy0 - 1 + ey, gz = gz0 - 1 + ez;
-            double e = 0.0;
+            dfloat e = df_zero();
             if (gx >= 0 && gx < P.nx && gy >= 0 && gy < P.ny && gz >= 0 && gz < P.nz)
-                e = E64[P.elem_off + ((int64_t)gz * P.ny + gy) * P.pitch_e + gx];
-            sE[l] = df_from(e);
+                e = Edf[P.elem_off + ((int64_t)gz * P.ny + gy) * P.pitch_e + gx];
+            sE[l] = e;
         }
         dfloat acc[kRNodesPerThread][3];
 #pragma unroll
@@ -2564,10 +2564,11 @@ __global__ void mf_dot_chunks_kernel(const MfChunkDesc *__restrict__ chunks, int
     }
 }
 
-// unpadded element array (x-fastest) -> padded FP32 / FP64 tables of problem P
+// unpadded element array (x-fastest) -> padded FP32, double-float (the outer
+// residual's moduli) and FP64 (dE/drho) tables of problem P
 __global__ void pack_elems_kernel(const MfProblem *__restrict__ probs, int pi,
                                   const double *__restrict__ E, const double *__restrict__ dE,
-                                  float *__restrict__ E32, double *__restrict__ E64,
+                                  float *__restrict__ E32, dfloat *__restrict__ Edf,
                                   double *__restrict__ dE64) {
     const MfProblem P = probs[pi];
     const int64_t ne = (int64_t)P.nx * P.ny * P.nz;
@@ -2576,7 +2577,7 @@ __global__ void pack_elems_kernel(const MfProblem *__restrict__ probs, int pi,
         const int64_t ex = e % P.nx, row = e / P.nx;
         const int64_t o = P.elem_off + row * P.pitch_e + ex;
         if (E) {
-            E64[o] = E[e];
+            Edf[o] = df_from(E[e]);
             E32[o] = (float)E[e];
         }
         if (dE) dE64[o] = dE[e];
@@ -3258,7 +3259,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_TRY(dev_alloc_n(&b.fac_maps, (size_t)b.n_probs * kFacMaps));
     MG_CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&b.states_host), b.n_probs * sizeof(MfState)));
     MG_TRY(dev_alloc_n(&b.E32, (size_t)el + 4));
-    MG_TRY(dev_alloc_n(&b.E64, (size_t)el + 4));
+    MG_TRY(dev_alloc_n(&b.Edf, (size_t)el + 4));
     MG_TRY(dev_alloc_n(&b.dE64, (size_t)el + 4));
     MG_TRY(dev_alloc_n(&b.node_fix, (size_t)nd));
     float **f32s[] = {&b.x, &b.r, &b.z, &b.p0, &b.p1, &b.q, &b.dinv, &b.xdbg,
@@ -3362,7 +3363,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     MG_CUDA_TRY(cudaMemsetAsync(b.f64, 0, dof * 8, s));
     MG_CUDA_TRY(cudaMemsetAsync(b.node_fix, 0, nd, s));
     MG_CUDA_TRY(cudaMemsetAsync(b.E32, 0, (el + 4) * 4, s));
-    MG_CUDA_TRY(cudaMemsetAsync(b.E64, 0, (el + 4) * 8, s));
+    MG_CUDA_TRY(cudaMemsetAsync(b.Edf, 0, (el + 4) * sizeof(dfloat), s));
     MG_CUDA_TRY(cudaMemsetAsync(b.dE64, 0, (el + 4) * 8, s));
     float *zero_vecs[] = {b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.mb, b.mx, b.md, b.my, b.mr};
     for (float *v : zero_vecs) MG_CUDA_TRY(cudaMemsetAsync(v, 0, dof * 4, s));
@@ -3373,7 +3374,7 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
 void mf_batch_free(MfBatch &b) {
     if (b.stream) cudaStreamSynchronize(b.stream);
     if (b.graph) cudaGraphExecDestroy(b.graph);
-    void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.E64, b.dE64,
+    void *ptrs[] = {b.probs, b.bricks, b.chunks, b.states, b.tmaps, b.E32, b.Edf, b.dE64,
                     b.node_fix, b.x, b.r, b.z, b.p0, b.p1, b.q, b.dinv, b.xdbg, b.u64, b.r64,
                     b.f64, b.brick_part, b.chunk_part, b.err, b.K0, b.mb, b.mx, b.md,
                     b.my, b.mr, b.diag_list, b.heads, b.cols, b.col_part, b.Bop2, b.fac_tiles, b.fac_maps,
@@ -3426,7 +3427,7 @@ int mf_batch_set_moduli(MfBatch &b, int i, const double *E_dev, const double *dE
     const MfProblem &P = b.h_probs[i];
     const int64_t ne = (int64_t)P.nx * P.ny * P.nz;
     pack_elems_kernel<<<std::min(blocks_for(ne, 256), 4096u), 256, 0, b.stream>>>(
-        b.probs, i, E_dev, dE_dev, b.E32, b.E64, b.dE64);
+        b.probs, i, E_dev, dE_dev, b.E32, b.Edf, b.dE64);
     MG_CUDA_TRY(cudaGetLastError());
     count_launches(1);
     if (E_dev)
@@ -3649,7 +3650,7 @@ long long enqueue_step(MfBatch &b, const MfSolveParams &prm, int parity) {
     const int maxit = prm.max_iterations > 0 ? prm.max_iterations : 100000;
     const int max_ref = prm.max_refinements > 0 ? prm.max_refinements : 30;
     launch_pdl(mf_residual64_kernel, std::max(1, std::min(nb0, b.apply_grid)), kThreads, kResidSmem, s, 
-        b.probs, b.bricks, nb0, b.E64, b.node_fix, b.u64, b.f64, b.facdf, b.r64, b.states,
+        b.probs, b.bricks, nb0, b.Edf, b.node_fix, b.u64, b.f64, b.facdf, b.r64, b.states,
         b.brick_part, prm.rtol * prm.rtol, max_ref);
     launch_pdl(mf_inner_init_kernel, vg0, kThreads, 0, s, 
         b.chunks, n0, b.probs, b.r64, b.x, b.r, b.z, b.p0, b.p1, b.dinv, b.states, b.chunk_part,

@@ -58,7 +58,7 @@ struct MfProblem {
     int64_t n_dofs;       // 3 NX NY NZ
     int64_t n_pad;        // pitch NY NZ
     int64_t dof_off;      // offset into the concatenated padded dof vectors
-    int64_t elem_off;     // offset into the padded element tables (E32, E64, dE64)
+    int64_t elem_off;     // offset into the padded element tables (E32, Edf, dE64)
     int64_t node_off;     // offset into the node Dirichlet masks (unpadded)
     int brick_begin, brick_count;
     int chunk_begin, chunk_count;
@@ -142,7 +142,8 @@ struct MfBatch {
     CUtensorMap *tmaps = nullptr;    // kMapsPerProblem per problem
     // element / node tables
     float *E32 = nullptr;
-    double *E64 = nullptr, *dE64 = nullptr;
+    dfloat *Edf = nullptr;      // the moduli as double-float pairs (the outer residual)
+    double *dE64 = nullptr;
     uint8_t *node_fix = nullptr;
     // FP32 inner CG vectors (padded layout)
     float *x = nullptr, *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr,
