@@ -195,6 +195,16 @@ int mg_set_side_loads(mg_problem *p, int64_t n, const int32_t *elems, const int3
 /* ---- design / properties ---- */
 int mg_set_design(mg_problem *p, const double *rho_elem);
 int mg_set_design_device(mg_problem *p, const double *rho_elem_device);
+/* Nodal SIMP density field, n_nodes values in [0,1]: the design of MAST example 6,
+   a FIRST-order LAGRANGE "rho" read through MeshFieldFunction
+   (examples/structural/example_6/example_6.cpp:104-137, 250-252; MeshFieldFunction,
+   src/base/mesh_field_function.cpp:205-350).  The modulus is evaluated at each
+   Gauss point from the trilinear field there, E = E0 (rmin + (1 - rmin) rho^p);
+   mg_compliance then returns dC/drho per node (n_nodes values).  Linear-strain HEX8
+   on the plain FP64 path: the mixed-precision solve, the KS stress output and the
+   per-element sensitivity entry points answer MG_ENOTSUP while a nodal field is
+   set (mg_set_design goes back to element densities). */
+int mg_set_design_nodal(mg_problem *p, const double *rho_nodes);
 int mg_set_elem_scale(mg_problem *p, const double *s_elem);
 
 /* ---- assembly (plain FP64) ---- */
@@ -213,7 +223,8 @@ const double *mg_solution_device(mg_problem *p);
 int mg_sensitivity_assemble(mg_problem *p, const double *X, int32_t param_kind,
                             int64_t param_index, double *dRdp);
 /* compliance C = F.X; dc_drho (nullable) by the adjoint: lambda = -X for the linear
-   form, K_T(X) lambda = F on the GPU for MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR */
+   form, K_T(X) lambda = F on the GPU for MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR; one value
+   per element, or per node after mg_set_design_nodal */
 int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc_drho);
 /* KS-aggregated von Mises stress over every element (KSStressStrainOutput,
    ks_stress_output.cpp:41-99) at X (host, nullable: the resident solution):

@@ -89,7 +89,7 @@ template <int MODE>
 __global__ void __launch_bounds__(256) hex8_kernel(
     const double *__restrict__ coords, const int32_t *__restrict__ conn,
     const int32_t *__restrict__ elem_list, int64_t first, int64_t n_items,
-    const double *__restrict__ E_elem, double lam1, double mu1,
+    const double *__restrict__ E_elem, const double *__restrict__ E_qp, double lam1, double mu1,
     const int32_t *__restrict__ rowptr, const uint16_t *__restrict__ emap,
     double *__restrict__ vals, double *__restrict__ Ke_out,
     const double *__restrict__ va, const double *__restrict__ vb,
@@ -153,7 +153,8 @@ __global__ void __launch_bounds__(256) hex8_kernel(
             double S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
             for (int qq = 0; qq < 8; qq++) {
-                const double wq = sh_w[w][qq];
+                // a nodal density field gives the modulus per Gauss point (E_qp), else per element
+                const double wq = E_qp ? sh_w[w][qq] * E_qp[e * 8 + qq] : sh_w[w][qq];
                 double ga[3], gb[3];
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(256) hex8_kernel(
 #pragma unroll
                     for (int j = 0; j < 3; j++) S[i * 3 + j] = fma(ga[i], gb[j], S[i * 3 + j]);
             }
-            const double Ee = (MODE == 2) ? 1.0 : E_elem[e];
+            const double Ee = (MODE == 2 || E_qp) ? 1.0 : E_elem[e];
             const double lam = Ee * lam1, mu = Ee * mu1, tr = S[0] + S[4] + S[8];
             double K[9];
 #pragma unroll
@@ -729,6 +730,136 @@ __global__ void simp_modulus_kernel(const double *__restrict__ rho, int64_t n, d
     dE[e] = E0 * (1.0 - rmin) * penal * rp1;
 }
 
+// SIMP modulus of a nodal density field (the MeshFieldFunction "rho" of
+// example_6.cpp:104-137 over FIRST-order LAGRANGE, :250-252): rho at Gauss point
+// q of element e is sum_a N_a(x_q) rho_a (the trilinear shape functions, the same
+// points as the element kernels), E_q = E0 (rmin + (1 - rmin) rho_q^p), dE_q/drho_q.
+// One thread per (element, point); rho_a outside [0, 1] or NaN sets status bit 4.
+__global__ void simp_nodal_modulus_kernel(const int32_t *__restrict__ conn, const double *__restrict__ rho,
+                                          int64_t n_elems, double E0, double rmin, double penal,
+                                          double *__restrict__ Eq, double *__restrict__ dEq,
+                                          int *__restrict__ status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_elems * 8) return;
+    const int64_t e = t >> 3;
+    const int q = (int)(t & 7);
+    const double xi = gauss_coord(q & 1), eta = gauss_coord(q >> 1 & 1), zeta = gauss_coord(q >> 2 & 1);
+    double r = 0.0;
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+        double sx, sy, sz;
+        hex8_sign(a, sx, sy, sz);
+        const double ra = rho[conn[e * 8 + a]];
+        if (!(ra >= 0.0 && ra <= 1.0)) atomicOr(status, 4);
+        r = fma(0.125 * (1.0 + sx * xi) * (1.0 + sy * eta) * (1.0 + sz * zeta), ra, r);
+    }
+    double rp, rp1;
+    const int ip = (int)penal;
+    if ((double)ip == penal && ip >= 1 && ip <= 8) {
+        rp1 = 1.0;
+        for (int k = 1; k < ip; k++) rp1 *= r;
+        rp = rp1 * r;
+    } else {
+        rp = pow(r, penal);
+        rp1 = pow(r, penal - 1.0);
+    }
+    Eq[t] = E0 * (rmin + (1.0 - rmin) * rp);
+    dEq[t] = E0 * (1.0 - rmin) * penal * rp1;
+}
+
+// Strain energy at each Gauss point at unit modulus, times dE_q/drho_q:
+// out[8 e + q] = dE_q det J_q (lam1 tr(eps)^2 + 2 mu1 eps : eps), eps the linear strain
+// of u at point q (unit Gauss weights; constrained dofs read as 0).  One warp per
+// element, lanes 0-7 one point each.
+__global__ void __launch_bounds__(256) hex8_qp_energy_kernel(
+    const double *__restrict__ coords, const int32_t *__restrict__ conn, int64_t n_elems,
+    const double *__restrict__ dEq, double lam1, double mu1, const double *__restrict__ u,
+    const uint8_t *__restrict__ fixed, double *__restrict__ out) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    for (int64_t e = (int64_t)blockIdx.x * kWarpsPerBlock + w; e < n_elems; e += (int64_t)gridDim.x * kWarpsPerBlock) {
+        const int32_t *en = conn + e * 8;
+        double xv = 0.0, uv = 0.0;
+        if (lane < 24) {
+            const int64_t g = (int64_t)en[lane / 3] * 3 + lane % 3;
+            xv = coords[g];
+            uv = (fixed && fixed[g]) ? 0.0 : u[g];
+        }
+        const int q = lane & 7;
+        double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            double d[3];
+            hex8_dref(q, a, d);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const double x = __shfl_sync(full, xv, a * 3 + j);
+#pragma unroll
+                for (int i = 0; i < 3; i++) J[i * 3 + j] = fma(d[i], x, J[i * 3 + j]);
+            }
+        }
+        const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                           J[2] * (J[3] * J[7] - J[4] * J[6]);
+        double inv[9];
+        inv[0] = (J[4] * J[8] - J[5] * J[7]) / det;
+        inv[1] = (J[2] * J[7] - J[1] * J[8]) / det;
+        inv[2] = (J[1] * J[5] - J[2] * J[4]) / det;
+        inv[3] = (J[5] * J[6] - J[3] * J[8]) / det;
+        inv[4] = (J[0] * J[8] - J[2] * J[6]) / det;
+        inv[5] = (J[2] * J[3] - J[0] * J[5]) / det;
+        inv[6] = (J[3] * J[7] - J[4] * J[6]) / det;
+        inv[7] = (J[1] * J[6] - J[0] * J[7]) / det;
+        inv[8] = (J[0] * J[4] - J[1] * J[3]) / det;
+        double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // H[i][j] = d u_i / d x_j
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            double d[3];
+            hex8_dref(q, a, d);
+            double g[3];
+#pragma unroll
+            for (int j = 0; j < 3; j++) g[j] = inv[j * 3] * d[0] + inv[j * 3 + 1] * d[1] + inv[j * 3 + 2] * d[2];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const double ua = __shfl_sync(full, uv, a * 3 + i);
+#pragma unroll
+                for (int j = 0; j < 3; j++) H[i * 3 + j] = fma(ua, g[j], H[i * 3 + j]);
+            }
+        }
+        const double tr = H[0] + H[4] + H[8];
+        double ee = 0.0;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const double eij = 0.5 * (H[i * 3 + j] + H[j * 3 + i]);
+                ee = fma(eij, eij, ee);
+            }
+        if (lane < 8) out[e * 8 + q] = dEq[e * 8 + q] * det * (lam1 * tr * tr + 2.0 * mu1 * ee);
+    }
+}
+
+// dc[n] = -sum over the (element, corner) incidences of node n, in element order,
+// of sum_q N_corner(x_q) out[8 e + q]
+__global__ void nodal_gather_kernel(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                    int64_t n_nodes, const double *__restrict__ out,
+                                    double *__restrict__ dc) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= n_nodes) return;
+    double s = 0.0;
+    for (int32_t k = ptr[n]; k < ptr[n + 1]; k++) {
+        const int64_t e = inc[k] >> 3;
+        const int a = inc[k] & 7;
+        double sx, sy, sz;
+        hex8_sign(a, sx, sy, sz);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const double xi = gauss_coord(q & 1), eta = gauss_coord(q >> 1 & 1), zeta = gauss_coord(q >> 2 & 1);
+            s = fma(0.125 * (1.0 + sx * xi) * (1.0 + sy * eta) * (1.0 + sz * zeta), out[e * 8 + q], s);
+        }
+    }
+    dc[n] = -s;
+}
+
 // residual fix-up: constrained rows R_d = X_d, point loads enter as -F
 __global__ void residual_finish_kernel(double *__restrict__ R, const double *__restrict__ X,
                                        const double *__restrict__ F, const uint8_t *__restrict__ fixed,
@@ -772,6 +903,35 @@ int compute_modulus(mg_problem *p) {
         p->d_rho, p->n_elems, p->mat.E0, rmin, p->mat.penal, p->d_E, p->d_dE, st);
     MG_CUDA_TRY(cudaGetLastError());
     return read_status(p, st);
+}
+
+int compute_nodal_modulus(mg_problem *p) {
+    int *st = status_slot(p);
+    MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(int), p->stream));
+    const double rmin = p->mat.Emin / p->mat.E0;
+    simp_nodal_modulus_kernel<<<blocks_for(p->n_elems * 8, 256), 256, 0, p->stream>>>(
+        p->d_conn, p->d_rho_nodes, p->n_elems, p->mat.E0, rmin, p->mat.penal, p->d_Eq, p->d_dEq, st);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return read_status(p, st);
+}
+
+// dC/drho_n of the compliance C = F.u at the solution u (the adjoint is -u):
+// -u^T dK/drho_n u, dK/drho_n = sum over the node's elements and Gauss points of
+// dE_q N_n(x_q) K1_q (K1_q the unit-modulus stiffness of point q); n_nodes values
+// into dc_dev
+int nodal_compliance_sensitivity(mg_problem *p, const double *d_u, double *dc_dev) {
+    double lam1, mu1;
+    lame_3d(p->mat.nu, lam1, mu1);
+    hex8_qp_energy_kernel<<<std::max(1u, std::min(blocks_for(p->n_elems, kWarpsPerBlock), 65535u)), 256, 0,
+                            p->stream>>>(p->d_coords, p->d_conn, p->n_elems, p->d_dEq, lam1, mu1, d_u,
+                                         p->d_fixed, p->d_qp_out);
+    MG_CUDA_TRY(cudaGetLastError());
+    nodal_gather_kernel<<<blocks_for(p->n_nodes, 256), 256, 0, p->stream>>>(
+        p->d_node_inc_ptr, p->d_node_inc, p->n_nodes, p->d_qp_out, dc_dev);
+    MG_CUDA_TRY(cudaGetLastError());
+    count_launches(2);
+    return MG_OK;
 }
 
 int launch_simp_modulus(const double *d_rho, int64_t n, const mg_material_desc &mat, double *d_E,
@@ -872,8 +1032,8 @@ int assemble_system(mg_problem *p, const double *d_X, double *d_R, bool want_jac
                 unsigned grid = blocks_for(cnt, kWarpsPerBlock);
                 hex8_kernel<0><<<grid, 256, 0, p->stream>>>(
                     p->d_coords, p->d_conn, p->d_color_elems + p->color_ptr[c], 0, cnt, p->d_E,
-                    lam1, mu1, p->A.rowptr, p->d_emap, p->A.vals, nullptr, nullptr, nullptr,
-                    nullptr, nullptr, st);
+                    p->nodal_design ? p->d_Eq : nullptr, lam1, mu1, p->A.rowptr, p->d_emap, p->A.vals,
+                    nullptr, nullptr, nullptr, nullptr, nullptr, st);
                 MG_CUDA_TRY(cudaGetLastError());
             }
         } else {
@@ -1027,8 +1187,8 @@ int element_matrices(mg_problem *p, const double *d_X, int64_t first, int64_t co
         double lam1, mu1;
         lame_3d(p->mat.nu, lam1, mu1);
         hex8_kernel<1><<<blocks_for(count, kWarpsPerBlock), 256, 0, p->stream>>>(
-            p->d_coords, p->d_conn, nullptr, first, count, p->d_E, lam1, mu1, nullptr, nullptr,
-            nullptr, d_Ke, nullptr, nullptr, nullptr, nullptr, st);
+            p->d_coords, p->d_conn, nullptr, first, count, p->d_E, p->nodal_design ? p->d_Eq : nullptr,
+            lam1, mu1, nullptr, nullptr, nullptr, d_Ke, nullptr, nullptr, nullptr, nullptr, st);
     } else if (p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
         double lam1, mu1;
         lame_3d(p->mat.nu, lam1, mu1);
@@ -1067,7 +1227,7 @@ int elem_sensitivity(mg_problem *p, const double *d_X, const double *d_lambda, i
         double lam1, mu1;
         lame_3d(p->mat.nu, lam1, mu1);
         hex8_kernel<2><<<blocks_for(p->n_elems, kWarpsPerBlock), 256, 0, p->stream>>>(
-            p->d_coords, p->d_conn, nullptr, 0, p->n_elems, p->d_dE, lam1, mu1, nullptr,
+            p->d_coords, p->d_conn, nullptr, 0, p->n_elems, p->d_dE, nullptr, lam1, mu1, nullptr,
             nullptr, nullptr, nullptr, d_lambda, d_X, p->d_fixed, d_out_elem, st);
     } else if (p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR && kind == MG_PARAM_DENSITY) {
         // out[e] = dE_e lambda_e . f1_e(X)
@@ -1108,8 +1268,8 @@ int assemble_param_residual(mg_problem *p, const double *d_X, int kind, int64_t 
         lame_3d(p->mat.nu, lam1, mu1);
         if (p->physics == MG_PHYSICS_ELASTICITY_HEX8) {
             hex8_kernel<1><<<1, 256, 0, p->stream>>>(p->d_coords, p->d_conn, nullptr, index, 1,
-                                                     p->d_dE, lam1, mu1, nullptr, nullptr, nullptr,
-                                                     Ke, nullptr, nullptr, nullptr, nullptr, st);
+                                                     p->d_dE, nullptr, lam1, mu1, nullptr, nullptr,
+                                                     nullptr, Ke, nullptr, nullptr, nullptr, nullptr, st);
             MG_CUDA_TRY(cudaGetLastError());
             elem_matvec_kernel<<<1, 32, 0, p->stream>>>(Ke, d_X, p->d_conn, index, 1, 8, 3, fe);
         } else {
@@ -1247,8 +1407,8 @@ int element_sensitivity(mg_problem *p, int64_t e, const double *d_sol, int kind,
         double *Ke = p->d_tmp2;  // 576 doubles
         if (p->physics == MG_PHYSICS_ELASTICITY_HEX8) {
             hex8_kernel<1><<<1, 256, 0, p->stream>>>(p->d_coords, p->d_conn, nullptr, e, 1, p->d_dE,
-                                                     lam1, mu1, nullptr, nullptr, nullptr, Ke, nullptr,
-                                                     nullptr, nullptr, nullptr, st);
+                                                     nullptr, lam1, mu1, nullptr, nullptr, nullptr, Ke,
+                                                     nullptr, nullptr, nullptr, nullptr, st);
             MG_CUDA_TRY(cudaGetLastError());
             elem_matvec_kernel<<<1, 32, 0, p->stream>>>(Ke, p->d_tmp, p->d_conn, e, 1, 8, 3, d_dfe);
         } else {

@@ -143,7 +143,8 @@ int release(mg_problem *p) {
     void *ptrs[] = {p->d_coords, p->d_conn, p->d_color_elems, p->d_fixed, p->d_F, p->d_rho,
                     p->d_E, p->d_dE, p->d_s, p->d_q, p->d_conv_mask, p->A.rowptr, p->A.cols,
                     p->A.vals, p->d_emap, p->d_fix_zero, p->d_fix_diag, p->d_X, p->d_R,
-                    p->d_tmp, p->d_tmp2, p->d_elem_out, p->d_red, p->d_ks, p->d_side};
+                    p->d_tmp, p->d_tmp2, p->d_elem_out, p->d_red, p->d_ks, p->d_side, p->d_rho_nodes,
+                    p->d_Eq, p->d_dEq, p->d_qp_out, p->d_node_out, p->d_node_inc_ptr, p->d_node_inc};
     for (void *q : ptrs) dev_free(q);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -469,6 +470,17 @@ using namespace mg;
 
 extern "C" {
 
+namespace {
+// entry points whose element kernels take one modulus per element
+int element_design_only(mg_problem *p, const char *what) {
+    if (p && p->nodal_design) {
+        set_error("%s: takes element densities (the problem has a nodal density field)", what);
+        return MG_ENOTSUP;
+    }
+    return MG_OK;
+}
+}  // namespace
+
 int mg_version(void) { return MG_ABI_VERSION; }
 
 const char *mg_status_string(int s) {
@@ -567,6 +579,7 @@ int mg_set_design(mg_problem *p, const double *rho) {
         }
     MG_TRY(to_device_vec(p, rho, p->d_rho, p->n_elems));
     MG_TRY(compute_modulus(p));
+    p->nodal_design = false;
     p->jacobian_valid = false;
     return MG_OK;
 }
@@ -576,6 +589,50 @@ int mg_set_design_device(mg_problem *p, const double *rho_dev) {
     if (p->physics == MG_PHYSICS_HEAT_QUAD4) return MG_ENOTSUP;
     MG_CUDA_TRY(cudaMemcpyAsync(p->d_rho, rho_dev, p->n_elems * 8, cudaMemcpyDeviceToDevice, p->stream));
     MG_TRY(compute_modulus(p));
+    p->nodal_design = false;
+    p->jacobian_valid = false;
+    return MG_OK;
+}
+
+int mg_set_design_nodal(mg_problem *p, const double *rho_nodes) {
+    // the MeshFieldFunction density of example_6.cpp:104-137 (FIRST-order LAGRANGE
+    // "rho", :250-252): the modulus at each Gauss point from the trilinear field there
+    if (!p || !rho_nodes) {
+        set_error("mg_set_design_nodal: invalid argument");
+        return MG_EINVAL;
+    }
+    if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) {
+        set_error("a nodal density field needs the linear-strain HEX8 physics");
+        return MG_ENOTSUP;
+    }
+    for (int64_t n = 0; n < p->n_nodes; n++)
+        if (!(rho_nodes[n] >= 0.0 && rho_nodes[n] <= 1.0)) {
+            set_error("nodal density %lld = %g outside [0,1]", (long long)n, rho_nodes[n]);
+            return MG_EINVAL;
+        }
+    if (!p->d_rho_nodes) {
+        MG_TRY(dev_alloc_n(&p->d_rho_nodes, (size_t)p->n_nodes));
+        MG_TRY(dev_alloc_n(&p->d_node_out, (size_t)p->n_nodes));
+        MG_TRY(dev_alloc_n(&p->d_Eq, (size_t)p->n_elems * 8));
+        MG_TRY(dev_alloc_n(&p->d_dEq, (size_t)p->n_elems * 8));
+        MG_TRY(dev_alloc_n(&p->d_qp_out, (size_t)p->n_elems * 8));
+        // node -> (element, corner) incidences in element order
+        std::vector<int32_t> ptr(p->n_nodes + 1, 0), inc((size_t)p->n_elems * 8);
+        for (int64_t k = 0; k < p->n_elems * 8; k++) ptr[p->h_conn[k] + 1]++;
+        for (int64_t n = 0; n < p->n_nodes; n++) ptr[n + 1] += ptr[n];
+        std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+        for (int64_t k = 0; k < p->n_elems * 8; k++) inc[fill[p->h_conn[k]]++] = (int32_t)k;
+        MG_TRY(dev_alloc_n(&p->d_node_inc_ptr, ptr.size()));
+        MG_TRY(dev_alloc_n(&p->d_node_inc, inc.size()));
+        MG_CUDA_TRY(cudaMemcpyAsync(p->d_node_inc_ptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice,
+                                    p->stream));
+        MG_CUDA_TRY(cudaMemcpyAsync(p->d_node_inc, inc.data(), inc.size() * 4, cudaMemcpyHostToDevice,
+                                    p->stream));
+        MG_CUDA_TRY(cudaStreamSynchronize(p->stream));  // ptr / inc are host temporaries
+    }
+    MG_TRY(to_device_vec(p, rho_nodes, p->d_rho_nodes, p->n_nodes));
+    MG_TRY(compute_nodal_modulus(p));
+    p->nodal_design = true;
     p->jacobian_valid = false;
     return MG_OK;
 }
@@ -659,6 +716,7 @@ int mg_solve(mg_problem *p, const mg_solve_opts *opts, double *X, mg_solve_repor
                  : solve_linear(p, o, &r);
     } else {
         if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) { set_error("mixed precision needs the linear-strain HEX8 SIMP form"); return MG_ENOTSUP; }
+        MG_TRY(element_design_only(p, "the mixed-precision solve"));
         rc = matfree_solve(p, o, &r, !o.warm_start && !X);
     }
     p->last_solve_mixed = (o.precision != MG_PLAIN_FP64);
@@ -683,6 +741,7 @@ const double *mg_solution_device(mg_problem *p) { return p ? p->d_X : nullptr; }
 int mg_sensitivity_assemble(mg_problem *p, const double *X, int32_t kind, int64_t index,
                             double *dRdp) {
     if (!p || !dRdp) return MG_EINVAL;
+    MG_TRY(element_design_only(p, "mg_sensitivity_assemble"));
     const double *dX = p->d_X;
     if (X) {
         MG_TRY(to_device_vec(p, X, p->d_tmp, p->n_dofs));
@@ -702,6 +761,11 @@ int mg_compliance(mg_problem *p, const double *X, double *compliance, double *dc
         dX = p->d_tmp;
     }
     if (compliance) MG_TRY(dot(p, p->d_F, dX, p->n_dofs, compliance));
+    if (dc && p->nodal_design) {
+        // one value per node: -u^T dK/drho_n u
+        MG_TRY(nodal_compliance_sensitivity(p, dX, p->d_node_out));
+        return to_host_vec(p, p->d_node_out, dc, p->n_nodes);
+    }
     if (dc && p->physics == MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
         // C = F.u with f_int(u, rho) = F: dC/drho_e = -lambda . d f_int / d rho_e, where
         // K_T(u)^T lambda = F (the tangent is symmetric) and d f_int / d rho_e = dE_e f1_e(u)
@@ -774,6 +838,7 @@ int mg_ks_stress(mg_problem *p, const double *X, double p_ks, double sigma0, dou
     // dR/drho_e (K(X)^T lambda = -dq/dX, the residual at the material's SIMP exponent) plus the
     // direct term through the stress modulus (functional_sensitivity_for_elem, :117-151)
     if (!p || !(p_ks > 0) || !(sigma0 > 0)) return MG_EINVAL;
+    MG_TRY(element_design_only(p, "mg_ks_stress"));
     if (p->physics != MG_PHYSICS_ELASTICITY_HEX8 && p->physics != MG_PHYSICS_ELASTICITY_HEX8_NONLINEAR) {
         set_error("the stress output needs HEX8 elasticity");
         return MG_ENOTSUP;
@@ -857,6 +922,7 @@ int mg_sensitivity_solve(mg_problem *p, const double *X, int32_t kind, int64_t i
         set_error("mg_sensitivity_solve: invalid argument");
         return MG_EINVAL;
     }
+    MG_TRY(element_design_only(p, "mg_sensitivity_solve"));
     mg_solve_opts o;
     if (opts) o = *opts; else mg_default_solve_opts(&o);
     double *dX = p->d_tmp;  // the resident solution is left as it is
@@ -964,6 +1030,7 @@ int mg_element_sensitivity(mg_problem *p, int64_t elem, const double *sol_elem, 
         set_error("mg_element_sensitivity: invalid argument");
         return MG_EINVAL;
     }
+    MG_TRY(element_design_only(p, "mg_element_sensitivity"));
     const int nd = p->npe * p->dpn;
     ElemBuffers b;
     MG_TRY(b.alloc(nd));
@@ -1022,6 +1089,7 @@ long long mg_launch_count(void) { return g_launches.load(); }
 
 int mg_compliance_resident(mg_problem *p, double *compliance) {
     if (!p) return MG_EINVAL;
+    MG_TRY(element_design_only(p, "mg_compliance_resident"));
     if (p->physics != MG_PHYSICS_ELASTICITY_HEX8) return MG_ENOTSUP;
     if (p->last_solve_mixed) return matfree_compliance_resident(p, compliance);
     if (compliance) MG_TRY(dot(p, p->d_F, p->d_X, p->n_dofs, compliance));

@@ -99,6 +99,13 @@ struct mg_problem {
     uint8_t *d_fixed = nullptr;
     double *d_F = nullptr;
     double *d_rho = nullptr, *d_E = nullptr, *d_dE = nullptr;
+    // nodal density field (MeshFieldFunction over FIRST-order LAGRANGE): the
+    // modulus and dE/drho at each Gauss point (n_elems x 8), the node -> (element,
+    // corner) incidences 8 e + a in element order, scratch of the sensitivity
+    bool nodal_design = false;
+    double *d_rho_nodes = nullptr, *d_Eq = nullptr, *d_dEq = nullptr, *d_qp_out = nullptr,
+           *d_node_out = nullptr;
+    int32_t *d_node_inc_ptr = nullptr, *d_node_inc = nullptr;
     double *d_s = nullptr, *d_q = nullptr;
     uint8_t *d_conv_mask = nullptr;  // per element bit mask of convection sides
     double conv_h = 0, conv_Tinf = 0;
@@ -143,6 +150,8 @@ int ks_stress_combine(mg_problem *p, const double *d_ks, double inv_s0I, const d
 int compute_modulus(mg_problem *p);
 // SIMP E(rho), dE/drho of n elements on stream s; bit 4 of *d_status marks a
 // density outside [0,1] or NaN
+int compute_nodal_modulus(mg_problem *p);
+int nodal_compliance_sensitivity(mg_problem *p, const double *d_u, double *dc_dev);
 int launch_simp_modulus(const double *d_rho, int64_t n, const mg_material_desc &mat, double *d_E,
                         double *d_dE, int *d_status, cudaStream_t s);
 int build_emap(mg_problem *p);

@@ -751,7 +751,18 @@ public:
         _rho = rho;
         _Emin = Emin;
         _penal = penal;
+        _nodal = false;
         if (_p) check(mg_set_design(_p, _rho.data()), "set_simp");
+    }
+    // a nodal density field (example_6.cpp:104-137: the ElasticityFunction reads a
+    // FIRST-order LAGRANGE "rho" through MeshFieldFunction): the modulus at each Gauss
+    // point from the trilinear field; density parameters then index nodes
+    void set_simp_nodal(const std::vector<Real> &rho_nodes, Real Emin, Real penal) {
+        _rho = rho_nodes;
+        _Emin = Emin;
+        _penal = penal;
+        _nodal = true;
+        if (_p) check(mg_set_design_nodal(_p, _rho.data()), "set_simp_nodal");
     }
     // per-element conductivity scale s_e (heat)
     void set_conductivity_scale(const std::vector<Real> &s) {
@@ -845,7 +856,7 @@ public:
             for (size_t i = 0; i < X.size(); i++)
                 if (std::fabs(adj_sol(i) + X(i)) > 1e-12 * (1 + std::fabs(X(i))))
                     throw std::runtime_error("compliance adjoint must be -u");
-            std::vector<Real> dc(_sys->mesh().n_elem());
+            std::vector<Real> dc(_nodal ? _sys->mesh().n_nodes() : _sys->mesh().n_elem());
             Real c = 0;
             check(mg_compliance(p, X.data(), &c, dc.data()), "adjoint sensitivity");
             for (size_t i = 0; i < p_vec.size(); i++) {
@@ -1034,7 +1045,8 @@ public:
         }
         if (!se.empty())
             check(mg_set_side_loads(_p, (int64_t)se.size(), se.data(), ss.data(), sv.data()), "side loads");
-        if (!_rho.empty()) check(mg_set_design(_p, _rho.data()), "set_simp");
+        if (!_rho.empty())
+            check(_nodal ? mg_set_design_nodal(_p, _rho.data()) : mg_set_design(_p, _rho.data()), "set_simp");
         if (!_scale.empty()) check(mg_set_elem_scale(_p, _scale.data()), "set_conductivity_scale");
     }
 
@@ -1048,6 +1060,7 @@ private:
     AssemblyElemOperations *_ops = nullptr;
     mg_problem *_p = nullptr;
     std::vector<Real> _rho, _scale, _lvals, _src;
+    bool _nodal = false;  // _rho per node (set_simp_nodal) rather than per element
     std::vector<int64_t> _fixed, _ldofs;
     std::vector<int32_t> _ce, _cs;
     Real _Emin = 1e-9, _penal = 3.0, _res_l2 = 0.0;

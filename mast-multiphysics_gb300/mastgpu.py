@@ -196,6 +196,7 @@ def lib(autobuild=True):
     L.mg_problem_stream.restype = _vp
     L.mg_set_design.argtypes = [_vp, _vp]
     L.mg_set_design_device.argtypes = [_vp, _vp]
+    L.mg_set_design_nodal.argtypes = [_vp, _vp]
     L.mg_set_elem_scale.argtypes = [_vp, _vp]
     L.mg_residual_and_jacobian.argtypes = [_vp, _vp, _vp, ctypes.c_int]
     L.mg_get_csr.argtypes = [_vp, _vp, _vp, _vp]
@@ -387,9 +388,19 @@ class Problem:
     def set_design(self, rho):
         rho = np.ascontiguousarray(rho, dtype=np.float64)
         check(lib().mg_set_design(self.h, _p(rho)), "mg_set_design")
+        self.nodal = False
 
     def set_design_device(self, ptr):
         check(lib().mg_set_design_device(self.h, ctypes.c_void_p(ptr)), "mg_set_design_device")
+        self.nodal = False
+
+    def set_design_nodal(self, rho_nodes):
+        """Nodal density field (n_nodes values): the modulus per Gauss point from
+        the trilinear field (mg_set_design_nodal); compliance() then returns
+        dC/drho per node."""
+        rho_nodes = np.ascontiguousarray(rho_nodes, dtype=np.float64)
+        check(lib().mg_set_design_nodal(self.h, _p(rho_nodes)), "mg_set_design_nodal")
+        self.nodal = True
 
     def set_elem_scale(self, s):
         s = np.ascontiguousarray(s, dtype=np.float64)
@@ -455,7 +466,7 @@ class Problem:
     def compliance(self, X=None, want_sens=True):
         Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
         c = ctypes.c_double()
-        dc = np.zeros(self.n_elems) if want_sens else None
+        dc = np.zeros(self.n_nodes if getattr(self, "nodal", False) else self.n_elems) if want_sens else None
         check(lib().mg_compliance(self.h, _p(Xa), ctypes.byref(c), _p(dc)), "mg_compliance")
         return c.value, dc
 

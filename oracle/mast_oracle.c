@@ -190,13 +190,16 @@ static void hex8_B(const double dphi[24], double B[144]) {
    f += JxW B^T sigma (:296-297), K += JxW B^T C B (:327-329).  Only the
    translational 24x24 block is returned (rotational dofs are decoupled and
    regularised at :415-417). */
-int or_hex8_internal(const double X[24], double E, double nu, const double u[24],
-                     double f[24], double K[576]) {
+/* Eq non-NULL: the modulus at each quadrature point (a MeshFieldFunction
+   density interpolated there, example_6.cpp:104-137), else E throughout */
+static int hex8_internal_impl(const double X[24], double E, const double *Eq, double nu,
+                              const double u[24], double f[24], double K[576]) {
     double C[36], phi[8], dphi[24], B[144], JxW;
     or_iso_stiffness_3d(E, nu, C);
     memset(f, 0, 24 * sizeof(double));
     if (K) memset(K, 0, 576 * sizeof(double));
     for (int qp = 0; qp < 8; qp++) {
+        if (Eq) or_iso_stiffness_3d(Eq[qp], nu, C);
         if (hex8_qp(X, qp, phi, dphi, &JxW) <= 0.) return -1;
         hex8_B(dphi, B);
         double eps[6] = {0}, sig[6] = {0};
@@ -226,6 +229,16 @@ int or_hex8_internal(const double X[24], double E, double nu, const double u[24]
         }
     }
     return 0;
+}
+
+int or_hex8_internal(const double X[24], double E, double nu, const double u[24],
+                     double f[24], double K[576]) {
+    return hex8_internal_impl(X, E, NULL, nu, u, f, K);
+}
+
+int or_hex8_internal_qp(const double X[24], const double Eq[8], double nu, const double u[24],
+                        double f[24], double K[576]) {
+    return hex8_internal_impl(X, 0.0, Eq, nu, u, f, K);
 }
 
 /* StructuralElement3D::internal_residual, nonlinear-strain branch
@@ -764,10 +777,10 @@ static void apply_fixed(int64_t n, const int32_t *rowptr, const int32_t *cols,
    (src/base/nonlinear_implicit_assembly.cpp:111-186): gather, element
    calculation, scatter add into the global matrix.  Colours make the
    parallel scatter race-free. */
-int or_assemble_hex8(int64_t n_nodes, int64_t n_elems, const double *coords,
-                     const int32_t *conn, const double *E_elem, double nu,
-                     const int32_t *rowptr, const int32_t *cols, double *vals,
-                     const uint8_t *fixed, int n_colors, const int32_t *color) {
+static int assemble_hex8_impl(int64_t n_nodes, int64_t n_elems, const double *coords,
+                              const int32_t *conn, const double *E_elem, const double *E_qp,
+                              double nu, const int32_t *rowptr, const int32_t *cols, double *vals,
+                              const uint8_t *fixed, int n_colors, const int32_t *color) {
     int64_t n = n_nodes * 3;
     memset(vals, 0, (size_t)rowptr[n] * sizeof(double));
     int bad = 0;
@@ -780,7 +793,9 @@ int or_assemble_hex8(int64_t n_nodes, int64_t n_elems, const double *coords,
             double X[24], u0[24] = {0}, f[24], K[576];
             for (int a = 0; a < 8; a++)
                 for (int d = 0; d < 3; d++) X[a * 3 + d] = coords[(int64_t)en[a] * 3 + d];
-            if (or_hex8_internal(X, E_elem[e], nu, u0, f, K)) bad |= 1;
+            if (E_qp ? or_hex8_internal_qp(X, E_qp + e * 8, nu, u0, f, K)
+                     : or_hex8_internal(X, E_elem[e], nu, u0, f, K))
+                bad |= 1;
             for (int a = 0; a < 8; a++)
                 for (int i = 0; i < 3; i++) {
                     int64_t row = (int64_t)en[a] * 3 + i;
@@ -794,6 +809,22 @@ int or_assemble_hex8(int64_t n_nodes, int64_t n_elems, const double *coords,
     }
     apply_fixed(n, rowptr, cols, vals, fixed);
     return bad ? -1 : 0;
+}
+
+int or_assemble_hex8(int64_t n_nodes, int64_t n_elems, const double *coords,
+                     const int32_t *conn, const double *E_elem, double nu,
+                     const int32_t *rowptr, const int32_t *cols, double *vals,
+                     const uint8_t *fixed, int n_colors, const int32_t *color) {
+    return assemble_hex8_impl(n_nodes, n_elems, coords, conn, E_elem, NULL, nu, rowptr, cols, vals,
+                              fixed, n_colors, color);
+}
+
+int or_assemble_hex8_qp(int64_t n_nodes, int64_t n_elems, const double *coords,
+                        const int32_t *conn, const double *E_qp, double nu,
+                        const int32_t *rowptr, const int32_t *cols, double *vals,
+                        const uint8_t *fixed, int n_colors, const int32_t *color) {
+    return assemble_hex8_impl(n_nodes, n_elems, coords, conn, NULL, E_qp, nu, rowptr, cols, vals,
+                              fixed, n_colors, color);
 }
 
 int or_assemble_quad4_membrane(int64_t n_nodes, int64_t n_elems, const double *coords,
@@ -1082,6 +1113,23 @@ void or_simp_modulus(const or_simp_desc *d, int64_t n_el, const double *rho, dou
     }
 }
 
+/* Nodal density (example_6.cpp:104-137: a FIRST-order LAGRANGE "rho" field read
+   through MeshFieldFunction): rho(x_q) = sum_a phi_a(x_q) rho_a at each Gauss
+   point of each element, E_q = E0 (rmin + (1 - rmin) rho_q^p) and dE_q/drho_q. */
+void or_simp_nodal_modulus(const or_simp_desc *d, int64_t n_el, const int32_t *conn,
+                           const double *rho_nodes, double *Eq, double *dEq) {
+    double rmin = d->Emin / d->E0;
+    for (int64_t e = 0; e < n_el; e++)
+        for (int qp = 0; qp < 8; qp++) {
+            double xi[3] = {GP[qp & 1], GP[(qp >> 1) & 1], GP[(qp >> 2) & 1]}, phi[8], dref[24];
+            or_hex8_shape(xi, phi, dref);
+            double r = 0;
+            for (int a = 0; a < 8; a++) r += phi[a] * rho_nodes[conn[e * 8 + a]];
+            if (Eq) Eq[e * 8 + qp] = d->E0 * (rmin + (1. - rmin) * pow(r, d->penal));
+            if (dEq) dEq[e * 8 + qp] = d->E0 * (1. - rmin) * d->penal * pow(r, d->penal - 1.);
+        }
+}
+
 /* Nodal -z load on the x = max, z = 0 edge spread evenly over the node span;
    enters the residual as -F (nonlinear_implicit_assembly.cpp:189-247). */
 void or_simp_load_vector(const or_simp_desc *d, double *F) {
@@ -1109,8 +1157,8 @@ void or_simp_fixed_mask(const or_simp_desc *d, uint8_t *fixed) {
    assemble K, solve K u = F, C = F.u (point loads are not in ComplianceOutput,
    compliance_output.cpp:71-102), dC/drho_e = -u_e^T dK_e/drho_e u_e (the
    compliance adjoint is -u, assembly_base.cpp:594-639). */
-int or_simp_solve(const or_simp_desc *d, const double *rho, double *u, double *dc,
-                  or_simp_report *rep) {
+static int simp_solve_impl(const or_simp_desc *d, const double *rho, int nodal, double *u,
+                           double *dc, or_simp_report *rep) {
     int64_t n_el = (int64_t)d->nx * d->ny * d->nz;
     int64_t n_nodes = (int64_t)(d->nx + 1) * (d->ny + 1) * (d->nz + 1);
     int64_t n = n_nodes * 3;
@@ -1125,15 +1173,19 @@ int or_simp_solve(const or_simp_desc *d, const double *rho, double *u, double *d
     double *vals = (double *)malloc((size_t)nnz * sizeof(double));
     int32_t *color = (int32_t *)malloc((size_t)n_el * sizeof(int32_t));
     int ncol = or_color_elements(8, n_nodes, n_el, conn, color);
-    double *E = (double *)malloc((size_t)n_el * sizeof(double));
-    double *dE = (double *)malloc((size_t)n_el * sizeof(double));
-    or_simp_modulus(d, n_el, rho, E, dE);
+    const int64_t nE = nodal ? n_el * 8 : n_el;
+    double *E = (double *)malloc((size_t)nE * sizeof(double));
+    double *dE = (double *)malloc((size_t)nE * sizeof(double));
+    if (nodal)
+        or_simp_nodal_modulus(d, n_el, conn, rho, E, dE);
+    else
+        or_simp_modulus(d, n_el, rho, E, dE);
     uint8_t *fixed = (uint8_t *)malloc((size_t)n);
     or_simp_fixed_mask(d, fixed);
     double *F = (double *)malloc((size_t)n * sizeof(double));
     or_simp_load_vector(d, F);
-    int st = or_assemble_hex8(n_nodes, n_el, coords, conn, E, d->nu, rowptr, cols, vals,
-                              fixed, ncol, color);
+    int st = assemble_hex8_impl(n_nodes, n_el, coords, conn, nodal ? NULL : E, nodal ? E : NULL,
+                                d->nu, rowptr, cols, vals, fixed, ncol, color);
     double t1 = or_wtime();
     memset(u, 0, (size_t)n * sizeof(double));
     double relres = 0;
@@ -1148,7 +1200,42 @@ int or_simp_solve(const or_simp_desc *d, const double *rho, double *u, double *d
         fn += F[i] * F[i];
         comp += F[i] * u[i];
     }
-    if (dc) {
+    if (dc && nodal) {
+        /* dC/drho_n = -sum over the elements of n and their Gauss points q of
+           dE_q phi_n(x_q) u_e^T K1_q u_e, K1_q the unit-modulus stiffness of point q
+           alone: per element first, then summed into the nodes in element order */
+        double *contrib = (double *)malloc((size_t)n_el * 8 * sizeof(double));
+#pragma omp parallel for schedule(static)
+        for (int64_t e = 0; e < n_el; e++) {
+            double X[24], ue[24], df[24], eq[8], s[8];
+            const int32_t *en = conn + e * 8;
+            for (int a = 0; a < 8; a++)
+                for (int c = 0; c < 3; c++) {
+                    X[a * 3 + c] = coords[(int64_t)en[a] * 3 + c];
+                    int64_t g = (int64_t)en[a] * 3 + c;
+                    ue[c * 8 + a] = fixed[g] ? 0.0 : u[g];
+                }
+            for (int q = 0; q < 8; q++) {
+                for (int k = 0; k < 8; k++) eq[k] = k == q ? 1.0 : 0.0;
+                or_hex8_internal_qp(X, eq, d->nu, ue, df, NULL);
+                s[q] = 0;
+                for (int i = 0; i < 24; i++) s[q] += ue[i] * df[i];
+            }
+            for (int a = 0; a < 8; a++) {
+                double acc = 0;
+                for (int q = 0; q < 8; q++) {
+                    double xi[3] = {GP[q & 1], GP[(q >> 1) & 1], GP[(q >> 2) & 1]}, phi[8], dref[24];
+                    or_hex8_shape(xi, phi, dref);
+                    acc += dE[e * 8 + q] * phi[a] * s[q];
+                }
+                contrib[e * 8 + a] = acc;
+            }
+        }
+        memset(dc, 0, (size_t)n_nodes * sizeof(double));
+        for (int64_t e = 0; e < n_el; e++)
+            for (int a = 0; a < 8; a++) dc[conn[e * 8 + a]] -= contrib[e * 8 + a];
+        free(contrib);
+    } else if (dc) {
 #pragma omp parallel for schedule(static)
         for (int64_t e = 0; e < n_el; e++) {
             double X[24], ue[24], df[24];
@@ -1177,6 +1264,17 @@ int or_simp_solve(const or_simp_desc *d, const double *rho, double *u, double *d
     free(coords); free(conn); free(rowptr); free(cols); free(vals); free(color);
     free(E); free(dE); free(fixed); free(F); free(Ku);
     return st ? st : (it < 0 ? it : 0);
+}
+
+int or_simp_solve(const or_simp_desc *d, const double *rho, double *u, double *dc,
+                  or_simp_report *rep) {
+    return simp_solve_impl(d, rho, 0, u, dc, rep);
+}
+
+/* the same with a nodal density field (n_nodes values; dc per node) */
+int or_simp_solve_nodal(const or_simp_desc *d, const double *rho_nodes, double *u, double *dc,
+                        or_simp_report *rep) {
+    return simp_solve_impl(d, rho_nodes, 1, u, dc, rep);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -45,6 +45,8 @@ void or_quad4_shape(const double xi[2], double phi[4], double dphi[8]);
 /* element routines (var-blocked order; K may be NULL) */
 int or_hex8_internal(const double X[24], double E, double nu, const double u[24],
                      double f[24], double K[576]);
+int or_hex8_internal_qp(const double X[24], const double Eq[8], double nu, const double u[24],
+                        double f[24], double K[576]);
 /* HEX8 total-Lagrangian Green-Lagrange element (nonlinear-strain branch):
    f = int B_L^T S, K = int (B_L^T C B_L + geometric stiffness); var-blocked dofs */
 int or_hex8_internal_gl(const double X[24], double E, double nu, const double u[24],
@@ -87,6 +89,10 @@ void or_csr_transpose(int64_t n, const int32_t *rowptr, const int32_t *cols,
 /* assembly into a CSR with a given pattern; fixed[dof]!=0 -> identity row/col */
 int or_assemble_hex8(int64_t n_nodes, int64_t n_elems, const double *coords,
                      const int32_t *conn, const double *E_elem, double nu,
+                     const int32_t *rowptr, const int32_t *cols, double *vals,
+                     const uint8_t *fixed, int n_colors, const int32_t *color);
+int or_assemble_hex8_qp(int64_t n_nodes, int64_t n_elems, const double *coords,
+                     const int32_t *conn, const double *E_qp, double nu,
                      const int32_t *rowptr, const int32_t *cols, double *vals,
                      const uint8_t *fixed, int n_colors, const int32_t *color);
 int or_assemble_quad4_membrane(int64_t n_nodes, int64_t n_elems, const double *coords,
@@ -134,6 +140,12 @@ typedef struct {
 
 int or_simp_solve(const or_simp_desc *d, const double *rho, double *u, double *dc,
                   or_simp_report *rep);
+/* nodal density field (MeshFieldFunction, trilinear per element): rho_nodes has
+   (nx+1)(ny+1)(nz+1) values, dc one per node */
+int or_simp_solve_nodal(const or_simp_desc *d, const double *rho_nodes, double *u, double *dc,
+                        or_simp_report *rep);
+void or_simp_nodal_modulus(const or_simp_desc *d, int64_t n_el, const int32_t *conn,
+                           const double *rho_nodes, double *Eq, double *dEq);
 void or_simp_load_vector(const or_simp_desc *d, double *F);
 void or_simp_fixed_mask(const or_simp_desc *d, uint8_t *fixed);
 void or_simp_modulus(const or_simp_desc *d, int64_t n_el, const double *rho, double *E,

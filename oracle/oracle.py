@@ -100,6 +100,10 @@ def lib():
         L.or_bicgstab.argtypes = L.or_pcg.argtypes
         L.or_simp_solve.argtypes = [ctypes.POINTER(SimpDesc), _f64p, _f64p, vp,
                                     ctypes.POINTER(SimpReport)]
+        L.or_simp_solve_nodal.argtypes = [ctypes.POINTER(SimpDesc), _f64p, _f64p, vp,
+                                          ctypes.POINTER(SimpReport)]
+        L.or_simp_nodal_modulus.argtypes = [ctypes.POINTER(SimpDesc), i64, _i32p, _f64p, vp, vp]
+        L.or_hex8_internal_qp.argtypes = [_f64p, _f64p, d, _f64p, _f64p, vp]
         L.or_simp_load_vector.argtypes = [ctypes.POINTER(SimpDesc), _f64p]
         L.or_simp_fixed_mask.argtypes = [ctypes.POINTER(SimpDesc), _u8p]
         L.or_simp_modulus.argtypes = [ctypes.POINTER(SimpDesc), i64, _f64p, vp, vp]
@@ -460,6 +464,32 @@ def simp_solve(desc, rho, want_sens=True):
     return u, dc, rep
 
 
+def simp_solve_nodal(desc, rho_nodes, want_sens=True):
+    """The ex-6 sequence with a nodal density field (MeshFieldFunction over a
+    FIRST-order LAGRANGE "rho", example_6.cpp:104-137, 250-252): the modulus at
+    each Gauss point from the trilinear density there; dc per node."""
+    n_nodes = (desc.nx + 1) * (desc.ny + 1) * (desc.nz + 1)
+    u = np.zeros(3 * n_nodes)
+    dc = np.zeros(n_nodes) if want_sens else None
+    rep = SimpReport()
+    rc = lib().or_simp_solve_nodal(ctypes.byref(desc), np.ascontiguousarray(rho_nodes, np.float64), u,
+                                   _ptr(dc), ctypes.byref(rep))
+    if rc:
+        raise RuntimeError("oracle nodal SIMP solve failed (%d)" % rc)
+    return u, dc, rep
+
+
+def hex8_internal_qp(X, Eq, nu, u, want_K=True):
+    """Element force and stiffness with the modulus given per Gauss point."""
+    f = np.zeros(24)
+    K = np.zeros(576) if want_K else None
+    rc = lib().or_hex8_internal_qp(np.ascontiguousarray(X, np.float64), np.ascontiguousarray(Eq, np.float64),
+                                   nu, np.ascontiguousarray(u, np.float64), f, _ptr(K))
+    if rc:
+        raise RuntimeError("non-positive Jacobian")
+    return f, (K.reshape(24, 24) if want_K else None)
+
+
 def simp_load_vector(desc):
     n = (desc.nx + 1) * (desc.ny + 1) * (desc.nz + 1) * 3
     F = np.zeros(n)
@@ -472,6 +502,17 @@ def simp_fixed_mask(desc):
     fx = np.zeros(n, dtype=np.uint8)
     lib().or_simp_fixed_mask(ctypes.byref(desc), fx)
     return fx
+
+
+def simp_nodal_modulus(desc, conn, rho_nodes):
+    """Moduli and dE/drho at the Gauss points of the elements `conn` (n x 8)."""
+    conn = np.ascontiguousarray(conn, np.int32)
+    n = conn.shape[0]
+    Eq = np.zeros(n * 8)
+    dEq = np.zeros(n * 8)
+    lib().or_simp_nodal_modulus(ctypes.byref(desc), n, conn.ravel(), np.ascontiguousarray(rho_nodes, np.float64),
+                                _ptr(Eq), _ptr(dEq))
+    return Eq.reshape(n, 8), dEq.reshape(n, 8)
 
 
 def simp_modulus(desc, rho):

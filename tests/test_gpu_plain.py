@@ -110,6 +110,36 @@ def test_random_density_sensitivity_vs_oracle():
     assert rel(dc, dc_ref) < RTOL_SOL
 
 
+def test_nodal_density_field_vs_oracle():
+    """MAST example 6's design is a nodal (FIRST-order LAGRANGE) density read
+    through MeshFieldFunction: the modulus at each Gauss point from the trilinear
+    field.  Solution, compliance and dC/drho per node against the oracle's nodal
+    path; element matrices against the oracle element with per-point moduli; the
+    mixed-precision solve refuses a nodal field."""
+    nx, ny, nz = 8, 4, 4
+    nn = (nx + 1) * (ny + 1) * (nz + 1)
+    rho = np.random.default_rng(12).uniform(0.05, 1.0, nn)
+    desc = O.simp_desc(nx, ny, nz, rtol=1e-14, maxit=400000)
+    with M.simp_cantilever(nx, ny, nz) as p:
+        p.set_design_nodal(rho)
+        u, rep = p.solve(M.default_opts(rtol=1e-13, max_iterations=100000))
+        c, dc = p.compliance()
+        Ke = p.element_matrices(5, 1)[0][0]
+        with pytest.raises(M.MastGpuError):
+            p.solve(M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8))
+        conn = p.conn.copy()
+        coords = p.coords.copy()
+    u_ref, dc_ref, r = O.simp_solve_nodal(desc, rho)
+    assert dc.shape == (nn,)
+    assert rel(u, u_ref) < RTOL_SOL
+    assert abs(c - r.compliance) / r.compliance < RTOL_SOL
+    assert rel(dc, dc_ref) < RTOL_SOL
+    Eq, _ = O.simp_nodal_modulus(desc, conn[5:6], rho)
+    X = coords[conn[5]].ravel()
+    _, K_ref = O.hex8_internal_qp(X, Eq[0], 0.3, np.zeros(24))
+    assert np.abs(Ke - K_ref).max() <= 1e-12 * np.abs(K_ref).max()
+
+
 def test_assembly_is_deterministic():
     nx, ny, nz = 6, 4, 4
     rho = np.random.default_rng(5).uniform(0.01, 1.0, nx * ny * nz)
