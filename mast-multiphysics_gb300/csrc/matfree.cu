@@ -32,6 +32,7 @@
 // partial and the last brick (chunk) of a problem -- found with a per-problem
 // counter -- sums that problem's partials in index order.  A problem's result
 // is therefore bitwise independent of which other problems share the batch.
+#include <cstdlib>
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -3214,7 +3215,13 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     }
     if (bottom_cluster && !b.h_heads.empty()) {
         // the largest cluster (16 CTAs: non-portable size) the device can place
-        for (int cs = kClusterMax; cs >= 1 && !b.bottom_cluster; cs /= 2) {
+        // MASTGPU_BOTTOM_CLUSTER caps the cluster (1, 2, 4, 8 or 16 CTAs): a test knob,
+        // the result does not depend on the cluster size
+        int cap = kClusterMax;
+        if (const char *env = std::getenv("MASTGPU_BOTTOM_CLUSTER")) cap = std::max(1, std::min(kClusterMax, std::atoi(env)));
+        int first = 1;
+        while (first * 2 <= cap) first *= 2;
+        for (int cs = first; cs >= 1 && !b.bottom_cluster; cs /= 2) {
             std::vector<ClusterChain> chains;
             const int64_t smem = cluster_layout(b, cs, chains);
             if (smem < 0 || smem > kBottomSmemMax) continue;

@@ -208,3 +208,21 @@ def test_cluster_bottom_vcycle_matches_the_one_cta_form(shape):
     _, dc_ref, r = O.simp_solve(O.simp_desc(nx, ny, nz, rtol=1e-12, maxit=10 ** 6), rho)
     assert abs(c - r.compliance) / r.compliance < 1e-6
     assert np.abs(dc - dc_ref).max() / np.abs(dc_ref).max() < 1e-6
+
+
+def test_cluster_bottom_result_does_not_depend_on_the_cluster_size(monkeypatch):
+    """Every dof of the cluster V-cycle is computed by one thread in a fixed order,
+    whichever CTA owns it: 16, 4 and 1 CTA per chain give bitwise the same solve."""
+    nx, ny, nz = 32, 16, 16
+    rho = np.random.default_rng(13).uniform(0.01, 1.0, nx * ny * nz)
+    o = M.default_opts(precision=M.MIXED_TF32X3, rtol=1e-8, inner_rtol=1e-3, timeout_s=300.0)
+    out = []
+    for cs in ("16", "4", "1"):
+        monkeypatch.setenv("MASTGPU_BOTTOM_CLUSTER", cs)
+        with M.simp_cantilever(nx, ny, nz) as p:
+            p.set_design(rho)
+            u, rep = p.solve(o)
+        assert rep.status == 0 and rep.relres <= 1e-8
+        out.append((u, rep.krylov_iterations))
+    for u, its in out[1:]:
+        assert its == out[0][1] and np.array_equal(u, out[0][0])
