@@ -572,13 +572,17 @@ void *mg_problem_stream(mg_problem *p) { return p ? (void *)p->stream : nullptr;
 int mg_set_design(mg_problem *p, const double *rho) {
     if (!p || !rho) return MG_EINVAL;
     if (p->physics == MG_PHYSICS_HEAT_QUAD4) { set_error("heat physics has no density design"); return MG_ENOTSUP; }
-    for (int64_t e = 0; e < p->n_elems; e++)
-        if (!(rho[e] >= 0.0 && rho[e] <= 1.0)) {
-            set_error("density %lld = %g outside [0,1]", (long long)e, rho[e]);
-            return MG_EINVAL;
-        }
     MG_TRY(to_device_vec(p, rho, p->d_rho, p->n_elems));
-    MG_TRY(compute_modulus(p));
+    // the modulus kernel flags densities outside [0,1] (or NaN); the host looks for
+    // the first one only then, for the message
+    const int rc = compute_modulus(p);
+    if (rc == MG_EINVAL)
+        for (int64_t e = 0; e < p->n_elems; e++)
+            if (!(rho[e] >= 0.0 && rho[e] <= 1.0)) {
+                set_error("density %lld = %g outside [0,1]", (long long)e, rho[e]);
+                break;
+            }
+    MG_TRY(rc);
     p->nodal_design = false;
     p->jacobian_valid = false;
     return MG_OK;

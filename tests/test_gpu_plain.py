@@ -140,6 +140,23 @@ def test_nodal_density_field_vs_oracle():
     assert np.abs(Ke - K_ref).max() <= 1e-12 * np.abs(K_ref).max()
 
 
+def test_design_outside_the_unit_interval_is_rejected():
+    """mg_set_design: the modulus kernel flags densities outside [0,1] or NaN;
+    the call returns MG_EINVAL naming the first such element."""
+    with M.simp_cantilever(4, 2, 2) as p:
+        rho = np.full(16, 0.5)
+        rho[9] = 1.5
+        with pytest.raises(M.MastGpuError) as ei:
+            p.set_design(rho)
+        assert ei.value.status == M.MG_EINVAL and "density 9" in str(ei.value)
+        rho[9] = np.nan
+        with pytest.raises(M.MastGpuError):
+            p.set_design(rho)
+        p.set_design(np.full(16, 0.5))  # and a valid design is taken afterwards
+        u, rep = p.solve(M.default_opts(rtol=1e-10))
+        assert rep.status == 0
+
+
 def test_assembly_is_deterministic():
     nx, ny, nz = 6, 4, 4
     rho = np.random.default_rng(5).uniform(0.01, 1.0, nx * ny * nz)
