@@ -2493,32 +2493,35 @@ __global__ void mf_diag_kernel(const MfProblem *__restrict__ probs, const int *_
             const int gx = xin / 3, c = xin - 3 * gx;
             const int gy = (int)(row % P.NY), gz = (int)(row / P.NY);
             const int64_t gn = gx + (int64_t)P.NX * (gy + (int64_t)P.NY * gz);
-            double d = 0.0;
+            // FP32 (the Jacobi inverse is stored in FP32; GB300's FP64 pipe issues two
+            // DFMA per cycle per SM), the node's elements in a fixed order
+            float d = 0.0f;
             for (int dz = 0; dz < 2; dz++)
                 for (int dy = 0; dy < 2; dy++)
                     for (int dx = 0; dx < 2; dx++) {
                         const int ex = gx - dx, ey = gy - dy, ez = gz - dz;
                         if (ex < 0 || ey < 0 || ez < 0 || ex >= P.nx || ey >= P.ny || ez >= P.nz) continue;
                         const int k = 3 * corner_index(dx, dy, dz) + c;
-                        d += (double)E32[P.elem_off + ((int64_t)ez * P.ny + ey) * P.pitch_e + ex] *
-                             K0[k * 24 + k];
+                        d = fmaf(E32[P.elem_off + ((int64_t)ez * P.ny + ey) * P.pitch_e + ex], (float)K0[k * 24 + k], d);
                     }
             const bool fixed = (node_fix[P.node_off + gn] >> c) & 1;
-            out = (fixed || d == 0.0) ? 0.0f : (float)(1.0 / d);
+            out = (fixed || d == 0.0f) ? 0.0f : 1.0f / d;
         }
         dinv[P.dof_off + i] = out;
     }
 }
 
-// compliance adjoint sensitivity dC/drho_e = -dE_e u_e^T K0 u_e (FP64), written
+// compliance adjoint sensitivity dC/drho_e = -dE_e u_e^T K0 u_e, written
 // unpadded (element order x-fastest) at dc + out_off[prob]
-// dc_e = -dE_e u_e^T K0 u_e in FP64 for the listed problems, in the factored form:
-// u_e^T K0 u_e = u~^T (Khat / 64) u~ with u~ the sum/difference modes of u_e
-// (72 butterfly additions, 45 + 21 FMA instead of the 600 of the dense product;
-// GB300's FP64 pipe issues two DFMA per cycle per SM)
+// dc_e = -dE_e u_e^T K0 u_e for the listed problems, in the factored form:
+// u_e^T K0 u_e = u~^T (Khat / 64) u~ with u~ the sum/difference modes of u_e (72
+// butterfly additions, 45 + 21 products instead of the 600 of the dense product),
+// in double-float arithmetic on the FP32 pipes (48-bit significand; GB300's FP64
+// pipe issues two DFMA per cycle per SM) from the FP64 u and Khat, the final
+// product with dE_e in FP64
 __global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
                                const double *__restrict__ dE64, const uint8_t *__restrict__ node_fix,
-                               const double *__restrict__ u64, FacK<double> K,
+                               const double *__restrict__ u64, FacK<dfloat> K,
                                const int64_t *__restrict__ out_off, double *__restrict__ dc) {
     const int pi = blockIdx.y;
     if (pi >= n_probs) return;
@@ -2528,7 +2531,7 @@ __global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int ex = (int)(e % P.nx), ey = (int)((e / P.nx) % P.ny), ez = (int)(e / ((int64_t)P.nx * P.ny));
-        double v[3][8];  // component c at lexicographic corner b = bx + 2 by + 4 bz
+        dfloat v[3][8];  // component c at lexicographic corner b = bx + 2 by + 4 bz
 #pragma unroll
         for (int b = 0; b < 8; b++) {
             const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
@@ -2536,17 +2539,17 @@ __global__ void mf_sens_kernel(const MfProblem *__restrict__ probs, int n_probs,
             const uint8_t fx = node_fix[P.node_off + gn];
             const double *u = u64 + dof_index(P, ex + bx, ey + by, ez + bz, 0);
 #pragma unroll
-            for (int c = 0; c < 3; c++) v[c][b] = ((fx >> c) & 1) ? 0.0 : u[c];
+            for (int c = 0; c < 3; c++) v[c][b] = ((fx >> c) & 1) ? df_zero() : df_split(u[c]);
         }
         hex8_factored_forward(v);
-        double yh[3][8];
+        dfloat yh[3][8];
         hex8_factored_khat(K, v, yh);
-        double s = 0.0;
+        dfloat s = df_zero();
 #pragma unroll
         for (int c = 0; c < 3; c++)
 #pragma unroll
-            for (int m = 1; m < 8; m++) s = fma(v[c][m], yh[c][m], s);
-        dc[out_off[pi] + e] = -dE64[P.elem_off + ((int64_t)ez * P.ny + ey) * P.pitch_e + ex] * s;
+            for (int m = 1; m < 8; m++) s = fma_t(v[c][m], yh[c][m], s);
+        dc[out_off[pi] + e] = -dE64[P.elem_off + ((int64_t)ez * P.ny + ey) * P.pitch_e + ex] * df_to(s);
     }
 }
 
@@ -3881,7 +3884,7 @@ int mf_batch_compliance(MfBatch &b, double *compliance_host, double *dc_unpadded
         }
         MG_CUDA_TRY(cudaMemcpyAsync(b.sens_offs, offs, b.n_fine * 8, cudaMemcpyHostToDevice, s));
         dim3 grid(std::max(1u, std::min(blocks_for(max_ne, 128), 4096u)), b.n_fine);
-        mf_sens_kernel<<<grid, 128, 0, s>>>(b.probs, b.n_fine, b.dE64, b.node_fix, b.u64, b.fac64,
+        mf_sens_kernel<<<grid, 128, 0, s>>>(b.probs, b.n_fine, b.dE64, b.node_fix, b.u64, b.facdf,
                                             b.sens_offs, dc_unpadded_dev);
         cudaError_t e = cudaGetLastError();
         cudaStreamSynchronize(s);
