@@ -614,25 +614,31 @@ int mg_set_design_nodal(mg_problem *p, const double *rho_nodes) {
             set_error("nodal density %lld = %g outside [0,1]", (long long)n, rho_nodes[n]);
             return MG_EINVAL;
         }
-    if (!p->d_rho_nodes) {
-        MG_TRY(dev_alloc_n(&p->d_rho_nodes, (size_t)p->n_nodes));
-        MG_TRY(dev_alloc_n(&p->d_node_out, (size_t)p->n_nodes));
-        MG_TRY(dev_alloc_n(&p->d_Eq, (size_t)p->n_elems * 8));
-        MG_TRY(dev_alloc_n(&p->d_dEq, (size_t)p->n_elems * 8));
-        MG_TRY(dev_alloc_n(&p->d_qp_out, (size_t)p->n_elems * 8));
+    if (!p->d_node_inc) {  // the last buffer allocated: a failed first call is retried whole
+        if (!p->d_rho_nodes) MG_TRY(dev_alloc_n(&p->d_rho_nodes, (size_t)p->n_nodes));
+        if (!p->d_node_out) MG_TRY(dev_alloc_n(&p->d_node_out, (size_t)p->n_nodes));
+        if (!p->d_Eq) MG_TRY(dev_alloc_n(&p->d_Eq, (size_t)p->n_elems * 8));
+        if (!p->d_dEq) MG_TRY(dev_alloc_n(&p->d_dEq, (size_t)p->n_elems * 8));
+        if (!p->d_qp_out) MG_TRY(dev_alloc_n(&p->d_qp_out, (size_t)p->n_elems * 8));
         // node -> (element, corner) incidences in element order
         std::vector<int32_t> ptr(p->n_nodes + 1, 0), inc((size_t)p->n_elems * 8);
         for (int64_t k = 0; k < p->n_elems * 8; k++) ptr[p->h_conn[k] + 1]++;
         for (int64_t n = 0; n < p->n_nodes; n++) ptr[n + 1] += ptr[n];
         std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
         for (int64_t k = 0; k < p->n_elems * 8; k++) inc[fill[p->h_conn[k]]++] = (int32_t)k;
-        MG_TRY(dev_alloc_n(&p->d_node_inc_ptr, ptr.size()));
-        MG_TRY(dev_alloc_n(&p->d_node_inc, inc.size()));
+        if (!p->d_node_inc_ptr) MG_TRY(dev_alloc_n(&p->d_node_inc_ptr, ptr.size()));
+        int32_t *inc_dev = nullptr;
+        MG_TRY(dev_alloc_n(&inc_dev, inc.size()));
         MG_CUDA_TRY(cudaMemcpyAsync(p->d_node_inc_ptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice,
                                     p->stream));
-        MG_CUDA_TRY(cudaMemcpyAsync(p->d_node_inc, inc.data(), inc.size() * 4, cudaMemcpyHostToDevice,
-                                    p->stream));
-        MG_CUDA_TRY(cudaStreamSynchronize(p->stream));  // ptr / inc are host temporaries
+        MG_CUDA_TRY(cudaMemcpyAsync(inc_dev, inc.data(), inc.size() * 4, cudaMemcpyHostToDevice, p->stream));
+        const cudaError_t e = cudaStreamSynchronize(p->stream);  // ptr / inc are host temporaries
+        if (e != cudaSuccess) {
+            dev_free(inc_dev);
+            set_error("nodal design tables: %s", cudaGetErrorString(e));
+            return MG_ECUDA;
+        }
+        p->d_node_inc = inc_dev;
     }
     MG_TRY(to_device_vec(p, rho_nodes, p->d_rho_nodes, p->n_nodes));
     MG_TRY(compute_nodal_modulus(p));

@@ -3165,94 +3165,99 @@ int mf_batch_init(MfBatch &b, const std::vector<MfProblem> &shapes, double hx, d
     // whole GPU (the one-CTA kernel is bound by one SM's shared-memory pipe there).
     // With a cluster per chain (bottom_cluster: single-design solves), the first
     // level with at most kClusterMaxHeadNodes nodes.
-    b.h_heads.clear();
-    b.h_head_root.clear();
-    b.bottom_smem = 0;
-    b.bottom_cluster = 0;
-    for (int r = 0; r < b.n_fine; r++) {
-        for (int q = b.h_probs[r].coarse; q >= 0; q = b.h_probs[q].coarse) {
-            int64_t floats = 576 + 800, depth = 0;
-            for (int t = q; t >= 0; t = b.h_probs[t].coarse, depth++) {
-                const MfProblem &T = b.h_probs[t];
-                // x, b, r, d, y, D^-1 per dof and E per element
-                floats += 18LL * T.NX * T.NY * T.NZ + (int64_t)T.nx * T.ny * T.nz;
-            }
-            const int64_t bytes = floats * 4;
-            const MfProblem &Hd = b.h_probs[q];
-            const int64_t head_nodes = (int64_t)Hd.NX * Hd.NY * Hd.NZ;
-            const bool fits = bottom_cluster ? head_nodes <= kClusterMaxHeadNodes
-                                             : bytes <= kBottomSmemMax && head_nodes <= kBottomMaxHeadNodes;
-            if (depth <= kBottomMaxLevels && fits) {
-                b.h_heads.push_back(q);
-                b.h_head_root.push_back(r);
-                b.bottom_smem = bottom_cluster ? (576 + 800) * 4 : std::max(b.bottom_smem, (int)bytes);
-                for (int t = q; t >= 0; t = b.h_probs[t].coarse) b.h_probs[t].bottom = 1;
-                break;
+    // (a device on which no cluster of the bottom kernel can be placed falls back
+    // to the one-CTA chains)
+    int64_t inv_floats = 0;
+    for (int attempt = bottom_cluster ? 0 : 1; attempt < 2; attempt++) {
+        const bool use_cluster = attempt == 0;
+        b.h_heads.clear();
+        b.h_head_root.clear();
+        b.bottom_smem = 0;
+        b.bottom_cluster = 0;
+        for (MfProblem &T : b.h_probs) T.bottom = 0;
+        for (int r = 0; r < b.n_fine; r++) {
+            for (int q = b.h_probs[r].coarse; q >= 0; q = b.h_probs[q].coarse) {
+                int64_t floats = 576 + 800, depth = 0;
+                for (int t = q; t >= 0; t = b.h_probs[t].coarse, depth++) {
+                    const MfProblem &T = b.h_probs[t];
+                    // x, b, r, d, y, D^-1 per dof and E per element
+                    floats += 18LL * T.NX * T.NY * T.NZ + (int64_t)T.nx * T.ny * T.nz;
+                }
+                const int64_t bytes = floats * 4;
+                const MfProblem &Hd = b.h_probs[q];
+                const int64_t head_nodes = (int64_t)Hd.NX * Hd.NY * Hd.NZ;
+                const bool fits = use_cluster ? head_nodes <= kClusterMaxHeadNodes
+                                              : bytes <= kBottomSmemMax && head_nodes <= kBottomMaxHeadNodes;
+                if (depth <= kBottomMaxLevels && fits) {
+                    b.h_heads.push_back(q);
+                    b.h_head_root.push_back(r);
+                    b.bottom_smem = use_cluster ? (576 + 800) * 4 : std::max(b.bottom_smem, (int)bytes);
+                    for (int t = q; t >= 0; t = b.h_probs[t].coarse) b.h_probs[t].bottom = 1;
+                    break;
+                }
             }
         }
+        // direct coarse solves: the chains whose coarsest grid is small enough and
+        // whose inverse fits the bottom kernel's shared memory beside the levels
+        {
+            inv_floats = 0;
+            b.h_coarse_off.assign(b.h_heads.size(), -1);
+            for (size_t h = 0; h < b.h_heads.size(); h++) {
+                int64_t floats = 576 + 800;
+                int c = b.h_heads[h];
+                for (int t = c; t >= 0; t = b.h_probs[t].coarse) {
+                    const MfProblem &T = b.h_probs[t];
+                    floats += 18LL * T.NX * T.NY * T.NZ + (int64_t)T.nx * T.ny * T.nz;
+                    c = t;
+                }
+                const MfProblem &C = b.h_probs[c];
+                const int64_t nd = 3LL * C.NX * C.NY * C.NZ;
+                if (nd <= kCoarseDirectMax && (use_cluster || (floats + nd * nd) * 4 <= kBottomSmemMax)) {
+                    b.h_coarse_off[h] = inv_floats;
+                    inv_floats += nd * nd;
+                    if (!use_cluster) b.bottom_smem = std::max(b.bottom_smem, (int)((floats + nd * nd) * 4));
+                }
+            }
+        }
+        if (!use_cluster || b.h_heads.empty()) break;
+        {
+            // the largest cluster (16 CTAs: non-portable size) the device can place
+            // MASTGPU_BOTTOM_CLUSTER caps the cluster (1, 2, 4, 8 or 16 CTAs): a test knob,
+            // the result does not depend on the cluster size
+            int cap = kClusterMax;
+            if (const char *env = std::getenv("MASTGPU_BOTTOM_CLUSTER")) cap = std::max(1, std::min(kClusterMax, std::atoi(env)));
+            int first = 1;
+            while (first * 2 <= cap) first *= 2;
+            for (int cs = first; cs >= 1 && !b.bottom_cluster; cs /= 2) {
+                std::vector<ClusterChain> chains;
+                const int64_t smem = cluster_layout(b, cs, chains);
+                if (smem < 0 || smem > kBottomSmemMax) continue;
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(cs);
+                cfg.blockDim = dim3(kClusterThreads);
+                cfg.dynamicSmemBytes = smem;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = (unsigned)cs;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                int n = 0;
+                if (cudaOccupancyMaxActiveClusters(&n, mg_bottom_cluster_kernel, &cfg) == cudaSuccess && n >= 1) {
+                    b.bottom_cluster = cs;
+                    b.bottom_smem = (int)smem;
+                    b.h_cl_chains.swap(chains);
+                }
+                else
+                    cudaGetLastError();  // clear the failed query
+            }
+        }
+        if (b.bottom_cluster) break;
     }
-    // direct coarse solves: the chains whose coarsest grid is small enough and
-    // whose inverse fits the bottom kernel's shared memory beside the levels
-    {
-        int64_t inv_floats = 0;
-        b.h_coarse_off.assign(b.h_heads.size(), -1);
-        for (size_t h = 0; h < b.h_heads.size(); h++) {
-            int64_t floats = 576 + 800;
-            int c = b.h_heads[h];
-            for (int t = c; t >= 0; t = b.h_probs[t].coarse) {
-                const MfProblem &T = b.h_probs[t];
-                floats += 18LL * T.NX * T.NY * T.NZ + (int64_t)T.nx * T.ny * T.nz;
-                c = t;
-            }
-            const MfProblem &C = b.h_probs[c];
-            const int64_t nd = 3LL * C.NX * C.NY * C.NZ;
-            if (nd <= kCoarseDirectMax && (bottom_cluster || (floats + nd * nd) * 4 <= kBottomSmemMax)) {
-                b.h_coarse_off[h] = inv_floats;
-                inv_floats += nd * nd;
-                if (!bottom_cluster) b.bottom_smem = std::max(b.bottom_smem, (int)((floats + nd * nd) * 4));
-            }
-        }
-        MG_TRY(dev_alloc_n(&b.coarse_off, std::max<size_t>(1, b.h_coarse_off.size())));
-        MG_TRY(dev_alloc_n(&b.coarse_inv, (size_t)std::max<int64_t>(1, inv_floats)));
-        MG_TRY(dev_alloc_n(&b.coarse_ok, std::max<size_t>(1, b.h_coarse_off.size())));
-    }
-    if (bottom_cluster && !b.h_heads.empty()) {
-        // the largest cluster (16 CTAs: non-portable size) the device can place
-        // MASTGPU_BOTTOM_CLUSTER caps the cluster (1, 2, 4, 8 or 16 CTAs): a test knob,
-        // the result does not depend on the cluster size
-        int cap = kClusterMax;
-        if (const char *env = std::getenv("MASTGPU_BOTTOM_CLUSTER")) cap = std::max(1, std::min(kClusterMax, std::atoi(env)));
-        int first = 1;
-        while (first * 2 <= cap) first *= 2;
-        for (int cs = first; cs >= 1 && !b.bottom_cluster; cs /= 2) {
-            std::vector<ClusterChain> chains;
-            const int64_t smem = cluster_layout(b, cs, chains);
-            if (smem < 0 || smem > kBottomSmemMax) continue;
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(cs);
-            cfg.blockDim = dim3(kClusterThreads);
-            cfg.dynamicSmemBytes = smem;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = (unsigned)cs;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            int n = 0;
-            if (cudaOccupancyMaxActiveClusters(&n, mg_bottom_cluster_kernel, &cfg) == cudaSuccess && n >= 1) {
-                b.bottom_cluster = cs;
-                b.bottom_smem = (int)smem;
-                b.h_cl_chains.swap(chains);
-            }
-            else
-                cudaGetLastError();  // clear the failed query
-        }
-        if (!b.bottom_cluster) {
-            set_error("no thread-block cluster of the bottom kernel fits the device");
-            return MG_ECUDA;
-        }
-    }
+    MG_TRY(dev_alloc_n(&b.coarse_off, std::max<size_t>(1, b.h_coarse_off.size())));
+    MG_TRY(dev_alloc_n(&b.coarse_inv, (size_t)std::max<int64_t>(1, inv_floats)));
+    MG_TRY(dev_alloc_n(&b.coarse_ok, std::max<size_t>(1, b.h_coarse_off.size())));
     b.apply_grid = std::max(1, std::min(nb, 2 * sms));  // FP64 residual: two CTAs per SM
     b.col_grid = std::max(1, std::min(b.n_cols, kColCtas * sms));  // column CTAs per SM
     b.fac_grid = 2 * sms;                                     // two factored-operator CTAs per SM
