@@ -315,7 +315,8 @@ int mg_debug_launch_assembly(mg_problem *p, const double *X, int reps);
    MG_STATIC_PCG_MAX_N (larger n returns MG_EINVAL).  Each call looks the
    array's address up in the current device's context (cudaGetSymbolAddress).
    The call blocks the calling thread until the solve ends: it synchronises
-   `stream` every 16 iterations to read the convergence state.  All calls share
+   `stream` every 16 iterations to read the convergence state, so it must not be
+   called while `stream` is being captured into a graph.  All calls share
    the array, so calls that overlap on the GPU race; serialise them.  Returns
    MG_OK, MG_ENOCONV, MG_EBREAKDOWN or MG_ENAN; *iterations and *relres
    (nullable) report the iteration count and final relative residual. */
