@@ -513,6 +513,26 @@ void mg_filter_destroy(mg_filter *f);
    coordinates).  Nodes in ascending GRID id, elements in ascending element id,
    element nodes in the card's order (libMesh's local order); constraints and
    loads of every set id.  The arrays feed mg_mesh_desc / mg_bc_desc. */
+/* ---- ExodusII files (host only) ----
+   MAST writes its solutions through libMesh's ExodusII_IO
+   (examples/structural/example_7/example_7.cpp:256-281: write_timestep of the
+   mesh, nodal and element variables).  mg_exodus_write writes one time step of a
+   HEX8 (nodes_per_elem 8, dim 3) or QUAD4 (4, dim 2 or 3) mesh in the netCDF
+   classic format with 64-bit offsets: coordinates (n_nodes x dim), one element
+   block (0-based conn, written 1-based), n_nodal_vars nodal fields
+   (n_nodal_vars x n_nodes, e.g. displacement components) and n_elem_vars element
+   fields (n_elem_vars x n_elems, e.g. density, dC/drho).  mg_exodus_read_sizes /
+   mg_exodus_read_mesh read the mesh of a netCDF classic (CDF-1 or CDF-2) ExodusII
+   file: coordinates and the connectivity of every element block (one element
+   type), 0-based.  netCDF-4 / HDF5 files are not read (MG_EINVAL). */
+int mg_exodus_write(const char *path, const char *title, int32_t dim, int32_t nodes_per_elem, int64_t n_nodes,
+                    const double *coords, int64_t n_elems, const int32_t *conn, int32_t n_nodal_vars,
+                    const char *const *nodal_names, const double *nodal_vals, int32_t n_elem_vars,
+                    const char *const *elem_names, const double *elem_vals, double time);
+int mg_exodus_read_sizes(const char *path, int32_t *dim, int32_t *nodes_per_elem, int64_t *n_nodes,
+                         int64_t *n_elems);
+int mg_exodus_read_mesh(const char *path, double *coords, int32_t *conn);
+
 typedef struct mg_bdf_mesh mg_bdf_mesh;
 int mg_bdf_read(const char *path, mg_bdf_mesh **out);
 int mg_bdf_parse(const char *text, int64_t len, mg_bdf_mesh **out);

@@ -246,6 +246,12 @@ def lib(autobuild=True):
     L.mg_filter_destroy.argtypes = [_vp]
     L.mg_filter_destroy.restype = None
     L.mg_bdf_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(_vp)]
+    L.mg_exodus_write.argtypes = [ctypes.c_char_p, ctypes.c_char_p, _i32, _i32, _i64, _vp, _i64, _vp, _i32,
+                                  ctypes.POINTER(ctypes.c_char_p), _vp, _i32, ctypes.POINTER(ctypes.c_char_p),
+                                  _vp, ctypes.c_double]
+    L.mg_exodus_read_sizes.argtypes = [ctypes.c_char_p, ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                                       ctypes.POINTER(_i64), ctypes.POINTER(_i64)]
+    L.mg_exodus_read_mesh.argtypes = [ctypes.c_char_p, _vp, _vp]
     L.mg_bdf_parse.argtypes = [ctypes.c_char_p, _i64, ctypes.POINTER(_vp)]
     L.mg_bdf_sizes.argtypes = [_vp, _vp, _vp, _vp]
     L.mg_bdf_nodes.argtypes = [_vp, _vp, _vp]
@@ -341,6 +347,10 @@ class Problem:
         self.n_nodes = self.coords.shape[0]
         self.n_elems = self.conn.shape[0]
         self.n_dofs = self.n_nodes * self.dpn
+        # the boundary conditions as given (to rebuild the same problem on another mesh)
+        self.fixed_dofs = np.asarray(fixed_dofs, dtype=np.int64).copy()
+        self.load_dofs = np.asarray(load_dofs, dtype=np.int64).copy()
+        self.load_values = np.asarray(load_values, dtype=np.float64).copy()
         mesh = MeshDesc(physics, 0, self.n_nodes, self.n_elems, _p(self.coords), _p(self.conn),
                         grid[0], grid[1], grid[2], 0)
         mat = MaterialDesc(**material)
@@ -863,6 +873,37 @@ def read_bdf(path=None, text=None, dpn=3):
         L.mg_bdf_destroy(h)
     return dict(coords=coords, conn=conn, grid_ids=gids, elem_ids=eids, pids=pids, fixed_dofs=fixed,
                 load_dofs=ld, load_values=lv)
+
+
+def write_exodus(path, coords, conn, nodal=None, elem=None, title=None, time=0.0):
+    """One time step of a HEX8 / QUAD4 mesh with nodal and element fields
+    (dicts name -> array) as an ExodusII file (mg_exodus_write)."""
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    nodal = nodal or {}
+    elem = elem or {}
+    nn, dim = coords.shape
+    ne, npe = conn.shape
+    nn_names = (ctypes.c_char_p * max(1, len(nodal)))(*[k.encode() for k in nodal])
+    ne_names = (ctypes.c_char_p * max(1, len(elem)))(*[k.encode() for k in elem])
+    nv = np.ascontiguousarray(np.array([np.asarray(v, np.float64).reshape(nn) for v in nodal.values()]).reshape(-1))
+    ev = np.ascontiguousarray(np.array([np.asarray(v, np.float64).reshape(ne) for v in elem.values()]).reshape(-1))
+    check(lib().mg_exodus_write(os.fsencode(path), (title or "").encode(), dim, npe, nn, _p(coords), ne, _p(conn),
+                                len(nodal), nn_names, _p(nv) if nodal else None, len(elem), ne_names,
+                                _p(ev) if elem else None, float(time)), "mg_exodus_write")
+
+
+def read_exodus(path):
+    """Mesh of an ExodusII file (mg_exodus_read_mesh): coords (n x dim) and conn
+    (n_elems x nodes per element, 0-based) of every element block."""
+    L = lib()
+    dim, npe, nn, ne = _i32(), _i32(), _i64(), _i64()
+    check(L.mg_exodus_read_sizes(os.fsencode(path), ctypes.byref(dim), ctypes.byref(npe), ctypes.byref(nn),
+                                 ctypes.byref(ne)), "mg_exodus_read_sizes")
+    coords = np.zeros((nn.value, dim.value))
+    conn = np.zeros((ne.value, npe.value), dtype=np.int32)
+    check(L.mg_exodus_read_mesh(os.fsencode(path), _p(coords), _p(conn)), "mg_exodus_read_mesh")
+    return coords, conn
 
 
 BATCH_SIZES = ((16, 8, 8), (32, 16, 16), (48, 24, 24), (64, 32, 32), (96, 48, 48))
