@@ -617,6 +617,10 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     clocks = Clocks(local)
+    # one more untimed step once the sampler runs: the GPU idled while nvidia-smi
+    # started, and its first queries land here rather than in a timed step
+    step_resident()
+    torch.cuda.synchronize()
     launches0 = M.lib().mg_launch_count()
     ev = []
     reps = []
