@@ -409,7 +409,9 @@ __global__ void __launch_bounds__(kColThreads, kColCtas) mf_col_kernel(
     const float *__restrict__ dinv, const float *__restrict__ rhs, float *__restrict__ p0,
     float *__restrict__ p1, float *__restrict__ y, MfState *states, double *__restrict__ col_part,
     int *err) {
-    pdl_enter();
+    // the prologue (barriers, TMEM, the constant B tiles, the zeroed records) overlaps
+    // the previous kernel; everything after pdl_wait may read its results
+    pdl_trigger();
     using PR = Prec<PREC>;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -467,6 +469,7 @@ __global__ void __launch_bounds__(kColThreads, kColCtas) mf_col_kernel(
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
+    pdl_wait();
 
     if (warp == 0) {
         // ------------------------------------------------------------ TMA producer
@@ -802,8 +805,18 @@ __global__ void __launch_bounds__(kColThreads, kColCtas) mf_col_kernel(
                     last = __shfl_sync(0xffffffffu, last, 0);
                     if (last) {
                         __threadfence();
+                        // eight independent loads in flight per lane, added in column order
                         double s = 0.0;
-                        for (int c = lane; c < P.col_count; c += 32) s += __ldcg(col_part + P.col_begin + c);
+                        for (int c0 = lane; c0 < P.col_count; c0 += 32 * 8) {
+                            double pv[8];
+#pragma unroll
+                            for (int t = 0; t < 8; t++) {
+                                const int c = c0 + 32 * t;
+                                pv[t] = c < P.col_count ? __ldcg(col_part + P.col_begin + c) : 0.0;
+                            }
+#pragma unroll
+                            for (int t = 0; t < 8; t++) s += pv[t];
+                        }
 #pragma unroll
                         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
                         if (lane == 0) {
