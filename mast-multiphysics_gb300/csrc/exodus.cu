@@ -242,14 +242,21 @@ struct NcFile {
         const RVar &v = it->second;
         const int ts = type_size(v.type);
         if (ts == 0 || v.type == kNcChar) return false;
+        // every size is checked against the file before it is multiplied or added, so
+        // that no header value can wrap an offset past the end of the data
+        const uint64_t limit = raw.size() / (uint64_t)ts;
         uint64_t count = 1;
         bool is_rec = false;
         for (size_t k = 0; k < v.dims.size(); k++) {
             if ((int)v.dims[k] == record_dim && k == 0) { is_rec = true; continue; }
-            count *= dims[v.dims[k]].second;
+            const uint64_t len = dims[v.dims[k]].second;
+            if (len != 0 && count > limit / len) return false;
+            count *= len;
         }
+        if (v.begin > raw.size() || (is_rec && recsize != 0 && rec > (raw.size() - v.begin) / recsize))
+            return false;
         const uint64_t start = v.begin + (is_rec ? rec * recsize : 0);
-        if (start + count * ts > raw.size()) return false;
+        if (start > raw.size() || count > (raw.size() - start) / (uint64_t)ts) return false;
         out.resize((size_t)count);
         const uint8_t *p = raw.data() + start;
         for (uint64_t i = 0; i < count; i++, p += ts) {
@@ -302,7 +309,15 @@ int blocks(const NcFile &f, int *npe, std::string *etype, int64_t *n_elems) {
             set_error("ExodusII block %d has no connectivity", b);
             return MG_EINVAL;
         }
-        const int n = (int)f.dims[it->second.dims[1]].second;
+        const RVar &cv = it->second;
+        // an element block is a fixed-size [num_el_in_blk][num_nod_per_el] integer table
+        const uint64_t rows = f.dims[cv.dims[0]].second, cols = f.dims[cv.dims[1]].second;
+        if ((int)cv.dims[0] == f.record_dim || (int)cv.dims[1] == f.record_dim || cols < 1 || cols > 64 ||
+            rows > f.raw.size() || type_size(cv.type) == 0 || cv.type == kNcChar) {
+            set_error("ExodusII block %d: connectivity is not an element x node table", b);
+            return MG_EINVAL;
+        }
+        const int n = (int)cols;
         std::string t;
         auto at = it->second.text_atts.find("elem_type");
         if (at != it->second.text_atts.end()) t = at->second;
@@ -314,7 +329,7 @@ int blocks(const NcFile &f, int *npe, std::string *etype, int64_t *n_elems) {
             set_error("ExodusII blocks of different element types (%d and %d nodes)", *npe, n);
             return MG_EINVAL;
         }
-        *n_elems += (int64_t)f.dims[it->second.dims[0]].second;
+        *n_elems += (int64_t)rows;
     }
     return MG_OK;
 }
@@ -515,13 +530,18 @@ int mg_exodus_read_mesh(const char *path, double *coords, int32_t *conn) {
             set_error("ExodusII block %d connectivity unreadable", b);
             return MG_EINVAL;
         }
+        // the table holds exactly the block's elements (blocks() counted them), so the
+        // writes stay inside the caller's n_elems x nodes_per_elem array
+        if ((int64_t)v.size() % npe != 0 || e0 + (int64_t)v.size() / npe > ne) {
+            set_error("ExodusII block %d connectivity has the wrong size", b);
+            return MG_EINVAL;
+        }
         for (size_t i = 0; i < v.size(); i++) {
-            const int64_t node = (int64_t)v[i] - 1;
-            if (node < 0 || node >= nn) {
-                set_error("ExodusII block %d: node %lld out of range", b, (long long)v[i]);
+            if (!(v[i] >= 1.0 && v[i] <= (double)nn && v[i] == (double)(int64_t)v[i])) {
+                set_error("ExodusII block %d: node %g out of range", b, v[i]);
                 return MG_EINVAL;
             }
-            conn[e0 * npe + (int64_t)i] = (int32_t)node;
+            conn[e0 * npe + (int64_t)i] = (int32_t)((int64_t)v[i] - 1);
         }
         e0 += (int64_t)v.size() / npe;
     }

@@ -86,6 +86,52 @@ def test_not_a_classic_file_is_rejected(tmp_path):
         M.write_exodus(str(tmp_path / "x.exo"), np.zeros((8, 3)), np.full((1, 8), 9, np.int32))  # node 9 of 8
 
 
+def _hex_file(path, conn_values, conn_type="i", record=False):
+    coords, _ = M.grid_hex8(1, 1, 1)
+    with netcdf_file(path, "w", version=2) as f:
+        f.createDimension("time_step", None)
+        f.createDimension("num_dim", 3)
+        f.createDimension("num_nodes", coords.shape[0])
+        f.createDimension("num_elem", 1)
+        f.createDimension("num_el_blk", 1)
+        f.createDimension("num_el_in_blk1", 1)
+        f.createDimension("num_nod_per_el1", 8)
+        for k, ax in enumerate(("coordx", "coordy", "coordz")):
+            f.createVariable(ax, "d", ("num_nodes",))[:] = coords[:, k]
+        dims = ("time_step", "num_nod_per_el1") if record else ("num_el_in_blk1", "num_nod_per_el1")
+        v = f.createVariable("connect1", conn_type, dims)
+        v[:] = np.asarray(conn_values).reshape(1, 8)
+        v.elem_type = "HEX8"
+
+
+def test_malformed_files_are_rejected(tmp_path):
+    """Headers and tables that do not describe the data are errors, never reads or
+    writes outside the file or the caller's arrays: a truncated file, a connectivity
+    stored as a record variable, node numbers that are not integers in 1..num_nodes."""
+    good = str(tmp_path / "good.exo")
+    _hex_file(good, np.arange(1, 9))
+    c, k = M.read_exodus(good)
+    assert c.shape == (8, 3) and np.array_equal(k[0], np.arange(8))
+    raw = open(good, "rb").read()
+    for cut in (len(raw) - 4, len(raw) // 2, 12):
+        bad = tmp_path / ("cut%d.exo" % cut)
+        bad.write_bytes(raw[:cut])
+        with pytest.raises(M.MastGpuError) as e:
+            M.read_exodus(str(bad))
+        assert e.value.status == M.MG_EINVAL
+    cases = {"record.exo": dict(conn_values=np.arange(1, 9), record=True),
+             "nan.exo": dict(conn_values=[1, 2, 3, 4, 5, 6, 7, np.nan], conn_type="d"),
+             "frac.exo": dict(conn_values=[1, 2, 3, 4, 5, 6, 7, 7.5], conn_type="d"),
+             "zero.exo": dict(conn_values=[0, 2, 3, 4, 5, 6, 7, 8]),
+             "high.exo": dict(conn_values=[1, 2, 3, 4, 5, 6, 7, 9])}
+    for name, kw in cases.items():
+        path = str(tmp_path / name)
+        _hex_file(path, **kw)
+        with pytest.raises(M.MastGpuError) as e:
+            M.read_exodus(path)
+        assert e.value.status == M.MG_EINVAL, name
+
+
 @pytest.mark.gpu
 def test_exodus_mesh_solves_like_the_oracle(tmp_path):
     """A cantilever mesh written to ExodusII and read back, clamped and loaded as
