@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -339,7 +340,7 @@ int blocks(const NcFile &f, int *npe, std::string *etype, int64_t *n_elems) {
 
 using namespace mg;
 
-int mg_exodus_write(const char *path, const char *title, int32_t dim, int32_t nodes_per_elem, int64_t n_nodes,
+static int exodus_write(const char *path, const char *title, int32_t dim, int32_t nodes_per_elem, int64_t n_nodes,
                     const double *coords, int64_t n_elems, const int32_t *conn, int32_t n_nodal_vars,
                     const char *const *nodal_names, const double *nodal_vals, int32_t n_elem_vars,
                     const char *const *elem_names, const double *elem_vals, double time) {
@@ -348,6 +349,16 @@ int mg_exodus_write(const char *path, const char *title, int32_t dim, int32_t no
         (n_nodal_vars > 0 && (!nodal_names || !nodal_vals)) || (n_elem_vars > 0 && (!elem_names || !elem_vals)) ||
         n_nodes > INT32_MAX || n_elems > INT32_MAX) {
         set_error("mg_exodus_write: invalid argument");
+        return MG_EINVAL;
+    }
+    for (int32_t i = 0; i < n_nodal_vars; i++)
+        if (!nodal_names[i]) { set_error("mg_exodus_write: nodal variable %d has no name", i); return MG_EINVAL; }
+    for (int32_t i = 0; i < n_elem_vars; i++)
+        if (!elem_names[i]) { set_error("mg_exodus_write: element variable %d has no name", i); return MG_EINVAL; }
+    // the classic format's 32-bit per-variable size field: every variable below 4 GiB
+    if ((uint64_t)std::max<int64_t>(n_nodes, n_elems * nodes_per_elem / 2) * 8 >= 0xFFFFFFFCull) {
+        set_error("mg_exodus_write: a variable of %lld values exceeds the classic format's 4 GiB variable size",
+                  (long long)std::max<int64_t>(n_nodes, n_elems * nodes_per_elem));
         return MG_EINVAL;
     }
     const int len_name = 33;
@@ -476,7 +487,7 @@ int mg_exodus_write(const char *path, const char *title, int32_t dim, int32_t no
     return MG_OK;
 }
 
-int mg_exodus_read_sizes(const char *path, int32_t *dim, int32_t *nodes_per_elem, int64_t *n_nodes,
+static int exodus_read_sizes(const char *path, int32_t *dim, int32_t *nodes_per_elem, int64_t *n_nodes,
                          int64_t *n_elems) {
     if (!path) return MG_EINVAL;
     NcFile f;
@@ -492,7 +503,7 @@ int mg_exodus_read_sizes(const char *path, int32_t *dim, int32_t *nodes_per_elem
     return MG_OK;
 }
 
-int mg_exodus_read_mesh(const char *path, double *coords, int32_t *conn) {
+static int exodus_read_mesh(const char *path, double *coords, int32_t *conn) {
     if (!path || !coords || !conn) return MG_EINVAL;
     NcFile f;
     MG_TRY(load(path, f));
@@ -546,4 +557,37 @@ int mg_exodus_read_mesh(const char *path, double *coords, int32_t *conn) {
         e0 += (int64_t)v.size() / npe;
     }
     return MG_OK;
+}
+
+// the ABI entry points: host allocation failures come back as MG_ENOMEM
+int mg_exodus_write(const char *path, const char *title, int32_t dim, int32_t nodes_per_elem, int64_t n_nodes,
+                    const double *coords, int64_t n_elems, const int32_t *conn, int32_t n_nodal_vars,
+                    const char *const *nodal_names, const double *nodal_vals, int32_t n_elem_vars,
+                    const char *const *elem_names, const double *elem_vals, double time) {
+    try {
+        return exodus_write(path, title, dim, nodes_per_elem, n_nodes, coords, n_elems, conn, n_nodal_vars,
+                            nodal_names, nodal_vals, n_elem_vars, elem_names, elem_vals, time);
+    } catch (const std::bad_alloc &) {
+        set_error("mg_exodus_write: out of host memory");
+        return MG_ENOMEM;
+    }
+}
+
+int mg_exodus_read_sizes(const char *path, int32_t *dim, int32_t *nodes_per_elem, int64_t *n_nodes,
+                         int64_t *n_elems) {
+    try {
+        return exodus_read_sizes(path, dim, nodes_per_elem, n_nodes, n_elems);
+    } catch (const std::bad_alloc &) {
+        set_error("mg_exodus_read_sizes: out of host memory");
+        return MG_ENOMEM;
+    }
+}
+
+int mg_exodus_read_mesh(const char *path, double *coords, int32_t *conn) {
+    try {
+        return exodus_read_mesh(path, coords, conn);
+    } catch (const std::bad_alloc &) {
+        set_error("mg_exodus_read_mesh: out of host memory");
+        return MG_ENOMEM;
+    }
 }
