@@ -21,6 +21,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
+#include <new>
 #include <set>
 #include <string>
 #include <vector>
@@ -303,20 +305,23 @@ int build_mesh(const std::vector<Card> &cards, mg_bdf_mesh &m) {
 }
 
 int parse_into(const std::string &text, mg_bdf_mesh **out) {
-    std::vector<Card> cards;
-    std::string err;
-    if (!parse_cards(text, cards, err)) {
-        set_error("BDF: %s", err.c_str());
-        return MG_EINVAL;
+    // a deck larger than host memory allows comes back as MG_ENOMEM
+    try {
+        std::vector<Card> cards;
+        std::string err;
+        if (!parse_cards(text, cards, err)) {
+            set_error("BDF: %s", err.c_str());
+            return MG_EINVAL;
+        }
+        std::unique_ptr<mg_bdf_mesh> m(new mg_bdf_mesh());
+        const int rc = build_mesh(cards, *m);
+        if (rc != MG_OK) return rc;
+        *out = m.release();
+        return MG_OK;
+    } catch (const std::bad_alloc &) {
+        set_error("BDF: out of host memory");
+        return MG_ENOMEM;
     }
-    mg_bdf_mesh *m = new mg_bdf_mesh();
-    const int rc = build_mesh(cards, *m);
-    if (rc != MG_OK) {
-        delete m;
-        return rc;
-    }
-    *out = m;
-    return MG_OK;
 }
 
 }  // namespace
@@ -329,7 +334,12 @@ extern "C" {
 int mg_bdf_parse(const char *text, int64_t len, mg_bdf_mesh **out) {
     if (!text || len < 0 || !out) return MG_EINVAL;
     *out = nullptr;
-    return parse_into(std::string(text, (size_t)len), out);
+    try {
+        return parse_into(std::string(text, (size_t)len), out);
+    } catch (const std::bad_alloc &) {
+        set_error("BDF: out of host memory");
+        return MG_ENOMEM;
+    }
 }
 
 int mg_bdf_read(const char *path, mg_bdf_mesh **out) {
@@ -343,7 +353,13 @@ int mg_bdf_read(const char *path, mg_bdf_mesh **out) {
     std::string text;
     char buf[1 << 16];
     size_t n;
-    while ((n = std::fread(buf, 1, sizeof(buf), fp)) > 0) text.append(buf, n);
+    try {
+        while ((n = std::fread(buf, 1, sizeof(buf), fp)) > 0) text.append(buf, n);
+    } catch (const std::bad_alloc &) {
+        std::fclose(fp);
+        set_error("BDF: out of host memory");
+        return MG_ENOMEM;
+    }
     std::fclose(fp);
     return parse_into(text, out);
 }
