@@ -629,10 +629,11 @@ int mg_set_design_nodal(mg_problem *p, const double *rho_nodes) {
         if (!p->d_node_inc_ptr) MG_TRY(dev_alloc_n(&p->d_node_inc_ptr, ptr.size()));
         int32_t *inc_dev = nullptr;
         MG_TRY(dev_alloc_n(&inc_dev, inc.size()));
-        MG_CUDA_TRY(cudaMemcpyAsync(p->d_node_inc_ptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice,
-                                    p->stream));
-        MG_CUDA_TRY(cudaMemcpyAsync(inc_dev, inc.data(), inc.size() * 4, cudaMemcpyHostToDevice, p->stream));
-        const cudaError_t e = cudaStreamSynchronize(p->stream);  // ptr / inc are host temporaries
+        cudaError_t e = cudaMemcpyAsync(p->d_node_inc_ptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice,
+                                        p->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(inc_dev, inc.data(), inc.size() * 4, cudaMemcpyHostToDevice, p->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);  // ptr / inc are host temporaries
         if (e != cudaSuccess) {
             dev_free(inc_dev);
             set_error("nodal design tables: %s", cudaGetErrorString(e));
