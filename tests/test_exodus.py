@@ -132,6 +132,21 @@ def test_malformed_files_are_rejected(tmp_path):
         assert e.value.status == M.MG_EINVAL, name
 
 
+def test_writer_rejects_unnamed_variables(tmp_path):
+    """A null entry in a name table is an argument error of the C ABI, not a crash."""
+    import ctypes
+    coords, conn = M.grid_hex8(1, 1, 1)
+    coords = np.ascontiguousarray(coords)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    vals = np.zeros(2 * coords.shape[0])  # two nodal variables, kept alive over the call
+    names = (ctypes.c_char_p * 2)(b"a", None)
+    rc = M.lib().mg_exodus_write(os.fsencode(str(tmp_path / "x.exo")), None, 3, 8, coords.shape[0],
+                                 coords.ctypes.data, conn.shape[0], conn.ctypes.data, 2, names,
+                                 vals.ctypes.data, 0, None, None, 0.0)
+    assert rc == M.MG_EINVAL
+    assert not (tmp_path / "x.exo").exists()
+
+
 @pytest.mark.gpu
 def test_exodus_mesh_solves_like_the_oracle(tmp_path):
     """A cantilever mesh written to ExodusII and read back, clamped and loaded as
